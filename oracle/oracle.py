@@ -1,0 +1,528 @@
+"""Python face of the FP64 oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, and only as the checker or as the CPU timing baseline.  The product
+library in casa-rs_gb300/ never imports it.
+
+The heavy loops live in casa_oracle.c; this module adds the parts the
+reference delegates to rustfft 6.4.1 (the centred 2-D DFT, restated here with
+numpy's float64 pocketfft) and the image-domain normalisation.  Each function
+cites the reference function (file:line, relative to crates/casa-imaging/src)
+it restates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _build.build()
+        _LIB = C.CDLL(path)
+        _declare(_LIB)
+    return _LIB
+
+
+_d = C.c_double
+_f = C.c_float
+_i32 = C.c_int32
+_i64 = C.c_int64
+_p = C.c_void_p
+
+
+class Accum(C.Structure):
+    _fields_ = [("normalization_sumwt", _d), ("reported_sumwt", _d),
+                ("gridded", _i64), ("skipped", _i64)]
+
+
+class StdParams(C.Structure):
+    _fields_ = [("gnx", _i64), ("gny", _i64), ("oversampling", _i32), ("support", _i32),
+                ("du", _d), ("dv", _d), ("taps", _p), ("tap_rows", _i32)]
+
+
+class WpParams(C.Structure):
+    _fields_ = [("gnx", _i64), ("gny", _i64), ("du", _d), ("dv", _d), ("planes", _i32),
+                ("sampling", _i32), ("w_scale", _d), ("width", _i32), ("support", _p),
+                ("kernels", _p), ("norm_radius", _i32), ("norm_table", _p)]
+
+
+def _declare(L):
+    sig = {
+        "oc_casa_composite_padded_len": (_i64, [_i64, _d]),
+        "oc_image_blc": (None, [_i64, _i64, C.POINTER(_i64)]),
+        "oc_grdsf": (_d, [_d]),
+        "oc_spheroidal_kernel": (_f, [_d, _d]),
+        "oc_std_kernel_table": (None, [_i32, _i32, _p]),
+        "oc_std_tap_rows": (_i32, [_i32]),
+        "oc_std_normalized_taps": (None, [_p, _i32, _i32, _i32, _p]),
+        "oc_correction_axis": (None, [_i64, _p]),
+        "oc_gridder_correction_axis": (None, [_i64, _p]),
+        "oc_sinc_axis": (None, [_i64, _i64, _p]),
+        "oc_std_plan": (C.c_int, [C.POINTER(StdParams), _d, _d, C.POINTER(_i64),
+                                  C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
+        "oc_std_grid_dirty": (None, [C.POINTER(StdParams), _i64, _p, _p, _p, _p, _p, _p, _p,
+                                     _p, C.POINTER(Accum), _i32]),
+        "oc_std_degrid": (None, [C.POINTER(StdParams), _p, _i64, _p, _p, _p]),
+        "oc_std_residual": (None, [C.POINTER(StdParams), _p, _i64, _p, _p, _p, _p, _p, _p,
+                                   _p, _p, C.POINTER(Accum), _i32]),
+        "oc_wproj_suggested_planes": (_i64, [_i64, _i64, _d, _d, _d]),
+        "oc_wproj_max_uvw": (_d, [_d, _d, C.c_int]),
+        "oc_wproj_build": (C.c_int, [_i64, _i64, _d, _d, _i64, _i64, _d, _i32, C.c_int, _i32,
+                                     _i32, _i32, _i32, _i32, C.POINTER(_d), _p,
+                                     C.POINTER(_i32), _p, _p]),
+        "oc_wproj_plane_index": (_i32, [C.POINTER(WpParams), _d]),
+        "oc_wproj_plan": (C.c_int, [C.POINTER(WpParams), _d, _d, _d, C.POINTER(_i64),
+                                    C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64),
+                                    C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_d)]),
+        "oc_wproj_grid_dirty": (None, [C.POINTER(WpParams), _i64, _p, _p, _p, _p, _p, _p,
+                                       _p, _p, _p, C.POINTER(Accum), _i32]),
+        "oc_wproj_degrid": (None, [C.POINTER(WpParams), _p, _i64, _p, _p, _p, _p, _i32]),
+        "oc_wproj_residual": (None, [C.POINTER(WpParams), _p, _i64, _p, _p, _p, _p, _p, _p,
+                                     _p, _p, C.POINTER(Accum), _i32]),
+        "oc_density_cell": (C.c_int, [_i64, _i64, _d, _d, _d, _d, C.c_int, C.POINTER(_i64),
+                                      C.POINTER(_i64)]),
+        "oc_density_grid": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, _p]),
+        "oc_briggs_f2": (_f, [_p, _i64, _f]),
+        "oc_briggs_denominator": (_f, [_f, _f]),
+        "oc_reweight": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, _p, C.c_int, _f, _p]),
+        "oc_peak_location": (C.c_int, [_p, _p, _i64, _i64, C.POINTER(_i64), C.POINTER(_i64),
+                                       C.POINTER(_f)]),
+        "oc_minor_cycle_stop_reason": (C.c_int, [_f, _f, _f, _f]),
+        "oc_hogbom": (_i64, [_p, _p, _p, _p, _i64, _i64, _f, _f, _f, _f, _i64, C.c_int, _p,
+                             _p, _p, _p, C.POINTER(_i32), C.POINTER(_i64)]),
+        "oc_subtract_shifted_psf": (None, [_p, _p, _i64, _i64, _i64, _i64, _f]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _c(a, dtype):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)
+
+
+# --------------------------------------------------------------------------
+# geometry
+# --------------------------------------------------------------------------
+def padded_len(image_len: int, padding: float = 1.2) -> int:
+    """casa_composite_padded_len (gridder.rs:4152-4173)."""
+    return int(lib().oc_casa_composite_padded_len(image_len, padding))
+
+
+def image_blc(grid_len: int, image_len: int) -> int:
+    """image_blc (gridder.rs:401-404)."""
+    out = _i64()
+    lib().oc_image_blc(grid_len, image_len, C.byref(out))
+    return int(out.value)
+
+
+def grdsf(nu: float) -> float:
+    return float(lib().oc_grdsf(nu))
+
+
+def correction_axis(size: int) -> np.ndarray:
+    """build_correction_axis (gridder.rs:4175-4188)."""
+    out = np.zeros(size, np.float32)
+    lib().oc_correction_axis(size, _ptr(out))
+    return out
+
+
+def sinc_axis(size: int, conv_sampling: int) -> np.ndarray:
+    """build_sinc_axis (gridder.rs:4211-4228)."""
+    out = np.zeros(size, np.float32)
+    lib().oc_sinc_axis(size, conv_sampling, _ptr(out))
+    return out
+
+
+def std_taps(oversampling: int, support: int = 3) -> np.ndarray:
+    """Kernel table and normalised tap rows (gridder.rs:407-416, 2026-2051)."""
+    tlen = oversampling * (support + 1)
+    table = np.zeros(tlen, np.float32)
+    lib().oc_std_kernel_table(oversampling, support, _ptr(table))
+    rows = int(lib().oc_std_tap_rows(oversampling))
+    taps = np.zeros((rows, 2 * support + 1), np.float32)
+    lib().oc_std_normalized_taps(_ptr(table), tlen, oversampling, support, _ptr(taps))
+    return taps
+
+
+# --------------------------------------------------------------------------
+# centred FFTs (fft.rs:600-630; rustfft's DFT restated as float64 pocketfft)
+# --------------------------------------------------------------------------
+def centered_ifft2(grid: np.ndarray) -> np.ndarray:
+    """ifftshift -> inverse DFT scaled by 1/(Nx Ny) -> fftshift (fft.rs:611-624)."""
+    g = np.asarray(grid, np.complex128)
+    return np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(g)))
+
+
+def centered_fft2(grid: np.ndarray) -> np.ndarray:
+    """ifftshift -> unscaled forward DFT -> fftshift (fft.rs:34, 600-630)."""
+    g = np.asarray(grid, np.complex128)
+    return np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(g)))
+
+
+# --------------------------------------------------------------------------
+# standard gridder
+# --------------------------------------------------------------------------
+@dataclass
+class Geometry:
+    nx: int
+    ny: int
+    cell_x: float
+    cell_y: float
+
+
+class StdGridder:
+    """StandardGridder (gridder.rs:322-443) at a chosen oversampling."""
+
+    def __init__(self, geom: Geometry, oversampling: int = 100, padding: float = 1.2):
+        self.geom = geom
+        self.os = oversampling
+        self.gnx = padded_len(geom.nx, padding)
+        self.gny = padded_len(geom.ny, padding)
+        self.blc_x = image_blc(self.gnx, geom.nx)
+        self.blc_y = image_blc(self.gny, geom.ny)
+        self.du = 1.0 / (self.gnx * geom.cell_x)
+        self.dv = 1.0 / (self.gny * geom.cell_y)
+        self.taps = std_taps(oversampling)
+        self.corr_x = correction_axis(self.gnx)
+        self.corr_y = correction_axis(self.gny)
+        self._p = StdParams(self.gnx, self.gny, oversampling, 3, self.du, self.dv,
+                            self.taps.ctypes.data, self.taps.shape[0])
+
+    def plan(self, u: float, v: float):
+        x0, y0, wx, wy = _i64(), _i64(), _i64(), _i64()
+        ok = lib().oc_std_plan(C.byref(self._p), u, v, C.byref(x0), C.byref(y0), C.byref(wx),
+                               C.byref(wy))
+        return (int(x0.value), int(y0.value), int(wx.value), int(wy.value)) if ok else None
+
+    def grid_dirty(self, u, v, weight, vis, sumwt_factor=None, gridable=None, threads=1):
+        """accumulate_dirty_psf_and_residual_standard_streaming_grid (lib.rs:68306-68500)."""
+        n = len(u)
+        u, v = _c(u, np.float64), _c(v, np.float64)
+        weight, sumwt_factor = _c(weight, np.float32), _c(sumwt_factor, np.float32)
+        gridable = _c(gridable, np.uint8)
+        vis = _c(vis, np.complex64)
+        psf = np.zeros((self.gnx, self.gny), np.complex128)
+        dirty = np.zeros((self.gnx, self.gny), np.complex128)
+        acc = Accum()
+        lib().oc_std_grid_dirty(C.byref(self._p), n, _ptr(u), _ptr(v), _ptr(weight),
+                                _ptr(sumwt_factor), _ptr(gridable), _ptr(vis), _ptr(psf),
+                                _ptr(dirty), C.byref(acc), threads)
+        return psf, dirty, acc
+
+    def degrid(self, model_grid, u, v):
+        """degrid_sample_taps_planned_normalized (gridder.rs:1278-1312), FP64."""
+        g = _c(model_grid, np.complex128)
+        u, v = _c(u, np.float64), _c(v, np.float64)
+        pred = np.zeros(len(u), np.complex128)
+        lib().oc_std_degrid(C.byref(self._p), _ptr(g), len(u), _ptr(u), _ptr(v), _ptr(pred))
+        return pred
+
+    def residual(self, model_grid, u, v, weight, vis, sumwt_factor=None, gridable=None,
+                 threads=1):
+        """degrid_model_and_grid_residual_taps_planned_f64 (gridder.rs:1315-1396)."""
+        n = len(u)
+        g = _c(model_grid, np.complex128)
+        u, v = _c(u, np.float64), _c(v, np.float64)
+        weight, sumwt_factor = _c(weight, np.float32), _c(sumwt_factor, np.float32)
+        gridable = _c(gridable, np.uint8)
+        vis = _c(vis, np.complex64)
+        res = np.zeros((self.gnx, self.gny), np.complex128)
+        pred = np.zeros(n, np.complex128)
+        acc = Accum()
+        lib().oc_std_residual(C.byref(self._p), _ptr(g), n, _ptr(u), _ptr(v), _ptr(weight),
+                              _ptr(sumwt_factor), _ptr(gridable), _ptr(vis), _ptr(res),
+                              _ptr(pred), C.byref(acc), threads)
+        return res, pred, acc
+
+    # image-domain stages --------------------------------------------------
+    def corrected_image(self, raw: np.ndarray) -> np.ndarray:
+        """corrected_image_from_grid_f64 (gridder.rs:1646-1657)."""
+        nx, ny = self.geom.nx, self.geom.ny
+        sub = raw[self.blc_x:self.blc_x + nx, self.blc_y:self.blc_y + ny].real
+        corr = (self.corr_x[self.blc_x:self.blc_x + nx, None].astype(np.float64)
+                * self.corr_y[None, self.blc_y:self.blc_y + ny].astype(np.float64))
+        return sub * corr
+
+    def apodize(self, model: np.ndarray) -> np.ndarray:
+        """apodize_model (gridder.rs:1554-1570)."""
+        out = np.zeros((self.gnx, self.gny), np.complex128)
+        nx, ny = self.geom.nx, self.geom.ny
+        corr = (self.corr_x[self.blc_x:self.blc_x + nx, None].astype(np.float64)
+                * self.corr_y[None, self.blc_y:self.blc_y + ny].astype(np.float64))
+        out[self.blc_x:self.blc_x + nx, self.blc_y:self.blc_y + ny] = model * corr
+        return out
+
+    def model_grid(self, model: np.ndarray) -> np.ndarray:
+        """centered_fft2(apodize_model(model)) (lib.rs:69000; gridder.rs:1554)."""
+        return centered_fft2(self.apodize(model))
+
+    def dirty_products(self, psf_grid, dirty_grid, acc: Accum):
+        """dirty_grids_to_psf_and_residual_owned (lib.rs:48987-49130)."""
+        if acc.normalization_sumwt <= 0.0:
+            raise ValueError("no usable samples")
+        psf = self.corrected_image(centered_ifft2(psf_grid)) / acc.normalization_sumwt
+        peak = float(np.max(np.abs(psf)))
+        psf = psf / peak
+        res = self.corrected_image(centered_ifft2(dirty_grid)) / acc.normalization_sumwt / peak
+        return psf, res, peak
+
+
+# --------------------------------------------------------------------------
+# W-projection
+# --------------------------------------------------------------------------
+class WProjector:
+    """WProjector (gridder.rs:3391-3855), FP64 kernels."""
+
+    def __init__(self, geom: Geometry, gridder: StdGridder, max_abs_w: float, planes=None,
+                 sampling=None, support_min=0, support_max=0, threads=8, max_width=4096):
+        self.geom = geom
+        self.gridder = gridder
+        explicit = planes is not None
+        if planes is None:
+            planes = max(1, int(lib().oc_wproj_suggested_planes(
+                geom.nx, geom.ny, geom.cell_x, geom.cell_y, max_abs_w)))
+        if sampling is None:
+            sampling = 4 if planes > 1 else 1
+        self.planes = planes
+        self.sampling = sampling
+        self.norm_radius = (sampling + 1) // 2
+        L = 2 * self.norm_radius + 1
+        conv = max(gridder.gnx, gridder.gny)
+        quarter = conv // 2 - 1
+        cap = min(max_width, quarter)
+        kern = np.zeros((planes, cap, cap), np.complex128)
+        norm = np.zeros((planes, L, L), np.float64)
+        support = np.zeros(planes, np.int32)
+        w_scale = _d()
+        width = _i32()
+        rc = lib().oc_wproj_build(geom.nx, geom.ny, geom.cell_x, geom.cell_y, gridder.gnx,
+                                  gridder.gny, max_abs_w, planes, int(explicit), sampling,
+                                  support_min, support_max, cap, threads, C.byref(w_scale),
+                                  _ptr(support), C.byref(width), _ptr(kern), _ptr(norm))
+        if rc != 0:
+            raise ValueError(f"oc_wproj_build failed with status {rc}")
+        W = int(width.value)
+        flat = kern.reshape(-1)[: planes * W * W]
+        self.kernels = np.ascontiguousarray(flat.reshape(planes, W, W))
+        self.norm = norm
+        self.support = support
+        self.width = W
+        self.w_scale = float(w_scale.value)
+        self._bind()
+
+    @classmethod
+    def from_arrays(cls, geom, gridder, w_scale, support, kernels, norm, sampling):
+        """A projector over given kernel arrays (for timing with kernels built elsewhere)."""
+        self = cls.__new__(cls)
+        self.geom, self.gridder = geom, gridder
+        self.planes = len(support)
+        self.sampling = sampling
+        self.norm_radius = (sampling + 1) // 2
+        self.kernels = np.ascontiguousarray(kernels, np.complex128)
+        self.norm = np.ascontiguousarray(norm, np.float64)
+        self.support = np.ascontiguousarray(support, np.int32)
+        self.width = self.kernels.shape[1]
+        self.w_scale = float(w_scale)
+        self._bind()
+        return self
+
+    def _bind(self):
+        g = self.gridder
+        self._p = WpParams(g.gnx, g.gny, g.du, g.dv, self.planes, self.sampling, self.w_scale,
+                           self.width, self.support.ctypes.data, self.kernels.ctypes.data,
+                           self.norm_radius, self.norm.ctypes.data)
+
+    def plan(self, u, v, w):
+        lx, ly, ox, oy = _i64(), _i64(), _i64(), _i64()
+        pl, cj, nrm = _i32(), _i32(), _d()
+        ok = lib().oc_wproj_plan(C.byref(self._p), u, v, w, C.byref(lx), C.byref(ly),
+                                 C.byref(ox), C.byref(oy), C.byref(pl), C.byref(cj),
+                                 C.byref(nrm))
+        if not ok:
+            return None
+        return dict(loc_x=lx.value, loc_y=ly.value, off_x=ox.value, off_y=oy.value,
+                    plane=pl.value, conj=bool(cj.value), normalization=nrm.value)
+
+    def grid_dirty(self, u, v, w, weight, vis, sumwt_factor=None, gridable=None, threads=1):
+        n = len(u)
+        u, v, w = _c(u, np.float64), _c(v, np.float64), _c(w, np.float64)
+        weight, sumwt_factor = _c(weight, np.float32), _c(sumwt_factor, np.float32)
+        gridable = _c(gridable, np.uint8)
+        vis = _c(vis, np.complex64)
+        g = self.gridder
+        psf = np.zeros((g.gnx, g.gny), np.complex128)
+        dirty = np.zeros((g.gnx, g.gny), np.complex128)
+        acc = Accum()
+        lib().oc_wproj_grid_dirty(C.byref(self._p), n, _ptr(u), _ptr(v), _ptr(w), _ptr(weight),
+                                  _ptr(sumwt_factor), _ptr(gridable), _ptr(vis), _ptr(psf),
+                                  _ptr(dirty), C.byref(acc), threads)
+        return psf, dirty, acc
+
+    def degrid(self, model_grid, u, v, w, threads=1):
+        g = _c(model_grid, np.complex128)
+        u, v, w = _c(u, np.float64), _c(v, np.float64), _c(w, np.float64)
+        pred = np.zeros(len(u), np.complex128)
+        lib().oc_wproj_degrid(C.byref(self._p), _ptr(g), len(u), _ptr(u), _ptr(v), _ptr(w),
+                              _ptr(pred), threads)
+        return pred
+
+    def residual(self, model_grid, u, v, w, weight, vis, sumwt_factor=None, gridable=None,
+                 threads=1):
+        n = len(u)
+        g = _c(model_grid, np.complex128)
+        u, v, w = _c(u, np.float64), _c(v, np.float64), _c(w, np.float64)
+        weight, sumwt_factor = _c(weight, np.float32), _c(sumwt_factor, np.float32)
+        gridable = _c(gridable, np.uint8)
+        vis = _c(vis, np.complex64)
+        gr = self.gridder
+        res = np.zeros((gr.gnx, gr.gny), np.complex128)
+        acc = Accum()
+        lib().oc_wproj_residual(C.byref(self._p), _ptr(g), n, _ptr(u), _ptr(v), _ptr(w),
+                                _ptr(weight), _ptr(sumwt_factor), _ptr(gridable), _ptr(vis),
+                                _ptr(res), C.byref(acc), threads)
+        return res, acc
+
+    # image-domain stages --------------------------------------------------
+    def _sinc(self):
+        g = self.gridder
+        return sinc_axis(max(g.gnx, g.gny), self.sampling).astype(np.float64)
+
+    def corrected_image(self, raw):
+        """corrected_w_project_image_from_grid (gridder.rs:1685-1715)."""
+        g = self.gridder
+        nx, ny = self.geom.nx, self.geom.ny
+        s = self._sinc()
+        sub = raw[g.blc_x:g.blc_x + nx, g.blc_y:g.blc_y + ny]
+        corr = (g.corr_x[g.blc_x:g.blc_x + nx, None].astype(np.float64)
+                * g.corr_y[None, g.blc_y:g.blc_y + ny].astype(np.float64))
+        sf = s[g.blc_x:g.blc_x + nx, None] * s[None, g.blc_y:g.blc_y + ny]
+        out = np.where(np.abs(sf) > 1e-6, (sub * (corr / np.where(sf == 0, 1, sf))).real, 0.0)
+        return out
+
+    def apodize(self, model):
+        """apodize_w_project_model (gridder.rs:1572-1592)."""
+        g = self.gridder
+        nx, ny = self.geom.nx, self.geom.ny
+        sx = sinc_axis(g.gnx, self.sampling).astype(np.float64)
+        sy = sinc_axis(g.gny, self.sampling).astype(np.float64)
+        f = (g.corr_x[g.blc_x:g.blc_x + nx, None].astype(np.float64)
+             * g.corr_y[None, g.blc_y:g.blc_y + ny].astype(np.float64)
+             * sx[g.blc_x:g.blc_x + nx, None] * sy[None, g.blc_y:g.blc_y + ny])
+        out = np.zeros((g.gnx, g.gny), np.complex128)
+        out[g.blc_x:g.blc_x + nx, g.blc_y:g.blc_y + ny] = model * f
+        return out
+
+    def model_grid(self, model):
+        return centered_fft2(self.apodize(model))
+
+    def dirty_products(self, psf_grid, dirty_grid, acc: Accum):
+        """compute_dirty_psf_and_residual_w_project_streaming (lib.rs:70539-70590)."""
+        if acc.normalization_sumwt <= 0.0:
+            raise ValueError("no usable samples")
+        psf = 2.0 * self.corrected_image(centered_ifft2(psf_grid)) / acc.normalization_sumwt
+        peak = float(np.max(np.abs(psf)))
+        psf = psf / peak
+        res = 2.0 * self.corrected_image(centered_ifft2(dirty_grid)) / acc.normalization_sumwt
+        res = res / peak
+        return psf, res, peak
+
+
+# --------------------------------------------------------------------------
+# weighting
+# --------------------------------------------------------------------------
+def density_cell(geom: Geometry, u: float, v: float, convention: int = 0):
+    cx, cy = _i64(), _i64()
+    ok = lib().oc_density_cell(geom.nx, geom.ny, geom.cell_x, geom.cell_y, u, v, convention,
+                               C.byref(cx), C.byref(cy))
+    return (int(cx.value), int(cy.value)) if ok else None
+
+
+def density_grid(geom: Geometry, u, v, weight):
+    """build_density_grid_serial (weighting.rs:1729-1854)."""
+    u, v, weight = _c(u, np.float64), _c(v, np.float64), _c(weight, np.float32)
+    d = np.zeros((geom.nx, geom.ny), np.float32)
+    lib().oc_density_grid(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u), _ptr(v),
+                          _ptr(weight), _ptr(d))
+    return d
+
+
+def briggs_f2(density, robust: float) -> float:
+    d = _c(density, np.float32)
+    return float(lib().oc_briggs_f2(_ptr(d), d.size, robust))
+
+
+def briggs_denominator(density: float, f2: float) -> float:
+    return float(lib().oc_briggs_denominator(density, f2))
+
+
+def apply_weighting(geom: Geometry, u, v, weight, mode: str = "natural", robust: float = 0.0):
+    """apply_weighting_with_density_source, Combined mode (weighting.rs:1055-1180)."""
+    u, v, weight = _c(u, np.float64), _c(v, np.float64), _c(weight, np.float32)
+    if mode == "natural":
+        return weight.copy(), None, 0.0
+    d = density_grid(geom, u, v, weight)
+    m = {"uniform": 1, "briggs": 2}[mode]
+    f2 = briggs_f2(d, robust) if m == 2 else 0.0
+    out = np.zeros_like(weight)
+    lib().oc_reweight(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u), _ptr(v),
+                      _ptr(weight), _ptr(d), m, f2, _ptr(out))
+    return out, d, f2
+
+
+# --------------------------------------------------------------------------
+# Hogbom
+# --------------------------------------------------------------------------
+def peak_location(image, mask=None):
+    img = _c(image, np.float32)
+    mk = _c(mask, np.uint8)
+    px, py, val = _i64(), _i64(), _f()
+    ok = lib().oc_peak_location(_ptr(img), _ptr(mk), img.shape[0], img.shape[1], C.byref(px),
+                                C.byref(py), C.byref(val))
+    return ((int(px.value), int(py.value)), float(val.value)) if ok else None
+
+
+def stop_reason(peak_abs, threshold, cycle_threshold, nsigma_threshold) -> int:
+    return int(lib().oc_minor_cycle_stop_reason(peak_abs, threshold, cycle_threshold,
+                                                nsigma_threshold))
+
+
+def hogbom(residual, psf, gain, niter, threshold=0.0, cycle_threshold=0.0,
+           nsigma_threshold=0.0, mask=None, model=None, inclusive=True):
+    """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883)."""
+    res = np.array(residual, np.float32, copy=True, order="C")
+    p = _c(psf, np.float32)
+    nx, ny = res.shape
+    mdl = np.zeros_like(res) if model is None else np.array(model, np.float32, copy=True)
+    mk = _c(mask, np.uint8)
+    cap = niter + 1
+    cx = np.zeros(cap, np.int32)
+    cy = np.zeros(cap, np.int32)
+    cp = np.zeros(cap, np.float32)
+    cf = np.zeros(cap, np.float32)
+    stop = _i32()
+    reported = _i64()
+    n = lib().oc_hogbom(_ptr(mdl), _ptr(res), _ptr(p), _ptr(mk), nx, ny, gain, threshold,
+                        cycle_threshold, nsigma_threshold, niter, int(inclusive), _ptr(cx),
+                        _ptr(cy), _ptr(cp), _ptr(cf), C.byref(stop), C.byref(reported))
+    return dict(model=mdl, residual=res, x=cx[:n], y=cy[:n], peak=cp[:n], flux=cf[:n],
+                stop_reason=int(stop.value), actual=int(n), reported=int(reported.value))
+
+
+def radians_from_arcsec(a: float) -> float:
+    return a / 3600.0 * math.pi / 180.0
