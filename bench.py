@@ -1,0 +1,372 @@
+"""Benchmark: W-projection grid + degrid throughput (Mvis/s) at 4096^2.
+
+Workload (the W-projection dirty-image configuration): 27 antennas on a Y
+with arms to 21 km, 8 h of 2 s dumps at 1.4 GHz (5,054,400 rows, one
+channel), 200 seeded point sources 1 mJy - 1 Jy plus 5 mJy noise, a
+4096 x 4096 image (grid 5000 x 5000), 128 w-planes with support growing
+linearly with plane index from 8 to 64 pixels, oversampling 8.
+
+One step = one pass of the hot path over the batch: the per-sample plan
+(FP64 index selection, sort, deduplication), gridding of PSF and dirty grids
+and degridding of a model grid, with inputs resident in HBM.  Inputs are
+larger than L2, so no flush is needed between steps.  `e2e` repeats the same
+work through the reference-facing calls with host buffers (host -> device
+copies, the dirty image and the model visibilities back to host).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "casa-rs_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mvis/s grid+degrid (4096^2, W-proj)"
+UNIT = "Mvis/s"
+PLANES, SAMPLING, SUPPORT_LAW = 128, 8, (8, 64)
+SEED = 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rows-fraction", type=float, default=1.0,
+                    help="use every k-th row (profiling runs only)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(fraction=1.0):
+    from casars_cuda import synthetic as S
+    obs = S.config2_geometry(SEED)
+    if fraction < 1.0:
+        k = max(1, int(round(1.0 / fraction)))
+        obs.u, obs.v, obs.w = obs.u[::k].copy(), obs.v[::k].copy(), obs.w[::k].copy()
+    return obs
+
+
+def algorithmic_bytes(rows, grid_cells):
+    """Grid: u,v,w f64 + vis c64 + weight f32 + flag u8 per row, PSF and dirty
+    complex64 written once.  Degrid: u,v,w + flag per row, model grid read
+    once, model visibility written."""
+    grid = rows * (24 + 13) + grid_cells * 16
+    degrid = rows * (24 + 1 + 8) + grid_cells * 8
+    return grid, degrid
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons while timing."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": mx or None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(name="wp_grid_kernel_4096_wproj.md"):
+    """DRAM bytes per launch of the grid kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_rate(obs, kernels, norm, support, w_scale, model_grid, budget_s=12.0):
+    """Oracle (the C restatement of the reference CPU path, multi-threaded like
+    the reference) timed on host cores: grid + degrid of a bounded, evenly
+    strided sample of the same rows, with the same kernels."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    geom = O.Geometry(obs.nx, obs.ny, obs.cell, obs.cell)
+    og = O.StdGridder(geom, 100)
+    wp = O.WProjector.from_arrays(geom, og, w_scale, support, kernels.astype(np.complex128),
+                                  norm.astype(np.float64), SAMPLING)
+    mg = np.asarray(model_grid, np.complex128)
+    rng = np.random.default_rng(SEED)
+    vis = (rng.normal(size=len(obs.u)) + 1j * rng.normal(size=len(obs.u))).astype(np.complex64)
+    wt = np.ones(len(obs.u), np.float32)
+
+    def run(stride):
+        sl = slice(0, None, stride)
+        u, v, w = obs.u[sl], obs.v[sl], obs.w[sl]
+        t0 = time.perf_counter()
+        _, _, acc = wp.grid_dirty(u, v, w, wt[sl], vis[sl], threads=threads)
+        wp.degrid(mg, u, v, w, threads=threads)
+        return acc.gridded, time.perf_counter() - t0
+
+    stride = 1024
+    n, t = run(stride)
+    # scale the sample to the time budget, the pilot's fixed costs included
+    want = max(1, int(stride * t / budget_s)) if t > 0 else stride
+    stride = max(8, min(stride, want))
+    n, t = run(stride)
+    return n / t / 1e6, threads, f"every {stride}th row ({n} rows), grid+degrid, {threads} threads"
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU path (restated in C, the oracle; the
+    Rust original cannot be built here) on the host cores, with its own FP64
+    W-kernels, timed per step on a bounded sample of the same workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    obs = workload(1.0)
+    threads = os.cpu_count() or 1
+    geom = O.Geometry(obs.nx, obs.ny, obs.cell, obs.cell)
+    og = O.StdGridder(geom, 100)
+    wp = O.WProjector(geom, og, float(np.abs(obs.w).max()), planes=PLANES, sampling=SAMPLING,
+                      support_min=SUPPORT_LAW[0], support_max=SUPPORT_LAW[1], threads=threads)
+    rng = np.random.default_rng(SEED)
+    n_all = len(obs.u)
+    vis = (rng.normal(size=n_all) + 1j * rng.normal(size=n_all)).astype(np.complex64)
+    wt = np.ones(n_all, np.float32)
+    mg = np.zeros((og.gnx, og.gny), np.complex128)
+    mg[og.gnx // 2, og.gny // 2] = 1.0
+    stride = 400  # ~12.6k rows per step
+
+    def step():
+        sl = slice(0, None, stride)
+        t0 = time.perf_counter()
+        _, _, acc = wp.grid_dirty(obs.u[sl], obs.v[sl], obs.w[sl], wt[sl], vis[sl], threads=threads)
+        wp.degrid(mg, obs.u[sl], obs.v[sl], obs.w[sl], threads=threads)
+        return acc.gridded, time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, t = step()
+        tot_n += n
+        tot_t += t
+    value = tot_n / tot_t / 1e6
+    sample = f"every {stride}th row ({tot_n // max(args.steps, 1)} rows) per step, grid+degrid"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_t / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config2: W-proj dirty 4096^2, 5,054,400 rows, 128 planes, "
+                                   "support 8-64, oversampling 8", "rows": n_all,
+                       "sample_rows_per_step": tot_n // max(args.steps, 1)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+
+    import casars_cuda as cc
+    from casars_cuda import synthetic as S
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    obs = workload(args.rows_fraction)
+    n = obs.rows
+    ctx = cc.Context(local)
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(obs.nx, obs.ny, obs.cell, obs.cell), 100)
+    gw = cc.WProjector(gg, float(np.abs(obs.w).max()), planes=PLANES, sampling=SAMPLING,
+                       support_law=SUPPORT_LAW)
+    u = torch.as_tensor(obs.u, device=dev)
+    v = torch.as_tensor(obs.v, device=dev)
+    w = torch.as_tensor(obs.w, device=dev)
+    vis = S.visibilities_torch(obs.u, obs.v, obs.w, obs.sky, obs.nx, obs.ny, obs.cell, 5e-3,
+                               SEED, device=dev)
+    wt = torch.ones(n, dtype=torch.float32, device=dev)
+    batch = cc.VisibilityBatch(u, v, vis, wt, w)
+    model = torch.as_tensor(S.model_image(obs.sky, obs.nx, obs.ny), device=dev)
+    model_grid = cc.image_to_grid(gg, model, gw)
+    torch.cuda.synchronize()
+
+    grid_ms, degrid_ms = [], []
+    last = {}
+
+    def step(record):
+        psf, dirty, sums = cc.grid_dirty(gg, batch, gw)
+        tg = ctx.last_timings()
+        pred = cc.degrid(gg, batch, model_grid, gw)
+        td = ctx.last_timings()
+        if record:
+            grid_ms.append(tg["grid_ms"])
+            degrid_ms.append(td["degrid_ms"])
+        last["sums"] = sums
+        return pred
+
+    for _ in range(max(args.warmup, 0)):
+        step(False)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = ctx.launch_count
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        start.record()
+        for _ in range(args.steps):
+            step(True)
+        end.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / args.steps
+    launches = (ctx.launch_count - launches0)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    sums = last["sums"]
+    accepted = sums.gridded_samples
+    value = world * accepted / (ms * 1e-3) / 1e6
+
+    # dominant kernel roofline: the grid stage (tile lists + wp_grid_kernel)
+    gcells = gg.grid_shape()[0] * gg.grid_shape()[1]
+    b_grid, b_degrid = algorithmic_bytes(n, gcells)
+    g_ms = statistics.mean(grid_ms)
+    d_ms = statistics.mean(degrid_ms)
+    peak, peak_kind = measured_peaks()
+    achieved = b_grid / (g_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 index selection and sums)", "data": "synthetic",
+        "config": {"workload": "config2: W-proj dirty 4096^2 (grid 5000^2), 5,054,400 rows, "
+                               "1 channel, 128 w-planes, support 8-64 linear in plane, "
+                               "oversampling 8, 200 points + 5 mJy noise",
+                   "rows": n, "rows_fraction": args.rows_fraction,
+                   "unique_records": sums.unique_records, "parallelism": f"replicas{world}",
+                   "l2": "inputs (0.19 GB rows + 0.2 GB model grid + 0.4 GB output grids) exceed L2"},
+        "gpu_launches": launches,
+        "stages_ms": {"grid": g_ms, "degrid": d_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "wp_grid_kernel (grid stage)", "peak_kind": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": b_grid},
+        "clocks": clk.summary(),
+    }
+
+    if not args.no_e2e:
+        # the reference-facing calls with host (pinned) buffers
+        hu, hv, hw = (torch.as_tensor(a).pin_memory() for a in (obs.u, obs.v, obs.w))
+        hvis = vis.cpu().pin_memory()
+        hwt = wt.cpu().pin_memory()
+        hmodel = model.cpu().pin_memory()
+        hb = cc.VisibilityBatch(hu, hv, hvis, hwt, hw)
+
+        def e2e_step():
+            cc.dirty_image(gg, hb, gw)
+            cc.predict(gg, hb, hmodel, gw)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+        row_bytes = 24 + 8 + 4
+        result["e2e"] = {"value": world * accepted / (e_ms * 1e-3) / 1e6, "unit": UNIT,
+                         "h2d_bytes_per_step": 2 * n * row_bytes + obs.nx * obs.ny * 4,
+                         "d2h_bytes_per_step": 2 * obs.nx * obs.ny * 4 + n * 8,
+                         "ms_per_step": e_ms, "calls": "cr_dirty_image + cr_predict"}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        support, kern, norm = gw.tables()
+        rate, cores, sample = cpu_rate(obs, kern, norm, support, gw.w_scale,
+                                       model_grid.cpu().numpy())
+        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": sample}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,580 @@
+// cr_api.cu -- the extern "C" boundary of libcasars_cuda.
+//
+// Every entry point catches internal errors and turns them into the
+// reference shims' convention: an int status and a heap message in *err.
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "cr_internal.cuh"
+
+using namespace cr;
+
+namespace {
+
+void set_err(char** err, const std::string& msg) {
+    if (!err) return;
+    char* s = (char*)std::malloc(msg.size() + 1);
+    if (s) std::memcpy(s, msg.c_str(), msg.size() + 1);
+    *err = s;
+}
+
+template <class F>
+int guarded(char** err, F&& f) {
+    if (err) *err = nullptr;
+    try {
+        f();
+        return CR_OK;
+    } catch (const Error& e) {
+        set_err(err, e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_err(err, e.what());
+        return CR_INVALID;
+    } catch (...) {
+        set_err(err, "unknown error");
+        return CR_INVALID;
+    }
+}
+
+void need(bool c, const char* what) {
+    if (!c) fail(CR_INVALID, what);
+}
+
+struct StageTimer {
+    cr_ctx* ctx;
+    int n = 0;
+    explicit StageTimer(cr_ctx* c) : ctx(c) {}
+    void mark() {
+        if (n < 8) CR_CUDA_CHECK(cudaEventRecord(ctx->ev[n++], ctx->stream));
+    }
+    float between(int a, int b) {
+        if (b >= n || a >= n) return 0.0f;
+        float ms = 0.0f;
+        CR_CUDA_CHECK(cudaEventSynchronize(ctx->ev[b]));
+        CR_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]));
+        return ms;
+    }
+};
+
+void bind(cr_ctx* ctx) { CR_CUDA_CHECK(cudaSetDevice(ctx->device)); }
+
+Records plan(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const DeviceBatch& b) {
+    return wp ? plan_wproj(ctx, wp, b) : plan_standard(ctx, g, b);
+}
+
+void grid_records(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const Records& r, float2* psf,
+                  float2* dirty, int mode) {
+    if (wp)
+        wproj_grid(ctx, wp, r, psf, dirty, mode);
+    else
+        std_grid(ctx, g, r, psf, dirty, mode);
+}
+
+void degrid_records(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const Records& r,
+                    const float2* grid) {
+    if (wp)
+        wproj_degrid(ctx, wp, r, grid);
+    else
+        std_degrid(ctx, g, r, grid);
+}
+
+size_t grid_bytes(const cr_gridder* g) { return (size_t)g->info.grid_nx * g->info.grid_ny * 8; }
+size_t image_pixels(const cr_gridder* g) { return (size_t)g->geom.nx * g->geom.ny; }
+
+// output pointer on the device: the caller's buffer when it is device memory,
+// else a named workspace that is copied out afterwards
+template <class T>
+T* out_ptr(cr_ctx* ctx, void* user, int32_t loc, size_t bytes, const char* name) {
+    if (loc == CR_DEVICE) {
+        need(user != nullptr, "output pointer is null");
+        return (T*)user;
+    }
+    need(loc == CR_HOST, "location must be CR_HOST or CR_DEVICE");
+    return (T*)workspace(ctx, std::string("out_") + name, bytes);
+}
+
+void check_wp(cr_gridder* g, cr_wproj* wp) {
+    need(g != nullptr, "gridder is null");
+    if (wp) need(wp->g == g, "W-projector belongs to another gridder");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cr_version(void) { return "casars_cuda 0.1 (sm_103a)"; }
+
+void cr_free_error(char* err) { std::free(err); }
+
+int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
+    return guarded(err, [&] {
+        need(out != nullptr, "out is null");
+        *out = nullptr;
+        int n = 0;
+        CR_CUDA_CHECK(cudaGetDeviceCount(&n));
+        need(device >= 0 && device < n, "no such CUDA device");
+        CR_CUDA_CHECK(cudaSetDevice(device));
+        cr_ctx* c = new cr_ctx();
+        c->device = device;
+        CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+        c->stream = c->own_stream;
+        for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
+        CR_CUDA_CHECK(cudaMallocHost(&c->pinned, 4096));
+        *out = c;
+    });
+}
+
+void cr_ctx_destroy(cr_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->ws)
+        if (kv.second.ptr) cudaFreeAsync(kv.second.ptr, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->fft_plans) cufftDestroy(kv.second);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int cr_ctx_set_stream(cr_ctx* ctx, void* stream, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    });
+}
+
+void* cr_ctx_stream(cr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int cr_ctx_synchronize(cr_ctx* ctx, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_ctx_last_timings(cr_ctx* ctx, cr_timings* out) {
+    if (!ctx || !out) return CR_INVALID;
+    *out = ctx->timings;
+    return CR_OK;
+}
+
+int64_t cr_ctx_launch_count(cr_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int cr_gridder_create(cr_ctx* ctx, const cr_geometry* geom, double padding, int32_t oversampling,
+                      cr_gridder** out, cr_grid_info* info, char** err) {
+    return guarded(err, [&] {
+        need(ctx && geom && out, "null argument");
+        *out = nullptr;
+        need(geom->nx > 0 && geom->ny > 0, "image shape must be positive");
+        need(std::isfinite(geom->cell_x_rad) && std::isfinite(geom->cell_y_rad) &&
+                 geom->cell_x_rad > 0.0 && geom->cell_y_rad > 0.0,
+             "cell sizes must be finite and positive");
+        need(oversampling >= 1 && oversampling <= 254, "oversampling must be in [1, 254]");
+        need(padding >= 1.0 && padding < 8.0, "padding must be in [1, 8)");
+        bind(ctx);
+        cr_gridder* g = new cr_gridder();
+        g->ctx = ctx;
+        g->geom = *geom;
+        int64_t gnx = casa_composite_padded_len(geom->nx, padding);
+        int64_t gny = casa_composite_padded_len(geom->ny, padding);
+        g->info.grid_nx = gnx;
+        g->info.grid_ny = gny;
+        g->info.blc_x = image_blc(gnx, geom->nx);
+        g->info.blc_y = image_blc(gny, geom->ny);
+        g->info.du = 1.0 / ((double)gnx * geom->cell_x_rad);
+        g->info.dv = 1.0 / ((double)gny * geom->cell_y_rad);
+        g->info.oversampling = oversampling;
+        g->taps_h = std_normalized_taps(oversampling, 3);
+        g->tap_rows = 2 * (oversampling / 2) + 1;
+        g->corr_x_h = correction_axis(gnx);
+        g->corr_y_h = correction_axis(gny);
+        try {
+            CR_CUDA_CHECK(cudaMalloc(&g->taps_d, g->taps_h.size() * 4));
+            CR_CUDA_CHECK(cudaMalloc(&g->corr_x_d, (size_t)gnx * 4));
+            CR_CUDA_CHECK(cudaMalloc(&g->corr_y_d, (size_t)gny * 4));
+            CR_CUDA_CHECK(cudaMemcpy(g->taps_d, g->taps_h.data(), g->taps_h.size() * 4, cudaMemcpyHostToDevice));
+            CR_CUDA_CHECK(cudaMemcpy(g->corr_x_d, g->corr_x_h.data(), (size_t)gnx * 4, cudaMemcpyHostToDevice));
+            CR_CUDA_CHECK(cudaMemcpy(g->corr_y_d, g->corr_y_h.data(), (size_t)gny * 4, cudaMemcpyHostToDevice));
+        } catch (...) {
+            cr_gridder_destroy(g);
+            throw;
+        }
+        if (info) *info = g->info;
+        *out = g;
+    });
+}
+
+void cr_gridder_destroy(cr_gridder* g) {
+    if (!g) return;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    cudaFree(g->taps_d);
+    cudaFree(g->corr_x_d);
+    cudaFree(g->corr_y_d);
+    delete g;
+}
+
+int cr_gridder_tables(cr_gridder* g, float* taps, float* corr_x, float* corr_y, char** err) {
+    return guarded(err, [&] {
+        need(g != nullptr, "gridder is null");
+        if (taps) std::memcpy(taps, g->taps_h.data(), g->taps_h.size() * 4);
+        if (corr_x) std::memcpy(corr_x, g->corr_x_h.data(), g->corr_x_h.size() * 4);
+        if (corr_y) std::memcpy(corr_y, g->corr_y_h.data(), g->corr_y_h.size() * 4);
+    });
+}
+
+int cr_wproj_create(cr_ctx* ctx, cr_gridder* g, double max_abs_w, int32_t planes,
+                    int32_t sampling, int32_t support_min, int32_t support_max, cr_wproj** out,
+                    cr_wproj_info* info, char** err) {
+    return guarded(err, [&] {
+        need(ctx && g && out, "null argument");
+        need(g->ctx == ctx, "gridder belongs to another context");
+        *out = nullptr;
+        need(std::isfinite(max_abs_w) && max_abs_w >= 0.0, "max_abs_w must be finite");
+        need(sampling <= 64, "sampling above 64");
+        bind(ctx);
+        cr_wproj* wp = new cr_wproj();
+        wp->ctx = ctx;
+        wp->g = g;
+        try {
+            build_wproj(ctx, wp, max_abs_w, planes, sampling, support_min, support_max);
+        } catch (...) {
+            cr_wproj_destroy(wp);
+            throw;
+        }
+        if (info) *info = wp->info;
+        *out = wp;
+    });
+}
+
+void cr_wproj_destroy(cr_wproj* wp) {
+    if (!wp) return;
+    cudaSetDevice(wp->ctx->device);
+    cudaStreamSynchronize(wp->ctx->stream);
+    cudaFree(wp->support_d);
+    cudaFree(wp->slab_off_d);
+    cudaFree(wp->kernels_d);
+    cudaFree(wp->norm_d);
+    cudaFree(wp->slabs_d);
+    cudaFree(wp->sinc_x_d);
+    cudaFree(wp->sinc_gx_d);
+    cudaFree(wp->sinc_gy_d);
+    delete wp;
+}
+
+int cr_wproj_tables(cr_wproj* wp, int32_t* support, float* kernels, float* norm, char** err) {
+    return guarded(err, [&] {
+        need(wp != nullptr, "W-projector is null");
+        bind(wp->ctx);
+        const cr_wproj_info& i = wp->info;
+        if (support) std::memcpy(support, wp->support_h.data(), (size_t)i.planes * 4);
+        if (kernels)
+            CR_CUDA_CHECK(cudaMemcpy(kernels, wp->kernels_d,
+                                     (size_t)i.planes * i.kernel_width * i.kernel_width * 8,
+                                     cudaMemcpyDeviceToHost));
+        if (norm)
+            CR_CUDA_CHECK(cudaMemcpy(norm, wp->norm_d, (size_t)i.planes * wp->axis * wp->axis * 4,
+                                     cudaMemcpyDeviceToHost));
+    });
+}
+
+int cr_grid_dirty(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                  float* psf_grid, float* dirty_grid, int32_t out_location, cr_sums* sums,
+                  char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        check_wp(g, wp);
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        float2* psf = out_ptr<float2>(ctx, psf_grid, out_location, gb, "psf_grid");
+        float2* dirty = out_ptr<float2>(ctx, dirty_grid, out_location, gb, "dirty_grid");
+        CR_CUDA_CHECK(cudaMemsetAsync(psf, 0, gb, ctx->stream));
+        CR_CUDA_CHECK(cudaMemsetAsync(dirty, 0, gb, ctx->stream));
+        Records r = plan(ctx, g, wp, b);
+        tm.mark();
+        grid_records(ctx, g, wp, r, psf, dirty, 0);
+        tm.mark();
+        if (out_location == CR_HOST) {
+            copy_out(ctx, psf_grid, psf, gb, CR_HOST);
+            copy_out(ctx, dirty_grid, dirty, gb, CR_HOST);
+        }
+        cr_sums s{};
+        read_sums(ctx, r, &s);
+        if (sums) *sums = s;
+        ctx->timings = cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, 0.f, 0.f};
+    });
+}
+
+int cr_degrid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+              const float* model_grid, int32_t grid_location, float* pred, int32_t out_location,
+              char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && model_grid != nullptr, "null argument");
+        check_wp(g, wp);
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        const float2* grid = (const float2*)device_input(ctx, model_grid, grid_bytes(g),
+                                                         grid_location, "model_grid");
+        Records r = plan(ctx, g, wp, b);
+        tm.mark();
+        degrid_records(ctx, g, wp, r, grid);
+        float2* out = out_ptr<float2>(ctx, pred, out_location, (size_t)b.n * 8 + 8, "pred");
+        broadcast_pred(ctx, r, out);
+        tm.mark();
+        if (out_location == CR_HOST) copy_out(ctx, pred, out, (size_t)b.n * 8, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        ctx->timings = cr_timings{tm.between(0, 1), 0.f, tm.between(1, 2), 0.f, 0.f};
+    });
+}
+
+int cr_grid_residual(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                     const float* model_grid, int32_t grid_location, float* residual_grid,
+                     int32_t out_location, cr_sums* sums, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        check_wp(g, wp);
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        Records r = plan(ctx, g, wp, b);
+        if (model_grid) {
+            const float2* grid = (const float2*)device_input(ctx, model_grid, gb, grid_location,
+                                                             "model_grid");
+            degrid_records(ctx, g, wp, r, grid);
+        } else {
+            CR_CUDA_CHECK(cudaMemsetAsync(r.rec_pred, 0, (size_t)(b.n > 0 ? b.n : 1) * 8, ctx->stream));
+        }
+        float2* res = out_ptr<float2>(ctx, residual_grid, out_location, gb, "residual_grid");
+        CR_CUDA_CHECK(cudaMemsetAsync(res, 0, gb, ctx->stream));
+        grid_records(ctx, g, wp, r, nullptr, res, 1);
+        if (out_location == CR_HOST) copy_out(ctx, residual_grid, res, gb, CR_HOST);
+        cr_sums s{};
+        read_sums(ctx, r, &s);
+        if (sums) *sums = s;
+    });
+}
+
+int cr_grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* grid,
+                     int32_t grid_location, float scale, float* image, int32_t out_location,
+                     char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && grid != nullptr, "null argument");
+        check_wp(g, wp);
+        bind(ctx);
+        size_t gb = grid_bytes(g);
+        float2* work = (float2*)workspace(ctx, "fft_grid", gb);
+        CR_CUDA_CHECK(cudaMemcpyAsync(work, grid, gb,
+                                      grid_location == CR_HOST ? cudaMemcpyHostToDevice
+                                                               : cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        size_t ib = image_pixels(g) * 4;
+        float* img = out_ptr<float>(ctx, image, out_location, ib, "image");
+        grid_to_image(ctx, g, wp, work, scale, img);
+        if (out_location == CR_HOST) copy_out(ctx, image, img, ib, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
+                     int32_t model_location, float* grid, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && model != nullptr, "null argument");
+        check_wp(g, wp);
+        bind(ctx);
+        const float* m = (const float*)device_input(ctx, model, image_pixels(g) * 4,
+                                                    model_location, "model");
+        size_t gb = grid_bytes(g);
+        float2* out = out_ptr<float2>(ctx, grid, out_location, gb, "model_grid");
+        image_to_grid(ctx, g, wp, m, out);
+        if (out_location == CR_HOST) copy_out(ctx, grid, out, gb, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                   float* psf_out, float* residual_out, int32_t out_location,
+                   cr_psf_state* state, cr_sums* sums, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        check_wp(g, wp);
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        float2* psf = (float2*)workspace(ctx, "di_psf", gb);
+        float2* dirty = (float2*)workspace(ctx, "di_dirty", gb);
+        CR_CUDA_CHECK(cudaMemsetAsync(psf, 0, gb, ctx->stream));
+        CR_CUDA_CHECK(cudaMemsetAsync(dirty, 0, gb, ctx->stream));
+        Records r = plan(ctx, g, wp, b);
+        tm.mark();
+        grid_records(ctx, g, wp, r, psf, dirty, 0);
+        tm.mark();
+        cr_sums s{};
+        read_sums(ctx, r, &s);
+        if (sums) *sums = s;
+        if (s.normalization_sumwt <= 0.0 || s.reported_sumwt <= 0.0)
+            fail(CR_NO_SAMPLES, "no usable samples");
+        const float k = wp ? 2.0f : 1.0f;
+        const float sumwt_f = (float)s.normalization_sumwt;
+        const size_t np = image_pixels(g);
+        float* psf_img = out_ptr<float>(ctx, psf_out, out_location, np * 4, "psf_image");
+        float* res_img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "res_image");
+        unsigned int* peak_d = (unsigned int*)workspace(ctx, "di_peak", 4);
+        grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img);
+        abs_peak(ctx, psf_img, (int64_t)np, peak_d);
+        unsigned int peak_bits = 0;
+        CR_CUDA_CHECK(cudaMemcpyAsync(&peak_bits, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        float peak;
+        std::memcpy(&peak, &peak_bits, 4);
+        if (!(std::isfinite(peak) && peak > 0.0f))
+            fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
+        scale_image(ctx, psf_img, (int64_t)np, 1.0f, peak_d);
+        grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img);
+        scale_image(ctx, res_img, (int64_t)np, 1.0f, peak_d);
+        tm.mark();
+        if (out_location == CR_HOST) {
+            copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
+            copy_out(ctx, residual_out, res_img, np * 4, CR_HOST);
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        if (state) *state = cr_psf_state{peak, sumwt_f, (float)s.reported_sumwt};
+        ctx->timings = cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, tm.between(2, 3), 0.f};
+    });
+}
+
+int cr_residual_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                      const float* model, int32_t model_location, const cr_psf_state* state,
+                      float* residual_out, int32_t out_location, cr_sums* sums, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && state != nullptr && model != nullptr, "null argument");
+        need(state->normalization_sumwt > 0.0f && state->psf_peak > 0.0f, "invalid PSF state");
+        check_wp(g, wp);
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        const size_t np = image_pixels(g);
+        const float* m = (const float*)device_input(ctx, model, np * 4, model_location, "model");
+        float2* mgrid = (float2*)workspace(ctx, "ri_model_grid", gb);
+        image_to_grid(ctx, g, wp, m, mgrid);
+        Records r = plan(ctx, g, wp, b);
+        degrid_records(ctx, g, wp, r, mgrid);
+        float2* res = (float2*)workspace(ctx, "ri_residual_grid", gb);
+        CR_CUDA_CHECK(cudaMemsetAsync(res, 0, gb, ctx->stream));
+        grid_records(ctx, g, wp, r, nullptr, res, 1);
+        float* img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "ri_image");
+        const float k = wp ? 2.0f : 1.0f;
+        grid_to_image(ctx, g, wp, res, k / state->normalization_sumwt, img);
+        scale_image(ctx, img, (int64_t)np, 1.0f / state->psf_peak, nullptr);
+        if (out_location == CR_HOST) copy_out(ctx, residual_out, img, np * 4, CR_HOST);
+        cr_sums s{};
+        read_sums(ctx, r, &s);
+        if (sums) *sums = s;
+    });
+}
+
+int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+               const float* model, int32_t model_location, float* pred, int32_t out_location,
+               char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && model != nullptr, "null argument");
+        check_wp(g, wp);
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        const float* m = (const float*)device_input(ctx, model, image_pixels(g) * 4,
+                                                    model_location, "model");
+        float2* mgrid = (float2*)workspace(ctx, "pr_model_grid", gb);
+        image_to_grid(ctx, g, wp, m, mgrid);
+        Records r = plan(ctx, g, wp, b);
+        degrid_records(ctx, g, wp, r, mgrid);
+        float2* out = out_ptr<float2>(ctx, pred, out_location, (size_t)b.n * 8 + 8, "pred");
+        broadcast_pred(ctx, r, out);
+        if (out_location == CR_HOST) copy_out(ctx, pred, out, (size_t)b.n * 8, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+               float* image, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr, "context is null");
+        check_wp(g, wp);
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        size_t gb = grid_bytes(g);
+        Records r = plan(ctx, g, wp, b);
+        CR_CUDA_CHECK(cudaMemsetAsync(r.rec_pred, 0, (size_t)(b.n > 0 ? b.n : 1) * 8, ctx->stream));
+        float2* grid = (float2*)workspace(ctx, "adj_grid", gb);
+        CR_CUDA_CHECK(cudaMemsetAsync(grid, 0, gb, ctx->stream));
+        grid_records(ctx, g, wp, r, nullptr, grid, 1);
+        const size_t np = image_pixels(g);
+        float* img = out_ptr<float>(ctx, image, out_location, np * 4, "adj_image");
+        // F^H = (Nx Ny) x the scaled inverse; the image-side factor is the
+        // forward apodisation's (corr, times sinc for W-projection)
+        float n2 = (float)((double)g->info.grid_nx * (double)g->info.grid_ny);
+        grid_to_image_adjoint(ctx, g, wp, grid, n2, img);
+        if (out_location == CR_HOST) copy_out(ctx, image, img, np * 4, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_apply_weighting(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch, int32_t mode,
+                       float robust, float* out_weight, int32_t out_location, float* f2,
+                       char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr, "null argument");
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, false);
+        float* out = out_ptr<float>(ctx, out_weight, out_location, (size_t)b.n * 4 + 4, "weights");
+        apply_weighting(ctx, g, b, mode, robust, out, f2);
+        if (out_location == CR_HOST) copy_out(ctx, out_weight, out, (size_t)b.n * 4, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
+              int32_t nx, int32_t ny, int32_t location, float gain, float threshold,
+              float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+              int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+              float* comp_flux, int64_t* actual, int64_t* reported, int32_t* stop_reason,
+              char** err) {
+    return guarded(err, [&] {
+        need(ctx && model && residual && psf, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        need(location == CR_HOST || location == CR_DEVICE, "bad location");
+        need(!comp_x == !comp_y && !comp_x == !comp_peak && !comp_x == !comp_flux,
+             "component arrays must be all given or all null");
+        bind(ctx);
+        size_t nb = (size_t)nx * ny * 4;
+        float* m = location == CR_DEVICE ? model : (float*)workspace(ctx, "hog_model", nb);
+        float* r = location == CR_DEVICE ? residual : (float*)workspace(ctx, "hog_residual", nb);
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(m, model, nb, cudaMemcpyHostToDevice, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(r, residual, nb, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const float* p = (const float*)device_input(ctx, psf, nb, location, "hog_psf");
+        const uint8_t* mk = (const uint8_t*)device_input(ctx, mask, (size_t)nx * ny, location,
+                                                         "hog_mask");
+        cr::hogbom(ctx, m, r, p, mk, nx, ny, gain, threshold, cycle_threshold, nsigma_threshold,
+                   cycle_niter, inclusive, comp_x, comp_y, comp_peak, comp_flux, actual, reported,
+                   stop_reason);
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(model, m, nb, cudaMemcpyDeviceToHost, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(residual, r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+}  // extern "C"

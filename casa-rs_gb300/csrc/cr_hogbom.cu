@@ -1,0 +1,307 @@
+// cr_hogbom.cu -- the Hogbom minor cycle as one persistent device loop.
+//
+// Restates run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883):
+// repeat up to the component budget (hogbom_component_budget, lib.rs:64541-
+// 64552): find the unmasked pixel of largest |residual| with ties going to
+// the smallest y*nx + x (peak_location_masked_in_bounds_zero_tolerance,
+// lib.rs:74064-74118), stop on the threshold rules (minor_cycle_stop_reason,
+// lib.rs:74653-74676), add gain*peak to the model and subtract the shifted
+// PSF over the overlap (subtract_shifted_kernel_in_window, lib.rs:74805-
+// 74870) as a float32 multiply then subtract.
+//
+// Each block owns a contiguous range of pixels.  One pass per iteration
+// subtracts the previous component and finds the block's next candidate with
+// a warp-shuffle argmax; one grid barrier publishes the candidates, and every
+// block reduces all candidates to the same global peak.  The kernel is
+// launched cooperatively (all blocks resident); the barrier's wait is bounded
+// and reports CR_TIMEOUT instead of spinning forever.
+#include "cr_internal.cuh"
+
+namespace cr {
+
+namespace {
+
+constexpr int kHogThreads = 512;
+constexpr long long kBarrierSpinLimit = 1ll << 24;  // x ~64 ns sleeps: about a second
+
+struct Cand {
+    float absval;  // -1 when the block has no cleanable pixel
+    int key;       // y * nx + x
+    float value;
+    int pad;
+};
+
+struct HogArgs {
+    float* model;
+    float* residual;
+    const float* psf;
+    const uint8_t* mask;
+    int nx, ny;
+    float gain, threshold, cycle_threshold, nsigma_threshold;
+    long long budget;
+    Cand* cands;  // [2][gridDim]
+    unsigned int* bar;  // [0] arrivals, [1] generation
+    int* comp_x;
+    int* comp_y;
+    float* comp_peak;
+    float* comp_flux;
+    long long* out_actual;
+    int* out_stop;
+    int* out_status;
+};
+
+__device__ __forceinline__ bool better(float a_abs, int a_key, float b_abs, int b_key) {
+    return a_abs > b_abs || (a_abs == b_abs && a_key < b_key);
+}
+
+__device__ __forceinline__ void warp_argmax(float& a, int& k, float& v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float a2 = __shfl_xor_sync(0xffffffffu, a, o);
+        int k2 = __shfl_xor_sync(0xffffffffu, k, o);
+        float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        if (better(a2, k2, a, k)) {
+            a = a2;
+            k = k2;
+            v = v2;
+        }
+    }
+}
+
+// Block argmax of (abs, key, value); result valid in thread 0.
+__device__ Cand block_argmax(float a, int k, float v) {
+    __shared__ Cand sh[kHogThreads / 32];
+    warp_argmax(a, k, v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = Cand{a, k, v, 0};
+    __syncthreads();
+    Cand c{-1.0f, 0x7fffffff, 0.0f, 0};
+    if (warp == 0) {
+        Cand m = lane < (int)(blockDim.x >> 5) ? sh[lane] : Cand{-1.0f, 0x7fffffff, 0.0f, 0};
+        a = m.absval;
+        k = m.key;
+        v = m.value;
+        warp_argmax(a, k, v);
+        c = Cand{a, k, v, 0};
+    }
+    __syncthreads();
+    return c;
+}
+
+// Bounded grid barrier (all blocks are co-resident under the cooperative
+// launch).  Returns false on every thread of a block whose wait timed out.
+__device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* gen = bar + 1;
+        unsigned int g = *gen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&bar[0], 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (++spins > kBarrierSpinLimit) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool threshold_reached(float peak, float thr) {
+    if (thr <= 0.0f) return peak <= thr;
+    float tol = fmaxf(__fmul_rn(0.01f, thr), 2.0e-8f);
+    return peak <= thr || fabsf(__fsub_rn(peak, thr)) <= tol;
+}
+
+__device__ int stop_reason(float peak_abs, float thr, float cyc, float nsig) {
+    bool floor_active = thr > 0.0f && __fmul_rn(0.01f, thr) < 2.0e-8f && cyc <= thr;
+    if (peak_abs < thr || (floor_active && threshold_reached(peak_abs, thr)))
+        return CR_STOP_GLOBAL_THRESHOLD;
+    if (cyc >= nsig) return peak_abs < cyc ? CR_STOP_CYCLE_THRESHOLD : 0;
+    if (nsig > thr) return peak_abs < nsig ? CR_STOP_NSIGMA_THRESHOLD : 0;
+    return 0;
+}
+
+__global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
+    const int64_t npix = (int64_t)a.nx * a.ny;
+    const int64_t chunk = (npix + gridDim.x - 1) / gridDim.x;
+    const int64_t p0 = (int64_t)blockIdx.x * chunk;
+    const int64_t p1 = min(npix, p0 + chunk);
+    const int kcx = a.nx / 2, kcy = a.ny / 2;
+    __shared__ Cand s_best;
+    __shared__ int s_stop;
+
+    // initial candidates
+    {
+        float ba = -1.0f, bv = 0.0f;
+        int bk = 0x7fffffff;
+        for (int64_t t = p0 + threadIdx.x; t < p1; t += blockDim.x) {
+            if (a.mask && !a.mask[t]) continue;
+            int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
+            float v = a.residual[t];
+            float av = fabsf(v);
+            int key = y * a.nx + x;
+            if (better(av, key, ba, bk)) {
+                ba = av;
+                bk = key;
+                bv = v;
+            }
+        }
+        Cand c = block_argmax(ba, bk, bv);
+        if (threadIdx.x == 0) a.cands[blockIdx.x] = c;
+    }
+    if (!grid_barrier(a.bar, gridDim.x)) {
+        if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
+        return;
+    }
+    long long it = 0;
+    int stop = CR_STOP_NONE;
+    for (; it < a.budget; ++it) {
+        const Cand* cur = a.cands + (it & 1) * gridDim.x;
+        Cand* nxt = a.cands + ((it + 1) & 1) * gridDim.x;
+        // every block reduces all candidates to the same global peak
+        {
+            float ba = -1.0f, bv = 0.0f;
+            int bk = 0x7fffffff;
+            for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+                // other blocks wrote these: read through L2, not a stale L1 line
+                int4 raw = __ldcg(reinterpret_cast<const int4*>(cur) + i);
+                Cand c{__int_as_float(raw.x), raw.y, __int_as_float(raw.z), 0};
+                if (better(c.absval, c.key, ba, bk)) {
+                    ba = c.absval;
+                    bk = c.key;
+                    bv = c.value;
+                }
+            }
+            Cand c = block_argmax(ba, bk, bv);
+            if (threadIdx.x == 0) {
+                s_best = c;
+                int r = 0;
+                if (c.absval < 0.0f)
+                    r = CR_STOP_NO_CLEANABLE_PIXELS;
+                else
+                    r = stop_reason(c.absval, a.threshold, a.cycle_threshold, a.nsigma_threshold);
+                s_stop = r;
+            }
+            __syncthreads();
+        }
+        if (s_stop) {
+            stop = s_stop;
+            break;
+        }
+        const Cand best = s_best;
+        const int px = best.key % a.nx, py = best.key / a.nx;
+        const float comp = __fmul_rn(a.gain, best.value);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            int64_t m = (int64_t)px * a.ny + py;
+            a.model[m] = __fadd_rn(a.model[m], comp);
+            if (a.comp_x) {
+                a.comp_x[it] = px;
+                a.comp_y[it] = py;
+                a.comp_peak[it] = best.value;
+                a.comp_flux[it] = comp;
+            }
+        }
+        // subtract the shifted PSF over the block's pixels and find the next
+        // candidate in the same pass
+        float ba = -1.0f, bv = 0.0f;
+        int bk = 0x7fffffff;
+        for (int64_t t = p0 + threadIdx.x; t < p1; t += blockDim.x) {
+            int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
+            int kx = x - px + kcx, ky = y - py + kcy;
+            float v = a.residual[t];
+            if (kx >= 0 && kx < a.nx && ky >= 0 && ky < a.ny) {
+                v = __fsub_rn(v, __fmul_rn(comp, a.psf[(int64_t)kx * a.ny + ky]));
+                a.residual[t] = v;
+            }
+            if (a.mask && !a.mask[t]) continue;
+            float av = fabsf(v);
+            int key = y * a.nx + x;
+            if (better(av, key, ba, bk)) {
+                ba = av;
+                bk = key;
+                bv = v;
+            }
+        }
+        Cand c = block_argmax(ba, bk, bv);
+        if (threadIdx.x == 0) nxt[blockIdx.x] = c;
+        if (!grid_barrier(a.bar, gridDim.x)) {
+            if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
+            return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.out_actual = it;
+        *a.out_stop = stop;
+    }
+}
+
+}  // namespace
+
+void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
+            int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
+            float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
+            int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
+            int64_t* reported, int32_t* stop_reason_out) {
+    if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
+    if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
+    if (cycle_niter < 0) fail(CR_INVALID, "cycle_niter is negative");
+    long long budget = inclusive ? cycle_niter + 1 : cycle_niter;
+    int sms = 0, per_sm = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hogbom_kernel,
+                                                                kHogThreads, 0));
+    if (per_sm < 1) fail(CR_CUDA, "Hogbom kernel cannot be resident");
+    int64_t npix = (int64_t)nx * ny;
+    int blocks = (int)std::min<int64_t>((int64_t)sms * std::min(per_sm, 2),
+                                        std::max<int64_t>(1, (npix + kHogThreads - 1) / kHogThreads));
+    size_t cap = (size_t)(budget > 0 ? budget : 1);
+    char* wsp = (char*)workspace(ctx, "hog_ws", 256 + (size_t)blocks * 2 * sizeof(Cand) + cap * 16);
+    unsigned int* bar = (unsigned int*)wsp;
+    long long* out_actual = (long long*)(wsp + 16);
+    int* out_stop = (int*)(wsp + 24);
+    int* out_status = (int*)(wsp + 28);
+    Cand* cands = (Cand*)(wsp + 256);
+    int* cx = (int*)(wsp + 256 + (size_t)blocks * 2 * sizeof(Cand));
+    int* cy = cx + cap;
+    float* cp = (float*)(cy + cap);
+    float* cf = cp + cap;
+    CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, 256, ctx->stream));
+    HogArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
+              nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual, out_stop,
+              out_status};
+    void* args[] = {&a};
+    CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_kernel, dim3(blocks), dim3(kHogThreads),
+                                              args, 0, ctx->stream));
+    note_launch(ctx, "hogbom_kernel");
+    struct {
+        long long actual;
+        int stop, status;
+    } h;
+    CR_CUDA_CHECK(cudaMemcpyAsync(&h, out_actual, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (h.status) fail(CR_TIMEOUT, "Hogbom grid barrier timed out");
+    if (comp_x && h.actual > 0) {
+        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+    }
+    if (actual) *actual = h.actual;
+    if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
+    if (stop_reason_out) *stop_reason_out = h.stop;
+}
+
+}  // namespace cr

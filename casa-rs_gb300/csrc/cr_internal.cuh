@@ -1,0 +1,202 @@
+// cr_internal.cuh -- shared internals of libcasars_cuda (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "casars_cuda.h"
+
+namespace cr {
+
+// Error carried from any internal function to the C-ABI boundary, where it
+// becomes a status code plus a heap message.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what);
+void check_cufft(cufftResult r, const char* what);
+
+#define CR_CUDA_CHECK(call) ::cr::check_cuda((call), #call)
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace cr
+
+// A context: one device, one stream, grow-only device workspaces, cached
+// cuFFT plans and a launch counter.
+struct cr_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::map<std::string, cr::DevBuf> ws;
+    std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
+    cudaEvent_t ev[8] = {};
+    cr_timings timings = {};
+    int64_t launches = 0;
+    // small pinned host buffer for device->host scalars
+    void* pinned = nullptr;
+};
+
+// Standard (PSWF) gridder state.
+struct cr_gridder {
+    cr_ctx* ctx = nullptr;
+    cr_geometry geom = {};
+    cr_grid_info info = {};
+    int32_t tap_rows = 0;
+    std::vector<float> taps_h, corr_x_h, corr_y_h;
+    float* taps_d = nullptr;     // [tap_rows][7]
+    float* corr_x_d = nullptr;   // [grid_nx]
+    float* corr_y_d = nullptr;   // [grid_ny]
+};
+
+// W-projection state: cropped kernels, normalisation table and the
+// per-offset kernel slabs the gridder and degridder read.
+struct cr_wproj {
+    cr_ctx* ctx = nullptr;
+    cr_gridder* g = nullptr;
+    cr_wproj_info info = {};
+    int32_t radius = 0;          // (sampling + 1) / 2: offsets lie in [-radius, radius]
+    int32_t axis = 0;            // 2 * radius + 1
+    std::vector<int32_t> support_h;
+    std::vector<int64_t> slab_off_h;  // [planes] start of each plane's slabs (float2 units)
+    int32_t* support_d = nullptr;
+    int64_t* slab_off_d = nullptr;
+    float2* kernels_d = nullptr;      // [planes][width][width]
+    float* norm_d = nullptr;          // [planes][axis][axis]
+    float2* slabs_d = nullptr;        // per plane [axis][axis][W_p][W_p], W_p = 2 S_p + 1
+    float* sinc_x_d = nullptr;        // sinc axis for the image correction (max(g) long)
+    float* sinc_gx_d = nullptr;       // sinc axes for the model apodisation
+    float* sinc_gy_d = nullptr;
+};
+
+namespace cr {
+
+// ---- context helpers -------------------------------------------------------
+void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes);
+void note_launch(cr_ctx* ctx, const char* what);
+cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
+
+// ---- host-side tables (restated from gridder.rs) ----------------------------
+int64_t casa_composite_padded_len(int64_t image_len, double padding);
+int64_t image_blc(int64_t grid_len, int64_t image_len);
+double grdsf(double nu);
+std::vector<float> std_normalized_taps(int32_t oversampling, int32_t support);
+std::vector<float> correction_axis(int64_t size);
+std::vector<float> gridder_correction_axis(int64_t size);
+std::vector<float> sinc_axis(int64_t size, int64_t conv_sampling);
+
+// ---- device primitives -------------------------------------------------------
+// Exclusive scan of n uint32 values into out (may alias in); *total_dev (if
+// non-null, device pointer) receives the sum as uint64.
+void exclusive_scan_u32(cr_ctx* ctx, const uint32_t* in, uint32_t* out, int64_t n,
+                        unsigned long long* total_dev);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` bits.
+// Sorted output ends in keys/vals.
+void radix_sort_pairs(cr_ctx* ctx, uint64_t* keys, uint32_t* vals, int64_t n, int bits);
+
+// ---- batch upload ------------------------------------------------------------
+struct DeviceBatch {
+    int64_t n = 0;
+    const double* u = nullptr;
+    const double* v = nullptr;
+    const double* w = nullptr;
+    const float* weight = nullptr;
+    const float* sumwt_factor = nullptr;
+    const uint8_t* gridable = nullptr;
+    const float2* vis = nullptr;
+};
+DeviceBatch device_batch(cr_ctx* ctx, const cr_vis_batch* b, bool need_w);
+
+// Host or device source -> device pointer (copies host data into a named
+// workspace).
+const void* device_input(cr_ctx* ctx, const void* p, size_t bytes, int32_t location,
+                         const char* name);
+void copy_out(cr_ctx* ctx, void* dst, const void* src_dev, size_t bytes, int32_t location);
+
+// ---- records: the deduplicated sample plan ------------------------------------
+// Samples with identical (cell, kernel offset, w-plane, conjugation) get
+// identical taps; they are summed into one record before gridding.
+struct Records {
+    int64_t n_samples = 0;
+    uint64_t* keys = nullptr;        // sorted keys [n]
+    uint32_t* order = nullptr;       // sorted sample indices [n]
+    int32_t* sample_rec = nullptr;   // [n] record of each sample, -1 when skipped
+    int32_t* rec_x = nullptr;        // anchor / start cell x   [n]
+    int32_t* rec_y = nullptr;        // [n]
+    int32_t* rec_a = nullptr;        // plane (wproj) or x tap row (standard)  [n]
+    int32_t* rec_b = nullptr;        // offset index (wproj) or y tap row      [n]
+    int32_t* rec_conj = nullptr;     // [n]
+    double2* rec_vsum = nullptr;     // sum vis * weight  [n]
+    double* rec_wsum = nullptr;      // sum weight        [n]
+    float2* rec_pred = nullptr;      // degridded value   [n]
+    uint32_t* tile_start = nullptr;  // [ntiles + 1] first record of each home tile
+    int64_t ntx = 0, nty = 0;        // home tiles (32 x 32 cells)
+    // device scalars: [0] gridded, [1] skipped, [2] unique records
+    unsigned long long* counts = nullptr;
+    double* sums = nullptr;          // [0] normalisation sumwt, [1] reported sumwt
+};
+
+constexpr int kTile = 32;            // home/output tile edge in grid cells
+
+Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b);
+Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b);
+void read_sums(cr_ctx* ctx, const Records& r, cr_sums* out);
+
+// ---- gridding kernels ----------------------------------------------------------
+// mode 0: PSF + dirty from the record sums; mode 1: residual
+// (vsum - pred * wsum) into `dirty` only.
+void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2* dirty,
+                int mode);
+void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* grid);
+void std_grid(cr_ctx* ctx, cr_gridder* g, const Records& r, float2* psf, float2* dirty,
+              int mode);
+void std_degrid(cr_ctx* ctx, cr_gridder* g, const Records& r, const float2* grid);
+void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
+
+// ---- FFT stage -------------------------------------------------------------------
+// grid (device, modified in place) -> image * scale (device)
+void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
+                   float* image);
+// the exact adjoint of image_to_grid's image-side factor (no sinc division)
+void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
+                           float* image);
+// model image (device) -> centred model grid (device)
+void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid);
+// max |image| into *peak_dev (float bits as uint32)
+void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev);
+// image *= scale, then / *peak_dev when peak_dev != null
+void scale_image(cr_ctx* ctx, float* image, int64_t n, float scale, const unsigned int* peak_dev);
+
+// ---- W-projection build ----------------------------------------------------------
+void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
+                 int32_t sampling, int32_t support_min, int32_t support_max);
+
+// ---- weighting / Hogbom ----------------------------------------------------------
+void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t mode,
+                     float robust, float* out_weight, float* f2_out);
+void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
+            int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
+            float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
+            int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
+            int64_t* reported, int32_t* stop_reason);
+
+inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned int)b;
+}
+
+}  // namespace cr

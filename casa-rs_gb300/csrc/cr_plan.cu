@@ -1,0 +1,469 @@
+// cr_plan.cu -- per-sample planning (FP64 index selection), key sort and
+// deduplication into records.
+//
+// The plan restates WProjector::plan_sample (gridder.rs:3588-3624) and
+// StandardGridder::plan_positive_taps / sample_tap_span (gridder.rs:540-566,
+// 1877-1886, 1958-1995) in FP64 with the reference's rounding (round half
+// away from zero), so the chosen cell, oversampling offset and w-plane are
+// bit-identical to the reference's.  Each valid sample gets a 64-bit key
+//   home tile | (plane | conj | offset)  or  (x tap row | y tap row) | cell
+// and the keys are radix-sorted.  Samples with equal keys have identical taps;
+// their weighted visibilities and weights are summed into one record, so
+// every distinct tap footprint is convolved once.  The sort is stable and the
+// record sums are accumulated in FP64.
+#include <cmath>
+
+#include "cr_internal.cuh"
+
+namespace cr {
+
+namespace {
+
+__host__ __device__ inline int bits_for(uint64_t max_value) {
+    int b = 0;
+    while ((max_value >> b) != 0) ++b;
+    return b;
+}
+
+struct WpPlanArgs {
+    int64_t n;
+    const double *u, *v, *w;
+    const float *weight, *sumwt;
+    const uint8_t* gridable;
+    const float2* vis;
+    int64_t gnx, gny;
+    double du, dv, w_scale;
+    int32_t sampling, planes, radius, axis;
+    const int32_t* support;
+    const float* norm;
+    int64_t nty;
+    int plane_bits, off_bits;
+    uint64_t* keys;
+    uint32_t* vals;
+    double* sums;
+    unsigned long long* counts;
+};
+
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u(unsigned long long x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Block-wide accumulation of the two FP64 sums and two counters.
+__device__ void block_accumulate(double s0, double s1, unsigned long long c0,
+                                 unsigned long long c1, double* sums,
+                                 unsigned long long* counts) {
+    __shared__ double sh_s[2][32];
+    __shared__ unsigned long long sh_c[2][32];
+    s0 = warp_sum_d(s0);
+    s1 = warp_sum_d(s1);
+    c0 = warp_sum_u(c0);
+    c1 = warp_sum_u(c1);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        sh_s[0][warp] = s0;
+        sh_s[1][warp] = s1;
+        sh_c[0][warp] = c0;
+        sh_c[1][warp] = c1;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        s0 = lane < nw ? sh_s[0][lane] : 0.0;
+        s1 = lane < nw ? sh_s[1][lane] : 0.0;
+        c0 = lane < nw ? sh_c[0][lane] : 0ull;
+        c1 = lane < nw ? sh_c[1][lane] : 0ull;
+        s0 = warp_sum_d(s0);
+        s1 = warp_sum_d(s1);
+        c0 = warp_sum_u(c0);
+        c1 = warp_sum_u(c1);
+        if (lane == 0) {
+            if (s0 != 0.0) atomicAdd(&sums[0], s0);
+            if (s1 != 0.0) atomicAdd(&sums[1], s1);
+            if (c0) atomicAdd(&counts[0], c0);
+            if (c1) atomicAdd(&counts[1], c1);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
+
+// WProjector::plan_sample (gridder.rs:3588-3624) + raw_w_project_sample_is_valid
+// (lib.rs:73666-73676) + w_project_accumulation_for_sample (lib.rs:71463-71470).
+__global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
+    double s_norm = 0.0, s_rep = 0.0;
+    unsigned long long c_ok = 0, c_skip = 0;
+    const uint64_t invalid = ~0ull;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t key = invalid;
+        float wt = a.weight[i];
+        float f = a.sumwt ? a.sumwt[i] : 1.0f;
+        float2 vis = a.vis[i];
+        double u = a.u[i], v = a.v[i], w = a.w[i];
+        bool ok = (!a.gridable || a.gridable[i]) && finite_f(wt) && wt > 0.0f && finite_f(f) &&
+                  f > 0.0f && finite_f(vis.x) && finite_f(vis.y) && isfinite(u) &&
+                  isfinite(v) && isfinite(w);
+        if (ok) {
+            double px = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+            double py = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+            ok = isfinite(px) && isfinite(py) && fabs(px) < 1.0e15 && fabs(py) < 1.0e15;
+            if (ok) {
+                int64_t lx = (int64_t)round(px), ly = (int64_t)round(py);
+                int64_t ox = (int64_t)round(__dmul_rn(__dsub_rn((double)lx, px), (double)a.sampling));
+                int64_t oy = (int64_t)round(__dmul_rn(__dsub_rn((double)ly, py), (double)a.sampling));
+                int32_t plane = 0;
+                if (a.planes > 1) {
+                    double c = sqrt(fmax(__dmul_rn(a.w_scale, fabs(w)), 0.0));
+                    double r = round(c);
+                    r = fmin(fmax(r, 0.0), (double)(a.planes - 1));
+                    plane = (int32_t)r;
+                }
+                int64_t s = a.support[plane];
+                ok = s > 0 && lx - s >= 0 && ly - s >= 0 && lx + s < a.gnx && ly + s < a.gny &&
+                     ox >= -a.radius && ox <= a.radius && oy >= -a.radius && oy <= a.radius;
+                if (ok) {
+                    int offidx = (int)(ox + a.radius) * a.axis + (int)(oy + a.radius);
+                    float nrm = a.norm[((int64_t)plane * a.axis) * a.axis + offidx];
+                    s_norm += 2.0 * (double)wt * (double)nrm;
+                    s_rep += (double)wt * (double)f;
+                    uint64_t tile = (uint64_t)(lx >> 5) * (uint64_t)a.nty + (uint64_t)(ly >> 5);
+                    uint64_t cell = (uint64_t)(((lx & 31) << 5) | (ly & 31));
+                    key = tile;
+                    key = (key << a.plane_bits) | (uint64_t)plane;
+                    key = (key << 1) | (uint64_t)(w > 0.0 ? 1 : 0);
+                    key = (key << a.off_bits) | (uint64_t)offidx;
+                    key = (key << 10) | cell;
+                }
+            }
+        }
+        if (ok)
+            c_ok++;
+        else
+            c_skip++;
+        a.keys[i] = key;
+        a.vals[i] = (uint32_t)i;
+    }
+    block_accumulate(s_norm, s_rep, c_ok, c_skip, a.sums, a.counts);
+}
+
+struct StdPlanArgs {
+    int64_t n;
+    const double *u, *v;
+    const float *weight, *sumwt;
+    const uint8_t* gridable;
+    int64_t gnx, gny;
+    double du, dv;
+    int32_t os, tap_rows;
+    int64_t nty;
+    uint64_t* keys;
+    uint32_t* vals;
+    double* sums;
+    unsigned long long* counts;
+};
+
+// sample_tap_span (gridder.rs:1976-1995): start cell and tap row.
+__device__ __forceinline__ bool tap_span(double coord, int64_t size, int32_t os, int32_t rows,
+                                         int64_t* start, int32_t* row) {
+    if (!isfinite(coord) || !(fabs(coord) < 1.0e15)) return false;
+    int64_t anchor = (int64_t)round(coord);
+    int64_t off = (int64_t)round(__dmul_rn(__dsub_rn((double)anchor, coord), (double)os));
+    int64_t s = anchor - 3, e = anchor + 3;
+    if (s < 0 || e >= size) return false;
+    int64_t idx = off + os / 2;
+    if (idx < 0 || idx >= rows) return false;
+    *start = s;
+    *row = (int32_t)idx;
+    return true;
+}
+
+// accumulate_dirty_psf_and_residual_standard_streaming_grid_serial
+// (lib.rs:68433-68500): validity, taps, sum of weights grid_weight = w*f.
+__global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
+    double s_norm = 0.0;
+    unsigned long long c_ok = 0, c_skip = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t key = ~0ull;
+        float wt = a.weight[i];
+        float f = a.sumwt ? a.sumwt[i] : 1.0f;
+        bool ok = (!a.gridable || a.gridable[i]) && finite_f(wt) && wt > 0.0f && finite_f(f) &&
+                  f > 0.0f;
+        if (ok) {
+            double x = __dadd_rn(__ddiv_rn(a.u[i], a.du), (double)a.gnx / 2.0);
+            double y = __dadd_rn(__ddiv_rn(-a.v[i], a.dv), (double)a.gny / 2.0);
+            int64_t x0 = 0, y0 = 0;
+            int32_t rx = 0, ry = 0;
+            ok = tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) &&
+                 tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry);
+            if (ok) {
+                s_norm += (double)(wt * f);
+                uint64_t tile = (uint64_t)(x0 >> 5) * (uint64_t)a.nty + (uint64_t)(y0 >> 5);
+                uint64_t cell = (uint64_t)(((x0 & 31) << 5) | (y0 & 31));
+                key = (((tile << 8 | (uint64_t)rx) << 8 | (uint64_t)ry) << 10) | cell;
+            }
+        }
+        if (ok)
+            c_ok++;
+        else
+            c_skip++;
+        a.keys[i] = key;
+        a.vals[i] = (uint32_t)i;
+    }
+    block_accumulate(s_norm, s_norm, c_ok, c_skip, a.sums, a.counts);
+}
+
+__global__ void head_flags(const uint64_t* keys, const unsigned long long* counts, int64_t n,
+                           uint32_t* flags) {
+    int64_t nv = (int64_t)counts[0];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        flags[i] = (i < nv && (i == 0 || keys[i] != keys[i - 1])) ? 1u : 0u;
+}
+
+struct RecArgs {
+    const uint64_t* keys;
+    const uint32_t* vals;
+    const uint32_t* flags;
+    const uint32_t* excl;
+    const unsigned long long* counts;
+    int64_t n;
+    int mode;  // 0 wproj, 1 standard
+    int plane_bits, off_bits;
+    int64_t nty;
+    int32_t *rx, *ry, *ra, *rb, *rconj;
+    double2* vsum;
+    double* wsum;
+    int32_t* sample_rec;
+    const float* weight;
+    const float* sumwt;
+    const float2* vis;
+    uint32_t* tile_of;
+};
+
+// Record fields decoded from the head key of each run.
+__global__ void records_init(RecArgs a) {
+    int64_t nv = (int64_t)a.counts[0];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (!a.flags[i]) continue;
+        uint32_t r = a.excl[i];
+        uint64_t k = a.keys[i];
+        int cx = (int)((k >> 5) & 31), cy = (int)(k & 31);
+        k >>= 10;
+        uint64_t tile;
+        if (a.mode == 0) {
+            a.rb[r] = (int32_t)(k & ((1ull << a.off_bits) - 1));
+            k >>= a.off_bits;
+            a.rconj[r] = (int32_t)(k & 1);
+            k >>= 1;
+            a.ra[r] = (int32_t)(k & ((1ull << a.plane_bits) - 1));
+            k >>= a.plane_bits;
+            tile = k;
+        } else {
+            a.rb[r] = (int32_t)(k & 255);
+            a.ra[r] = (int32_t)((k >> 8) & 255);
+            a.rconj[r] = 0;
+            tile = k >> 16;
+        }
+        a.tile_of[r] = (uint32_t)tile;
+        a.rx[r] = (int32_t)((tile / (uint64_t)a.nty) * 32 + cx);
+        a.ry[r] = (int32_t)((tile % (uint64_t)a.nty) * 32 + cy);
+        a.vsum[r] = make_double2(0.0, 0.0);
+        a.wsum[r] = 0.0;
+    }
+}
+
+// Sums of weight * vis per record: a warp-level segmented reduction over the
+// sorted run, then one FP64 atomic per segment piece.
+__global__ void records_accumulate(RecArgs a) {
+    int64_t nv = (int64_t)a.counts[0];
+    const int lane = threadIdx.x & 31;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t limit = ((nv + 31) / 32) * 32;
+    for (int64_t i = start; i < limit; i += stride) {
+        bool valid = i < nv;
+        int32_t r = -1;
+        double vr = 0.0, vi = 0.0, ww = 0.0;
+        if (valid) {
+            r = (int32_t)(a.flags[i] ? a.excl[i] : a.excl[i] - 1);
+            uint32_t s = a.vals[i];
+            a.sample_rec[s] = r;
+            float wt = a.weight[s];
+            float f = a.sumwt ? a.sumwt[s] : 1.0f;
+            float gw = a.mode == 0 ? wt : wt * f;
+            float2 v = a.vis[s];
+            ww = (double)gw;
+            if (isfinite(v.x) && isfinite(v.y)) {
+                vr = (double)v.x * ww;
+                vi = (double)v.y * ww;
+            }
+        }
+        // segmented inclusive scan by record id
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double tr = __shfl_up_sync(0xffffffffu, vr, o);
+            double ti = __shfl_up_sync(0xffffffffu, vi, o);
+            double tw = __shfl_up_sync(0xffffffffu, ww, o);
+            int32_t rr = __shfl_up_sync(0xffffffffu, r, o);
+            if (lane >= o && rr == r) {
+                vr += tr;
+                vi += ti;
+                ww += tw;
+            }
+        }
+        int32_t next = __shfl_down_sync(0xffffffffu, r, 1);
+        bool last = (lane == 31) || (next != r);
+        if (valid && last) {
+            atomicAdd(&a.vsum[r].x, vr);
+            atomicAdd(&a.vsum[r].y, vi);
+            atomicAdd(&a.wsum[r], ww);
+        }
+    }
+}
+
+__global__ void fill_u32(uint32_t* p, int64_t n, const unsigned long long* value) {
+    uint32_t v = (uint32_t)*value;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// tile_start[t] = first record whose home tile is >= t.
+__global__ void tile_starts(const uint32_t* tile_of, const unsigned long long* counts,
+                            uint32_t* start) {
+    int64_t nr = (int64_t)counts[2];
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nr;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t prev = r == 0 ? -1 : (int64_t)tile_of[r - 1];
+        int64_t cur = tile_of[r];
+        for (int64_t t = prev + 1; t <= cur; ++t) start[t] = (uint32_t)r;
+    }
+}
+
+Records allocate_records(cr_ctx* ctx, int64_t n, int64_t ntx, int64_t nty) {
+    Records r;
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    r.n_samples = n;
+    r.ntx = ntx;
+    r.nty = nty;
+    r.keys = (uint64_t*)workspace(ctx, "rec_keys", nn * 8);
+    r.order = (uint32_t*)workspace(ctx, "rec_order", nn * 4);
+    r.sample_rec = (int32_t*)workspace(ctx, "rec_sample", nn * 4);
+    r.rec_x = (int32_t*)workspace(ctx, "rec_x", nn * 4);
+    r.rec_y = (int32_t*)workspace(ctx, "rec_y", nn * 4);
+    r.rec_a = (int32_t*)workspace(ctx, "rec_a", nn * 4);
+    r.rec_b = (int32_t*)workspace(ctx, "rec_b", nn * 4);
+    r.rec_conj = (int32_t*)workspace(ctx, "rec_conj", nn * 4);
+    r.rec_vsum = (double2*)workspace(ctx, "rec_vsum", nn * 16);
+    r.rec_wsum = (double*)workspace(ctx, "rec_wsum", nn * 8);
+    r.rec_pred = (float2*)workspace(ctx, "rec_pred", nn * 8);
+    r.tile_start = (uint32_t*)workspace(ctx, "rec_tile_start", (size_t)(ntx * nty + 1) * 4);
+    r.counts = (unsigned long long*)workspace(ctx, "rec_counts", 4 * 8);
+    r.sums = (double*)workspace(ctx, "rec_sums", 2 * 8);
+    CR_CUDA_CHECK(cudaMemsetAsync(r.counts, 0, 4 * 8, ctx->stream));
+    CR_CUDA_CHECK(cudaMemsetAsync(r.sums, 0, 2 * 8, ctx->stream));
+    CR_CUDA_CHECK(cudaMemsetAsync(r.sample_rec, 0xFF, nn * 4, ctx->stream));
+    return r;
+}
+
+void finish_records(cr_ctx* ctx, Records& r, int mode, int key_bits, int plane_bits,
+                    int off_bits, const DeviceBatch& b) {
+    const int64_t n = r.n_samples;
+    const unsigned T = 256;
+    radix_sort_pairs(ctx, r.keys, r.order, n, key_bits);
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    uint32_t* flags = (uint32_t*)workspace(ctx, "rec_flags", nn * 4);
+    uint32_t* excl = (uint32_t*)workspace(ctx, "rec_excl", nn * 4);
+    uint32_t* tile_of = (uint32_t*)workspace(ctx, "rec_tile_of", nn * 4);
+    if (n > 0) {
+        head_flags<<<grid_blocks(n, T), T, 0, ctx->stream>>>(r.keys, r.counts, n, flags);
+        note_launch(ctx, "head_flags");
+    }
+    exclusive_scan_u32(ctx, flags, excl, n, r.counts + 2);
+    RecArgs a{r.keys, r.order, flags, excl, r.counts, n, mode, plane_bits, off_bits, r.nty,
+              r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum,
+              r.sample_rec, b.weight, b.sumwt_factor, b.vis, tile_of};
+    if (n > 0) {
+        records_init<<<grid_blocks(n, T), T, 0, ctx->stream>>>(a);
+        note_launch(ctx, "records_init");
+        records_accumulate<<<grid_blocks(n, T), T, 0, ctx->stream>>>(a);
+        note_launch(ctx, "records_accumulate");
+    }
+    int64_t ntiles = r.ntx * r.nty;
+    fill_u32<<<grid_blocks(ntiles + 1, T), T, 0, ctx->stream>>>(r.tile_start, ntiles + 1,
+                                                                 r.counts + 2);
+    note_launch(ctx, "fill_u32");
+    if (n > 0) {
+        tile_starts<<<grid_blocks(n, T), T, 0, ctx->stream>>>(tile_of, r.counts, r.tile_start);
+        note_launch(ctx, "tile_starts");
+    }
+}
+
+}  // namespace
+
+Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b) {
+    const cr_grid_info& gi = wp->g->info;
+    int64_t ntx = (gi.grid_nx + kTile - 1) / kTile, nty = (gi.grid_ny + kTile - 1) / kTile;
+    Records r = allocate_records(ctx, b.n, ntx, nty);
+    int tile_bits = bits_for((uint64_t)(ntx * nty));
+    int plane_bits = bits_for((uint64_t)(wp->info.planes > 1 ? wp->info.planes - 1 : 1));
+    int off_bits = bits_for((uint64_t)(wp->axis * wp->axis - 1));
+    int key_bits = tile_bits + plane_bits + 1 + off_bits + 10;
+    if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");
+    if (b.n > 0) {
+        WpPlanArgs a{b.n, b.u, b.v, b.w, b.weight, b.sumwt_factor, b.gridable, b.vis,
+                     gi.grid_nx, gi.grid_ny, gi.du, gi.dv, wp->info.w_scale,
+                     wp->info.sampling, wp->info.planes, wp->radius, wp->axis,
+                     wp->support_d, wp->norm_d, nty, plane_bits, off_bits, r.keys, r.order,
+                     r.sums, r.counts};
+        wp_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
+        note_launch(ctx, "wp_plan_kernel");
+    }
+    finish_records(ctx, r, 0, key_bits, plane_bits, off_bits, b);
+    return r;
+}
+
+Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b) {
+    const cr_grid_info& gi = g->info;
+    int64_t ntx = (gi.grid_nx + kTile - 1) / kTile, nty = (gi.grid_ny + kTile - 1) / kTile;
+    Records r = allocate_records(ctx, b.n, ntx, nty);
+    int tile_bits = bits_for((uint64_t)(ntx * nty));
+    int key_bits = tile_bits + 16 + 10;
+    if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");
+    if (b.n > 0) {
+        StdPlanArgs a{b.n, b.u, b.v, b.weight, b.sumwt_factor, b.gridable, gi.grid_nx,
+                      gi.grid_ny, gi.du, gi.dv, gi.oversampling, g->tap_rows, nty, r.keys,
+                      r.order, r.sums, r.counts};
+        std_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
+        note_launch(ctx, "std_plan_kernel");
+    }
+    finish_records(ctx, r, 1, key_bits, 0, 0, b);
+    return r;
+}
+
+void read_sums(cr_ctx* ctx, const Records& r, cr_sums* out) {
+    if (!out) return;
+    struct {
+        unsigned long long c[4];
+        double s[2];
+    }* host = (decltype(host))ctx->pinned;
+    CR_CUDA_CHECK(cudaMemcpyAsync(host->c, r.counts, 32, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaMemcpyAsync(host->s, r.sums, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    out->gridded = (int64_t)host->c[0];
+    out->skipped = (int64_t)host->c[1];
+    out->unique_records = (int64_t)host->c[2];
+    out->normalization_sumwt = host->s[0];
+    out->reported_sumwt = host->s[1];
+}
+
+}  // namespace cr

@@ -1,0 +1,702 @@
+// cr_wproj.cu -- W-projection kernels: construction, gridding, degridding.
+//
+// Construction restates WProjector::new (gridder.rs:3403-3586): per w-plane a
+// phase screen corr(l)corr(m) exp(2 pi i w_k (sqrt(1-l^2-m^2) - 1)) with the
+// phase in FP64, a forward 2-D FFT (cuFFT, the bare transform), a crop to
+// the plane's support, division by the plane-zero integral, and the
+// per-(plane, offset) normalisation table.  The cropped kernels are then
+// re-laid out as one dense "slab" per (plane, x offset, y offset): slab
+// element (i, j) holds K[|(i - S) s + off_x|, |(j - S) s + off_y|], so the
+// taps of a sample are a contiguous (2S+1)^2 block and a warp reads 32
+// consecutive taps of a row.
+//
+// Gridding is output-stationary: a block owns a 32 x 32 tile of the grid in
+// registers (each of 8 warps owns 4 rows, each lane one column), streams the
+// deduplicated records whose windows can reach the tile, and adds
+// value * kernel for every owned cell inside a record's window.  The tile is
+// flushed once per work item with FP32 atomics.  Degridding is a gather: a
+// warp per record reads the window of the model grid and the slab.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "cr_internal.cuh"
+
+namespace cr {
+
+namespace {
+
+constexpr int kGridThreads = 256;
+constexpr int kRowsPerWarp = kTile / (kGridThreads / 32);  // 4
+constexpr int kMaxSegRadius = 4;
+constexpr int kMaxSeg = (2 * kMaxSegRadius + 1) * (2 * kMaxSegRadius + 1);
+constexpr int kChunk = 1024;  // candidate records per work item
+
+// ---- construction ----------------------------------------------------------------
+__global__ void screen_kernel(float2* buf, int64_t conv, int64_t inner, int planes_in_batch,
+                              int plane0, int32_t nplanes, double w_scale, double s0, double s1,
+                              const float* corr) {
+    const int64_t half = inner / 2;
+    const int64_t total = inner * inner * planes_in_batch;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int b = (int)(t / (inner * inner));
+        int64_t rem = t - (int64_t)b * inner * inner;
+        int64_t ixi = rem / inner, iyi = rem - ixi * inner;
+        int64_t ix = ixi - half, iy = iyi - half;
+        int plane = plane0 + b;
+        double w = nplanes > 1 ? (double)((int64_t)plane * plane) / w_scale : 0.0;
+        double l = s0 * (double)ix, m = s1 * (double)iy;
+        double rsq = __dadd_rn(__dmul_rn(l, l), __dmul_rn(m, m));
+        if (rsq >= 1.0) continue;
+        double phase = __dmul_rn(__dmul_rn(6.283185307179586476925, w), sqrt(1.0 - rsq) - 1.0);
+        double sn, cs;
+        sincos(phase, &sn, &cs);
+        float c = __fmul_rn(corr[ixi], corr[iyi]);
+        int64_t x = ix >= 0 ? ix : ix + conv;
+        int64_t y = iy >= 0 ? iy : iy + conv;
+        buf[(int64_t)b * conv * conv + x * conv + y] =
+            make_float2(__fmul_rn(c, (float)cs), __fmul_rn(c, (float)sn));
+    }
+}
+
+__global__ void crop_kernel(const float2* buf, int64_t conv, int planes_in_batch, int plane0,
+                            const int32_t* crop, int32_t width, float2* kernels) {
+    const int64_t total = (int64_t)planes_in_batch * width * width;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int b = (int)(t / ((int64_t)width * width));
+        int64_t rem = t - (int64_t)b * width * width;
+        int x = (int)(rem / width), y = (int)(rem - (int64_t)x * width);
+        int plane = plane0 + b;
+        int cw = crop[plane];
+        float2 v = make_float2(0.0f, 0.0f);
+        if (x < cw && y < cw) v = buf[(int64_t)b * conv * conv + (int64_t)x * conv + y];
+        kernels[(int64_t)plane * width * width + (int64_t)x * width + y] = v;
+    }
+}
+
+__global__ void axis_kernel(const float2* buf, int64_t conv, int planes_in_batch,
+                            int64_t axis_len, double* axes) {
+    const int64_t total = (int64_t)planes_in_batch * axis_len;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int b = (int)(t / axis_len);
+        int64_t c = t - (int64_t)b * axis_len;
+        const float2* p = buf + (int64_t)b * conv * conv;
+        float2 ax = p[c * conv];  // T(c, 0)
+        float2 ay = p[c];         // T(0, c)
+        axes[((int64_t)b * 2) * axis_len + c] = hypot((double)ax.x, (double)ax.y);
+        axes[((int64_t)b * 2 + 1) * axis_len + c] = hypot((double)ay.x, (double)ay.y);
+    }
+}
+
+// FP64 sum of Re K over the integer taps of one plane (w_project_plane_sum,
+// gridder.rs:3991-4002), or over one offset (compute_w_project_sample_
+// normalization, gridder.rs:3782-3799).  One block per (plane, offset).
+__global__ void tap_sum_kernel(const float2* kernels, int32_t width, const int32_t* support,
+                               int32_t sampling, int32_t radius, int32_t axis, int plane0,
+                               double* out_double, float* out_float) {
+    int plane = plane0 + blockIdx.y;
+    int offidx = blockIdx.x;
+    int ox = offidx / axis - radius, oy = offidx % axis - radius;
+    int s = support[plane];
+    int w = 2 * s + 1;
+    const float2* k = kernels + (int64_t)plane * width * width;
+    double acc = 0.0;
+    bool ok = true;
+    for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+        int ix = t / w - s, iy = t % w - s;
+        int kx = abs(ix * sampling + ox), ky = abs(iy * sampling + oy);
+        if (kx >= width || ky >= width) {
+            ok = false;
+            continue;
+        }
+        acc += (double)k[(int64_t)kx * width + ky].x;
+    }
+    __shared__ double sh[32];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    if (!ok) bad = 1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+        if (bad) t = 0.0;
+        int64_t idx = ((int64_t)plane * axis) * axis + offidx;
+        if (out_double) out_double[idx] = t;
+        if (out_float) out_float[idx] = (float)t;
+    }
+}
+
+__global__ void scale_kernels(float2* k, int64_t n, float scale) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        float2 v = k[t];
+        k[t] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+__global__ void slab_kernel(const float2* kernels, int32_t width, int plane, int32_t s,
+                            int32_t sampling, int32_t radius, int32_t axis, float2* slab) {
+    const int w = 2 * s + 1;
+    const int64_t total = (int64_t)axis * axis * w * w;
+    const float2* k = kernels + (int64_t)plane * width * width;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t offidx = t / ((int64_t)w * w);
+        int64_t rem = t - offidx * w * w;
+        int i = (int)(rem / w), j = (int)(rem - (int64_t)i * w);
+        int ox = (int)(offidx / axis) - radius, oy = (int)(offidx % axis) - radius;
+        int kx = abs((i - s) * sampling + ox), ky = abs((j - s) * sampling + oy);
+        slab[t] = (kx < width && ky < width) ? k[(int64_t)kx * width + ky] : make_float2(0.f, 0.f);
+    }
+}
+
+// ---- gridding ----------------------------------------------------------------------
+struct GridArgs {
+    const int32_t *rx, *ry, *rplane, *roff, *rconj;
+    const double2* vsum;
+    const double* wsum;
+    const float2* pred;
+    const uint32_t* tile_start;
+    int64_t ntx, nty;
+    const int32_t* support;
+    const int64_t* slab_off;
+    const float2* slabs;
+    int32_t axis;
+    int32_t seg_radius;
+    const uint32_t* item_tile;
+    const uint32_t* item_begin;
+    const unsigned long long* n_items;
+    unsigned int* item_counter;
+    float2* psf;
+    float2* dirty;
+    int64_t gnx, gny;
+};
+
+struct Entry {
+    int64_t slab;    // element offset of this record's slab
+    int32_t ra, cb;  // slab row of tile row 0, slab column of tile column 0
+    int32_t w;       // slab width 2S+1
+    float vr, vi, tvi, tvr, pw, tpw;
+};
+
+template <bool RESIDUAL>
+__global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
+    __shared__ int s_item;
+    __shared__ uint32_t s_seg_start[kMaxSeg];
+    __shared__ uint32_t s_seg_pref[kMaxSeg + 1];
+    __shared__ int s_nseg;
+    __shared__ Entry s_list[kGridThreads];
+    __shared__ int s_nlist;
+    __shared__ int s_warp_cnt[kGridThreads / 32];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long n_items = *a.n_items;
+    const int R = a.seg_radius;
+    const int side = 2 * R + 1;
+
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if ((unsigned long long)item >= n_items) break;
+        const uint32_t T = a.item_tile[item];
+        const uint32_t begin = a.item_begin[item];
+        const int64_t tx = T / a.nty, ty = T % a.nty;
+        const int x0 = (int)(tx * kTile), y0 = (int)(ty * kTile);
+        if (tid == 0) {
+            int ns = 0;
+            uint32_t run = 0;
+            for (int dx = -R; dx <= R; ++dx) {
+                int64_t hx = tx + dx;
+                if (hx < 0 || hx >= a.ntx) continue;
+                int64_t h0 = hx * a.nty + (ty - R < 0 ? 0 : ty - R);
+                int64_t h1 = hx * a.nty + (ty + R >= a.nty ? a.nty - 1 : ty + R);
+                // the home tiles of one column dx are consecutive: one segment
+                uint32_t st = a.tile_start[h0], en = a.tile_start[h1 + 1];
+                s_seg_start[ns] = st;
+                s_seg_pref[ns] = run;
+                run += en - st;
+                ns++;
+            }
+            s_seg_pref[ns] = run;
+            s_nseg = ns;
+        }
+        __syncthreads();
+        const int nseg = s_nseg;
+        const uint32_t total = s_seg_pref[nseg];
+        const uint32_t end = min(total, begin + (uint32_t)kChunk);
+
+        float pr[kRowsPerWarp], pi[kRowsPerWarp], dr[kRowsPerWarp], di[kRowsPerWarp];
+#pragma unroll
+        for (int k = 0; k < kRowsPerWarp; ++k) pr[k] = pi[k] = dr[k] = di[k] = 0.0f;
+
+        for (uint32_t base = begin; base < end; base += kGridThreads) {
+            // 1. candidates -> overlapping entries
+            uint32_t vidx = base + tid;
+            bool take = false;
+            Entry e;
+            if (vidx < end) {
+                int k = 0;
+                while (k + 1 < nseg && s_seg_pref[k + 1] <= vidx) ++k;
+                uint32_t r = s_seg_start[k] + (vidx - s_seg_pref[k]);
+                int lx = a.rx[r], ly = a.ry[r];
+                int plane = a.rplane[r];
+                int s = a.support[plane];
+                if (lx - s <= x0 + kTile - 1 && lx + s >= x0 && ly - s <= y0 + kTile - 1 &&
+                    ly + s >= y0) {
+                    take = true;
+                    int w = 2 * s + 1;
+                    e.w = w;
+                    e.slab = a.slab_off[plane] + (int64_t)a.roff[r] * w * w;
+                    e.ra = x0 - lx + s;
+                    e.cb = y0 - ly + s;
+                    double2 vs = a.vsum[r];
+                    double ws = a.wsum[r];
+                    float vr, vi;
+                    if (RESIDUAL) {
+                        float2 p = a.pred[r];
+                        vr = (float)(vs.x - (double)p.x * ws);
+                        vi = (float)(vs.y - (double)p.y * ws);
+                    } else {
+                        vr = (float)vs.x;
+                        vi = (float)vs.y;
+                    }
+                    float t = a.rconj[r] ? -1.0f : 1.0f;
+                    e.vr = vr;
+                    e.vi = vi;
+                    e.tvi = t * vi;
+                    e.tvr = t * vr;
+                    e.pw = (float)ws;
+                    e.tpw = t * (float)ws;
+                }
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, take);
+            if (lane == 0) s_warp_cnt[warp] = __popc(bal);
+            __syncthreads();
+            if (take) {
+                int off = 0;
+                for (int w2 = 0; w2 < warp; ++w2) off += s_warp_cnt[w2];
+                off += __popc(bal & ((1u << lane) - 1u));
+                s_list[off] = e;
+            }
+            if (tid == 0) {
+                int t = 0;
+                for (int w2 = 0; w2 < kGridThreads / 32; ++w2) t += s_warp_cnt[w2];
+                s_nlist = t;
+            }
+            __syncthreads();
+            // 2. accumulate the entries into the register tile
+            const int nlist = s_nlist;
+            for (int q = 0; q < nlist; ++q) {
+                const Entry& en = s_list[q];
+                const int w = en.w;
+                const int col = en.cb + lane;
+                const bool colok = (unsigned)col < (unsigned)w;
+                const float2* slab = a.slabs + en.slab;
+#pragma unroll
+                for (int k = 0; k < kRowsPerWarp; ++k) {
+                    const int row = en.ra + warp + k * (kGridThreads / 32);
+                    if ((unsigned)row < (unsigned)w && colok) {
+                        const float2 kv = __ldg(&slab[(int64_t)row * w + col]);
+                        if (!RESIDUAL) {
+                            pr[k] = fmaf(en.pw, kv.x, pr[k]);
+                            pi[k] = fmaf(en.tpw, kv.y, pi[k]);
+                        }
+                        dr[k] = fmaf(-en.tvi, kv.y, fmaf(en.vr, kv.x, dr[k]));
+                        di[k] = fmaf(en.vi, kv.x, fmaf(en.tvr, kv.y, di[k]));
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // 3. flush the tile
+#pragma unroll
+        for (int k = 0; k < kRowsPerWarp; ++k) {
+            int64_t x = x0 + warp + k * (kGridThreads / 32);
+            int64_t y = y0 + lane;
+            if (x < a.gnx && y < a.gny) {
+                int64_t cell = x * a.gny + y;
+                if (!RESIDUAL && (pr[k] != 0.0f || pi[k] != 0.0f))
+                    atomicAdd(&a.psf[cell], make_float2(pr[k], pi[k]));
+                if (dr[k] != 0.0f || di[k] != 0.0f)
+                    atomicAdd(&a.dirty[cell], make_float2(dr[k], di[k]));
+            }
+        }
+    }
+}
+
+// Work items: per output tile, the candidate records of its neighbourhood,
+// cut into chunks of kChunk.
+__global__ void tile_work_count(const uint32_t* tile_start, int64_t ntx, int64_t nty, int R,
+                                uint32_t* nchunks) {
+    int64_t ntiles = ntx * nty;
+    for (int64_t T = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; T < ntiles;
+         T += (int64_t)gridDim.x * blockDim.x) {
+        int64_t tx = T / nty, ty = T % nty;
+        uint64_t total = 0;
+        for (int dx = -R; dx <= R; ++dx) {
+            int64_t hx = tx + dx;
+            if (hx < 0 || hx >= ntx) continue;
+            int64_t h0 = hx * nty + (ty - R < 0 ? 0 : ty - R);
+            int64_t h1 = hx * nty + (ty + R >= nty ? nty - 1 : ty + R);
+            total += tile_start[h1 + 1] - tile_start[h0];
+        }
+        nchunks[T] = (uint32_t)((total + kChunk - 1) / kChunk);
+    }
+}
+
+__global__ void tile_work_fill(const uint32_t* nchunks, const uint32_t* first, int64_t ntiles,
+                               uint32_t* item_tile, uint32_t* item_begin) {
+    for (int64_t T = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; T < ntiles;
+         T += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t c = nchunks[T], f = first[T];
+        for (uint32_t k = 0; k < c; ++k) {
+            item_tile[f + k] = (uint32_t)T;
+            item_begin[f + k] = k * kChunk;
+        }
+    }
+}
+
+// ---- degridding --------------------------------------------------------------------
+struct DegridArgs {
+    const int32_t *rx, *ry, *rplane, *roff, *rconj;
+    const unsigned long long* counts;
+    const int32_t* support;
+    const int64_t* slab_off;
+    const float2* slabs;
+    const float2* grid;
+    int64_t gny;
+    float2* pred;
+};
+
+__global__ void __launch_bounds__(256) wp_degrid_kernel(DegridArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nrec = (int64_t)a.counts[2];
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrec;
+         r += nwarps) {
+        const int plane = a.rplane[r];
+        const int s = a.support[plane];
+        const int w = 2 * s + 1;
+        const float2* slab = a.slabs + a.slab_off[plane] + (int64_t)a.roff[r] * w * w;
+        const float2* g = a.grid + (int64_t)(a.rx[r] - s) * a.gny + (a.ry[r] - s);
+        float A = 0.f, B = 0.f, C = 0.f, D = 0.f;
+        for (int i = 0; i < w; ++i) {
+            const float2* grow = g + (int64_t)i * a.gny;
+            const float2* krow = slab + (int64_t)i * w;
+            for (int j = lane; j < w; j += 32) {
+                float2 gv = grow[j];
+                float2 kv = __ldg(&krow[j]);
+                A = fmaf(kv.x, gv.x, A);
+                B = fmaf(kv.y, gv.y, B);
+                C = fmaf(kv.x, gv.y, C);
+                D = fmaf(kv.y, gv.x, D);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            A += __shfl_xor_sync(0xffffffffu, A, o);
+            B += __shfl_xor_sync(0xffffffffu, B, o);
+            C += __shfl_xor_sync(0xffffffffu, C, o);
+            D += __shfl_xor_sync(0xffffffffu, D, o);
+        }
+        if (lane == 0)
+            a.pred[r] = a.rconj[r] ? make_float2(A - B, C + D) : make_float2(A + B, C - D);
+    }
+}
+
+__global__ void broadcast_kernel(const int32_t* sample_rec, const float2* rec_pred, int64_t n,
+                                 float2* pred) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t r = sample_rec[i];
+        pred[i] = r >= 0 ? rec_pred[r] : make_float2(0.0f, 0.0f);
+    }
+}
+
+int sm_count(cr_ctx* ctx) {
+    int v = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device));
+    return v;
+}
+
+}  // namespace
+
+// ---- construction driver ------------------------------------------------------------
+void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
+                 int32_t sampling, int32_t support_min, int32_t support_max) {
+    cr_gridder* g = wp->g;
+    const cr_geometry& geom = g->geom;
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    bool explicit_planes = planes > 0;
+    if (!explicit_planes) {
+        // choose_w_project_plane_count (gridder.rs:3801-3830)
+        int64_t p = 1;
+        if (std::isfinite(max_abs_w) && max_abs_w > 0.0) {
+            double half = std::max((double)geom.nx * std::fabs(geom.cell_x_rad),
+                                   (double)geom.ny * std::fabs(geom.cell_y_rad)) / 2.0;
+            p = (int64_t)(1.05 * max_abs_w * std::fabs(std::sin(half)));
+        }
+        planes = (int32_t)std::max<int64_t>(p, 1);
+    }
+    if (planes > 4096) fail(CR_INVALID, "more than 4096 w-planes");
+    if (sampling <= 0) sampling = planes > 1 ? 4 : 1;
+    const int64_t conv = std::max(gnx, gny);
+    const int64_t inner = std::max<int64_t>(conv / sampling, 2);
+    const int64_t quarter = conv / 2 - 1;
+    const int32_t radius = (sampling + 1) / 2;
+    const int32_t axis = 2 * radius + 1;
+    double s0 = std::fabs(geom.cell_x_rad) * sampling * (double)gnx / (double)conv;
+    double s1 = std::fabs(geom.cell_y_rad) * sampling * (double)gny / (double)conv;
+    double eff = explicit_planes ? 0.25 / std::fabs(geom.cell_x_rad) : 1.05 * max_abs_w;
+    double w_scale = (planes > 1 && std::isfinite(eff) && eff > 0.0)
+                         ? (double)((int64_t)(planes - 1) * (planes - 1)) / eff
+                         : 1.0;
+    const bool law = support_min > 0;
+    std::vector<int32_t> support(planes, 0), crop(planes, 0);
+    if (law) {
+        if (support_max < support_min) fail(CR_INVALID, "support_max < support_min");
+        for (int32_t p = 0; p < planes; ++p) {
+            double frac = planes > 1 ? (double)p / (double)(planes - 1) : 0.0;
+            support[p] = support_min + (int32_t)std::llround((double)(support_max - support_min) * frac);
+            int64_t cw = (int64_t)support[p] * sampling + radius + 1;
+            if (cw > quarter) fail(CR_INVALID, "W-projection support too large for the grid");
+            crop[p] = (int32_t)cw;
+        }
+    } else {
+        int64_t ms = std::max<int64_t>(quarter / sampling - 1, 1);
+        int64_t cw = std::min<int64_t>(ms * sampling + radius + 1, quarter);
+        for (int32_t p = 0; p < planes; ++p) crop[p] = (int32_t)std::max<int64_t>(cw, 1);
+    }
+    int32_t stride = *std::max_element(crop.begin(), crop.end());
+
+    std::vector<float> corr = gridder_correction_axis(inner);
+    float* corr_d = (float*)workspace(ctx, "wk_corr", (size_t)inner * 4);
+    CR_CUDA_CHECK(cudaMemcpyAsync(corr_d, corr.data(), (size_t)inner * 4, cudaMemcpyHostToDevice, ctx->stream));
+    int32_t* crop_d = (int32_t*)workspace(ctx, "wk_crop", (size_t)planes * 4);
+    CR_CUDA_CHECK(cudaMemcpyAsync(crop_d, crop.data(), (size_t)planes * 4, cudaMemcpyHostToDevice, ctx->stream));
+
+    // raw (unnormalised) crops at the largest crop width
+    float2* raw = nullptr;
+    CR_CUDA_CHECK(cudaMallocAsync(&raw, (size_t)planes * stride * stride * 8, ctx->stream));
+    const size_t plane_bytes = (size_t)conv * conv * 8;
+    int batch = (int)std::max<int64_t>(1, std::min<int64_t>(planes, (int64_t)(2ull << 30) / (int64_t)plane_bytes));
+    float2* buf = nullptr;
+    CR_CUDA_CHECK(cudaMallocAsync(&buf, plane_bytes * batch, ctx->stream));
+    cufftHandle plan;
+    {
+        int n[2] = {(int)conv, (int)conv};
+        check_cufft(cufftPlanMany(&plan, 2, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2C, batch),
+                    "cufftPlanMany");
+        check_cufft(cufftSetStream(plan, ctx->stream), "cufftSetStream");
+    }
+    const int64_t axis_len = law ? 0 : std::max<int64_t>(quarter, 1);
+    std::vector<double> axes_h;
+    double* axes_d = nullptr;
+    if (!law) {
+        axes_d = (double*)workspace(ctx, "wk_axes", (size_t)batch * 2 * axis_len * 8);
+        axes_h.resize((size_t)batch * 2 * axis_len);
+    }
+    double peak = 0.0;
+    for (int32_t p0 = 0; p0 < planes; p0 += batch) {
+        int nb = std::min<int32_t>(batch, planes - p0);
+        CR_CUDA_CHECK(cudaMemsetAsync(buf, 0, plane_bytes * nb, ctx->stream));
+        screen_kernel<<<grid_blocks(inner * inner * nb, 256, 152 * 64), 256, 0, ctx->stream>>>(
+            buf, conv, inner, nb, p0, planes, w_scale, s0, s1, corr_d);
+        note_launch(ctx, "screen_kernel");
+        // cufftExecC2C on a plan of `batch` transforms; a short final batch
+        // transforms zero-filled spare planes, which are ignored
+        if (nb < batch)
+            CR_CUDA_CHECK(cudaMemsetAsync((char*)buf + plane_bytes * nb, 0,
+                                          plane_bytes * (batch - nb), ctx->stream));
+        check_cufft(cufftExecC2C(plan, (cufftComplex*)buf, (cufftComplex*)buf, CUFFT_FORWARD),
+                    "cufftExecC2C");
+        if (p0 == 0) {
+            float2 t00;
+            CR_CUDA_CHECK(cudaMemcpyAsync(&t00, buf, 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+            peak = std::hypot((double)t00.x, (double)t00.y);
+            if (!(peak > 0.0)) fail(CR_NORMALIZATION, "wproject plane-zero kernel peak is zero");
+        }
+        if (!law) {
+            axis_kernel<<<grid_blocks(nb * axis_len, 256), 256, 0, ctx->stream>>>(buf, conv, nb,
+                                                                                axis_len, axes_d);
+            note_launch(ctx, "axis_kernel");
+            CR_CUDA_CHECK(cudaMemcpyAsync(axes_h.data(), axes_d, (size_t)nb * 2 * axis_len * 8,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+            for (int b = 0; b < nb; ++b) {
+                // find_w_project_support_from_transformed (gridder.rs:3832-3855)
+                const double* ax = &axes_h[(size_t)(2 * b) * axis_len];
+                const double* ay = &axes_h[(size_t)(2 * b + 1) * axis_len];
+                int64_t trial = 0;
+                bool found = false;
+                for (int64_t c = quarter - 1; c >= 1; --c) {
+                    if (ax[c] / peak > 1.0e-3 || ay[c] / peak > 1.0e-3) {
+                        trial = c;
+                        found = true;
+                        break;
+                    }
+                }
+                int64_t ms = std::max<int64_t>(quarter / sampling - 1, 1);
+                int64_t s = found ? std::min<int64_t>(
+                                        (int64_t)std::floor((float)trial / (float)sampling + 0.5f) + 1, ms)
+                                  : ms;
+                support[p0 + b] = (int32_t)s;
+                int64_t cw = std::min<int64_t>(s * sampling + radius + 1, quarter);
+                crop[p0 + b] = (int32_t)std::max<int64_t>(cw, 1);
+            }
+            CR_CUDA_CHECK(cudaMemcpyAsync(crop_d + p0, crop.data() + p0, (size_t)nb * 4,
+                                          cudaMemcpyHostToDevice, ctx->stream));
+        }
+        crop_kernel<<<grid_blocks((int64_t)nb * stride * stride, 256), 256, 0, ctx->stream>>>(
+            buf, conv, nb, p0, crop_d, stride, raw);
+        note_launch(ctx, "crop_kernel");
+    }
+    cufftDestroy(plan);
+    CR_CUDA_CHECK(cudaFreeAsync(buf, ctx->stream));
+
+    const int32_t width = *std::max_element(crop.begin(), crop.end());
+    // compact to the common width
+    float2* kernels = nullptr;
+    CR_CUDA_CHECK(cudaMalloc(&kernels, (size_t)planes * width * width * 8));
+    // rows of a plane are `stride` apart in raw and `width` apart in kernels
+    for (int32_t p = 0; p < planes; ++p)
+        CR_CUDA_CHECK(cudaMemcpy2DAsync(kernels + (size_t)p * width * width, (size_t)width * 8,
+                                        raw + (size_t)p * stride * stride, (size_t)stride * 8,
+                                        (size_t)width * 8, (size_t)width, cudaMemcpyDeviceToDevice,
+                                        ctx->stream));
+    CR_CUDA_CHECK(cudaFreeAsync(raw, ctx->stream));
+
+    wp->radius = radius;
+    wp->axis = axis;
+    wp->support_h = support;
+    CR_CUDA_CHECK(cudaMalloc(&wp->support_d, (size_t)planes * 4));
+    CR_CUDA_CHECK(cudaMemcpyAsync(wp->support_d, support.data(), (size_t)planes * 4,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    // plane-zero integral over the integer taps: K = T / sum Re T0(|i s|, |j s|)
+    double* pb_d = (double*)workspace(ctx, "wk_pb", (size_t)axis * axis * 8);
+    {
+        dim3 grid_pb(axis * axis, 1);
+        tap_sum_kernel<<<grid_pb, 256, 0, ctx->stream>>>(kernels, width, wp->support_d, sampling,
+                                                          radius, axis, 0, pb_d, nullptr);
+        note_launch(ctx, "tap_sum_kernel");
+    }
+    double pb_raw = 0.0;
+    {
+        int centre = radius * axis + radius;  // offset (0, 0)
+        CR_CUDA_CHECK(cudaMemcpyAsync(&pb_raw, pb_d + centre, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (!(std::isfinite(pb_raw) && pb_raw / peak > 0.0))
+        fail(CR_NORMALIZATION, "wproject plane-zero kernel integral is non-positive");
+    scale_kernels<<<grid_blocks((int64_t)planes * width * width, 256), 256, 0, ctx->stream>>>(
+        kernels, (int64_t)planes * width * width, (float)(1.0 / pb_raw));
+    note_launch(ctx, "scale_kernels");
+    wp->kernels_d = kernels;
+    CR_CUDA_CHECK(cudaMalloc(&wp->norm_d, (size_t)planes * axis * axis * 4));
+    {
+        dim3 grid_n(axis * axis, planes);
+        tap_sum_kernel<<<grid_n, 256, 0, ctx->stream>>>(kernels, width, wp->support_d, sampling,
+                                                         radius, axis, 0, nullptr, wp->norm_d);
+        note_launch(ctx, "tap_sum_kernel");
+    }
+    // per-offset slabs
+    wp->slab_off_h.resize(planes);
+    int64_t total = 0;
+    for (int32_t p = 0; p < planes; ++p) {
+        wp->slab_off_h[p] = total;
+        int64_t w = 2 * (int64_t)support[p] + 1;
+        total += (int64_t)axis * axis * w * w;
+    }
+    CR_CUDA_CHECK(cudaMalloc(&wp->slabs_d, (size_t)total * 8));
+    CR_CUDA_CHECK(cudaMalloc(&wp->slab_off_d, (size_t)planes * 8));
+    CR_CUDA_CHECK(cudaMemcpyAsync(wp->slab_off_d, wp->slab_off_h.data(), (size_t)planes * 8,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    for (int32_t p = 0; p < planes; ++p) {
+        int64_t w = 2 * (int64_t)support[p] + 1;
+        slab_kernel<<<grid_blocks((int64_t)axis * axis * w * w, 256), 256, 0, ctx->stream>>>(
+            kernels, width, p, support[p], sampling, radius, axis, wp->slabs_d + wp->slab_off_h[p]);
+        note_launch(ctx, "slab_kernel");
+    }
+    // sinc axes for the image correction and the model apodisation
+    {
+        int64_t m = std::max(gnx, gny);
+        std::vector<float> s = sinc_axis(m, sampling);
+        std::vector<float> sx = sinc_axis(gnx, sampling), sy = sinc_axis(gny, sampling);
+        CR_CUDA_CHECK(cudaMalloc(&wp->sinc_x_d, (size_t)m * 4));
+        CR_CUDA_CHECK(cudaMalloc(&wp->sinc_gx_d, (size_t)gnx * 4));
+        CR_CUDA_CHECK(cudaMalloc(&wp->sinc_gy_d, (size_t)gny * 4));
+        CR_CUDA_CHECK(cudaMemcpy(wp->sinc_x_d, s.data(), (size_t)m * 4, cudaMemcpyHostToDevice));
+        CR_CUDA_CHECK(cudaMemcpy(wp->sinc_gx_d, sx.data(), (size_t)gnx * 4, cudaMemcpyHostToDevice));
+        CR_CUDA_CHECK(cudaMemcpy(wp->sinc_gy_d, sy.data(), (size_t)gny * 4, cudaMemcpyHostToDevice));
+    }
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    wp->info.planes = planes;
+    wp->info.sampling = sampling;
+    wp->info.w_scale = w_scale;
+    wp->info.max_support = *std::max_element(support.begin(), support.end());
+    wp->info.kernel_width = width;
+    wp->info.slab_elements = total;
+}
+
+// ---- gridding / degridding drivers ------------------------------------------------------
+void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2* dirty,
+                int mode) {
+    const int64_t ntiles = r.ntx * r.nty;
+    int R = (31 + wp->info.max_support) / kTile;
+    if (R > kMaxSegRadius) fail(CR_INVALID, "W-projection support above 127 is not supported");
+    uint32_t* nchunks = (uint32_t*)workspace(ctx, "wg_nchunks", (size_t)ntiles * 4);
+    uint32_t* first = (uint32_t*)workspace(ctx, "wg_first", (size_t)ntiles * 4);
+    unsigned long long* nitems = (unsigned long long*)workspace(ctx, "wg_nitems", 16);
+    tile_work_count<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(r.tile_start, r.ntx, r.nty,
+                                                                        R, nchunks);
+    note_launch(ctx, "tile_work_count");
+    exclusive_scan_u32(ctx, nchunks, first, ntiles, nitems);
+    // upper bound on the items: every candidate list chunked
+    size_t max_items = (size_t)ntiles + (size_t)((2 * R + 1) * (2 * R + 1)) *
+                                            (size_t)(r.n_samples / kChunk + 1);
+    uint32_t* item_tile = (uint32_t*)workspace(ctx, "wg_item_tile", max_items * 4);
+    uint32_t* item_begin = (uint32_t*)workspace(ctx, "wg_item_begin", max_items * 4);
+    tile_work_fill<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(nchunks, first, ntiles,
+                                                                       item_tile, item_begin);
+    note_launch(ctx, "tile_work_fill");
+    unsigned int* counter = (unsigned int*)(nitems + 1);
+    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 4, ctx->stream));
+    GridArgs a{r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum,
+               r.rec_pred, r.tile_start, r.ntx, r.nty, wp->support_d, wp->slab_off_d,
+               wp->slabs_d, wp->axis, R, item_tile, item_begin, nitems, counter, psf, dirty,
+               wp->g->info.grid_nx, wp->g->info.grid_ny};
+    int blocks = sm_count(ctx) * 8;
+    if (mode == 0) {
+        wp_grid_kernel<false><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
+        note_launch(ctx, "wp_grid_kernel");
+    } else {
+        wp_grid_kernel<true><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
+        note_launch(ctx, "wp_grid_kernel_residual");
+    }
+}
+
+void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* grid) {
+    DegridArgs a{r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.counts, wp->support_d,
+                 wp->slab_off_d, wp->slabs_d, grid, wp->g->info.grid_ny, r.rec_pred};
+    int blocks = sm_count(ctx) * 8;
+    wp_degrid_kernel<<<blocks, 256, 0, ctx->stream>>>(a);
+    note_launch(ctx, "wp_degrid_kernel");
+}
+
+void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred) {
+    if (r.n_samples <= 0) return;
+    broadcast_kernel<<<grid_blocks(r.n_samples, 256), 256, 0, ctx->stream>>>(
+        r.sample_rec, r.rec_pred, r.n_samples, pred);
+    note_launch(ctx, "broadcast_kernel");
+}
+
+}  // namespace cr

@@ -1,0 +1,245 @@
+/*
+ * casars_cuda.h -- C ABI of the GB300 (sm_103a) imaging hot path.
+ *
+ * One shared library, libcasars_cuda.so, that a casa-imaging host (the Rust
+ * crate, Python through ctypes, or C++) calls at the seams where casa-imaging
+ * selects a backend today.  Each entry point names the reference function or
+ * seam it replaces (paths relative to the casa-rs repository;
+ * `lib.rs` = crates/casa-imaging/src/lib.rs, `gridder.rs`, `weighting.rs`,
+ * `fft.rs` likewise).
+ *
+ * Conventions (the reference's, gridder_interop.rs:40-80 and
+ * casacore_cpp_gridder_shim.cpp:24-121):
+ *   - every call returns int status: CR_OK (0) or an error code; on error a
+ *     heap string is stored in *err (if err is non-NULL) and must be released
+ *     with cr_free_error();
+ *   - arrays are x-major: grids flat = x * grid_ny + y, images flat =
+ *     x * ny + y; complex values are interleaved (re, im) float32;
+ *   - caller-owned buffers are host or device memory as the call's
+ *     `location` argument says (CR_HOST / CR_DEVICE); the library owns its
+ *     device workspaces, which live in the context;
+ *   - a context is one CUDA stream; calls on one context are serialised by
+ *     the caller; distinct contexts may be used from distinct threads.
+ */
+#ifndef CASARS_CUDA_H
+#define CASARS_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes: 1-3 as the reference's C shims, 4-6 added for the device */
+#define CR_OK 0
+#define CR_INVALID 1          /* invalid arguments (ImagingError::InvalidRequest) */
+#define CR_NO_SAMPLES 2       /* no usable samples (ImagingError::NoUsableSamples) */
+#define CR_BUFFER_SMALL 3     /* a caller buffer is too small */
+#define CR_CUDA 4             /* CUDA runtime / cuFFT failure */
+#define CR_NORMALIZATION 5    /* zero or non-finite peak (ImagingError::Normalization) */
+#define CR_TIMEOUT 6          /* a device-side bounded wait gave up */
+
+#define CR_HOST 0
+#define CR_DEVICE 1
+
+/* weighting modes (types.rs:145-180) */
+#define CR_WEIGHT_NATURAL 0
+#define CR_WEIGHT_UNIFORM 1
+#define CR_WEIGHT_BRIGGS 2
+
+/* Hogbom stop reasons (CleanStopReason, lib.rs:74653-74676) */
+#define CR_STOP_NONE 0
+#define CR_STOP_GLOBAL_THRESHOLD 1
+#define CR_STOP_CYCLE_THRESHOLD 2
+#define CR_STOP_NSIGMA_THRESHOLD 3
+#define CR_STOP_NO_CLEANABLE_PIXELS 4
+
+typedef struct cr_ctx cr_ctx;
+typedef struct cr_gridder cr_gridder;
+typedef struct cr_wproj cr_wproj;
+
+/* ImageGeometry (types.rs:885-930). */
+typedef struct {
+    int32_t nx, ny;
+    double cell_x_rad, cell_y_rad;
+} cr_geometry;
+
+/* Grid shape chosen by casa_composite_padded_len (gridder.rs:371-443). */
+typedef struct {
+    int64_t grid_nx, grid_ny;
+    int64_t blc_x, blc_y;
+    double du, dv;            /* grid spacing in wavelengths */
+    int32_t oversampling;
+} cr_grid_info;
+
+/* WProjector summary (gridder.rs:3391-3586). */
+typedef struct {
+    int32_t planes;
+    int32_t sampling;
+    double w_scale;
+    int32_t max_support;
+    int32_t kernel_width;     /* common cropped width */
+    int64_t slab_elements;    /* complex elements in the per-offset kernel slabs */
+} cr_wproj_info;
+
+/* VisibilityBatch (types.rs:1376-1405), structure of arrays.
+ * w may be NULL for the standard gridder; sumwt_factor NULL means 1;
+ * gridable NULL means every sample is gridable. */
+typedef struct {
+    int64_t n;
+    const double* u;
+    const double* v;
+    const double* w;
+    const float* weight;
+    const float* sumwt_factor;
+    const uint8_t* gridable;
+    const float* vis;         /* complex64 interleaved */
+    int32_t location;         /* CR_HOST or CR_DEVICE */
+} cr_vis_batch;
+
+/* WProjectGridAccumulation / DirtyGridAccumulation (lib.rs:70973-70988). */
+typedef struct {
+    double normalization_sumwt;
+    double reported_sumwt;
+    int64_t gridded;
+    int64_t skipped;
+    int64_t unique_records;   /* distinct (cell, offset, plane, sign) keys gridded */
+} cr_sums;
+
+/* PsfState essentials (lib.rs:64680-64690). */
+typedef struct {
+    float psf_peak;
+    float normalization_sumwt;
+    float reported_sumwt;
+} cr_psf_state;
+
+/* Per-stage device times of the last call, milliseconds (CUDA events). */
+typedef struct {
+    float plan_ms, grid_ms, degrid_ms, fft_ms, other_ms;
+} cr_timings;
+
+/* ---- context -------------------------------------------------------------
+ * New; the reference has no device context.  Thread-safe per context.      */
+int cr_ctx_create(int32_t device, cr_ctx** out, char** err);
+void cr_ctx_destroy(cr_ctx* ctx);
+void cr_free_error(char* err);
+/* Use an external cudaStream_t (e.g. torch's current stream); NULL restores
+ * the context's own stream. */
+int cr_ctx_set_stream(cr_ctx* ctx, void* stream, char** err);
+void* cr_ctx_stream(cr_ctx* ctx);
+int cr_ctx_synchronize(cr_ctx* ctx, char** err);
+int cr_ctx_last_timings(cr_ctx* ctx, cr_timings* out);
+/* Number of this library's kernel launches since the context was created. */
+int64_t cr_ctx_launch_count(cr_ctx* ctx);
+const char* cr_version(void);
+
+/* ---- gridders ------------------------------------------------------------
+ * cr_gridder_create replaces StandardGridder::new_with_padding_factor
+ * (gridder.rs:393-443); oversampling 100 is the reference default. */
+int cr_gridder_create(cr_ctx* ctx, const cr_geometry* geom, double padding,
+                      int32_t oversampling, cr_gridder** out, cr_grid_info* info, char** err);
+void cr_gridder_destroy(cr_gridder* g);
+/* Copies the normalised tap rows [(2*(os/2)+1) x 7] and the two correction
+ * axes (float32) to host buffers; any pointer may be NULL. */
+int cr_gridder_tables(cr_gridder* g, float* taps, float* corr_x, float* corr_y, char** err);
+
+/* WProjector::new (gridder.rs:3403-3586).  planes <= 0 chooses the count
+ * from max_abs_w (choose_w_project_plane_count, gridder.rs:3801-3806);
+ * sampling <= 0 keeps the reference rule (4 when planes > 1, else 1).
+ * support_min > 0 selects the law S_p = support_min +
+ * round((support_max - support_min) * p / (planes - 1)); support_min <= 0
+ * keeps the reference's threshold search (gridder.rs:3832-3855). */
+int cr_wproj_create(cr_ctx* ctx, cr_gridder* g, double max_abs_w, int32_t planes,
+                    int32_t sampling, int32_t support_min, int32_t support_max,
+                    cr_wproj** out, cr_wproj_info* info, char** err);
+void cr_wproj_destroy(cr_wproj* wp);
+/* Copies supports [planes], cropped kernels [planes][width][width] complex64
+ * and the normalisation table [planes][2r+1][2r+1] float32 to host. */
+int cr_wproj_tables(cr_wproj* wp, int32_t* support, float* kernels, float* norm, char** err);
+
+/* ---- gridding / degridding ---------------------------------------------
+ * cr_grid_dirty replaces accumulate_dirty_psf_and_residual_standard_streaming_grid
+ * (lib.rs:68306-68500) when wp is NULL, and accumulate_w_project_dirty_grids_streaming
+ * (lib.rs:71091-71138) when wp is given.  Outputs two grid_nx*grid_ny
+ * complex64 grids (PSF, dirty) at `out_location`. */
+int cr_grid_dirty(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                  float* psf_grid, float* dirty_grid, int32_t out_location, cr_sums* sums,
+                  char** err);
+/* degrid_sample_taps_planned_normalized (gridder.rs:1278-1312) /
+ * degrid_sample_planned (gridder.rs:3726-3747) for every sample of the batch:
+ * model_grid is grid_nx*grid_ny complex64 at `grid_location`, pred receives
+ * n complex64 at `out_location` (0 for samples that do not plan). */
+int cr_degrid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+              const float* model_grid, int32_t grid_location, float* pred,
+              int32_t out_location, char** err);
+/* Fused residual refresh: degrid_model_and_grid_residual_taps_planned_f64
+ * (gridder.rs:1315-1396) / accumulate_w_project_residual_streaming_sample
+ * (lib.rs:71514-71541): residual_grid = G((vis - D(model_grid)) * weight). */
+int cr_grid_residual(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                     const float* model_grid, int32_t grid_location, float* residual_grid,
+                     int32_t out_location, cr_sums* sums, char** err);
+
+/* ---- FFT, correction, normalisation ------------------------------------
+ * Centred inverse FFT (fft.rs:600-630) of a grid then crop x correction:
+ * corrected_image_from_grid_f64 (gridder.rs:1646-1657), or the W-projection
+ * correction (gridder.rs:1685-1715) when wp is given; the result is scaled
+ * by `scale` (float32 multiply).  cuFFT performs the bare transform only. */
+int cr_grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* grid,
+                     int32_t grid_location, float scale, float* image, int32_t out_location,
+                     char** err);
+/* apodize_model / apodize_w_project_model (gridder.rs:1554-1592) then the
+ * centred unscaled forward FFT (fft.rs:34): model image -> model grid. */
+int cr_image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
+                     int32_t model_location, float* grid, int32_t out_location, char** err);
+
+/* ---- whole stages (the run_imaging seams) --------------------------------
+ * compute_dirty_psf_and_residual_standard_streaming (lib.rs:68137-68185) with
+ * dirty_grids_to_psf_and_residual_owned (lib.rs:48987-49130), or
+ * compute_dirty_psf_and_residual_w_project_streaming (lib.rs:70539-70590).
+ * Writes the normalised PSF and residual images (nx*ny float32). */
+int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                   float* psf, float* residual, int32_t out_location, cr_psf_state* state,
+                   cr_sums* sums, char** err);
+/* compute_residual (lib.rs:68560-68620 / lib.rs:70592-70644): model image ->
+ * residual image normalised by the given PSF state. */
+int cr_residual_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                      const float* model, int32_t model_location, const cr_psf_state* state,
+                      float* residual, int32_t out_location, cr_sums* sums, char** err);
+/* Forward operator A of the forward/adjoint pair: model image -> model
+ * visibilities (apodize, centred FFT, degrid). */
+int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+               const float* model, int32_t model_location, float* pred,
+               int32_t out_location, char** err);
+/* Adjoint A^H: visibilities (the batch's vis, weighted) -> image, without
+ * normalisation: grid, centred inverse FFT scaled by Nx*Ny, crop, correct. */
+int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+               float* image, int32_t out_location, char** err);
+
+/* ---- weighting -----------------------------------------------------------
+ * apply_weighting_with_density_source, Combined density
+ * (weighting.rs:1055-1180): natural passes weights through; uniform and
+ * Briggs build the density grid with the Hermitian mirror and reweight.
+ * out_weight receives n float32 at `out_location`; f2 (Briggs) is returned. */
+int cr_apply_weighting(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch, int32_t mode,
+                       float robust, float* out_weight, int32_t out_location, float* f2,
+                       char** err);
+
+/* ---- Hogbom minor cycle --------------------------------------------------
+ * run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883): one
+ * persistent device loop of peak search (ties to the smallest y*nx+x),
+ * threshold tests, model update and shifted-PSF subtraction.  model,
+ * residual, psf (nx*ny float32) and mask (nx*ny uint8 or NULL) are at
+ * `location`; model and residual are updated in place.  Component arrays
+ * (capacity cycle_niter + 1) are host memory and may be NULL. */
+int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf,
+              const uint8_t* mask, int32_t nx, int32_t ny, int32_t location, float gain,
+              float threshold, float cycle_threshold, float nsigma_threshold,
+              int64_t cycle_niter, int32_t inclusive, int32_t* comp_x, int32_t* comp_y,
+              float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
+              int32_t* stop_reason, char** err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

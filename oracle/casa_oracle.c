@@ -570,12 +570,15 @@ static void oc_wk_plane_chunk(void* vctx, int64_t b, int64_t e, int32_t worker) 
             colsum_im[ixi] = csi;
             for (int64_t y = 0; y < ylen; ++y) {
                 double accr = 0.0, acci = 0.0;
+                /* twiddle index (y * iy) mod conv, advanced by y per step */
+                int64_t k = ((y * (-half)) % conv + conv) % conv;
+                const int64_t step = y % conv;
                 for (int64_t iyi = 0; iyi < inner; ++iyi) {
-                    int64_t iy = iyi - half;
-                    int64_t k = ((y * iy) % conv + conv) % conv;
                     double tr = j->tw_re[k], ti = j->tw_im[k];
                     accr += sre[iyi] * tr - sim[iyi] * ti;
                     acci += sre[iyi] * ti + sim[iyi] * tr;
+                    k += step;
+                    if (k >= conv) k -= conv;
                 }
                 are[ixi * ylen + y] = accr;
                 aim[ixi * ylen + y] = acci;
@@ -583,21 +586,38 @@ static void oc_wk_plane_chunk(void* vctx, int64_t b, int64_t e, int32_t worker) 
         }
         /* T[x][y] = sum_ix tw(x*ix) A[ix][y] for x, y < cw */
         double* out = j->out + (size_t)plane * j->width_stride * j->width_stride * 2;
+        double* tr_row = (double*)malloc((size_t)inner * sizeof(double));
+        double* ti_row = (double*)malloc((size_t)inner * sizeof(double));
+        double* accr = (double*)malloc((size_t)ylen * sizeof(double));
+        double* acci = (double*)malloc((size_t)ylen * sizeof(double));
         for (int64_t x = 0; x < cw; ++x) {
-            for (int64_t y = 0; y < cw; ++y) {
-                double accr = 0.0, acci = 0.0;
-                for (int64_t ixi = 0; ixi < inner; ++ixi) {
-                    int64_t ix = ixi - half;
-                    int64_t k = ((x * ix) % conv + conv) % conv;
-                    double tr = j->tw_re[k], ti = j->tw_im[k];
-                    double ar = are[ixi * ylen + y], ai = aim[ixi * ylen + y];
-                    accr += ar * tr - ai * ti;
-                    acci += ar * ti + ai * tr;
+            int64_t k = ((x * (-half)) % conv + conv) % conv;
+            const int64_t step = x % conv;
+            for (int64_t ixi = 0; ixi < inner; ++ixi) {
+                tr_row[ixi] = j->tw_re[k];
+                ti_row[ixi] = j->tw_im[k];
+                k += step;
+                if (k >= conv) k -= conv;
+            }
+            for (int64_t y = 0; y < cw; ++y) accr[y] = acci[y] = 0.0;
+            for (int64_t ixi = 0; ixi < inner; ++ixi) {
+                const double tr = tr_row[ixi], ti = ti_row[ixi];
+                const double* ar = are + ixi * ylen;
+                const double* ai = aim + ixi * ylen;
+                for (int64_t y = 0; y < cw; ++y) {
+                    accr[y] += ar[y] * tr - ai[y] * ti;
+                    acci[y] += ar[y] * ti + ai[y] * tr;
                 }
-                out[2 * (x * j->width_stride + y)] = accr;
-                out[2 * (x * j->width_stride + y) + 1] = acci;
+            }
+            for (int64_t y = 0; y < cw; ++y) {
+                out[2 * (x * j->width_stride + y)] = accr[y];
+                out[2 * (x * j->width_stride + y) + 1] = acci[y];
             }
         }
+        free(tr_row);
+        free(ti_row);
+        free(accr);
+        free(acci);
         /* support-search axes: T(c,0) = sum_ix tw(c*ix) colsum(ix);
          * T(0,c) = sum_ix A[ix][c] */
         for (int64_t c = 0; c < alen; ++c) {

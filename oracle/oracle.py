@@ -305,7 +305,11 @@ class WProjector:
         L = 2 * self.norm_radius + 1
         conv = max(gridder.gnx, gridder.gny)
         quarter = conv // 2 - 1
-        cap = min(max_width, quarter)
+        if support_min > 0:
+            cap = min(max_width, support_max * sampling + self.norm_radius + 1)
+        else:
+            cap = min(max_width, max(quarter // sampling - 1, 1) * sampling + self.norm_radius + 1,
+                      quarter)
         kern = np.zeros((planes, cap, cap), np.complex128)
         norm = np.zeros((planes, L, L), np.float64)
         support = np.zeros(planes, np.int32)
