@@ -1,7 +1,7 @@
 """Host mirror of casa-imaging's gridder/imaging/deconvolver seams over the
 GB300 CUDA library (libcasars_cuda.so).  See imaging.py for the API."""
 from ._lib import CasarsCudaError, load as load_library  # noqa: F401
-from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, PsfState,  # noqa: F401
+from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, PsfState,  # noqa: F401
                       StandardGridder, VisibilityBatch, WProjector, adjoint, apply_weighting,
                       degrid, dirty_image, grid_dirty, grid_residual, grid_to_image,
                       image_to_grid, predict, residual_image, run_hogbom_minor_cycle)

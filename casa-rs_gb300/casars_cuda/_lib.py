@@ -33,7 +33,7 @@ class GridInfo(C.Structure):
 
 class WProjInfo(C.Structure):
     _fields_ = [("planes", _i32), ("sampling", _i32), ("w_scale", _d), ("max_support", _i32),
-                ("kernel_width", _i32), ("slab_elements", _i64)]
+                ("kernel_width", _i32), ("cube_elements", _i64)]
 
 
 class VisBatch(C.Structure):
@@ -79,6 +79,12 @@ SIGNATURES = {
     "cr_degrid": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _i32, _p, _i32, _err]),
     "cr_grid_residual": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _i32, _p, _i32,
                                    C.POINTER(Sums), _err]),
+    "cr_plan_create": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), C.POINTER(_p),
+                                 C.POINTER(Sums), _err]),
+    "cr_plan_destroy": (None, [_p]),
+    "cr_plan_grid_dirty": (C.c_int, [_p, _p, _p, _p, _i32, _err]),
+    "cr_plan_degrid": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
+    "cr_plan_grid_residual": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
     "cr_grid_to_image": (C.c_int, [_p, _p, _p, _p, _i32, _f, _p, _i32, _err]),
     "cr_image_to_grid": (C.c_int, [_p, _p, _p, _p, _i32, _p, _i32, _err]),
     "cr_dirty_image": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _p, _i32,

@@ -378,6 +378,71 @@ def grid_residual(gridder, batch: VisibilityBatch, model_grid=None, wproj=None):
     return out, GridSums.from_c(s)
 
 
+class Plan:
+    """A materialised plan of one batch (cr_plan): FP64 index selection,
+    sort and deduplication done once, reused by grid_dirty / degrid /
+    grid_residual while the batch is unchanged (e.g. across major cycles)."""
+
+    def __init__(self, gridder, batch: VisibilityBatch, wproj=None):
+        ctx, g, wp = _handles(gridder, wproj)
+        arrs = _Arrays()
+        b = batch._bind(arrs, wproj is not None)
+        _prepare(gridder, arrs)
+        self.gridder, self.wproj, self.n = gridder, wproj, len(batch)
+        self.device = _device_of(batch.u_lambda)
+        self.location = arrs.location
+        h = C.c_void_p()
+        s = _lib.Sums()
+        call("cr_plan_create", ctx, g, wp, C.byref(b), C.byref(h), C.byref(s))
+        self._h = h
+        self.sums = GridSums.from_c(s)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().cr_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _out(self, shape, np_dtype, torch_dtype):
+        arrs = _Arrays()
+        arrs.location = self.location
+        if self.location == CR_DEVICE:
+            self.gridder.ctx.use_torch_stream()
+        else:
+            self.gridder.ctx.use_own_stream()
+        return arrs.out(shape, np_dtype, torch_dtype, self.device)
+
+    def grid_dirty(self):
+        tc = torch.complex64 if torch else None
+        psf, pp, loc = self._out(self.gridder.grid_shape(), np.complex64, tc)
+        dirty, dp, _ = self._out(self.gridder.grid_shape(), np.complex64, tc)
+        call("cr_plan_grid_dirty", self.gridder.ctx.handle, self._h, pp, dp, loc)
+        return psf, dirty
+
+    def degrid(self, model_grid):
+        arrs = _Arrays()
+        mp = arrs.ptr(model_grid, np.complex64, torch.complex64 if torch else None,
+                      self.gridder.grid_shape())
+        out, op, loc = self._out((self.n,), np.complex64, torch.complex64 if torch else None)
+        call("cr_plan_degrid", self.gridder.ctx.handle, self._h, mp, arrs.location, op, loc)
+        return out
+
+    def grid_residual(self, model_grid=None):
+        arrs = _Arrays()
+        mp = arrs.ptr(model_grid, np.complex64, torch.complex64 if torch else None,
+                      self.gridder.grid_shape())
+        out, op, loc = self._out(self.gridder.grid_shape(), np.complex64,
+                                 torch.complex64 if torch else None)
+        call("cr_plan_grid_residual", self.gridder.ctx.handle, self._h, mp,
+             arrs.location if arrs.location is not None else CR_HOST, op, loc)
+        return out
+
+
 def grid_to_image(gridder, grid, scale: float = 1.0, wproj=None):
     """Centred inverse FFT, crop and grid correction, times `scale`."""
     ctx, g, wp = _handles(gridder, wproj)

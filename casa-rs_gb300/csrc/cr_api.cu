@@ -59,8 +59,9 @@ struct StageTimer {
 
 void bind(cr_ctx* ctx) { CR_CUDA_CHECK(cudaSetDevice(ctx->device)); }
 
-Records plan(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const DeviceBatch& b) {
-    return wp ? plan_wproj(ctx, wp, b) : plan_standard(ctx, g, b);
+Records plan(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const DeviceBatch& b,
+             Pool* pool = nullptr) {
+    return wp ? plan_wproj(ctx, wp, b, pool) : plan_standard(ctx, g, b, pool);
 }
 
 void grid_records(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const Records& r, float2* psf,
@@ -256,10 +257,11 @@ void cr_wproj_destroy(cr_wproj* wp) {
     cudaSetDevice(wp->ctx->device);
     cudaStreamSynchronize(wp->ctx->stream);
     cudaFree(wp->support_d);
-    cudaFree(wp->slab_off_d);
+    cudaFree(wp->cube_off_d);
+    cudaFree(wp->cube_q_d);
     cudaFree(wp->kernels_d);
     cudaFree(wp->norm_d);
-    cudaFree(wp->slabs_d);
+    cudaFree(wp->cube_d);
     cudaFree(wp->sinc_x_d);
     cudaFree(wp->sinc_gx_d);
     cudaFree(wp->sinc_gy_d);
@@ -525,6 +527,107 @@ int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         float n2 = (float)((double)g->info.grid_nx * (double)g->info.grid_ny);
         grid_to_image_adjoint(ctx, g, wp, grid, n2, img);
         if (out_location == CR_HOST) copy_out(ctx, image, img, np * 4, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_plan_create(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                   cr_plan** out, cr_sums* sums, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && out != nullptr, "null argument");
+        check_wp(g, wp);
+        *out = nullptr;
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        cr_plan* p = new cr_plan();
+        p->ctx = ctx;
+        p->g = g;
+        p->wp = wp;
+        try {
+            p->rec = plan(ctx, g, wp, b, &p->pool);
+            tm.mark();
+            read_sums(ctx, p->rec, &p->sums);
+        } catch (...) {
+            cr_plan_destroy(p);
+            throw;
+        }
+        if (sums) *sums = p->sums;
+        ctx->timings = cr_timings{tm.between(0, 1), 0.f, 0.f, 0.f, 0.f};
+        *out = p;
+    });
+}
+
+void cr_plan_destroy(cr_plan* p) {
+    if (!p) return;
+    cudaSetDevice(p->ctx->device);
+    pool_free(p->ctx, p->pool);
+    cudaStreamSynchronize(p->ctx->stream);
+    delete p;
+}
+
+int cr_plan_grid_dirty(cr_ctx* ctx, cr_plan* p, float* psf_grid, float* dirty_grid,
+                       int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && p != nullptr && p->ctx == ctx, "plan belongs to another context");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        size_t gb = grid_bytes(p->g);
+        float2* psf = out_ptr<float2>(ctx, psf_grid, out_location, gb, "psf_grid");
+        float2* dirty = out_ptr<float2>(ctx, dirty_grid, out_location, gb, "dirty_grid");
+        CR_CUDA_CHECK(cudaMemsetAsync(psf, 0, gb, ctx->stream));
+        CR_CUDA_CHECK(cudaMemsetAsync(dirty, 0, gb, ctx->stream));
+        grid_records(ctx, p->g, p->wp, p->rec, psf, dirty, 0);
+        tm.mark();
+        if (out_location == CR_HOST) {
+            copy_out(ctx, psf_grid, psf, gb, CR_HOST);
+            copy_out(ctx, dirty_grid, dirty, gb, CR_HOST);
+        }
+        ctx->timings = cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f};
+    });
+}
+
+int cr_plan_degrid(cr_ctx* ctx, cr_plan* p, const float* model_grid, int32_t grid_location,
+                   float* pred, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && p != nullptr && p->ctx == ctx, "plan belongs to another context");
+        need(model_grid != nullptr, "model grid is null");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        const float2* grid = (const float2*)device_input(ctx, model_grid, grid_bytes(p->g),
+                                                         grid_location, "model_grid");
+        degrid_records(ctx, p->g, p->wp, p->rec, grid);
+        size_t n = (size_t)p->rec.n_samples;
+        float2* out = out_ptr<float2>(ctx, pred, out_location, n * 8 + 8, "pred");
+        broadcast_pred(ctx, p->rec, out);
+        tm.mark();
+        if (out_location == CR_HOST) copy_out(ctx, pred, out, n * 8, CR_HOST);
+        ctx->timings = cr_timings{0.f, 0.f, tm.between(0, 1), 0.f, 0.f};
+    });
+}
+
+int cr_plan_grid_residual(cr_ctx* ctx, cr_plan* p, const float* model_grid,
+                          int32_t grid_location, float* residual_grid, int32_t out_location,
+                          char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && p != nullptr && p->ctx == ctx, "plan belongs to another context");
+        bind(ctx);
+        size_t gb = grid_bytes(p->g);
+        size_t n = (size_t)(p->rec.n_samples > 0 ? p->rec.n_samples : 1);
+        if (model_grid) {
+            const float2* grid = (const float2*)device_input(ctx, model_grid, gb, grid_location,
+                                                             "model_grid");
+            degrid_records(ctx, p->g, p->wp, p->rec, grid);
+        } else {
+            CR_CUDA_CHECK(cudaMemsetAsync(p->rec.rec_pred, 0, n * 8, ctx->stream));
+        }
+        float2* res = out_ptr<float2>(ctx, residual_grid, out_location, gb, "residual_grid");
+        CR_CUDA_CHECK(cudaMemsetAsync(res, 0, gb, ctx->stream));
+        grid_records(ctx, p->g, p->wp, p->rec, nullptr, res, 1);
+        if (out_location == CR_HOST) copy_out(ctx, residual_grid, res, gb, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
 }

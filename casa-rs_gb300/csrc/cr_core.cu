@@ -17,11 +17,11 @@ void check_cufft(cufftResult r, const char* what) {
     if (r != CUFFT_SUCCESS) fail(CR_CUDA, std::string(what) + ": cuFFT error " + std::to_string((int)r));
 }
 
-// Grow-only, stream-ordered workspace: a request larger than the current
+// Grow-only, stream-ordered buffers: a request larger than the current
 // buffer frees it on the stream and allocates a larger one.
-void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes) {
+void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes) {
     if (bytes == 0) bytes = 16;
-    DevBuf& b = ctx->ws[name];
+    DevBuf& b = pool[name];
     if (b.bytes >= bytes) return b.ptr;
     if (b.ptr) CR_CUDA_CHECK(cudaFreeAsync(b.ptr, ctx->stream));
     size_t want = bytes + bytes / 8;
@@ -29,6 +29,16 @@ void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes) {
     CR_CUDA_CHECK(cudaMallocAsync(&b.ptr, want, ctx->stream));
     b.bytes = want;
     return b.ptr;
+}
+
+void pool_free(cr_ctx* ctx, Pool& pool) {
+    for (auto& kv : pool)
+        if (kv.second.ptr) cudaFreeAsync(kv.second.ptr, ctx->stream);
+    pool.clear();
+}
+
+void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes) {
+    return pool_alloc(ctx, ctx->ws, name, bytes);
 }
 
 void note_launch(cr_ctx* ctx, const char* what) {

@@ -32,6 +32,9 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// A named set of grow-only device buffers.
+using Pool = std::map<std::string, DevBuf>;
+
 }  // namespace cr
 
 // A context: one device, one stream, grow-only device workspaces, cached
@@ -40,7 +43,7 @@ struct cr_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    std::map<std::string, cr::DevBuf> ws;
+    cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
     cudaEvent_t ev[8] = {};
     cr_timings timings = {};
@@ -62,7 +65,7 @@ struct cr_gridder {
 };
 
 // W-projection state: cropped kernels, normalisation table and the
-// per-offset kernel slabs the gridder and degridder read.
+// residue cubes the gridder and degridder read.
 struct cr_wproj {
     cr_ctx* ctx = nullptr;
     cr_gridder* g = nullptr;
@@ -70,12 +73,14 @@ struct cr_wproj {
     int32_t radius = 0;          // (sampling + 1) / 2: offsets lie in [-radius, radius]
     int32_t axis = 0;            // 2 * radius + 1
     std::vector<int32_t> support_h;
-    std::vector<int64_t> slab_off_h;  // [planes] start of each plane's slabs (float2 units)
+    std::vector<int64_t> cube_off_h;  // [planes] start of each plane's residue cube
+    std::vector<int32_t> cube_q_h;    // [planes] residue extent Q of each cube
     int32_t* support_d = nullptr;
-    int64_t* slab_off_d = nullptr;
+    int64_t* cube_off_d = nullptr;
+    int32_t* cube_q_d = nullptr;
     float2* kernels_d = nullptr;      // [planes][width][width]
     float* norm_d = nullptr;          // [planes][axis][axis]
-    float2* slabs_d = nullptr;        // per plane [axis][axis][W_p][W_p], W_p = 2 S_p + 1
+    float2* cube_d = nullptr;         // per plane [s][s][Q][Q]: K[qx s + rx, qy s + ry]
     float* sinc_x_d = nullptr;        // sinc axis for the image correction (max(g) long)
     float* sinc_gx_d = nullptr;       // sinc axes for the model apodisation
     float* sinc_gy_d = nullptr;
@@ -85,6 +90,9 @@ namespace cr {
 
 // ---- context helpers -------------------------------------------------------
 void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes);
+// the same from another pool (stream-ordered on ctx's stream)
+void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes);
+void pool_free(cr_ctx* ctx, Pool& pool);
 void note_launch(cr_ctx* ctx, const char* what);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
 
@@ -150,8 +158,9 @@ struct Records {
 
 constexpr int kTile = 32;            // home/output tile edge in grid cells
 
-Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b);
-Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b);
+// The records live in `pool` (the context's workspaces when null).
+Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool = nullptr);
+Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* pool = nullptr);
 void read_sums(cr_ctx* ctx, const Records& r, cr_sums* out);
 
 // ---- gridding kernels ----------------------------------------------------------
@@ -200,3 +209,15 @@ inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) 
 }
 
 }  // namespace cr
+
+// A materialised plan of one batch (the device form of the reference's
+// planned taps): its records outlive the call that made them, in the plan's
+// own pool, and serve any number of gridding and degridding calls.
+struct cr_plan {
+    cr_ctx* ctx = nullptr;
+    cr_gridder* g = nullptr;
+    cr_wproj* wp = nullptr;
+    cr::Pool pool;
+    cr::Records rec;
+    cr_sums sums = {};
+};

@@ -349,26 +349,29 @@ __global__ void tile_starts(const uint32_t* tile_of, const unsigned long long* c
     }
 }
 
-Records allocate_records(cr_ctx* ctx, int64_t n, int64_t ntx, int64_t nty) {
+Records allocate_records(cr_ctx* ctx, int64_t n, int64_t ntx, int64_t nty, Pool* pool) {
     Records r;
     size_t nn = (size_t)(n > 0 ? n : 1);
     r.n_samples = n;
     r.ntx = ntx;
     r.nty = nty;
+    Pool& P = pool ? *pool : ctx->ws;
+    auto A = [&](const char* name, size_t bytes) { return pool_alloc(ctx, P, name, bytes); };
+    // keys and order are needed only while planning: always context workspaces
     r.keys = (uint64_t*)workspace(ctx, "rec_keys", nn * 8);
     r.order = (uint32_t*)workspace(ctx, "rec_order", nn * 4);
-    r.sample_rec = (int32_t*)workspace(ctx, "rec_sample", nn * 4);
-    r.rec_x = (int32_t*)workspace(ctx, "rec_x", nn * 4);
-    r.rec_y = (int32_t*)workspace(ctx, "rec_y", nn * 4);
-    r.rec_a = (int32_t*)workspace(ctx, "rec_a", nn * 4);
-    r.rec_b = (int32_t*)workspace(ctx, "rec_b", nn * 4);
-    r.rec_conj = (int32_t*)workspace(ctx, "rec_conj", nn * 4);
-    r.rec_vsum = (double2*)workspace(ctx, "rec_vsum", nn * 16);
-    r.rec_wsum = (double*)workspace(ctx, "rec_wsum", nn * 8);
-    r.rec_pred = (float2*)workspace(ctx, "rec_pred", nn * 8);
-    r.tile_start = (uint32_t*)workspace(ctx, "rec_tile_start", (size_t)(ntx * nty + 1) * 4);
-    r.counts = (unsigned long long*)workspace(ctx, "rec_counts", 4 * 8);
-    r.sums = (double*)workspace(ctx, "rec_sums", 2 * 8);
+    r.sample_rec = (int32_t*)A("rec_sample", nn * 4);
+    r.rec_x = (int32_t*)A("rec_x", nn * 4);
+    r.rec_y = (int32_t*)A("rec_y", nn * 4);
+    r.rec_a = (int32_t*)A("rec_a", nn * 4);
+    r.rec_b = (int32_t*)A("rec_b", nn * 4);
+    r.rec_conj = (int32_t*)A("rec_conj", nn * 4);
+    r.rec_vsum = (double2*)A("rec_vsum", nn * 16);
+    r.rec_wsum = (double*)A("rec_wsum", nn * 8);
+    r.rec_pred = (float2*)A("rec_pred", nn * 8);
+    r.tile_start = (uint32_t*)A("rec_tile_start", (size_t)(ntx * nty + 1) * 4);
+    r.counts = (unsigned long long*)A("rec_counts", 4 * 8);
+    r.sums = (double*)A("rec_sums", 2 * 8);
     CR_CUDA_CHECK(cudaMemsetAsync(r.counts, 0, 4 * 8, ctx->stream));
     CR_CUDA_CHECK(cudaMemsetAsync(r.sums, 0, 2 * 8, ctx->stream));
     CR_CUDA_CHECK(cudaMemsetAsync(r.sample_rec, 0xFF, nn * 4, ctx->stream));
@@ -410,10 +413,10 @@ void finish_records(cr_ctx* ctx, Records& r, int mode, int key_bits, int plane_b
 
 }  // namespace
 
-Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b) {
+Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) {
     const cr_grid_info& gi = wp->g->info;
     int64_t ntx = (gi.grid_nx + kTile - 1) / kTile, nty = (gi.grid_ny + kTile - 1) / kTile;
-    Records r = allocate_records(ctx, b.n, ntx, nty);
+    Records r = allocate_records(ctx, b.n, ntx, nty, pool);
     int tile_bits = bits_for((uint64_t)(ntx * nty));
     int plane_bits = bits_for((uint64_t)(wp->info.planes > 1 ? wp->info.planes - 1 : 1));
     int off_bits = bits_for((uint64_t)(wp->axis * wp->axis - 1));
@@ -432,10 +435,10 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b) {
     return r;
 }
 
-Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b) {
+Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* pool) {
     const cr_grid_info& gi = g->info;
     int64_t ntx = (gi.grid_nx + kTile - 1) / kTile, nty = (gi.grid_ny + kTile - 1) / kTile;
-    Records r = allocate_records(ctx, b.n, ntx, nty);
+    Records r = allocate_records(ctx, b.n, ntx, nty, pool);
     int tile_bits = bits_for((uint64_t)(ntx * nty));
     int key_bits = tile_bits + 16 + 10;
     if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");

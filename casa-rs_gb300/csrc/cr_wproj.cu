@@ -4,18 +4,25 @@
 // phase screen corr(l)corr(m) exp(2 pi i w_k (sqrt(1-l^2-m^2) - 1)) with the
 // phase in FP64, a forward 2-D FFT (cuFFT, the bare transform), a crop to
 // the plane's support, division by the plane-zero integral, and the
-// per-(plane, offset) normalisation table.  The cropped kernels are then
-// re-laid out as one dense "slab" per (plane, x offset, y offset): slab
-// element (i, j) holds K[|(i - S) s + off_x|, |(j - S) s + off_y|], so the
-// taps of a sample are a contiguous (2S+1)^2 block and a warp reads 32
-// consecutive taps of a row.
+// per-(plane, offset) normalisation table.
+//
+// The cropped kernel K_p[kx, ky] (kx = |i s + off_x| for tap i of a sample
+// with oversampling offset off_x) is stored once per plane as a residue cube
+//   C_p[rx][ry][qx][qy] = K_p[qx s + rx, qy s + ry],
+// so the address of tap (i, j) separates into A(i) + B(j) with
+//   A = rx s Q^2 + qx Q and B = ry Q^2 + qy  (Q = qx extent of the plane),
+// and consecutive taps of one row are consecutive in memory on each side of
+// the sample.  The cube holds each kernel value once (about 0.1 GB for 128
+// planes with supports up to 64 at oversampling 8), small enough to stay in
+// L2, where per-offset copies of the taps would not.
 //
 // Gridding is output-stationary: a block owns a 32 x 32 tile of the grid in
 // registers (each of 8 warps owns 4 rows, each lane one column), streams the
 // deduplicated records whose windows can reach the tile, and adds
 // value * kernel for every owned cell inside a record's window.  The tile is
 // flushed once per work item with FP32 atomics.  Degridding is a gather: a
-// warp per record reads the window of the model grid and the slab.
+// warp per record walks the record's (2S+1)^2 taps as one flat index, so
+// every lane carries a tap, and reduces with warp shuffles.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -141,20 +148,45 @@ __global__ void scale_kernels(float2* k, int64_t n, float scale) {
     }
 }
 
-__global__ void slab_kernel(const float2* kernels, int32_t width, int plane, int32_t s,
-                            int32_t sampling, int32_t radius, int32_t axis, float2* slab) {
-    const int w = 2 * s + 1;
-    const int64_t total = (int64_t)axis * axis * w * w;
+__global__ void cube_kernel(const float2* kernels, int32_t width, int plane, int32_t s,
+                            int32_t q, float2* cube) {
+    const int64_t qq = (int64_t)q * q;
+    const int64_t total = (int64_t)s * s * qq;
     const float2* k = kernels + (int64_t)plane * width * width;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t offidx = t / ((int64_t)w * w);
-        int64_t rem = t - offidx * w * w;
-        int i = (int)(rem / w), j = (int)(rem - (int64_t)i * w);
-        int ox = (int)(offidx / axis) - radius, oy = (int)(offidx % axis) - radius;
-        int kx = abs((i - s) * sampling + ox), ky = abs((j - s) * sampling + oy);
-        slab[t] = (kx < width && ky < width) ? k[(int64_t)kx * width + ky] : make_float2(0.f, 0.f);
+        int64_t res = t / qq;
+        int64_t rem = t - res * qq;
+        int rx = (int)(res / s), ry = (int)(res % s);
+        int qx = (int)(rem / q), qy = (int)(rem % q);
+        int kx = qx * s + rx, ky = qy * s + ry;
+        cube[t] = (kx < width && ky < width) ? k[(int64_t)kx * width + ky] : make_float2(0.f, 0.f);
     }
+}
+
+// floor(k / s) for 0 <= k < 2^26 and 1 <= s <= 64 by a multiply-high with
+// magic = floor(2^32 / s) + 1 (exact in that range).
+__device__ __forceinline__ int qdiv(int k, unsigned long long magic) {
+    return (int)(((unsigned long long)(unsigned)k * magic) >> 32);
+}
+
+struct CubeGeom {
+    int s;                     // sampling
+    unsigned long long magic;  // for qdiv by s
+};
+
+// Address parts of kernel tap t (t in [-S, S]) for offset off:
+// x-side A = rx s Q^2 + qx Q, y-side B = ry Q^2 + qy.
+__device__ __forceinline__ int cube_a(int t, int off, int q, const CubeGeom& c) {
+    int k = abs(t * c.s + off);
+    int qk = qdiv(k, c.magic);
+    return (k - qk * c.s) * c.s * q * q + qk * q;
+}
+
+__device__ __forceinline__ int cube_b(int t, int off, int q, const CubeGeom& c) {
+    int k = abs(t * c.s + off);
+    int qk = qdiv(k, c.magic);
+    return (k - qk * c.s) * q * q + qk;
 }
 
 // ---- gridding ----------------------------------------------------------------------
@@ -166,9 +198,11 @@ struct GridArgs {
     const uint32_t* tile_start;
     int64_t ntx, nty;
     const int32_t* support;
-    const int64_t* slab_off;
-    const float2* slabs;
-    int32_t axis;
+    const int64_t* cube_off;
+    const int32_t* cube_q;
+    const float2* cube;
+    CubeGeom cg;
+    int32_t radius, axis;
     int32_t seg_radius;
     const uint32_t* item_tile;
     const uint32_t* item_begin;
@@ -179,12 +213,19 @@ struct GridArgs {
     int64_t gnx, gny;
 };
 
-struct Entry {
-    int64_t slab;    // element offset of this record's slab
-    int32_t ra, cb;  // slab row of tile row 0, slab column of tile column 0
-    int32_t w;       // slab width 2S+1
-    float vr, vi, tvi, tvr, pw, tpw;
+struct __align__(16) Entry {
+    int64_t base;    // element offset of the record's plane cube
+    int32_t cb;      // window column of tile column 0
+    int32_t ra;      // window row of tile row 0
+    int32_t w;       // window width 2S+1
+    int32_t s;       // support S
+    int32_t ox, oy;  // oversampling offsets
+    int32_t q;       // cube extent Q of the plane
+    int32_t pad;
+    float vr, vi, tvi, tvr, pw, tpw, pad2, pad3;
 };
+
+constexpr int kCand = 128;  // candidate records examined per batch
 
 template <bool RESIDUAL>
 __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
@@ -192,14 +233,15 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
     __shared__ uint32_t s_seg_start[kMaxSeg];
     __shared__ uint32_t s_seg_pref[kMaxSeg + 1];
     __shared__ int s_nseg;
-    __shared__ Entry s_list[kGridThreads];
+    __shared__ Entry s_list[kCand];
+    // x-side cube address of each tile row per entry, -1 outside the window
+    __shared__ int s_rowa[kCand][kTile + 1];
     __shared__ int s_nlist;
-    __shared__ int s_warp_cnt[kGridThreads / 32];
+    __shared__ int s_warp_cnt[kCand / 32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned long long n_items = *a.n_items;
     const int R = a.seg_radius;
-    const int side = 2 * R + 1;
 
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
@@ -237,26 +279,30 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
 #pragma unroll
         for (int k = 0; k < kRowsPerWarp; ++k) pr[k] = pi[k] = dr[k] = di[k] = 0.0f;
 
-        for (uint32_t base = begin; base < end; base += kGridThreads) {
-            // 1. candidates -> overlapping entries
+        for (uint32_t base = begin; base < end; base += kCand) {
+            // 1. candidates -> overlapping entries (the first kCand threads)
             uint32_t vidx = base + tid;
             bool take = false;
             Entry e;
-            if (vidx < end) {
+            if (tid < kCand && vidx < end) {
                 int k = 0;
                 while (k + 1 < nseg && s_seg_pref[k + 1] <= vidx) ++k;
                 uint32_t r = s_seg_start[k] + (vidx - s_seg_pref[k]);
                 int lx = a.rx[r], ly = a.ry[r];
                 int plane = a.rplane[r];
-                int s = a.support[plane];
-                if (lx - s <= x0 + kTile - 1 && lx + s >= x0 && ly - s <= y0 + kTile - 1 &&
-                    ly + s >= y0) {
+                int sup = a.support[plane];
+                if (lx - sup <= x0 + kTile - 1 && lx + sup >= x0 && ly - sup <= y0 + kTile - 1 &&
+                    ly + sup >= y0) {
                     take = true;
-                    int w = 2 * s + 1;
-                    e.w = w;
-                    e.slab = a.slab_off[plane] + (int64_t)a.roff[r] * w * w;
-                    e.ra = x0 - lx + s;
-                    e.cb = y0 - ly + s;
+                    int off = a.roff[r];
+                    e.ox = off / a.axis - a.radius;
+                    e.oy = off % a.axis - a.radius;
+                    e.s = sup;
+                    e.w = 2 * sup + 1;
+                    e.q = a.cube_q[plane];
+                    e.base = a.cube_off[plane];
+                    e.ra = x0 - lx + sup;
+                    e.cb = y0 - ly + sup;
                     double2 vs = a.vsum[r];
                     double ws = a.wsum[r];
                     float vr, vi;
@@ -275,42 +321,61 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
                     e.tvr = t * vr;
                     e.pw = (float)ws;
                     e.tpw = t * (float)ws;
+                    e.pad = 0;
+                    e.pad2 = e.pad3 = 0.0f;
                 }
             }
-            unsigned bal = __ballot_sync(0xffffffffu, take);
-            if (lane == 0) s_warp_cnt[warp] = __popc(bal);
+            unsigned bal = 0;
+            if (tid < kCand) {  // whole warps: kCand is a multiple of 32
+                bal = __ballot_sync(0xffffffffu, take);
+                if (lane == 0) s_warp_cnt[warp] = __popc(bal);
+            }
             __syncthreads();
             if (take) {
-                int off = 0;
-                for (int w2 = 0; w2 < warp; ++w2) off += s_warp_cnt[w2];
-                off += __popc(bal & ((1u << lane) - 1u));
-                s_list[off] = e;
+                int slot = 0;
+                for (int w2 = 0; w2 < warp; ++w2) slot += s_warp_cnt[w2];
+                slot += __popc(bal & ((1u << lane) - 1u));
+                s_list[slot] = e;
             }
             if (tid == 0) {
                 int t = 0;
-                for (int w2 = 0; w2 < kGridThreads / 32; ++w2) t += s_warp_cnt[w2];
+                for (int w2 = 0; w2 < kCand / 32; ++w2) t += s_warp_cnt[w2];
                 s_nlist = t;
             }
             __syncthreads();
-            // 2. accumulate the entries into the register tile
+            // x-side cube address of every (entry, tile row), all threads
             const int nlist = s_nlist;
-            for (int q = 0; q < nlist; ++q) {
-                const Entry& en = s_list[q];
-                const int w = en.w;
+            for (int idx = tid; idx < nlist * kTile; idx += kGridThreads) {
+                const int qn = idx / kTile, rr = idx - (idx / kTile) * kTile;
+                const Entry& en = s_list[qn];
+                const int i = en.ra + rr;  // window row index
+                s_rowa[qn][rr] = (i >= 0 && i < en.w) ? cube_a(i - en.s, en.ox, en.q, a.cg) : -1;
+            }
+            __syncthreads();
+            // 2. accumulate the entries into the register tile
+            for (int qn = 0; qn < nlist; ++qn) {
+                const Entry& en = s_list[qn];
                 const int col = en.cb + lane;
-                const bool colok = (unsigned)col < (unsigned)w;
-                const float2* slab = a.slabs + en.slab;
+                const bool colok = (unsigned)col < (unsigned)en.w;
+                const int bcol = colok ? cube_b(col - en.s, en.oy, en.q, a.cg) : 0;
+                const float2* cube = a.cube + en.base + bcol;
+                float2 kv[kRowsPerWarp];
+                bool ok[kRowsPerWarp];
 #pragma unroll
                 for (int k = 0; k < kRowsPerWarp; ++k) {
-                    const int row = en.ra + warp + k * (kGridThreads / 32);
-                    if ((unsigned)row < (unsigned)w && colok) {
-                        const float2 kv = __ldg(&slab[(int64_t)row * w + col]);
+                    const int av = s_rowa[qn][warp + k * (kGridThreads / 32)];
+                    ok[k] = av >= 0 && colok;
+                    kv[k] = ok[k] ? __ldg(cube + av) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int k = 0; k < kRowsPerWarp; ++k) {
+                    if (ok[k]) {
                         if (!RESIDUAL) {
-                            pr[k] = fmaf(en.pw, kv.x, pr[k]);
-                            pi[k] = fmaf(en.tpw, kv.y, pi[k]);
+                            pr[k] = fmaf(en.pw, kv[k].x, pr[k]);
+                            pi[k] = fmaf(en.tpw, kv[k].y, pi[k]);
                         }
-                        dr[k] = fmaf(-en.tvi, kv.y, fmaf(en.vr, kv.x, dr[k]));
-                        di[k] = fmaf(en.vi, kv.x, fmaf(en.tvr, kv.y, di[k]));
+                        dr[k] = fmaf(-en.tvi, kv[k].y, fmaf(en.vr, kv[k].x, dr[k]));
+                        di[k] = fmaf(en.vi, kv[k].x, fmaf(en.tvr, kv[k].y, di[k]));
                     }
                 }
             }
@@ -369,35 +434,65 @@ struct DegridArgs {
     const int32_t *rx, *ry, *rplane, *roff, *rconj;
     const unsigned long long* counts;
     const int32_t* support;
-    const int64_t* slab_off;
-    const float2* slabs;
+    const int64_t* cube_off;
+    const int32_t* cube_q;
+    const float2* cube;
+    CubeGeom cg;
+    int32_t radius, axis;
     const float2* grid;
     int64_t gny;
     float2* pred;
 };
 
+// One warp per record; lane l takes taps l, l+32, ... of the flattened
+// (2S+1)^2 window, tracking its (row, column) incrementally, four taps per
+// step so that eight loads are in flight.
 __global__ void __launch_bounds__(256) wp_degrid_kernel(DegridArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t nrec = (int64_t)a.counts[2];
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int gny = (int)a.gny;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrec;
          r += nwarps) {
         const int plane = a.rplane[r];
         const int s = a.support[plane];
         const int w = 2 * s + 1;
-        const float2* slab = a.slabs + a.slab_off[plane] + (int64_t)a.roff[r] * w * w;
+        const int q = a.cube_q[plane];
+        const int off = a.roff[r];
+        const int ox = off / a.axis - a.radius, oy = off % a.axis - a.radius;
+        const float2* cube = a.cube + a.cube_off[plane];
         const float2* g = a.grid + (int64_t)(a.rx[r] - s) * a.gny + (a.ry[r] - s);
+        const int nt = w * w;
+        int i = lane / w, j = lane - (lane / w) * w;
+        int goff = i * gny + j;
+        int arow = cube_a(i - s, ox, q, a.cg);
         float A = 0.f, B = 0.f, C = 0.f, D = 0.f;
-        for (int i = 0; i < w; ++i) {
-            const float2* grow = g + (int64_t)i * a.gny;
-            const float2* krow = slab + (int64_t)i * w;
-            for (int j = lane; j < w; j += 32) {
-                float2 gv = grow[j];
-                float2 kv = __ldg(&krow[j]);
-                A = fmaf(kv.x, gv.x, A);
-                B = fmaf(kv.y, gv.y, B);
-                C = fmaf(kv.x, gv.y, C);
-                D = fmaf(kv.y, gv.x, D);
+        for (int t = lane; t < nt; t += 4 * 32) {
+            float2 gv[4], kv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool ok = t + u * 32 < nt;
+                const int b = cube_b(j - s, oy, q, a.cg);
+                gv[u] = ok ? g[goff] : make_float2(0.f, 0.f);
+                kv[u] = ok ? __ldg(cube + arow + b) : make_float2(0.f, 0.f);
+                // advance this lane's tap by 32
+                j += 32;
+                goff += 32;
+                bool wrapped = false;
+                while (j >= w) {
+                    j -= w;
+                    ++i;
+                    goff += gny - w;
+                    wrapped = true;
+                }
+                if (wrapped && i < w) arow = cube_a(i - s, ox, q, a.cg);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                A = fmaf(kv[u].x, gv[u].x, A);
+                B = fmaf(kv[u].y, gv[u].y, B);
+                C = fmaf(kv[u].x, gv[u].y, C);
+                D = fmaf(kv[u].y, gv[u].x, D);
             }
         }
 #pragma unroll
@@ -419,6 +514,13 @@ __global__ void broadcast_kernel(const int32_t* sample_rec, const float2* rec_pr
         int32_t r = sample_rec[i];
         pred[i] = r >= 0 ? rec_pred[r] : make_float2(0.0f, 0.0f);
     }
+}
+
+CubeGeom cube_geom(const cr_wproj* wp) {
+    CubeGeom c;
+    c.s = wp->info.sampling;
+    c.magic = (1ull << 32) / (unsigned long long)c.s + 1ull;
+    return c;
 }
 
 int sm_count(cr_ctx* ctx) {
@@ -608,23 +710,31 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
                                                          radius, axis, 0, nullptr, wp->norm_d);
         note_launch(ctx, "tap_sum_kernel");
     }
-    // per-offset slabs
-    wp->slab_off_h.resize(planes);
+    // residue cubes, one per plane: Q = (S s + radius) / s + 1 residue rows
+    wp->cube_off_h.resize(planes);
+    wp->cube_q_h.resize(planes);
     int64_t total = 0;
     for (int32_t p = 0; p < planes; ++p) {
-        wp->slab_off_h[p] = total;
-        int64_t w = 2 * (int64_t)support[p] + 1;
-        total += (int64_t)axis * axis * w * w;
+        int32_t q = (support[p] * sampling + radius) / sampling + 1;
+        wp->cube_q_h[p] = q;
+        wp->cube_off_h[p] = total;
+        total += (int64_t)sampling * sampling * q * q;
     }
-    CR_CUDA_CHECK(cudaMalloc(&wp->slabs_d, (size_t)total * 8));
-    CR_CUDA_CHECK(cudaMalloc(&wp->slab_off_d, (size_t)planes * 8));
-    CR_CUDA_CHECK(cudaMemcpyAsync(wp->slab_off_d, wp->slab_off_h.data(), (size_t)planes * 8,
+    if ((int64_t)(support.back() + 1) * sampling * sampling * 4 >= (1ll << 26))
+        fail(CR_INVALID, "W-projection support too large for the kernel cube addressing");
+    if (total >= (1ll << 31)) fail(CR_INVALID, "W-projection kernel cube above 2^31 elements");
+    CR_CUDA_CHECK(cudaMalloc(&wp->cube_d, (size_t)total * 8));
+    CR_CUDA_CHECK(cudaMalloc(&wp->cube_off_d, (size_t)planes * 8));
+    CR_CUDA_CHECK(cudaMalloc(&wp->cube_q_d, (size_t)planes * 4));
+    CR_CUDA_CHECK(cudaMemcpyAsync(wp->cube_off_d, wp->cube_off_h.data(), (size_t)planes * 8,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA_CHECK(cudaMemcpyAsync(wp->cube_q_d, wp->cube_q_h.data(), (size_t)planes * 4,
                                   cudaMemcpyHostToDevice, ctx->stream));
     for (int32_t p = 0; p < planes; ++p) {
-        int64_t w = 2 * (int64_t)support[p] + 1;
-        slab_kernel<<<grid_blocks((int64_t)axis * axis * w * w, 256), 256, 0, ctx->stream>>>(
-            kernels, width, p, support[p], sampling, radius, axis, wp->slabs_d + wp->slab_off_h[p]);
-        note_launch(ctx, "slab_kernel");
+        int64_t n = (int64_t)sampling * sampling * wp->cube_q_h[p] * wp->cube_q_h[p];
+        cube_kernel<<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
+            kernels, width, p, sampling, wp->cube_q_h[p], wp->cube_d + wp->cube_off_h[p]);
+        note_launch(ctx, "cube_kernel");
     }
     // sinc axes for the image correction and the model apodisation
     {
@@ -644,7 +754,7 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
     wp->info.w_scale = w_scale;
     wp->info.max_support = *std::max_element(support.begin(), support.end());
     wp->info.kernel_width = width;
-    wp->info.slab_elements = total;
+    wp->info.cube_elements = total;
 }
 
 // ---- gridding / degridding drivers ------------------------------------------------------
@@ -671,9 +781,9 @@ void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2
     unsigned int* counter = (unsigned int*)(nitems + 1);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 4, ctx->stream));
     GridArgs a{r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum,
-               r.rec_pred, r.tile_start, r.ntx, r.nty, wp->support_d, wp->slab_off_d,
-               wp->slabs_d, wp->axis, R, item_tile, item_begin, nitems, counter, psf, dirty,
-               wp->g->info.grid_nx, wp->g->info.grid_ny};
+               r.rec_pred, r.tile_start, r.ntx, r.nty, wp->support_d, wp->cube_off_d,
+               wp->cube_q_d, wp->cube_d, cube_geom(wp), wp->radius, wp->axis, R, item_tile,
+               item_begin, nitems, counter, psf, dirty, wp->g->info.grid_nx, wp->g->info.grid_ny};
     int blocks = sm_count(ctx) * 8;
     if (mode == 0) {
         wp_grid_kernel<false><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
@@ -686,7 +796,8 @@ void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2
 
 void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* grid) {
     DegridArgs a{r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.counts, wp->support_d,
-                 wp->slab_off_d, wp->slabs_d, grid, wp->g->info.grid_ny, r.rec_pred};
+                 wp->cube_off_d, wp->cube_q_d, wp->cube_d, cube_geom(wp), wp->radius, wp->axis,
+                 grid, wp->g->info.grid_ny, r.rec_pred};
     int blocks = sm_count(ctx) * 8;
     wp_degrid_kernel<<<blocks, 256, 0, ctx->stream>>>(a);
     note_launch(ctx, "wp_degrid_kernel");

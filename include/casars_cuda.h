@@ -58,6 +58,7 @@ extern "C" {
 typedef struct cr_ctx cr_ctx;
 typedef struct cr_gridder cr_gridder;
 typedef struct cr_wproj cr_wproj;
+typedef struct cr_plan cr_plan;
 
 /* ImageGeometry (types.rs:885-930). */
 typedef struct {
@@ -80,7 +81,7 @@ typedef struct {
     double w_scale;
     int32_t max_support;
     int32_t kernel_width;     /* common cropped width */
-    int64_t slab_elements;    /* complex elements in the per-offset kernel slabs */
+    int64_t cube_elements;    /* complex elements of the per-plane residue cubes */
 } cr_wproj_info;
 
 /* VisibilityBatch (types.rs:1376-1405), structure of arrays.
@@ -179,6 +180,25 @@ int cr_degrid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batc
 int cr_grid_residual(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
                      const float* model_grid, int32_t grid_location, float* residual_grid,
                      int32_t out_location, cr_sums* sums, char** err);
+
+/* ---- materialised plans -------------------------------------------------
+ * The device form of the reference's planned taps (plan_sample,
+ * gridder.rs:3588-3624; the materialised tap plans of
+ * StandardMfsCpuExecutor, execution.rs:53-160): FP64 index selection, sort
+ * and deduplication of one batch, done once and reused by any number of
+ * gridding, degridding and residual calls while the batch's coordinates,
+ * weights and visibilities stay unchanged (a major-cycle loop).  The plan
+ * keeps no pointer to the batch. */
+int cr_plan_create(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
+                   cr_plan** out, cr_sums* sums, char** err);
+void cr_plan_destroy(cr_plan* plan);
+int cr_plan_grid_dirty(cr_ctx* ctx, cr_plan* plan, float* psf_grid, float* dirty_grid,
+                       int32_t out_location, char** err);
+int cr_plan_degrid(cr_ctx* ctx, cr_plan* plan, const float* model_grid, int32_t grid_location,
+                   float* pred, int32_t out_location, char** err);
+int cr_plan_grid_residual(cr_ctx* ctx, cr_plan* plan, const float* model_grid,
+                          int32_t grid_location, float* residual_grid, int32_t out_location,
+                          char** err);
 
 /* ---- FFT, correction, normalisation ------------------------------------
  * Centred inverse FFT (fft.rs:600-630) of a grid then crop x correction:

@@ -19,7 +19,7 @@ def setup():
     ctx = cc.Context(0)
     nx, cell = 96, 1.2e-4
     gg = cc.StandardGridder(ctx, cc.ImageGeometry(nx, nx, cell, cell))
-    gw = cc.WProjector(gg, 400.0, planes=8, sampling=8, support_law=(4, 8))
+    gw = cc.WProjector(gg, 400.0, planes=8, sampling=4, support_law=(4, 8))
     du = 1.0 / (gg.grid_shape()[0] * cell)
     rng = np.random.default_rng(12)
     u, v, w, wt, vis = random_batch(rng, 8000, gg.grid_shape()[0], du, margin=10, w_max=400.0)
@@ -45,19 +45,30 @@ def test_autograd_gradient_matches_closed_form(setup):
     assert float(err) <= 1e-5
 
 
+def chi2_f64(x, gg, b, gw):
+    pred = cc.predict(gg, b, x, gw).to(torch.complex128)
+    r = b.visibility.to(torch.complex128) - pred
+    return float(torch.sum(b.weight.to(torch.float64) * (r.real ** 2 + r.imag ** 2)))
+
+
 def test_finite_differences(setup):
+    """chi^2 is quadratic in the image, so central differences are exact up
+    to rounding; start near the truth so chi^2 itself stays small."""
     ctx, gg, gw, b, nx = setup
     rng = np.random.default_rng(1)
-    x0 = torch.as_tensor(rng.uniform(0, 0.1, (nx, nx)).astype(np.float32), device="cuda")
+    truth = np.zeros((nx, nx), np.float32)
+    truth[40, 50] = 1.0
+    truth[60, 30] = 0.5
+    x0 = torch.as_tensor(truth + rng.uniform(0, 0.01, (nx, nx)).astype(np.float32), device="cuda")
     g = AG.chi2_gradient(x0, gg, b, gw)
-    h = 1e-2
-    for k in range(16):
+    h = 0.25
+    for k in range(64):
         i, j = rng.integers(0, nx, 2)
         xp, xm = x0.clone(), x0.clone()
         xp[i, j] += h
         xm[i, j] -= h
-        fd = (float(AG.chi2(xp, gg, b, gw)) - float(AG.chi2(xm, gg, b, gw))) / (2 * h)
-        assert abs(fd - float(g[i, j])) <= 2e-3 * max(1.0, abs(float(g[i, j])))
+        fd = (chi2_f64(xp, gg, b, gw) - chi2_f64(xm, gg, b, gw)) / (2 * h)
+        assert abs(fd - float(g[i, j])) <= 1e-3 * max(1.0, abs(float(g[i, j])))
 
 
 def test_projected_gradient_descends(setup):
