@@ -15,6 +15,9 @@
 // block reduces all candidates to the same global peak.  The kernel is
 // launched cooperatively (all blocks resident); the barrier's wait is bounded
 // and reports CR_TIMEOUT instead of spinning forever.
+#include <cstring>
+#include <mutex>
+
 #include "cr_internal.cuh"
 
 namespace cr {
@@ -305,3 +308,135 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
 }
 
 }  // namespace cr
+
+// ---- allocation-free variant ------------------------------------------------------
+//
+// For callers that must not allocate device memory once they are running:
+// a host that reserved its device memory up front (a fixed arena or budget
+// handed to it by a resource manager) and forbids allocations afterwards,
+// or a process in which another allocator already holds nearly all device
+// memory, so that a new cudaMalloc could fail or stall the device in the
+// middle of a minor cycle.  This entry point runs the same Hogbom kernel
+// with its scratch (grid-barrier words, per-block peak candidates and the
+// component list) in a fixed array in this library's device memory, which
+// every GPU that loads the library holds until the process exits.
+// Inputs and outputs stay the caller's device buffers.
+
+namespace cr {
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 1024;
+constexpr long long kNoAllocMaxComponents = 16384;
+constexpr size_t kNoAllocHeader = 256;  // barrier words and result scalars
+constexpr size_t kNoAllocCands = (size_t)2 * kNoAllocMaxBlocks * sizeof(Cand);
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocCands + (size_t)kNoAllocMaxComponents * 16;
+
+// 295,168 bytes per device: header, candidates, then x, y, peak and flux of
+// up to kNoAllocMaxComponents components.
+static __device__ __align__(256) unsigned char g_hogbom_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 256;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array for the current device, looked up once
+// per device (the caller has made `device` current).
+void* scratch_address(int device) {
+    if (device < 0 || device >= kMaxDevices) fail(CR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[device]) {
+        void* p = nullptr;
+        check_cuda(cudaGetSymbolAddress(&p, g_hogbom_scratch), "cudaGetSymbolAddress");
+        g_scratch_addr[device] = p;
+    }
+    return g_scratch_addr[device];
+}
+
+void hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                    const uint8_t* mask, int32_t nx, int32_t ny, float gain, float threshold,
+                    float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                    int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                    float* comp_flux, int64_t* actual, int64_t* reported,
+                    int32_t* stop_reason_out) {
+    if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
+    if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
+    if (cycle_niter < 0) fail(CR_INVALID, "cycle_niter is negative");
+    long long budget = inclusive ? cycle_niter + 1 : cycle_niter;
+    if (budget > kNoAllocMaxComponents)
+        fail(CR_INVALID, "cr_hogbom_noalloc: the component budget (cycle_niter, plus one when "
+                         "inclusive) exceeds its fixed scratch of 16384 components");
+    CR_CUDA_CHECK(cudaSetDevice(ctx->device));
+    char* base = (char*)scratch_address(ctx->device);
+    int sms = 0, per_sm = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hogbom_kernel,
+                                                                kHogThreads, 0));
+    if (per_sm < 1) fail(CR_CUDA, "Hogbom kernel cannot be resident");
+    int64_t npix = (int64_t)nx * ny;
+    int blocks = (int)std::min<int64_t>((int64_t)sms * std::min(per_sm, 2),
+                                        std::max<int64_t>(1, (npix + kHogThreads - 1) / kHogThreads));
+    blocks = std::min(blocks, kNoAllocMaxBlocks);
+    unsigned int* bar = (unsigned int*)base;
+    long long* out_actual = (long long*)(base + 16);
+    int* out_stop = (int*)(base + 24);
+    int* out_status = (int*)(base + 28);
+    Cand* cands = (Cand*)(base + kNoAllocHeader);
+    int* cx = (int*)(base + kNoAllocHeader + kNoAllocCands);
+    int* cy = cx + kNoAllocMaxComponents;
+    float* cp = (float*)(cy + kNoAllocMaxComponents);
+    float* cf = cp + kNoAllocMaxComponents;
+    // the array keeps the previous call's contents: the barrier and the
+    // result words must start at zero
+    CR_CUDA_CHECK(cudaMemsetAsync(base, 0, kNoAllocHeader, ctx->stream));
+    HogArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
+              nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual, out_stop,
+              out_status};
+    void* args[] = {&a};
+    CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_kernel, dim3(blocks), dim3(kHogThreads),
+                                              args, 0, ctx->stream));
+    note_launch(ctx, "hogbom_kernel");
+    struct {
+        long long actual;
+        int stop, status;
+    } h;
+    CR_CUDA_CHECK(cudaMemcpyAsync(&h, out_actual, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (h.status) fail(CR_TIMEOUT, "Hogbom grid barrier timed out");
+    if (comp_x && h.actual > 0) {
+        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+    }
+    if (actual) *actual = h.actual;
+    if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
+    if (stop_reason_out) *stop_reason_out = h.stop;
+}
+
+}  // namespace
+}  // namespace cr
+
+extern "C" int cr_hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                                 const uint8_t* mask, int32_t nx, int32_t ny, float gain,
+                                 float threshold, float cycle_threshold, float nsigma_threshold,
+                                 int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
+                                 int32_t* comp_y, float* comp_peak, float* comp_flux,
+                                 int64_t* actual, int64_t* reported, int32_t* stop_reason,
+                                 char** err) {
+    if (err) *err = nullptr;
+    try {
+        if (!ctx || !model || !residual || !psf) cr::fail(CR_INVALID, "null argument");
+        if (!comp_x != !comp_y || !comp_x != !comp_peak || !comp_x != !comp_flux)
+            cr::fail(CR_INVALID, "component arrays must be all given or all null");
+        cr::hogbom_noalloc(ctx, model, residual, psf, mask, nx, ny, gain, threshold,
+                           cycle_threshold, nsigma_threshold, cycle_niter, inclusive, comp_x,
+                           comp_y, comp_peak, comp_flux, actual, reported, stop_reason);
+        return CR_OK;
+    } catch (const cr::Error& e) {
+        if (err) *err = strdup(e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        if (err) *err = strdup(e.what());
+        return CR_INVALID;
+    }
+}

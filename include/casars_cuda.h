@@ -259,6 +259,33 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf,
               float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
               int32_t* stop_reason, char** err);
 
+/* ---- allocation-free Hogbom minor cycle ----------------------------------
+ * No counterpart in the reference.  The same minor cycle as cr_hogbom for
+ * callers that may not allocate device memory once they run: for example a
+ * host that reserved a fixed device-memory budget at start-up and forbids
+ * further allocation, or a process in which another allocator holds nearly
+ * all device memory, so a cudaMalloc could fail or stall the device in the
+ * middle of a deconvolution loop.  It calls no cudaMalloc, cudaFree or
+ * allocating library routine.  model, residual, psf and mask are DEVICE
+ * buffers (model and residual updated in place); the component arrays are
+ * host memory, as in cr_hogbom.
+ *
+ * Its scratch (barrier words, per-block peak candidates and the component
+ * list) is one fixed 295,168-byte array in the library's device memory, which
+ * every GPU that loads the library holds until the process exits.  Limit:
+ * at most 16384 components per call (cycle_niter, plus one when inclusive);
+ * a larger budget is rejected with CR_INVALID.  The first call on a device
+ * looks up the array's device address (once per device, with that device
+ * current); make that first call before any stream capture.  Every call on
+ * a device shares the one array: calls that overlap on the GPU (other
+ * streams, contexts or threads) race and must be serialised by the caller. */
+int cr_hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                      const uint8_t* mask, int32_t nx, int32_t ny, float gain, float threshold,
+                      float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                      int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                      float* comp_flux, int64_t* actual, int64_t* reported,
+                      int32_t* stop_reason, char** err);
+
 #ifdef __cplusplus
 }
 #endif
