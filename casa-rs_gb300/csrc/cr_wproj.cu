@@ -17,12 +17,14 @@
 // L2, where per-offset copies of the taps would not.
 //
 // Gridding is output-stationary: a block owns a 32 x 32 tile of the grid in
-// registers (each of 8 warps owns 4 rows, each lane one column), streams the
+// registers (each of 8 warps owns a band of 4 rows, each lane one column),
+// streams the
 // deduplicated records whose windows can reach the tile, and adds
 // value * kernel for every owned cell inside a record's window.  The tile is
 // flushed once per work item with FP32 atomics.  Degridding is a gather: a
-// warp per record walks the record's (2S+1)^2 taps as one flat index, so
-// every lane carries a tap, and reduces with warp shuffles.
+// warp per record takes the window's rows in pairs, 16 lanes per row, with
+// the cube column addresses held in registers, and reduces with warp
+// shuffles.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -352,9 +354,12 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
                 s_rowa[qn][rr] = (i >= 0 && i < en.w) ? cube_a(i - en.s, en.ox, en.q, a.cg) : -1;
             }
             __syncthreads();
-            // 2. accumulate the entries into the register tile
+            // 2. accumulate the entries into the register tile; warp w owns
+            // rows 4w .. 4w+3 and skips entries whose window misses them
+            const int band0 = warp * kRowsPerWarp;
             for (int qn = 0; qn < nlist; ++qn) {
                 const Entry& en = s_list[qn];
+                if (band0 > en.w - 1 - en.ra || band0 + kRowsPerWarp - 1 < -en.ra) continue;
                 const int col = en.cb + lane;
                 const bool colok = (unsigned)col < (unsigned)en.w;
                 const int bcol = colok ? cube_b(col - en.s, en.oy, en.q, a.cg) : 0;
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
                 bool ok[kRowsPerWarp];
 #pragma unroll
                 for (int k = 0; k < kRowsPerWarp; ++k) {
-                    const int av = s_rowa[qn][warp + k * (kGridThreads / 32)];
+                    const int av = s_rowa[qn][band0 + k];
                     ok[k] = av >= 0 && colok;
                     kv[k] = ok[k] ? __ldg(cube + av) : make_float2(0.f, 0.f);
                 }
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
         // 3. flush the tile
 #pragma unroll
         for (int k = 0; k < kRowsPerWarp; ++k) {
-            int64_t x = x0 + warp + k * (kGridThreads / 32);
+            int64_t x = x0 + warp * kRowsPerWarp + k;
             int64_t y = y0 + lane;
             if (x < a.gnx && y < a.gny) {
                 int64_t cell = x * a.gny + y;
@@ -444,11 +449,74 @@ struct DegridArgs {
     float2* pred;
 };
 
-// One warp per record; lane l takes taps l, l+32, ... of the flattened
-// (2S+1)^2 window, tracking its (row, column) incrementally, four taps per
-// step so that eight loads are in flight.
+// Rows of one record's window in pairs (lanes 0-15 row i, lanes 16-31 row
+// i+1), 16-lane column chunks whose cube column addresses stay in registers
+// for the whole record; NCH chunks cover windows up to 16*NCH wide.
+template <int NCH>
+__device__ __forceinline__ void degrid_rows(const float2* g, const float2* cube, int gny, int s,
+                                            int w, int ox, int oy, int q, const CubeGeom& cg,
+                                            int half, int hl, float& A, float& B, float& C,
+                                            float& D) {
+    int bcol[NCH];
+#pragma unroll
+    for (int c = 0; c < NCH; ++c) {
+        const int j = hl + 16 * c;
+        bcol[c] = j < w ? cube_b(j - s, oy, q, cg) : -1;
+    }
+    for (int i = half; i < w; i += 2) {
+        const float2* grow = g + (int64_t)i * gny + hl;
+        const float2* krow = cube + cube_a(i - s, ox, q, cg);
+        float2 gv[NCH], kv[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            const bool ok = bcol[c] >= 0;
+            gv[c] = ok ? grow[16 * c] : make_float2(0.f, 0.f);
+            kv[c] = ok ? __ldg(krow + bcol[c]) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            A = fmaf(kv[c].x, gv[c].x, A);
+            B = fmaf(kv[c].y, gv[c].y, B);
+            C = fmaf(kv[c].x, gv[c].y, C);
+            D = fmaf(kv[c].y, gv[c].x, D);
+        }
+    }
+}
+
+// Any window: lane l takes taps l, l+32, ... of the flattened (2S+1)^2
+// window, tracking its (row, column) incrementally.
+__device__ void degrid_flat(const float2* g, const float2* cube, int gny, int s, int w, int ox,
+                            int oy, int q, const CubeGeom& cg, int lane, float& A, float& B,
+                            float& C, float& D) {
+    const int nt = w * w;
+    int i = lane / w, j = lane - (lane / w) * w;
+    int goff = i * gny + j;
+    int arow = cube_a(i - s, ox, q, cg);
+    for (int t = lane; t < nt; t += 32) {
+        const float2 gv = g[goff];
+        const float2 kv = __ldg(cube + arow + cube_b(j - s, oy, q, cg));
+        A = fmaf(kv.x, gv.x, A);
+        B = fmaf(kv.y, gv.y, B);
+        C = fmaf(kv.x, gv.y, C);
+        D = fmaf(kv.y, gv.x, D);
+        j += 32;
+        goff += 32;
+        bool wrapped = false;
+        while (j >= w) {
+            j -= w;
+            ++i;
+            goff += gny - w;
+            wrapped = true;
+        }
+        if (wrapped && i < w) arow = cube_a(i - s, ox, q, cg);
+    }
+}
+
+// One warp per record: sum conj(cwt) * grid over the window
+// (degrid_sample_planned, gridder.rs:3726-3747), then warp shuffles.
 __global__ void __launch_bounds__(256) wp_degrid_kernel(DegridArgs a) {
     const int lane = threadIdx.x & 31;
+    const int half = lane >> 4, hl = lane & 15;
     const int64_t nrec = (int64_t)a.counts[2];
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int gny = (int)a.gny;
@@ -462,38 +530,24 @@ __global__ void __launch_bounds__(256) wp_degrid_kernel(DegridArgs a) {
         const int ox = off / a.axis - a.radius, oy = off % a.axis - a.radius;
         const float2* cube = a.cube + a.cube_off[plane];
         const float2* g = a.grid + (int64_t)(a.rx[r] - s) * a.gny + (a.ry[r] - s);
-        const int nt = w * w;
-        int i = lane / w, j = lane - (lane / w) * w;
-        int goff = i * gny + j;
-        int arow = cube_a(i - s, ox, q, a.cg);
         float A = 0.f, B = 0.f, C = 0.f, D = 0.f;
-        for (int t = lane; t < nt; t += 4 * 32) {
-            float2 gv[4], kv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const bool ok = t + u * 32 < nt;
-                const int b = cube_b(j - s, oy, q, a.cg);
-                gv[u] = ok ? g[goff] : make_float2(0.f, 0.f);
-                kv[u] = ok ? __ldg(cube + arow + b) : make_float2(0.f, 0.f);
-                // advance this lane's tap by 32
-                j += 32;
-                goff += 32;
-                bool wrapped = false;
-                while (j >= w) {
-                    j -= w;
-                    ++i;
-                    goff += gny - w;
-                    wrapped = true;
-                }
-                if (wrapped && i < w) arow = cube_a(i - s, ox, q, a.cg);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                A = fmaf(kv[u].x, gv[u].x, A);
-                B = fmaf(kv[u].y, gv[u].y, B);
-                C = fmaf(kv[u].x, gv[u].y, C);
-                D = fmaf(kv[u].y, gv[u].x, D);
-            }
+        switch ((w + 15) >> 4) {
+#define CR_DEGRID_CASE(N) \
+    case N:               \
+        degrid_rows<N>(g, cube, gny, s, w, ox, oy, q, a.cg, half, hl, A, B, C, D); \
+        break;
+            CR_DEGRID_CASE(1)
+            CR_DEGRID_CASE(2)
+            CR_DEGRID_CASE(3)
+            CR_DEGRID_CASE(4)
+            CR_DEGRID_CASE(5)
+            CR_DEGRID_CASE(6)
+            CR_DEGRID_CASE(7)
+            CR_DEGRID_CASE(8)
+            CR_DEGRID_CASE(9)
+#undef CR_DEGRID_CASE
+            default:
+                degrid_flat(g, cube, gny, s, w, ox, oy, q, a.cg, lane, A, B, C, D);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
