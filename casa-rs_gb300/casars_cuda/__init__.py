@@ -5,3 +5,4 @@ from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, Psf
                       StandardGridder, VisibilityBatch, WProjector, adjoint, apply_weighting,
                       degrid, dirty_image, grid_dirty, grid_residual, grid_to_image,
                       image_to_grid, predict, residual_image, run_hogbom_minor_cycle)
+from .clean import CleanConfig, CleanResult, clean_cycle_threshold, run_cotton_schwab  # noqa: F401

@@ -43,7 +43,7 @@ class VisBatch(C.Structure):
 
 class Sums(C.Structure):
     _fields_ = [("normalization_sumwt", _d), ("reported_sumwt", _d), ("gridded", _i64),
-                ("skipped", _i64), ("unique_records", _i64)]
+                ("skipped", _i64), ("unique_records", _i64), ("taps", _i64)]
 
 
 class PsfState(C.Structure):
@@ -52,7 +52,7 @@ class PsfState(C.Structure):
 
 class Timings(C.Structure):
     _fields_ = [("plan_ms", _f), ("grid_ms", _f), ("degrid_ms", _f), ("fft_ms", _f),
-                ("other_ms", _f)]
+                ("other_ms", _f), ("grid_kernel_ms", _f), ("degrid_kernel_ms", _f)]
 
 
 # name -> (restype, argtypes); the exported symbol set checked by the tests
@@ -85,6 +85,8 @@ SIGNATURES = {
     "cr_plan_grid_dirty": (C.c_int, [_p, _p, _p, _p, _i32, _err]),
     "cr_plan_degrid": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
     "cr_plan_grid_residual": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
+    "cr_plan_residual_image": (C.c_int, [_p, _p, _p, _i32, C.POINTER(PsfState), _p, _i32,
+                                         _err]),
     "cr_grid_to_image": (C.c_int, [_p, _p, _p, _p, _i32, _f, _p, _i32, _err]),
     "cr_image_to_grid": (C.c_int, [_p, _p, _p, _p, _i32, _p, _i32, _err]),
     "cr_dirty_image": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _p, _i32,

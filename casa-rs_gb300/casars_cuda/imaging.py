@@ -199,11 +199,12 @@ class GridSums:
     gridded_samples: int
     skipped_samples: int
     unique_records: int
+    taps: int = 0
 
     @staticmethod
     def from_c(s: _lib.Sums) -> "GridSums":
         return GridSums(s.normalization_sumwt, s.reported_sumwt, int(s.gridded), int(s.skipped),
-                        int(s.unique_records))
+                        int(s.unique_records), int(s.taps))
 
 
 @dataclass
@@ -440,6 +441,19 @@ class Plan:
                                  torch.complex64 if torch else None)
         call("cr_plan_grid_residual", self.gridder.ctx.handle, self._h, mp,
              arrs.location if arrs.location is not None else CR_HOST, op, loc)
+        return out
+
+    def residual_image(self, model, psf_state: "PsfState"):
+        """The major-cycle residual refresh (compute_residual, lib.rs:68560-68620
+        standard, 70592-70644 W-projection) over this plan's records."""
+        geom = self.gridder.geometry
+        arrs = _Arrays()
+        mp = arrs.ptr(model, np.float32, torch.float32 if torch else None, (geom.nx, geom.ny))
+        out, op, loc = self._out((geom.nx, geom.ny), np.float32,
+                                 torch.float32 if torch else None)
+        st = psf_state.to_c()
+        call("cr_plan_residual_image", self.gridder.ctx.handle, self._h, mp,
+             arrs.location if arrs.location is not None else CR_HOST, C.byref(st), op, loc)
         return out
 
 

@@ -44,7 +44,7 @@ void need(bool c, const char* what) {
 struct StageTimer {
     cr_ctx* ctx;
     int n = 0;
-    explicit StageTimer(cr_ctx* c) : ctx(c) {}
+    explicit StageTimer(cr_ctx* c) : ctx(c) { ctx->kev_used = 0; }
     void mark() {
         if (n < 8) CR_CUDA_CHECK(cudaEventRecord(ctx->ev[n++], ctx->stream));
     }
@@ -56,6 +56,19 @@ struct StageTimer {
         return ms;
     }
 };
+
+// Stage times of a call plus the bracketed kernel times recorded during it.
+void set_timings(cr_ctx* ctx, cr_timings t) {
+    for (int k = 0; k < 2; ++k) {
+        if (!(ctx->kev_used & (1 << k))) continue;
+        float ms = 0.0f;
+        CR_CUDA_CHECK(cudaEventSynchronize(ctx->kev[2 * k + 1]));
+        CR_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->kev[2 * k], ctx->kev[2 * k + 1]));
+        (k == 0 ? t.grid_kernel_ms : t.degrid_kernel_ms) = ms;
+    }
+    ctx->kev_used = 0;
+    ctx->timings = t;
+}
 
 void bind(cr_ctx* ctx) { CR_CUDA_CHECK(cudaSetDevice(ctx->device)); }
 
@@ -121,6 +134,7 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
         CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
         c->stream = c->own_stream;
         for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
+        for (auto& e : c->kev) CR_CUDA_CHECK(cudaEventCreate(&e));
         CR_CUDA_CHECK(cudaMallocHost(&c->pinned, 4096));
         *out = c;
     });
@@ -135,6 +149,8 @@ void cr_ctx_destroy(cr_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->fft_plans) cufftDestroy(kv.second);
     for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->kev)
         if (e) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -310,7 +326,7 @@ int cr_grid_dirty(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* 
         cr_sums s{};
         read_sums(ctx, r, &s);
         if (sums) *sums = s;
-        ctx->timings = cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, 0.f, 0.f};
+        set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, 0.f, 0.f});
     });
 }
 
@@ -334,7 +350,7 @@ int cr_degrid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batc
         tm.mark();
         if (out_location == CR_HOST) copy_out(ctx, pred, out, (size_t)b.n * 8, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-        ctx->timings = cr_timings{tm.between(0, 1), 0.f, tm.between(1, 2), 0.f, 0.f};
+        set_timings(ctx, cr_timings{tm.between(0, 1), 0.f, tm.between(1, 2), 0.f, 0.f});
     });
 }
 
@@ -451,7 +467,7 @@ int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         if (state) *state = cr_psf_state{peak, sumwt_f, (float)s.reported_sumwt};
-        ctx->timings = cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, tm.between(2, 3), 0.f};
+        set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, tm.between(2, 3), 0.f});
     });
 }
 
@@ -554,7 +570,7 @@ int cr_plan_create(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
             throw;
         }
         if (sums) *sums = p->sums;
-        ctx->timings = cr_timings{tm.between(0, 1), 0.f, 0.f, 0.f, 0.f};
+        set_timings(ctx, cr_timings{tm.between(0, 1), 0.f, 0.f, 0.f, 0.f});
         *out = p;
     });
 }
@@ -585,7 +601,7 @@ int cr_plan_grid_dirty(cr_ctx* ctx, cr_plan* p, float* psf_grid, float* dirty_gr
             copy_out(ctx, psf_grid, psf, gb, CR_HOST);
             copy_out(ctx, dirty_grid, dirty, gb, CR_HOST);
         }
-        ctx->timings = cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f};
+        set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f});
     });
 }
 
@@ -605,7 +621,7 @@ int cr_plan_degrid(cr_ctx* ctx, cr_plan* p, const float* model_grid, int32_t gri
         broadcast_pred(ctx, p->rec, out);
         tm.mark();
         if (out_location == CR_HOST) copy_out(ctx, pred, out, n * 8, CR_HOST);
-        ctx->timings = cr_timings{0.f, 0.f, tm.between(0, 1), 0.f, 0.f};
+        set_timings(ctx, cr_timings{0.f, 0.f, tm.between(0, 1), 0.f, 0.f});
     });
 }
 
@@ -629,6 +645,39 @@ int cr_plan_grid_residual(cr_ctx* ctx, cr_plan* p, const float* model_grid,
         grid_records(ctx, p->g, p->wp, p->rec, nullptr, res, 1);
         if (out_location == CR_HOST) copy_out(ctx, residual_grid, res, gb, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_plan_residual_image(cr_ctx* ctx, cr_plan* p, const float* model, int32_t model_location,
+                           const cr_psf_state* state, float* residual_out, int32_t out_location,
+                           char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && p != nullptr && p->ctx == ctx, "plan belongs to another context");
+        need(model != nullptr && state != nullptr, "null argument");
+        need(state->normalization_sumwt > 0.0f && state->psf_peak > 0.0f, "invalid PSF state");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        const size_t gb = grid_bytes(p->g);
+        const size_t np = image_pixels(p->g);
+        const float* m = (const float*)device_input(ctx, model, np * 4, model_location, "model");
+        float2* mgrid = (float2*)workspace(ctx, "ri_model_grid", gb);
+        image_to_grid(ctx, p->g, p->wp, m, mgrid);
+        tm.mark();
+        degrid_records(ctx, p->g, p->wp, p->rec, mgrid);
+        tm.mark();
+        float2* res = (float2*)workspace(ctx, "ri_residual_grid", gb);
+        CR_CUDA_CHECK(cudaMemsetAsync(res, 0, gb, ctx->stream));
+        grid_records(ctx, p->g, p->wp, p->rec, nullptr, res, 1);
+        tm.mark();
+        float* img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "ri_image");
+        const float k = p->wp ? 2.0f : 1.0f;
+        grid_to_image(ctx, p->g, p->wp, res, k / state->normalization_sumwt, img);
+        scale_image(ctx, img, (int64_t)np, 1.0f / state->psf_peak, nullptr);
+        tm.mark();
+        if (out_location == CR_HOST) copy_out(ctx, residual_out, img, np * 4, CR_HOST);
+        set_timings(ctx, cr_timings{0.f, tm.between(2, 3), tm.between(1, 2),
+                                  tm.between(0, 1) + tm.between(3, 4), 0.f});
     });
 }
 

@@ -47,6 +47,11 @@ void note_launch(cr_ctx* ctx, const char* what) {
     ctx->launches++;
 }
 
+void kernel_mark(cr_ctx* ctx, int which, bool end) {
+    CR_CUDA_CHECK(cudaEventRecord(ctx->kev[which * 2 + (end ? 1 : 0)], ctx->stream));
+    if (end) ctx->kev_used |= 1 << which;
+}
+
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny) {
     auto key = std::make_pair(nx, ny);
     auto it = ctx->fft_plans.find(key);

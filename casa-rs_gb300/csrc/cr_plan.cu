@@ -246,11 +246,14 @@ struct RecArgs {
     const float* sumwt;
     const float2* vis;
     uint32_t* tile_of;
+    const int32_t* support;   // per plane (W-projection); null: 7 x 7 standard taps
 };
 
 // Record fields decoded from the head key of each run.
+// Also counts the taps one grid pass applies (counts[3]).
 __global__ void records_init(RecArgs a) {
     int64_t nv = (int64_t)a.counts[0];
+    unsigned long long taps = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (!a.flags[i]) continue;
@@ -278,7 +281,14 @@ __global__ void records_init(RecArgs a) {
         a.ry[r] = (int32_t)((tile % (uint64_t)a.nty) * 32 + cy);
         a.vsum[r] = make_double2(0.0, 0.0);
         a.wsum[r] = 0.0;
+        const unsigned long long side =
+            a.support ? 2ull * (unsigned long long)a.support[a.ra[r]] + 1ull : 7ull;
+        taps += side * side;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) taps += __shfl_xor_sync(0xffffffffu, taps, o);
+    if ((threadIdx.x & 31) == 0 && taps)
+        atomicAdd(const_cast<unsigned long long*>(&a.counts[3]), taps);
 }
 
 // Sums of weight * vis per record: a warp-level segmented reduction over the
@@ -379,7 +389,7 @@ Records allocate_records(cr_ctx* ctx, int64_t n, int64_t ntx, int64_t nty, Pool*
 }
 
 void finish_records(cr_ctx* ctx, Records& r, int mode, int key_bits, int plane_bits,
-                    int off_bits, const DeviceBatch& b) {
+                    int off_bits, const DeviceBatch& b, const int32_t* support) {
     const int64_t n = r.n_samples;
     const unsigned T = 256;
     radix_sort_pairs(ctx, r.keys, r.order, n, key_bits);
@@ -394,7 +404,7 @@ void finish_records(cr_ctx* ctx, Records& r, int mode, int key_bits, int plane_b
     exclusive_scan_u32(ctx, flags, excl, n, r.counts + 2);
     RecArgs a{r.keys, r.order, flags, excl, r.counts, n, mode, plane_bits, off_bits, r.nty,
               r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum,
-              r.sample_rec, b.weight, b.sumwt_factor, b.vis, tile_of};
+              r.sample_rec, b.weight, b.sumwt_factor, b.vis, tile_of, support};
     if (n > 0) {
         records_init<<<grid_blocks(n, T), T, 0, ctx->stream>>>(a);
         note_launch(ctx, "records_init");
@@ -431,7 +441,7 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) 
         wp_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
         note_launch(ctx, "wp_plan_kernel");
     }
-    finish_records(ctx, r, 0, key_bits, plane_bits, off_bits, b);
+    finish_records(ctx, r, 0, key_bits, plane_bits, off_bits, b, wp->support_d);
     return r;
 }
 
@@ -449,7 +459,7 @@ Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* po
         std_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
         note_launch(ctx, "std_plan_kernel");
     }
-    finish_records(ctx, r, 1, key_bits, 0, 0, b);
+    finish_records(ctx, r, 1, key_bits, 0, 0, b, nullptr);
     return r;
 }
 
@@ -465,6 +475,7 @@ void read_sums(cr_ctx* ctx, const Records& r, cr_sums* out) {
     out->gridded = (int64_t)host->c[0];
     out->skipped = (int64_t)host->c[1];
     out->unique_records = (int64_t)host->c[2];
+    out->taps = (int64_t)host->c[3];
     out->normalization_sumwt = host->s[0];
     out->reported_sumwt = host->s[1];
 }

@@ -185,6 +185,7 @@ void std_grid(cr_ctx* ctx, cr_gridder* g, const Records& r, float2* psf, float2*
                   counter, psf, dirty, g->info.grid_nx, g->info.grid_ny};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    kernel_mark(ctx, 0, false);
     if (mode == 0) {
         std_grid_kernel<false><<<sms * 4, kStdThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "std_grid_kernel");
@@ -192,6 +193,7 @@ void std_grid(cr_ctx* ctx, cr_gridder* g, const Records& r, float2* psf, float2*
         std_grid_kernel<true><<<sms * 4, kStdThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "std_grid_kernel_residual");
     }
+    kernel_mark(ctx, 0, true);
 }
 
 void std_degrid(cr_ctx* ctx, cr_gridder* g, const Records& r, const float2* grid) {
@@ -199,8 +201,10 @@ void std_degrid(cr_ctx* ctx, cr_gridder* g, const Records& r, const float2* grid
                     g->info.grid_ny, r.rec_pred};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    kernel_mark(ctx, 1, false);
     std_degrid_kernel<<<sms * 8, 256, 0, ctx->stream>>>(a);
     note_launch(ctx, "std_degrid_kernel");
+    kernel_mark(ctx, 1, true);
 }
 
 }  // namespace cr

@@ -839,6 +839,7 @@ void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2
                wp->cube_q_d, wp->cube_d, cube_geom(wp), wp->radius, wp->axis, R, item_tile,
                item_begin, nitems, counter, psf, dirty, wp->g->info.grid_nx, wp->g->info.grid_ny};
     int blocks = sm_count(ctx) * 8;
+    kernel_mark(ctx, 0, false);
     if (mode == 0) {
         wp_grid_kernel<false><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "wp_grid_kernel");
@@ -846,6 +847,7 @@ void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2
         wp_grid_kernel<true><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "wp_grid_kernel_residual");
     }
+    kernel_mark(ctx, 0, true);
 }
 
 void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* grid) {
@@ -853,8 +855,10 @@ void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* gri
                  wp->cube_off_d, wp->cube_q_d, wp->cube_d, cube_geom(wp), wp->radius, wp->axis,
                  grid, wp->g->info.grid_ny, r.rec_pred};
     int blocks = sm_count(ctx) * 8;
+    kernel_mark(ctx, 1, false);
     wp_degrid_kernel<<<blocks, 256, 0, ctx->stream>>>(a);
     note_launch(ctx, "wp_degrid_kernel");
+    kernel_mark(ctx, 1, true);
 }
 
 void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred) {

@@ -106,6 +106,8 @@ typedef struct {
     int64_t gridded;
     int64_t skipped;
     int64_t unique_records;   /* distinct (cell, offset, plane, sign) keys gridded */
+    int64_t taps;             /* kernel taps one grid pass applies: sum over records of the
+                                 footprint (2S+1)^2 (49 for the standard gridder) */
 } cr_sums;
 
 /* PsfState essentials (lib.rs:64680-64690). */
@@ -115,9 +117,12 @@ typedef struct {
     float reported_sumwt;
 } cr_psf_state;
 
-/* Per-stage device times of the last call, milliseconds (CUDA events). */
+/* Per-stage device times of the last call, milliseconds (CUDA events);
+ * grid_kernel_ms / degrid_kernel_ms bracket the gridding / degridding kernel
+ * launch alone (0 when the call launched none). */
 typedef struct {
     float plan_ms, grid_ms, degrid_ms, fft_ms, other_ms;
+    float grid_kernel_ms, degrid_kernel_ms;
 } cr_timings;
 
 /* ---- context -------------------------------------------------------------
@@ -199,6 +204,15 @@ int cr_plan_degrid(cr_ctx* ctx, cr_plan* plan, const float* model_grid, int32_t 
 int cr_plan_grid_residual(cr_ctx* ctx, cr_plan* plan, const float* model_grid,
                           int32_t grid_location, float* residual_grid, int32_t out_location,
                           char** err);
+/* The major-cycle residual refresh of run_hogbom_cotton_schwab
+ * (lib.rs:59354-59636 calls it through refresh_residual; the refresh is
+ * compute_residual, lib.rs:68560-68620 standard, 70592-70644 W-projection):
+ * model image -> apodise + centred forward FFT -> degrid -> residual
+ * gridding -> centred inverse FFT + correction -> x k/sumwt (k = 2 for
+ * W-projection) -> / psf_peak, over the plan's materialised records. */
+int cr_plan_residual_image(cr_ctx* ctx, cr_plan* plan, const float* model,
+                           int32_t model_location, const cr_psf_state* state,
+                           float* residual_out, int32_t out_location, char** err);
 
 /* ---- FFT, correction, normalisation ------------------------------------
  * Centred inverse FFT (fft.rs:600-630) of a grid then crop x correction:

@@ -530,3 +530,115 @@ def hogbom(residual, psf, gain, niter, threshold=0.0, cycle_threshold=0.0,
 
 def radians_from_arcsec(a: float) -> float:
     return a / 3600.0 * math.pi / 180.0
+
+
+# --------------------------------------------------------------------------
+# Cotton-Schwab major/minor controller
+# --------------------------------------------------------------------------
+def threshold_reached_with_tolerance(peak_abs: float, threshold: float) -> bool:
+    """threshold_reached_with_tolerance (lib.rs:74628-74635), float32."""
+    f32 = np.float32
+    p, t = f32(peak_abs), f32(threshold)
+    if t <= 0:
+        return bool(p <= t)
+    tol = max(f32(0.01) * t, f32(2.0e-8))
+    return bool(p <= t or abs(p - t) <= tol)
+
+
+def tolerant_clean_stop_reason(peak_abs, threshold, nsigma_threshold):
+    """tolerant_clean_stop_reason (lib.rs:74637-74651)."""
+    if threshold_reached_with_tolerance(peak_abs, threshold):
+        return "GlobalThresholdReached"
+    if nsigma_threshold > threshold and threshold_reached_with_tolerance(peak_abs,
+                                                                         nsigma_threshold):
+        return "NsigmaThresholdReached"
+    return None
+
+
+def clean_cycle_threshold(peak, sidelobe, cyclefactor, min_frac, max_frac, threshold) -> float:
+    """clean_cycle_threshold (lib.rs:74120-74127), float32."""
+    f32 = np.float32
+    frac = min(max(f32(sidelobe) * f32(cyclefactor), f32(min_frac)), f32(max_frac))
+    return float(max(f32(peak) * f32(frac), f32(threshold)))
+
+
+_STOP_NAMES = {0: None, 1: "GlobalThresholdReached", 2: "CycleThresholdReached",
+               3: "NsigmaThresholdReached", 4: "NoCleanablePixels"}
+
+
+def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000,
+                  cyclefactor=1.0, min_psf_fraction=0.05, max_psf_fraction=0.8,
+                  major_cycle_limit=None, sidelobe=0.0, inclusive=True):
+    """run_hogbom_cotton_schwab (lib.rs:59354-59636) without mask and n-sigma
+    threshold.  `refresh(model) -> residual` is the measured major cycle.
+    Returns a dict with model, residual, major cycles, iterations, the stop
+    reason, the per-cycle thresholds and the component list."""
+    f32 = np.float32
+    res = np.array(residual, np.float32, copy=True)
+    model = np.zeros_like(res)
+    actual = reported = major = 0
+    stop = None
+    min_peak = f32(np.max(np.abs(res)))
+    needs_refresh = False
+    comps, thresholds = [], []
+    while reported < niter:
+        if major_cycle_limit is not None and major >= major_cycle_limit:
+            stop = "MajorCycleLimitReached"
+            break
+        pk = peak_location(res)
+        if pk is None:
+            stop = "NoCleanablePixels"
+            break
+        peak = abs(pk[1])
+        s = tolerant_clean_stop_reason(peak, threshold, 0.0)
+        if s is not None:
+            stop = s
+            break
+        cyc_niter = min(niter - reported, minor_cycle_length)
+        thr = clean_cycle_threshold(peak, sidelobe, cyclefactor, min_psf_fraction,
+                                    max_psf_fraction, threshold)
+        thresholds.append(thr)
+        out = hogbom(res, psf, gain, cyc_niter, threshold=threshold, cycle_threshold=thr,
+                     model=model, inclusive=inclusive)
+        model, res = out["model"], out["residual"]
+        comps.extend(zip(zip(out["x"].tolist(), out["y"].tolist()), out["flux"].tolist()))
+        actual += out["actual"]
+        reported += out["reported"]
+        reason = _STOP_NAMES[out["stop_reason"]]
+        updated = out["actual"] > 0
+        stop_after = None
+        if reason is not None:
+            if updated and reason in ("CycleThresholdReached", "NsigmaThresholdReached"):
+                pass
+            elif reason in ("CycleThresholdReached", "NsigmaThresholdReached"):
+                stop = reason
+            else:
+                stop = reason
+                stop_after = reason
+        if not updated:
+            break
+        needs_refresh = True
+        minor_peak = f32(np.max(np.abs(res)))
+        if minor_peak < min_peak:
+            min_peak = minor_peak
+        elif min_peak > 0 and (minor_peak - min_peak) / min_peak > f32(0.1):
+            stop = "DivergenceDetected"
+            break
+        if reported >= niter:
+            stop = "IterationLimitReached"
+            break
+        res = np.asarray(refresh(model), np.float32)
+        major += 1
+        needs_refresh = False
+        if stop_after is not None:
+            break
+        s = tolerant_clean_stop_reason(f32(np.max(np.abs(res))), threshold, 0.0)
+        if s is not None:
+            stop = s
+            break
+    if niter > 0 and stop is None:
+        stop = "IterationLimitReached"
+    if needs_refresh:
+        res = np.asarray(refresh(model), np.float32)
+    return dict(model=model, residual=res, major_cycles=major, actual=actual, reported=reported,
+                stop_reason=stop, thresholds=thresholds, components=comps)
