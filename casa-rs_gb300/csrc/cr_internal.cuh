@@ -46,6 +46,9 @@ struct cr_ctx {
     cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
     cudaEvent_t ev[8] = {};
+    // [0,1] bracket the last gridding kernel, [2,3] the last degridding kernel
+    cudaEvent_t kev[4] = {};
+    int kev_used = 0;
     cr_timings timings = {};
     int64_t launches = 0;
     // small pinned host buffer for device->host scalars
@@ -94,6 +97,8 @@ void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes);
 void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes);
 void pool_free(cr_ctx* ctx, Pool& pool);
 void note_launch(cr_ctx* ctx, const char* what);
+// Event pair around one gridding (which = 0) or degridding (which = 1) kernel.
+void kernel_mark(cr_ctx* ctx, int which, bool end);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
 
 // ---- host-side tables (restated from gridder.rs) ----------------------------
@@ -187,6 +192,40 @@ void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
 void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev);
 // image *= scale, then / *peak_dev when peak_dev != null
 void scale_image(cr_ctx* ctx, float* image, int64_t n, float scale, const unsigned int* peak_dev);
+
+// ---- batched cube (cr_cube.cu) ------------------------------------------------
+// Device views of a cube batch: rows' u, v in metres, [C][R] samples;
+// lambda_scale is a host array of C values.
+struct CubeInput {
+    int64_t R = 0;
+    int32_t C = 0;
+    const double* u = nullptr;
+    const double* v = nullptr;
+    const double* lambda_scale = nullptr;
+    const float2* vis = nullptr;
+    const float* weight = nullptr;
+    const uint8_t* flags = nullptr;
+};
+// Records of every channel binned by (channel, home tile).
+struct CubeRecords {
+    int64_t R = 0;
+    int32_t C = 0;
+    int64_t ntx = 0, nty = 0, ntiles = 0;
+    uint4* rec = nullptr;              // {cell | tap rows, c R + r, w vis}
+    float* rec_w = nullptr;
+    uint32_t* bin_start = nullptr;     // [C ntiles + 1]
+    double* sumwt = nullptr;           // [C]
+    unsigned long long* counts = nullptr;  // [C][2] gridded, skipped
+    unsigned long long* n_rec = nullptr;
+};
+CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
+                      float robust);
+// psf [C][gnx][gny] float32 (real part), dirty [C][gnx][gny] complex64
+void cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf, float2* dirty);
+// pred [C][R] complex64, zero for samples that are not gridded
+void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
+                 float2* pred);
+void cube_read_sums(cr_ctx* ctx, const CubeRecords& cr, cr_sums* out);
 
 // ---- W-projection build ----------------------------------------------------------
 void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
