@@ -4,5 +4,7 @@ from ._lib import CasarsCudaError, load as load_library  # noqa: F401
 from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, PsfState,  # noqa: F401
                       StandardGridder, VisibilityBatch, WProjector, adjoint, apply_weighting,
                       degrid, dirty_image, grid_dirty, grid_residual, grid_to_image,
-                      image_to_grid, predict, residual_image, run_hogbom_minor_cycle)
+                      image_to_grid, predict, residual_image, run_hogbom_minor_cycle,
+                      CubeBatch, cube_degrid, cube_grid_degrid, cube_grid_dirty,
+                      cube_sample_taps)
 from .clean import CleanConfig, CleanResult, clean_cycle_threshold, run_cotton_schwab  # noqa: F401

@@ -41,6 +41,12 @@ class VisBatch(C.Structure):
                 ("sumwt_factor", _p), ("gridable", _p), ("vis", _p), ("location", _i32)]
 
 
+class CubeBatch(C.Structure):
+    _fields_ = [("rows", _i64), ("channels", _i32), ("u_m", _p), ("v_m", _p),
+                ("lambda_scale", _p), ("vis", _p), ("weight", _p), ("flags", _p),
+                ("location", _i32)]
+
+
 class Sums(C.Structure):
     _fields_ = [("normalization_sumwt", _d), ("reported_sumwt", _d), ("gridded", _i64),
                 ("skipped", _i64), ("unique_records", _i64), ("taps", _i64)]
@@ -85,6 +91,14 @@ SIGNATURES = {
     "cr_plan_grid_dirty": (C.c_int, [_p, _p, _p, _p, _i32, _err]),
     "cr_plan_degrid": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
     "cr_plan_grid_residual": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
+    "cr_cube_grid_dirty": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _i32,
+                                     _p, _err]),
+    "cr_cube_degrid": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _i32, _p, _i32,
+                                 _err]),
+    "cr_cube_grid_degrid": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _p, _i32,
+                                      _p, _i32, _p, _err]),
+    "cr_cube_sample_taps": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _p, _p,
+                                      _p, _i32, _err]),
     "cr_plan_residual_image": (C.c_int, [_p, _p, _p, _i32, C.POINTER(PsfState), _p, _i32,
                                          _err]),
     "cr_grid_to_image": (C.c_int, [_p, _p, _p, _p, _i32, _f, _p, _i32, _err]),
@@ -96,6 +110,8 @@ SIGNATURES = {
     "cr_predict": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _i32, _p, _i32, _err]),
     "cr_adjoint": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _i32, _err]),
     "cr_apply_weighting": (C.c_int, [_p, _p, C.POINTER(VisBatch), _i32, _f, _p, _i32,
+                                     C.POINTER(_f), _err]),
+    "cr_apply_weighting_plane": (C.c_int, [_p, _p, C.POINTER(VisBatch), _i32, _f, _p, _i32,
                                      C.POINTER(_f), _err]),
     "cr_hogbom": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64, _i32,
                             _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i32),

@@ -551,9 +551,10 @@ WEIGHTING_MODES = {"natural": CR_WEIGHT_NATURAL, "uniform": CR_WEIGHT_UNIFORM,
 
 
 def apply_weighting(gridder, batch: VisibilityBatch, mode: str = "natural",
-                    robust: float = 0.0):
-    """apply_weighting (weighting.rs:904-1180), Combined density: returns the
-    imaging weights and Briggs f2."""
+                    robust: float = 0.0, per_plane: bool = False):
+    """apply_weighting (weighting.rs:904-1180): returns the imaging weights
+    and Briggs f2.  Combined density, or with per_plane the PerPlane density
+    of one cube channel (weighting.rs:1455-1483)."""
     ctx = gridder.ctx.handle
     arrs = _Arrays()
     b = batch._bind(arrs, False)
@@ -561,9 +562,133 @@ def apply_weighting(gridder, batch: VisibilityBatch, mode: str = "natural",
     out, op, loc = arrs.out((len(batch),), np.float32, torch.float32 if torch else None,
                             _device_of(batch.u_lambda))
     f2 = C.c_float()
-    call("cr_apply_weighting", ctx, gridder.handle, C.byref(b), WEIGHTING_MODES[mode],
-         float(robust), op, loc, C.byref(f2))
+    call("cr_apply_weighting_plane" if per_plane else "cr_apply_weighting", ctx, gridder.handle,
+         C.byref(b), WEIGHTING_MODES[mode], float(robust), op, loc, C.byref(f2))
     return out, float(f2.value)
+
+
+# ----------------------------------------------------------------------------
+# batched spectral cube
+# ----------------------------------------------------------------------------
+SPEED_OF_LIGHT_M_PER_S = 299_792_458.0
+
+
+@dataclass
+class CubeBatch:
+    """Rows shared by all channels (u_m, v_m in metres) and channel-major
+    [C][R] samples.  lambda_scale[c] = f_c / c (host array); channel c's
+    batch has u_lambda = u_m * lambda_scale[c] and leaves flagged samples out
+    (casars-imager/src/lib.rs:49571-49576)."""
+    u_m: object
+    v_m: object
+    lambda_scale: object
+    visibility: object              # [C][R] complex64
+    weight: object = None           # [C][R] float32
+    flags: object = None            # [C][R] bool / uint8
+
+    @staticmethod
+    def from_frequencies(u_m, v_m, freqs_hz, visibility, weight=None, flags=None):
+        ls = np.asarray(freqs_hz, np.float64) / SPEED_OF_LIGHT_M_PER_S
+        return CubeBatch(u_m, v_m, ls, visibility, weight, flags)
+
+    @property
+    def channels(self):
+        return int(np.asarray(self.lambda_scale).shape[0])
+
+    @property
+    def rows(self):
+        return int(self.u_m.shape[0])
+
+    def _bind(self, arrs: _Arrays) -> _lib.CubeBatch:
+        b = _lib.CubeBatch()
+        b.rows, b.channels = self.rows, self.channels
+        S = (b.channels, b.rows)
+        b.u_m = arrs.ptr(self.u_m, np.float64, torch.float64 if torch else None)
+        b.v_m = arrs.ptr(self.v_m, np.float64, torch.float64 if torch else None)
+        ls = np.ascontiguousarray(np.asarray(
+            self.lambda_scale.cpu() if _is_torch(self.lambda_scale) else self.lambda_scale,
+            np.float64))
+        arrs.keep.append(ls)
+        b.lambda_scale = ls.ctypes.data
+        b.vis = arrs.ptr(self.visibility, np.complex64, torch.complex64 if torch else None, S)
+        b.weight = arrs.ptr(self.weight, np.float32, torch.float32 if torch else None, S)
+        flags = self.flags
+        if flags is not None and _is_torch(flags) and flags.dtype == torch.bool:
+            flags = flags.to(torch.uint8)
+        b.flags = arrs.ptr(flags, np.uint8, torch.uint8 if torch else None, S)
+        b.location = CR_HOST if arrs.location is None else arrs.location
+        return b
+
+
+def _cube_call(gridder, cube, weighting, robust, grids, model_grids):
+    ctx = gridder.ctx
+    arrs = _Arrays()
+    b = cube._bind(arrs)
+    mp = None
+    if model_grids is not None:
+        mp = arrs.ptr(model_grids, np.complex64, torch.complex64 if torch else None,
+                      (cube.channels,) + tuple(gridder.grid_shape()))
+    _prepare(gridder, arrs)
+    dev = _device_of(cube.u_m, cube.visibility)
+    gs = (cube.channels,) + tuple(gridder.grid_shape())
+    psf = dirty = pred = None
+    pp = dp = prp = None
+    loc = CR_HOST if arrs.location is None else arrs.location
+    if grids:
+        psf, pp, loc = arrs.out(gs, np.float32, torch.float32 if torch else None, dev)
+        dirty, dp, _ = arrs.out(gs, np.complex64, torch.complex64 if torch else None, dev)
+    if model_grids is not None:
+        pred, prp, loc = arrs.out((cube.channels, cube.rows), np.complex64,
+                                  torch.complex64 if torch else None, dev)
+    sums = (_lib.Sums * cube.channels)()
+    mode = WEIGHTING_MODES[weighting]
+    if grids and model_grids is not None:
+        call("cr_cube_grid_degrid", ctx.handle, gridder.handle, C.byref(b), mode, float(robust),
+             pp, dp, mp, loc, prp, loc, sums)
+    elif grids:
+        call("cr_cube_grid_dirty", ctx.handle, gridder.handle, C.byref(b), mode, float(robust),
+             pp, dp, loc, sums)
+    else:
+        call("cr_cube_degrid", ctx.handle, gridder.handle, C.byref(b), mode, float(robust), mp,
+             loc, prp, loc)
+        sums = None
+    return psf, dirty, pred, ([GridSums.from_c(s) for s in sums] if sums is not None else None)
+
+
+def cube_grid_dirty(gridder, cube: CubeBatch, weighting: str = "natural", robust: float = 0.0):
+    """Every channel's PSF grid (float32, real part) and dirty grid
+    (complex64), [C][gnx][gny], with per-channel sums."""
+    psf, dirty, _, sums = _cube_call(gridder, cube, weighting, robust, True, None)
+    return psf, dirty, sums
+
+
+def cube_degrid(gridder, cube: CubeBatch, model_grids, weighting: str = "natural",
+                robust: float = 0.0):
+    """Model visibilities [C][R] of per-channel model grids [C][gnx][gny]."""
+    return _cube_call(gridder, cube, weighting, robust, False, model_grids)[2]
+
+
+def cube_grid_degrid(gridder, cube: CubeBatch, model_grids, weighting: str = "natural",
+                     robust: float = 0.0):
+    """One plan, then both: (psf grids, dirty grids, model visibilities, sums)."""
+    return _cube_call(gridder, cube, weighting, robust, True, model_grids)
+
+
+def cube_sample_taps(gridder, cube: CubeBatch, weighting: str = "natural", robust: float = 0.0):
+    """Per-sample plan [C][R]: (start x, start y, x tap row, y tap row,
+    imaging weight); -1 / 0 where the sample is not gridded."""
+    ctx = gridder.ctx
+    arrs = _Arrays()
+    b = cube._bind(arrs)
+    _prepare(gridder, arrs)
+    dev = _device_of(cube.u_m, cube.visibility)
+    S = (cube.channels, cube.rows)
+    outs = [arrs.out(S, np.int32, torch.int32 if torch else None, dev) for _ in range(4)]
+    wt = arrs.out(S, np.float32, torch.float32 if torch else None, dev)
+    loc = outs[0][2]
+    call("cr_cube_sample_taps", ctx.handle, gridder.handle, C.byref(b), WEIGHTING_MODES[weighting],
+         float(robust), *[o[1] for o in outs], wt[1], loc)
+    return tuple(o[0] for o in outs) + (wt[0],)
 
 
 # ----------------------------------------------------------------------------

@@ -168,3 +168,83 @@ def config2_geometry(seed: int = 2) -> Observation:
     """27 antennas out to 21 km, 8 h of 2 s dumps at 1.4 GHz (5,054,400 rows),
     4096 x 4096 image, 200 points 1 mJy-1 Jy; visibilities not yet made."""
     return observation(21000.0, 8.0, 2.0, 1.4e9, 4096, 200, 1e-3, 1.0, seed, "config2")
+
+
+# ----------------------------------------------------------------------------
+# spectral cube
+# ----------------------------------------------------------------------------
+@dataclass
+class CubeObservation:
+    nx: int
+    cell: float
+    freqs_hz: np.ndarray      # [C]
+    u_m: np.ndarray           # [R] metres, time-major rows
+    v_m: np.ndarray
+    sky: Sky
+    flag_fraction: np.ndarray  # [C]
+    seed: int
+
+    @property
+    def channels(self):
+        return len(self.freqs_hz)
+
+    @property
+    def rows(self):
+        return len(self.u_m)
+
+    @property
+    def lambda_scale(self):
+        return self.freqs_hz / C_LIGHT
+
+
+def cube_observation(channels: int = 256, nx: int = 1024, hours: float = 10.0,
+                     dump_s: float = 10.0, max_radius_m: float = 1000.0, f_lo: float = 1.0e9,
+                     f_hi: float = 2.0e9, n_sources: int = 20, max_flag: float = 0.6,
+                     seed: int = 4) -> CubeObservation:
+    """Channels linear in [f_lo, f_hi]; cell = 1/3 of the synthesised beam at
+    f_hi; per-channel flag fraction uniform in [0, max_flag]."""
+    um, vm, _ = uvw_metres(max_radius_m, hours, dump_s)
+    freqs = np.linspace(f_lo, f_hi, channels)
+    ls_hi = f_hi / C_LIGHT
+    cell = 1.0 / (3.0 * float(np.sqrt(um * um + vm * vm).max()) * ls_hi)
+    rng = np.random.default_rng(seed)
+    frac = rng.uniform(0.0, max_flag, channels)
+    sky = point_sky(rng, n_sources, nx, nx, 0.01, 1.0)
+    return CubeObservation(nx, cell, freqs, um, vm, sky, frac, seed)
+
+
+def cube_flags(obs: CubeObservation):
+    """[C][R] bool, per-sample Bernoulli with the channel's flag fraction."""
+    rng = np.random.default_rng(obs.seed + 7)
+    return rng.random((obs.channels, obs.rows)) < obs.flag_fraction[:, None]
+
+
+def cube_visibilities(obs: CubeObservation) -> np.ndarray:
+    """[C][R] complex64 point-source visibilities (FP64 DFT, no w-term)."""
+    l, m, _ = obs.sky.lmn(obs.nx, obs.nx, obs.cell)
+    out = np.empty((obs.channels, obs.rows), np.complex64)
+    for c, ls in enumerate(obs.lambda_scale):
+        ph = -2.0 * math.pi * (np.outer(obs.u_m * ls, l) + np.outer(obs.v_m * ls, m))
+        out[c] = (np.cos(ph) @ obs.sky.flux + 1j * (np.sin(ph) @ obs.sky.flux))
+    return out
+
+
+def cube_device_inputs(obs: CubeObservation, device="cuda"):
+    """Flags and visibilities generated on the GPU for the full-size cube
+    (float32 phases: the benchmark only needs their shape and spread)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(obs.seed + 7)
+    frac = torch.as_tensor(obs.flag_fraction, dtype=torch.float32, device=device)
+    flags = torch.empty((obs.channels, obs.rows), dtype=torch.uint8, device=device)
+    vis = torch.empty((obs.channels, obs.rows), dtype=torch.complex64, device=device)
+    l, m, _ = obs.sky.lmn(obs.nx, obs.nx, obs.cell)
+    L = torch.tensor(np.stack([l, m], 0), dtype=torch.float32, device=device)
+    Fx = torch.tensor(obs.sky.flux, dtype=torch.float32, device=device)
+    U = torch.stack([torch.as_tensor(obs.u_m, device=device),
+                     torch.as_tensor(obs.v_m, device=device)], 1).to(torch.float32)
+    for c in range(obs.channels):
+        flags[c] = (torch.rand(obs.rows, generator=g, device=device) < frac[c]).to(torch.uint8)
+        ph = (-2.0 * math.pi * float(obs.lambda_scale[c])) * (U @ L)
+        vis[c] = torch.complex(torch.cos(ph) @ Fx, torch.sin(ph) @ Fx)
+    return flags, vis

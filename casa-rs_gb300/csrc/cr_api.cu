@@ -113,6 +113,70 @@ void check_wp(cr_gridder* g, cr_wproj* wp) {
     if (wp) need(wp->g == g, "W-projector belongs to another gridder");
 }
 
+
+CubeInput cube_input(cr_ctx* ctx, const cr_cube_batch* b) {
+    need(b != nullptr, "cube batch is null");
+    need(b->rows >= 0 && b->channels > 0, "cube batch needs rows >= 0 and channels > 0");
+    need(b->lambda_scale != nullptr, "lambda_scale is null");
+    need(b->rows == 0 || (b->u_m && b->v_m && b->vis), "u_m, v_m and vis are required");
+    CubeInput in;
+    in.R = b->rows;
+    in.C = b->channels;
+    const size_t R = (size_t)b->rows, S = (size_t)b->rows * (size_t)b->channels;
+    in.lambda_scale = b->lambda_scale;
+    in.u = (const double*)device_input(ctx, b->u_m, R * 8, b->location, "cube_u");
+    in.v = (const double*)device_input(ctx, b->v_m, R * 8, b->location, "cube_v");
+    in.vis = (const float2*)device_input(ctx, b->vis, S * 8, b->location, "cube_vis");
+    in.weight = (const float*)device_input(ctx, b->weight, S * 4, b->location, "cube_weight");
+    in.flags = (const uint8_t*)device_input(ctx, b->flags, S, b->location, "cube_flags");
+    return in;
+}
+
+int cube_run(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t weighting,
+             float robust, float* psf_grids, float* dirty_grids, const float* model_grids,
+             int32_t grid_location, float* pred, int32_t out_location, cr_sums* sums,
+             char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr, "null argument");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        CubeInput in = cube_input(ctx, batch);
+        CubeRecords cr = cube_plan(ctx, g, in, weighting, robust);
+        tm.mark();
+        const size_t cells = (size_t)g->info.grid_nx * g->info.grid_ny;
+        const size_t C = (size_t)in.C;
+        float* psf = nullptr;
+        float2* dirty = nullptr;
+        if (psf_grids || dirty_grids) {
+            need(psf_grids && dirty_grids, "psf_grids and dirty_grids go together");
+            psf = out_ptr<float>(ctx, psf_grids, out_location, C * cells * 4, "cube_psf");
+            dirty = out_ptr<float2>(ctx, dirty_grids, out_location, C * cells * 8, "cube_dirty");
+            cube_grid(ctx, g, cr, psf, dirty);
+        }
+        tm.mark();
+        float2* pr = nullptr;
+        if (model_grids) {
+            need(pred != nullptr, "pred is null");
+            const float2* mg = (const float2*)device_input(ctx, model_grids, C * cells * 8,
+                                                           grid_location, "cube_model");
+            pr = out_ptr<float2>(ctx, pred, out_location, C * (size_t)in.R * 8 + 8, "cube_pred");
+            cube_degrid(ctx, g, cr, mg, pr);
+        }
+        tm.mark();
+        if (out_location == CR_HOST) {
+            if (psf) {
+                copy_out(ctx, psf_grids, psf, C * cells * 4, CR_HOST);
+                copy_out(ctx, dirty_grids, dirty, C * cells * 8, CR_HOST);
+            }
+            if (pr) copy_out(ctx, pred, pr, C * (size_t)in.R * 8, CR_HOST);
+        }
+        set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), tm.between(2, 3), 0.f, 0.f});
+        cube_read_sums(ctx, cr, sums);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 }  // namespace
 
 extern "C" {
@@ -681,18 +745,32 @@ int cr_plan_residual_image(cr_ctx* ctx, cr_plan* p, const float* model, int32_t 
     });
 }
 
-int cr_apply_weighting(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch, int32_t mode,
-                       float robust, float* out_weight, int32_t out_location, float* f2,
-                       char** err) {
+static int apply_weighting_conv(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch,
+                                int32_t mode, float robust, float* out_weight,
+                                int32_t out_location, float* f2, int32_t convention, char** err) {
     return guarded(err, [&] {
         need(ctx != nullptr && g != nullptr, "null argument");
         bind(ctx);
         DeviceBatch b = device_batch(ctx, batch, false);
         float* out = out_ptr<float>(ctx, out_weight, out_location, (size_t)b.n * 4 + 4, "weights");
-        apply_weighting(ctx, g, b, mode, robust, out, f2);
+        apply_weighting(ctx, g, b, mode, robust, out, f2, convention);
         if (out_location == CR_HOST) copy_out(ctx, out_weight, out, (size_t)b.n * 4, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
+}
+
+int cr_apply_weighting(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch, int32_t mode,
+                       float robust, float* out_weight, int32_t out_location, float* f2,
+                       char** err) {
+    return apply_weighting_conv(ctx, g, batch, mode, robust, out_weight, out_location, f2, 0,
+                                err);
+}
+
+int cr_apply_weighting_plane(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch,
+                             int32_t mode, float robust, float* out_weight,
+                             int32_t out_location, float* f2, char** err) {
+    return apply_weighting_conv(ctx, g, batch, mode, robust, out_weight, out_location, f2, 1,
+                                err);
 }
 
 int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
@@ -724,6 +802,68 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, cons
         if (location == CR_HOST) {
             CR_CUDA_CHECK(cudaMemcpyAsync(model, m, nb, cudaMemcpyDeviceToHost, ctx->stream));
             CR_CUDA_CHECK(cudaMemcpyAsync(residual, r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_cube_grid_dirty(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                       int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
+                       int32_t out_location, cr_sums* sums, char** err) {
+    if (!psf_grids || !dirty_grids) {
+        set_err(err, "psf_grids and dirty_grids are required");
+        return CR_INVALID;
+    }
+    return cube_run(ctx, g, batch, weighting, robust, psf_grids, dirty_grids, nullptr, CR_HOST,
+                    nullptr, out_location, sums, err);
+}
+
+int cr_cube_degrid(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t weighting,
+                   float robust, const float* model_grids, int32_t grid_location, float* pred,
+                   int32_t out_location, char** err) {
+    if (!model_grids) {
+        set_err(err, "model_grids is required");
+        return CR_INVALID;
+    }
+    return cube_run(ctx, g, batch, weighting, robust, nullptr, nullptr, model_grids,
+                    grid_location, pred, out_location, nullptr, err);
+}
+
+int cr_cube_grid_degrid(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
+                        const float* model_grids, int32_t grid_location, float* pred,
+                        int32_t out_location, cr_sums* sums, char** err) {
+    if (!psf_grids || !dirty_grids || !model_grids) {
+        set_err(err, "psf_grids, dirty_grids and model_grids are required");
+        return CR_INVALID;
+    }
+    return cube_run(ctx, g, batch, weighting, robust, psf_grids, dirty_grids, model_grids,
+                    grid_location, pred, out_location, sums, err);
+}
+
+int cr_cube_sample_taps(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, int32_t* start_x, int32_t* start_y,
+                        int32_t* row_x, int32_t* row_y, float* imaging_weight,
+                        int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr, "null argument");
+        need(start_x && start_y && row_x && row_y && imaging_weight, "output is null");
+        bind(ctx);
+        CubeInput in = cube_input(ctx, batch);
+        const size_t S = (size_t)in.C * (size_t)in.R;
+        CubeTaps t;
+        t.start_x = out_ptr<int32_t>(ctx, start_x, out_location, S * 4 + 4, "taps_sx");
+        t.start_y = out_ptr<int32_t>(ctx, start_y, out_location, S * 4 + 4, "taps_sy");
+        t.row_x = out_ptr<int32_t>(ctx, row_x, out_location, S * 4 + 4, "taps_rx");
+        t.row_y = out_ptr<int32_t>(ctx, row_y, out_location, S * 4 + 4, "taps_ry");
+        t.weight = out_ptr<float>(ctx, imaging_weight, out_location, S * 4 + 4, "taps_w");
+        cube_plan(ctx, g, in, weighting, robust, &t);
+        if (out_location == CR_HOST) {
+            copy_out(ctx, start_x, t.start_x, S * 4, CR_HOST);
+            copy_out(ctx, start_y, t.start_y, S * 4, CR_HOST);
+            copy_out(ctx, row_x, t.row_x, S * 4, CR_HOST);
+            copy_out(ctx, row_y, t.row_y, S * 4, CR_HOST);
+            copy_out(ctx, imaging_weight, t.weight, S * 4, CR_HOST);
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });

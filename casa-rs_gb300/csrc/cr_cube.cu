@@ -1,0 +1,696 @@
+// cr_cube.cu -- the batched spectral cube: every channel weighted, planned
+// and gridded (or degridded) by one sequence of launches whose number does
+// not depend on the number of channels.
+//
+// Channel c's visibility batch is the unflagged samples of rows r = 0..R-1
+// with u_lambda = u_m[r] * s_c, v_lambda = v_m[r] * s_c, s_c = f_c / c (the
+// cube batch assembly of casars-imager/src/lib.rs:49571-49576, which leaves
+// flagged samples out of the channel batch).  Per channel the path restates
+//   * PerPlane density weighting (apply_weighting_with_density_source,
+//     weighting.rs:1055-1180 with density_build_cell_convention /
+//     density_cell_convention = CubeBriggsWeightor{Density,Lookup},
+//     weighting.rs:1455-1483): the density is image-sized, a sample adds its
+//     weight at the rounded cell of (u, v) and of (-u, -v)
+//     (weight_density_cell_anchor, gridder.rs:1888-1934), f2 uses FP64 sums
+//     of d and d^2 (weighting.rs:1108-1121) and the reweight is w / d or
+//     w / (d f2 + 1) (casa_briggs_denominator, weighting.rs:2440-2443);
+//   * the standard PSWF plan (sample_tap_span, gridder.rs:1976-1995) and
+//     gridding (grid_sample_taps_real_complex_pair_planned_f64,
+//     gridder.rs:1021-1071) with sumwt = sum of f64 weights (lib.rs:68433-68500);
+//   * degridding (degrid_sample_taps_planned_normalized, gridder.rs:1278-1312).
+//
+// Layout: rows' u, v (f64 metres) are shared by all channels; vis, weight
+// and flags are channel-major [C][R].  Planning makes one pass to histogram
+// the samples by (channel, 32 x 32 home tile), a scan, and a second pass that
+// scatters 16-byte records {cell | tap rows, sample, w vis} plus the weight into
+// bin order.  The index selection runs on the integer fixed-point path of
+// cr_fixed.cuh with the FP64 operations as the fallback.  Gridding gives
+// every (channel, output tile) to one block, which gathers the records of
+// the four home tiles whose 7 x 7 footprints reach it, accumulates the tile
+// in shared memory and writes it once with coalesced stores -- no memset and
+// no global atomics on the output grids.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "cr_fixed.cuh"
+#include "cr_internal.cuh"
+
+namespace cr {
+
+namespace {
+
+constexpr int kCubeThreads = 256;
+constexpr int kRowsPerBlock = 4096;   // rows of one channel per planning block
+constexpr int kSmemBins = 8192;       // home tiles histogrammed in shared memory
+
+struct CubeChan {
+    double lscale;       // f / c
+    FixScale kx, ky;     // lscale / du, lscale / dv
+    FixScale kdx, kdy;   // lscale * nx cell_x, lscale * ny cell_y
+};
+
+struct CubeArgs {
+    int64_t R;
+    int32_t C;
+    const double* u;
+    const double* v;
+    const CubeChan* ch;
+    const float2* vis;
+    const float* weight;
+    const uint8_t* flags;
+    // gridder
+    double du, dv;
+    int64_t gnx, gny;
+    int32_t os, tap_rows;
+    int64_t ntx, nty;
+    long long cx_fix, cy_fix;
+    // density
+    int32_t nx, ny;
+    double dus, dvs, dcx, dcy;
+    long long dcx_fix, dcy_fix;
+    int32_t mode;
+    float* density;            // [C][nx][ny]
+    const float* f2;           // [C]
+    // planning
+    uint32_t* hist;            // [C * ntiles]
+    uint32_t* cursor;          // [C * ntiles]
+    double* sumwt;             // [C]
+    unsigned long long* counts;// [C][2]: gridded, skipped
+    uint4* rec;                // {meta, c R + r, w vis.re, w vis.im}
+    float* rec_w;
+};
+
+// weight_density_cell_anchor with the cube (rounded) conventions.
+__device__ __forceinline__ bool density_cell(const CubeArgs& a, const CubeChan& ch, double um,
+                                             double vm, bool mirror, int* ox, int* oy) {
+    long long tx, ty;
+    if (fix_mul(um, ch.kdx, &tx) && fix_mul(vm, ch.kdy, &ty)) {
+        const long long X = (mirror ? -tx : tx) + a.dcx_fix;
+        const long long Y = (mirror ? ty : -ty) + a.dcy_fix;
+        long long ax, ay;
+        if (fix_round(X, kFixMargin, &ax) && fix_round(Y, kFixMargin, &ay)) {
+            if (ax <= 0 || ay <= 0 || ax >= a.nx || ay >= a.ny) return false;
+            *ox = (int)ax;
+            *oy = (int)ay;
+            return true;
+        }
+    }
+    double u = __dmul_rn(um, ch.lscale), v = __dmul_rn(vm, ch.lscale);
+    if (mirror) {
+        u = -u;
+        v = -v;
+    }
+    const double x = __dadd_rn(__dmul_rn(u, a.dus), a.dcx);
+    const double y = __dadd_rn(__dmul_rn(-v, a.dvs), a.dcy);
+    if (!isfinite(x) || !isfinite(y)) return false;
+    const double rx = round(x), ry = round(y);
+    if (!(rx >= 1.0 && ry >= 1.0 && rx < (double)a.nx && ry < (double)a.ny)) return false;
+    *ox = (int)rx;
+    *oy = (int)ry;
+    return true;
+}
+
+__device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
+
+struct Eval {
+    bool ok;
+    uint32_t tile;
+    uint32_t meta;
+    float w;
+};
+
+// One sample of channel c: flags, reweighting, validity and taps.
+__device__ __forceinline__ Eval eval_sample(const CubeArgs& a, const CubeChan& ch, float f2,
+                                            int c, int64_t r) {
+    Eval e{false, 0u, 0u, 0.0f};
+    const int64_t i = (int64_t)c * a.R + r;
+    if (a.flags && a.flags[i]) return e;
+    float w = a.weight ? a.weight[i] : 1.0f;
+    const double um = a.u[r], vm = a.v[r];
+    if (a.mode != CR_WEIGHT_NATURAL) {
+        int x, y;
+        float nw = 0.0f;
+        if (density_cell(a, ch, um, vm, false, &x, &y)) {
+            const float d = a.density[((int64_t)c * a.nx + x) * a.ny + y];
+            if (finite_f(w) && w > 0.0f && finite_f(d) && d > 0.0f)
+                nw = a.mode == CR_WEIGHT_UNIFORM ? __fdiv_rn(w, d)
+                                                 : __fdiv_rn(w, __fadd_rn(__fmul_rn(d, f2), 1.0f));
+        }
+        w = nw;
+    }
+    if (!(finite_f(w) && w > 0.0f)) return e;
+    int64_t x0 = 0, y0 = 0;
+    int32_t rx = 0, ry = 0;
+    int sx = -1, sy = -1;
+    long long tx, ty;
+    if (fix_mul(um, ch.kx, &tx) && fix_mul(vm, ch.ky, &ty)) {
+        sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
+        if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
+        if (sx == 0 || sy == 0) return e;
+    }
+    if (sx < 0 || sy < 0) {
+        const double u = __dmul_rn(um, ch.lscale), v = __dmul_rn(vm, ch.lscale);
+        const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+        const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+        if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
+            !f64_tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry))
+            return e;
+    }
+    e.ok = true;
+    e.tile = (uint32_t)((x0 >> 5) * a.nty + (y0 >> 5));
+    e.meta = ((uint32_t)(x0 & 31) << 27) | ((uint32_t)(y0 & 31) << 22) |
+             ((uint32_t)rx << 11) | (uint32_t)ry;
+    e.w = w;
+    return e;
+}
+
+__global__ void __launch_bounds__(kCubeThreads) cube_density_kernel(CubeArgs a) {
+    const int c = blockIdx.y;
+    const CubeChan ch = a.ch[c];
+    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
+    float* dens = a.density + (int64_t)c * a.nx * a.ny;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
+        const int64_t i = (int64_t)c * a.R + r;
+        if (a.flags && a.flags[i]) continue;
+        const float w = a.weight ? a.weight[i] : 1.0f;
+        if (!(finite_f(w) && w > 0.0f)) continue;
+        int x, y;
+        if (density_cell(a, ch, a.u[r], a.v[r], false, &x, &y))
+            atomicAdd(&dens[(int64_t)x * a.ny + y], w);
+        if (density_cell(a, ch, a.u[r], a.v[r], true, &x, &y))
+            atomicAdd(&dens[(int64_t)x * a.ny + y], w);
+    }
+}
+
+// Per channel: sum d and sum d^2 (d > 0) in FP64, then f2 (weighting.rs:1108-1121).
+__global__ void __launch_bounds__(kCubeThreads) cube_density_sums(const float* density,
+                                                                  int64_t cells, double* sums) {
+    const int c = blockIdx.y;
+    const float* d = density + (int64_t)c * cells;
+    double s = 0.0, s2 = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const double v = (double)d[k];
+        s += v;
+        if (v > 0.0) s2 += v * v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sums[2 * c], s);
+        atomicAdd(&sums[2 * c + 1], s2);
+    }
+}
+
+__global__ void cube_f2_kernel(const double* sums, int32_t C, double a2, float* f2) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const double s = sums[2 * c], s2 = sums[2 * c + 1];
+    f2[c] = (s2 > 0.0 && s > 0.0) ? (float)__ddiv_rn(a2, __ddiv_rn(s2, s)) : 0.0f;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Pass 1: histogram of (channel, home tile), per-channel sumwt and counts.
+__global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
+    extern __shared__ uint32_t s_hist[];
+    __shared__ double s_sum[kCubeThreads / 32];
+    __shared__ unsigned long long s_ok[kCubeThreads / 32], s_skip[kCubeThreads / 32];
+    const int c = blockIdx.y;
+    const CubeChan ch = a.ch[c];
+    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
+    const int64_t ntiles = a.ntx * a.nty;
+    const bool smem = ntiles <= kSmemBins;
+    uint32_t* ghist = a.hist + (int64_t)c * ntiles;
+    if (smem)
+        for (int64_t k = threadIdx.x; k < ntiles; k += kCubeThreads) s_hist[k] = 0u;
+    __syncthreads();
+    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
+    double sw = 0.0;
+    unsigned long long n_ok = 0, n_skip = 0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
+        if (a.flags && a.flags[(int64_t)c * a.R + r]) continue;
+        const Eval e = eval_sample(a, ch, f2, c, r);
+        if (e.ok) {
+            ++n_ok;
+            sw += (double)e.w;
+            if (smem)
+                atomicAdd(&s_hist[e.tile], 1u);
+            else
+                atomicAdd(&ghist[e.tile], 1u);
+        } else {
+            ++n_skip;
+        }
+    }
+    sw = warp_sum(sw);
+    n_ok = warp_sum(n_ok);
+    n_skip = warp_sum(n_skip);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_sum[warp] = sw;
+        s_ok[warp] = n_ok;
+        s_skip[warp] = n_skip;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        unsigned long long o = 0, s = 0;
+        for (int k = 0; k < kCubeThreads / 32; ++k) {
+            t += s_sum[k];
+            o += s_ok[k];
+            s += s_skip[k];
+        }
+        if (t != 0.0) atomicAdd(&a.sumwt[c], t);
+        if (o) atomicAdd(&a.counts[2 * c], o);
+        if (s) atomicAdd(&a.counts[2 * c + 1], s);
+    }
+    if (smem)
+        for (int64_t k = threadIdx.x; k < ntiles; k += kCubeThreads)
+            if (s_hist[k]) atomicAdd(&ghist[k], s_hist[k]);
+}
+
+// Pass 2: scatter records into (channel, home tile) bins.
+__global__ void __launch_bounds__(kCubeThreads) cube_scatter_kernel(CubeArgs a) {
+    const int c = blockIdx.y;
+    const CubeChan ch = a.ch[c];
+    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
+    const int64_t ntiles = a.ntx * a.nty;
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
+    // warp-uniform trip count so that the warp-aggregated atomics see whole warps
+    for (int64_t base = r0 + (threadIdx.x & ~31); base < r1; base += kCubeThreads) {
+        const int64_t r = base + lane;
+        Eval e{false, 0u, 0u, 0.0f};
+        if (r < r1) e = eval_sample(a, ch, f2, c, r);
+        const unsigned act = __ballot_sync(0xffffffffu, e.ok);
+        if (!e.ok) continue;
+        const uint32_t bin = (uint32_t)((int64_t)c * ntiles + e.tile);
+        const unsigned peers = __match_any_sync(act, bin);
+        const int leader = __ffs(peers) - 1;
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        uint32_t pos0 = 0;
+        if (lane == leader) pos0 = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers));
+        pos0 = __shfl_sync(peers, pos0, leader);
+        const uint32_t pos = pos0 + rank;
+        const float2 vv = a.vis[(int64_t)c * a.R + r];
+        float vr = 0.0f, vi = 0.0f;
+        if (finite_f(vv.x) && finite_f(vv.y)) {
+            vr = __fmul_rn(vv.x, e.w);
+            vi = __fmul_rn(vv.y, e.w);
+        }
+        a.rec[pos] = make_uint4(e.meta, (uint32_t)((int64_t)c * a.R + r), __float_as_uint(vr),
+                                __float_as_uint(vi));
+        a.rec_w[pos] = e.w;
+    }
+}
+
+struct CubeGridArgs {
+    const uint4* rec;
+    const float* rec_w;
+    const uint32_t* bin_start;   // [C * ntiles + 1]
+    const float* taps;           // [tap_rows][7]
+    int64_t ntx, nty, gnx, gny;
+    int64_t n_items;             // C * ntiles
+    unsigned int* item_counter;
+    float* psf;                  // [C][gnx][gny] real part of the PSF grid
+    float2* dirty;               // [C][gnx][gny]
+};
+
+// One block per (channel, output tile): gather the footprints of the home
+// tiles (tx, ty), (tx-1, ty), (tx, ty-1), (tx-1, ty-1) that reach it.
+__global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a) {
+    __shared__ float s_psf[kTile * kTile];
+    __shared__ float s_re[kTile * kTile];
+    __shared__ float s_im[kTile * kTile];
+    __shared__ int s_item;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t ntiles = a.ntx * a.nty;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
+        __syncthreads();
+        const int64_t item = s_item;
+        if (item >= a.n_items) break;
+        const int64_t c = item / ntiles, T = item % ntiles;
+        const int64_t tx = T / a.nty, ty = T % a.nty;
+        uint32_t b0[4], b1[4];
+        int ox[4], oy[4];
+        int nsrc = 0;
+        for (int s = 0; s < 4; ++s) {
+            const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
+            if (sx < 0 || sy < 0) continue;
+            const int64_t bin = c * ntiles + sx * a.nty + sy;
+            const uint32_t lo = a.bin_start[bin], hi = a.bin_start[bin + 1];
+            if (lo == hi) continue;
+            b0[nsrc] = lo;
+            b1[nsrc] = hi;
+            ox[nsrc] = -(s & 1) * kTile;
+            oy[nsrc] = -(s >> 1) * kTile;
+            ++nsrc;
+        }
+        const int64_t gx0 = tx * kTile, gy0 = ty * kTile;
+        float* psf_c = a.psf + c * a.gnx * a.gny;
+        float2* dirty_c = a.dirty + c * a.gnx * a.gny;
+        if (nsrc == 0) {
+            for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
+                const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
+                if (x < a.gnx && y < a.gny) {
+                    psf_c[x * a.gny + y] = 0.0f;
+                    dirty_c[x * a.gny + y] = make_float2(0.0f, 0.0f);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
+            s_psf[k] = 0.0f;
+            s_re[k] = 0.0f;
+            s_im[k] = 0.0f;
+        }
+        __syncthreads();
+        for (int s = 0; s < nsrc; ++s) {
+            const int sox = ox[s], soy = oy[s];
+            for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kCubeThreads) {
+                // lanes look at 32 records; the warp then runs the relevant ones
+                const uint32_t rr = base + lane;
+                uint4 q = make_uint4(0u, 0u, 0u, 0u);
+                bool rel = false;
+                if (rr < b1[s]) {
+                    q = a.rec[rr];
+                    const int lx = sox + (int)(q.x >> 27), ly = soy + (int)((q.x >> 22) & 31);
+                    rel = lx + 6 >= 0 && ly + 6 >= 0;
+                }
+                unsigned m = __ballot_sync(0xffffffffu, rel);
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t meta = __shfl_sync(0xffffffffu, q.x, src);
+                    const float vr = __uint_as_float(__shfl_sync(0xffffffffu, q.z, src));
+                    const float vi = __uint_as_float(__shfl_sync(0xffffffffu, q.w, src));
+                    const float pw = a.rec_w[base + src];
+                    const int lx = sox + (int)(meta >> 27), ly = soy + (int)((meta >> 22) & 31);
+                    const float* wx = a.taps + ((meta >> 11) & 2047u) * 7;
+                    const float* wy = a.taps + (meta & 2047u) * 7;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int t = lane + 32 * h;
+                        if (t < 49) {
+                            const int ix = t / 7, iy = t - 7 * (t / 7);
+                            const int cx = lx + ix, cy = ly + iy;
+                            if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
+                                const float wgt = __fmul_rn(__ldg(&wx[ix]), __ldg(&wy[iy]));
+                                const int cell = cx * kTile + cy;
+                                atomicAdd(&s_psf[cell], pw * wgt);
+                                atomicAdd(&s_re[cell], vr * wgt);
+                                atomicAdd(&s_im[cell], vi * wgt);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
+            const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
+            if (x < a.gnx && y < a.gny) {
+                psf_c[x * a.gny + y] = s_psf[k];
+                dirty_c[x * a.gny + y] = make_float2(s_re[k], s_im[k]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+struct CubeDegridArgs {
+    const uint4* rec;
+    const uint32_t* bin_start;   // [C * ntiles + 1]
+    int64_t ntiles, nty, gnx, gny, R;
+    int64_t n_items;             // C * ntiles
+    unsigned int* item_counter;
+    const float* taps;
+    const float2* grid;          // [C][gnx][gny]
+    float2* pred;                // [C][R]
+};
+
+// Bins in turn; a warp per record: pred = sum grid * (wx wy) in float32,
+// written at the record's sample (channel-major index).
+__global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArgs a) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
+        __syncthreads();
+        const int64_t item = s_item;
+        __syncthreads();
+        if (item >= a.n_items) break;
+        const uint32_t lo = a.bin_start[item], hi = a.bin_start[item + 1];
+        if (lo == hi) continue;
+        const int64_t c = item / a.ntiles, T = item % a.ntiles;
+        const int64_t gx0 = (T / a.nty) * kTile, gy0 = (T % a.nty) * kTile;
+        const float2* g = a.grid + c * a.gnx * a.gny;
+        for (uint32_t k = lo + warp; k < hi; k += kCubeThreads / 32) {
+            const uint4 q = a.rec[k];
+            const uint32_t meta = q.x;
+            const float* wx = a.taps + ((meta >> 11) & 2047u) * 7;
+            const float* wy = a.taps + (meta & 2047u) * 7;
+            const float2* g0 = g + (gx0 + (int64_t)(meta >> 27)) * a.gny + gy0 +
+                               (int64_t)((meta >> 22) & 31);
+            float re = 0.0f, im = 0.0f;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int t = lane + 32 * h;
+                if (t < 49) {
+                    const int ix = t / 7, iy = t - 7 * (t / 7);
+                    const float wgt = __fmul_rn(__ldg(&wx[ix]), __ldg(&wy[iy]));
+                    const float2 gv = __ldg(&g0[(int64_t)ix * a.gny + iy]);
+                    re = fmaf(gv.x, wgt, re);
+                    im = fmaf(gv.y, wgt, im);
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) a.pred[q.y] = make_float2(re, im);
+        }
+    }
+}
+
+// Per-sample plan of every channel (start cells, tap rows, imaging weight).
+__global__ void __launch_bounds__(kCubeThreads) cube_taps_kernel(CubeArgs a, CubeTaps t) {
+    const int c = blockIdx.y;
+    const CubeChan ch = a.ch[c];
+    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
+    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
+        const int64_t i = (int64_t)c * a.R + r;
+        const Eval e = eval_sample(a, ch, f2, c, r);
+        if (e.ok) {
+            const int64_t tx = e.tile / a.nty, ty = e.tile % a.nty;
+            t.start_x[i] = (int32_t)(tx * kTile + (e.meta >> 27));
+            t.start_y[i] = (int32_t)(ty * kTile + ((e.meta >> 22) & 31));
+            t.row_x[i] = (int32_t)((e.meta >> 11) & 2047u);
+            t.row_y[i] = (int32_t)(e.meta & 2047u);
+            t.weight[i] = e.w;
+        } else {
+            t.start_x[i] = t.start_y[i] = t.row_x[i] = t.row_y[i] = -1;
+            t.weight[i] = 0.0f;
+        }
+    }
+}
+
+}  // namespace
+
+CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
+                      float robust, const CubeTaps* taps) {
+    if (mode != CR_WEIGHT_NATURAL && mode != CR_WEIGHT_UNIFORM && mode != CR_WEIGHT_BRIGGS)
+        fail(CR_INVALID, "unknown weighting mode");
+    if (in.C <= 0 || in.C > 65535) fail(CR_INVALID, "channels must lie in [1, 65535]");
+    if (in.R < 0) fail(CR_INVALID, "negative row count");
+    if ((uint64_t)in.C * (uint64_t)in.R >= (1ull << 32))
+        fail(CR_INVALID, "cube larger than 2^32 samples");
+    const cr_grid_info& gi = g->info;
+    if (gi.oversampling > 2046) fail(CR_INVALID, "oversampling above 2046");
+    CubeRecords cr{};
+    cr.R = in.R;
+    cr.C = in.C;
+    cr.ntx = (gi.grid_nx + kTile - 1) / kTile;
+    cr.nty = (gi.grid_ny + kTile - 1) / kTile;
+    cr.ntiles = cr.ntx * cr.nty;
+    const int64_t nbins = (int64_t)in.C * cr.ntiles;
+    const size_t ns = (size_t)std::max<int64_t>((int64_t)in.C * in.R, 1);
+    // per-channel constants
+    const double dus = (double)g->geom.nx * g->geom.cell_x_rad;
+    const double dvs = (double)g->geom.ny * g->geom.cell_y_rad;
+    std::vector<CubeChan> chh((size_t)in.C);
+    for (int c = 0; c < in.C; ++c) {
+        const double s = in.lambda_scale[c];
+        if (!(std::isfinite(s) && s > 0.0)) fail(CR_INVALID, "lambda_scale must be finite and > 0");
+        chh[c].lscale = s;
+        chh[c].kx = fix_scale_of(s, gi.du, false);
+        chh[c].ky = fix_scale_of(s, gi.dv, false);
+        chh[c].kdx = fix_scale_of(s, dus, true);
+        chh[c].kdy = fix_scale_of(s, dvs, true);
+    }
+    CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", chh.size() * sizeof(CubeChan));
+    CR_CUDA_CHECK(cudaMemcpyAsync(chd, chh.data(), chh.size() * sizeof(CubeChan),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    cr.rec = (uint4*)workspace(ctx, "cube_rec", ns * 16);
+    cr.rec_w = (float*)workspace(ctx, "cube_rec_w", ns * 4);
+    cr.bin_start = (uint32_t*)workspace(ctx, "cube_bin_start", (size_t)(nbins + 1) * 4);
+    uint32_t* hist = (uint32_t*)workspace(ctx, "cube_hist", (size_t)(nbins + 1) * 4);
+    cr.sumwt = (double*)workspace(ctx, "cube_sumwt", (size_t)in.C * 8);
+    cr.counts = (unsigned long long*)workspace(ctx, "cube_counts", (size_t)in.C * 16 + 8);
+    cr.n_rec = cr.counts + 2 * in.C;
+    CR_CUDA_CHECK(cudaMemsetAsync(hist, 0, (size_t)(nbins + 1) * 4, ctx->stream));
+    CR_CUDA_CHECK(cudaMemsetAsync(cr.sumwt, 0, (size_t)in.C * 8, ctx->stream));
+    CR_CUDA_CHECK(cudaMemsetAsync(cr.counts, 0, (size_t)in.C * 16 + 8, ctx->stream));
+
+    CubeArgs a{};
+    a.R = in.R;
+    a.C = in.C;
+    a.u = in.u;
+    a.v = in.v;
+    a.ch = chd;
+    a.vis = in.vis;
+    a.weight = in.weight;
+    a.flags = in.flags;
+    a.du = gi.du;
+    a.dv = gi.dv;
+    a.gnx = gi.grid_nx;
+    a.gny = gi.grid_ny;
+    a.os = gi.oversampling;
+    a.tap_rows = g->tap_rows;
+    a.ntx = cr.ntx;
+    a.nty = cr.nty;
+    a.cx_fix = (long long)gi.grid_nx << (kFixF - 1);
+    a.cy_fix = (long long)gi.grid_ny << (kFixF - 1);
+    a.nx = g->geom.nx;
+    a.ny = g->geom.ny;
+    a.dus = dus;
+    a.dvs = dvs;
+    a.dcx = (double)g->geom.nx / 2.0;
+    a.dcy = (double)g->geom.ny / 2.0;
+    a.dcx_fix = (long long)g->geom.nx << (kFixF - 1);
+    a.dcy_fix = (long long)g->geom.ny << (kFixF - 1);
+    a.mode = mode;
+    a.hist = hist;
+    a.cursor = hist;
+    a.sumwt = cr.sumwt;
+    a.counts = cr.counts;
+    a.rec = cr.rec;
+    a.rec_w = cr.rec_w;
+    const dim3 grid((unsigned)std::max<int64_t>((in.R + kRowsPerBlock - 1) / kRowsPerBlock, 1),
+                    (unsigned)in.C);
+    if (mode != CR_WEIGHT_NATURAL) {
+        const int64_t cells = (int64_t)g->geom.nx * g->geom.ny;
+        a.density = (float*)workspace(ctx, "cube_density", (size_t)(in.C * cells) * 4);
+        CR_CUDA_CHECK(cudaMemsetAsync(a.density, 0, (size_t)(in.C * cells) * 4, ctx->stream));
+        if (in.R > 0) {
+            cube_density_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
+            note_launch(ctx, "cube_density_kernel");
+        }
+        float* f2 = (float*)workspace(ctx, "cube_f2", (size_t)in.C * 4);
+        if (mode == CR_WEIGHT_BRIGGS) {
+            double* sums = (double*)workspace(ctx, "cube_dsums", (size_t)in.C * 16);
+            CR_CUDA_CHECK(cudaMemsetAsync(sums, 0, (size_t)in.C * 16, ctx->stream));
+            const dim3 sg((unsigned)std::min<int64_t>((cells + 255) / 256, 64), (unsigned)in.C);
+            cube_density_sums<<<sg, 256, 0, ctx->stream>>>(a.density, cells, sums);
+            note_launch(ctx, "cube_density_sums");
+            const double am = 5.0 * std::pow(10.0, -(double)robust);
+            cube_f2_kernel<<<(in.C + 127) / 128, 128, 0, ctx->stream>>>(sums, in.C, am * am, f2);
+            note_launch(ctx, "cube_f2_kernel");
+        }
+        a.f2 = f2;
+    }
+    if (taps) {
+        if (in.R > 0) {
+            cube_taps_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a, *taps);
+            note_launch(ctx, "cube_taps_kernel");
+        }
+        return cr;
+    }
+    if (in.R > 0) {
+        const size_t smem = cr.ntiles <= kSmemBins ? (size_t)cr.ntiles * 4 : 0;
+        cube_hist_kernel<<<grid, kCubeThreads, smem, ctx->stream>>>(a);
+        note_launch(ctx, "cube_hist_kernel");
+    }
+    exclusive_scan_u32(ctx, hist, cr.bin_start, nbins + 1, nullptr);
+    // the cursor starts at each bin's first slot; the total lands in n_rec
+    CR_CUDA_CHECK(cudaMemcpyAsync(hist, cr.bin_start, (size_t)(nbins + 1) * 4,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+    if (in.R > 0) {
+        cube_scatter_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
+        note_launch(ctx, "cube_scatter_kernel");
+    }
+    return cr;
+}
+
+void cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf, float2* dirty) {
+    const cr_grid_info& gi = g->info;
+    unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
+    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
+    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, g->taps_d, cr.ntx, cr.nty, gi.grid_nx,
+                   gi.grid_ny, (int64_t)cr.C * cr.ntiles, counter, psf, dirty};
+    int sms = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    kernel_mark(ctx, 0, false);
+    cube_grid_kernel<<<sms * 6, kCubeThreads, 0, ctx->stream>>>(a);
+    note_launch(ctx, "cube_grid_kernel");
+    kernel_mark(ctx, 0, true);
+}
+
+void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
+                 float2* pred) {
+    const cr_grid_info& gi = g->info;
+    CR_CUDA_CHECK(cudaMemsetAsync(pred, 0, (size_t)cr.C * cr.R * 8, ctx->stream));
+    unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
+    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
+    CubeDegridArgs a{cr.rec, cr.bin_start, cr.ntiles, cr.nty, gi.grid_nx, gi.grid_ny, cr.R,
+                     (int64_t)cr.C * cr.ntiles, counter, g->taps_d, grid, pred};
+    int sms = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    kernel_mark(ctx, 1, false);
+    cube_degrid_kernel<<<sms * 8, kCubeThreads, 0, ctx->stream>>>(a);
+    note_launch(ctx, "cube_degrid_kernel");
+    kernel_mark(ctx, 1, true);
+}
+
+void cube_read_sums(cr_ctx* ctx, const CubeRecords& cr, cr_sums* out) {
+    if (!out) return;
+    std::vector<double> sw((size_t)cr.C);
+    std::vector<unsigned long long> cnt((size_t)cr.C * 2);
+    CR_CUDA_CHECK(cudaMemcpyAsync(sw.data(), cr.sumwt, sw.size() * 8, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CR_CUDA_CHECK(cudaMemcpyAsync(cnt.data(), cr.counts, cnt.size() * 8, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < cr.C; ++c) {
+        out[c].normalization_sumwt = sw[c];
+        out[c].reported_sumwt = sw[c];
+        out[c].gridded = (int64_t)cnt[2 * c];
+        out[c].skipped = (int64_t)cnt[2 * c + 1];
+        out[c].unique_records = (int64_t)cnt[2 * c];
+        out[c].taps = 49 * (int64_t)cnt[2 * c];
+    }
+}
+
+}  // namespace cr

@@ -1,0 +1,129 @@
+// cr_fixed.cuh -- exact index selection with integer arithmetic.
+//
+// The reference chooses cells and oversampling offsets from FP64 values
+// such as x = RN(RN(RN(u_m * s) / du) + G/2) (grid_coordinate_x,
+// gridder.rs:1877-1879, after the cube batch scaling u = u_m * f/c of
+// casars-imager/src/lib.rs:49571-49573) and then rounds half away from zero
+// (sample_tap_span, gridder.rs:1976-1995).  FP64 runs at a small fraction of
+// the FP32/integer rate on this GPU, so the common path evaluates the exact
+// real value x* = u_m * (s/du) + G/2 in 64-bit fixed point instead:
+//
+//   * a = +-Ma 2^(ex-1075) (Ma the 53-bit significand) times a constant
+//     K = m 2^e (m a 64-bit significand computed on the host to at least 63
+//     correct bits) is formed with one 64 x 64 -> high-64 multiply and a
+//     shift to F = 40 fractional bits; its error is below 4 units of 2^-40;
+//   * the reference's own value differs from x* by at most 2^-38 for
+//     |x| < 2^14 (three roundings of relative size 2^-53);
+//   * every decision (the anchor, the offset, the density cell) compares x
+//     against boundaries -- half-integers, or anchor - (k + 1/2)/os -- and is
+//     taken only when x lies more than 2^-30 from the nearest one.
+//     Otherwise the caller redoes the sample with the reference's FP64
+//     operations (about one sample in 2^20).
+// Decisions taken on the fixed-point path therefore equal the FP64 ones.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+namespace cr {
+
+// K ~= m * 2^e with m in [2^63, 2^64).
+struct FixScale {
+    unsigned long long m;
+    int e;
+    int pad;
+};
+
+constexpr int kFixF = 40;
+constexpr long long kFixOne = 1ll << kFixF;
+constexpr long long kFixHalf = kFixOne >> 1;
+constexpr long long kFixMask = kFixOne - 1;
+constexpr long long kFixMargin = 1ll << (kFixF - 30);
+
+// K = num / den (or num * den when `multiply`), rounded to 64 significant
+// bits in long double (at least 64-bit significand on both supported hosts).
+inline FixScale fix_scale_of(double num, double den, bool multiply) {
+    long double k = multiply ? (long double)num * (long double)den
+                             : (long double)num / (long double)den;
+    FixScale s{0ull, 0, 0};
+    if (!(k > 0.0L) || !std::isfinite((double)k)) return s;
+    int e = 0;
+    long double f = std::frexp(k, &e);            // k = f 2^e, f in [0.5, 1)
+    long double mf = std::ldexp(f, 64);           // [2^63, 2^64)
+    unsigned long long m = (unsigned long long)mf;
+    if (m < (1ull << 63)) m = 1ull << 63;
+    s.m = m;
+    s.e = e - 64;
+    return s;
+}
+
+// t ~= a * K * 2^F (|error| < 4 units).  False when a is not finite, is
+// subnormal, or |a * K| >= 2^21 (the caller then takes the FP64 path).
+__device__ __forceinline__ bool fix_mul(double a, FixScale k, long long* t) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0) {
+        if ((b << 1) == 0ull) {
+            *t = 0;
+            return true;
+        }
+        return false;
+    }
+    if (ex == 0x7ff || k.m == 0ull) return false;
+    const unsigned long long ma = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 11;
+    const unsigned long long h = __umul64hi(ma, k.m);   // [2^62, 2^64)
+    // a * K = h * 2^(ex - 1086 + e + 64) up to the dropped low product
+    const int sh = ex - 1022 + k.e + kFixF;
+    if (sh > -3) return false;
+    const int r = -sh;
+    const unsigned long long v = r >= 64 ? 0ull : (h >> r);
+    *t = (b >> 63) ? -(long long)v : (long long)v;
+    return true;
+}
+
+// round half away from zero of X * 2^-F.  Returns false when X lies within
+// `margin` of a half-integer boundary.
+__device__ __forceinline__ bool fix_round(long long X, long long margin, long long* out) {
+    const long long ax = X < 0 ? -X : X;
+    const long long z = ax + kFixHalf;
+    const long long rem = z & kFixMask;
+    if (rem < margin || rem > kFixOne - margin) return false;
+    const long long q = z >> kFixF;
+    *out = X < 0 ? -q : q;
+    return true;
+}
+
+// sample_tap_span (gridder.rs:1976-1995) of the coordinate X * 2^-F:
+// 1 = accepted (start cell, tap row), 0 = rejected, -1 = too close to a
+// rounding boundary to decide.
+__device__ __forceinline__ int fix_tap_span(long long X, int64_t size, int32_t os, int32_t rows,
+                                            int64_t* start, int32_t* row) {
+    long long anchor;
+    if (!fix_round(X, kFixMargin, &anchor)) return -1;
+    if (anchor - 3 < 0 || anchor + 3 >= size) return 0;
+    const long long d = (anchor << kFixF) - X;   // (anchor - x) 2^F, |d| <= 1/2 + margin
+    long long off;
+    if (!fix_round(d * (long long)os, kFixMargin * (long long)os, &off)) return -1;
+    const long long idx = off + os / 2;
+    if (idx < 0 || idx >= rows) return 0;
+    *start = anchor - 3;
+    *row = (int32_t)idx;
+    return 1;
+}
+
+// sample_tap_span in the reference's FP64 operations.
+__device__ __forceinline__ bool f64_tap_span(double coord, int64_t size, int32_t os,
+                                             int32_t rows, int64_t* start, int32_t* row) {
+    if (!isfinite(coord) || !(fabs(coord) < 1.0e15)) return false;
+    const int64_t anchor = (int64_t)round(coord);
+    const int64_t off = (int64_t)round(__dmul_rn(__dsub_rn((double)anchor, coord), (double)os));
+    const int64_t s = anchor - 3, e = anchor + 3;
+    if (s < 0 || e >= size) return false;
+    const int64_t idx = off + os / 2;
+    if (idx < 0 || idx >= rows) return false;
+    *start = s;
+    *row = (int32_t)idx;
+    return true;
+}
+
+}  // namespace cr

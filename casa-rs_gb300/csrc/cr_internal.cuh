@@ -218,8 +218,14 @@ struct CubeRecords {
     unsigned long long* counts = nullptr;  // [C][2] gridded, skipped
     unsigned long long* n_rec = nullptr;
 };
+// Per-sample outputs of cube_sample_taps ([C][R], -1 / 0 when not gridded).
+struct CubeTaps {
+    int32_t *start_x, *start_y, *row_x, *row_y;
+    float* weight;
+};
+// With `taps`, only the weighting and the per-sample plan run.
 CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
-                      float robust);
+                      float robust, const CubeTaps* taps = nullptr);
 // psf [C][gnx][gny] float32 (real part), dirty [C][gnx][gny] complex64
 void cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf, float2* dirty);
 // pred [C][R] complex64, zero for samples that are not gridded
@@ -233,7 +239,7 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
 
 // ---- weighting / Hogbom ----------------------------------------------------------
 void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t mode,
-                     float robust, float* out_weight, float* f2_out);
+                     float robust, float* out_weight, float* f2_out, int32_t convention = 0);
 void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
             int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,

@@ -1,7 +1,8 @@
 // cr_weight.cu -- natural, uniform and Briggs weighting.
 //
-// Restates apply_weighting_with_density_source in the Combined density mode
-// (weighting.rs:1055-1180): the density grid is image-sized, every sample
+// Restates apply_weighting_with_density_source (weighting.rs:1055-1180) in the
+// Combined density mode, or with the cube PerPlane cells (rounded FP64
+// u*scale + centre, weighting.rs:1455-1483): the density grid is image-sized, every sample
 // with a finite positive weight adds its weight at its VisImagingWeight cell
 // and at the cell of its Hermitian mirror (accumulate_density_sample_serial,
 // weighting.rs:1831-1854; weight_density_cell_anchor, gridder.rs:1888-1934,
@@ -21,10 +22,23 @@ namespace {
 struct DensityCellParams {
     int32_t nx, ny;
     float u_scale, v_scale, cx, cy;
+    int32_t convention;          // 0 VisImagingWeight, 1 cube PerPlane (rounded, FP64)
+    double du_scale, dv_scale, dcx, dcy;
 };
 
 __device__ __forceinline__ bool density_cell(const DensityCellParams& p, double u, double v,
                                              int* ox, int* oy) {
+    if (p.convention == 1) {
+        // CubeBriggsWeightor{Density,Lookup}: u*scale + centre in FP64, rounded
+        const double x = __dadd_rn(__dmul_rn(u, p.du_scale), p.dcx);
+        const double y = __dadd_rn(__dmul_rn(-v, p.dv_scale), p.dcy);
+        if (!isfinite(x) || !isfinite(y)) return false;
+        const double rx = round(x), ry = round(y);
+        if (!(rx >= 1.0 && ry >= 1.0 && rx < (double)p.nx && ry < (double)p.ny)) return false;
+        *ox = (int)rx;
+        *oy = (int)ry;
+        return true;
+    }
     float uf = __double2float_rn(u), vf = __double2float_rn(v);
     float x = __fadd_rn(__fmul_rn(-uf, p.u_scale), p.cx);
     float y = __fadd_rn(__fmul_rn(vf, p.v_scale), p.cy);
@@ -95,7 +109,7 @@ __global__ void reweight_kernel(const double* u, const double* v, const float* w
 }  // namespace
 
 void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t mode,
-                     float robust, float* out_weight, float* f2_out) {
+                     float robust, float* out_weight, float* f2_out, int32_t convention) {
     if (mode != CR_WEIGHT_NATURAL && mode != CR_WEIGHT_UNIFORM && mode != CR_WEIGHT_BRIGGS)
         fail(CR_INVALID, "unknown weighting mode");
     const int32_t nx = g->geom.nx, ny = g->geom.ny;
@@ -106,6 +120,11 @@ void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t m
     p.v_scale = (float)((double)ny * g->geom.cell_y_rad);
     p.cx = (float)((double)nx / 2.0);
     p.cy = (float)((double)ny / 2.0);
+    p.convention = convention;
+    p.du_scale = (double)nx * g->geom.cell_x_rad;
+    p.dv_scale = (double)ny * g->geom.cell_y_rad;
+    p.dcx = (double)nx / 2.0;
+    p.dcy = (double)ny / 2.0;
     float f2 = 0.0f;
     float* density = nullptr;
     if (mode != CR_WEIGHT_NATURAL) {

@@ -250,6 +250,55 @@ int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
 int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
                float* image, int32_t out_location, char** err);
 
+/* ---- batched spectral cube ------------------------------------------------
+ * Channel c's batch is the unflagged samples of rows r = 0..rows-1 with
+ * u_lambda = u_m[r] * lambda_scale[c], v_lambda = v_m[r] * lambda_scale[c]
+ * (the cube batch assembly of casars-imager/src/lib.rs:49571-49576:
+ * lambda_scale = channel frequency / speed of light; flagged samples are left
+ * out of the channel batch).  vis, weight and flags are channel-major
+ * [channels][rows]; lambda_scale is host memory, the other arrays are at
+ * `location`.  Weighting is per channel with the PerPlane density of cube
+ * imaging (weighting.rs:1055-1180 with weighting.rs:1455-1483: the density
+ * at the rounded cell, Hermitian mirror included); gridding is the standard
+ * PSWF gridder (support 3) of every channel.  All channels are planned and
+ * gridded by one fixed sequence of launches (it does not grow with the
+ * number of channels).  channels * rows must stay below 2^32. */
+typedef struct {
+    int64_t rows;
+    int32_t channels;
+    const double* u_m;            /* [rows] metres */
+    const double* v_m;            /* [rows] metres */
+    const double* lambda_scale;   /* [channels], host memory */
+    const float* vis;             /* [channels][rows] complex64 */
+    const float* weight;          /* [channels][rows] or NULL (all 1) */
+    const uint8_t* flags;         /* [channels][rows], nonzero = flagged, or NULL */
+    int32_t location;
+} cr_cube_batch;
+
+/* psf_grids [channels][gnx][gny] float32 (real part of each channel's PSF
+ * grid), dirty_grids [channels][gnx][gny] complex64, sums[channels]. */
+int cr_cube_grid_dirty(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                       int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
+                       int32_t out_location, cr_sums* sums, char** err);
+/* pred [channels][rows] complex64 = degridded model_grids [channels][gnx][gny]
+ * complex64 (degrid_sample_taps_planned_normalized, gridder.rs:1278-1312);
+ * 0 for samples the gridder skips. */
+int cr_cube_degrid(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t weighting,
+                   float robust, const float* model_grids, int32_t grid_location, float* pred,
+                   int32_t out_location, char** err);
+/* Both from one plan of the batch (one grid + degrid pass of the cube). */
+int cr_cube_grid_degrid(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
+                        const float* model_grids, int32_t grid_location, float* pred,
+                        int32_t out_location, cr_sums* sums, char** err);
+/* The per-sample plan of every channel ([channels][rows] int32 / float32):
+ * start cell and tap row per axis (sample_tap_span, gridder.rs:1976-1995)
+ * and the imaging weight; -1 and 0 for samples that are not gridded. */
+int cr_cube_sample_taps(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, int32_t* start_x, int32_t* start_y,
+                        int32_t* row_x, int32_t* row_y, float* imaging_weight,
+                        int32_t out_location, char** err);
+
 /* ---- weighting -----------------------------------------------------------
  * apply_weighting_with_density_source, Combined density
  * (weighting.rs:1055-1180): natural passes weights through; uniform and
@@ -258,6 +307,12 @@ int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
 int cr_apply_weighting(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch, int32_t mode,
                        float robust, float* out_weight, int32_t out_location, float* f2,
                        char** err);
+/* The same with the PerPlane density of cube imaging, one channel's batch
+ * (density_build_cell_convention / density_cell_convention with
+ * WeightDensityMode::PerPlane, weighting.rs:1455-1483: rounded FP64 cells). */
+int cr_apply_weighting_plane(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch,
+                             int32_t mode, float robust, float* out_weight,
+                             int32_t out_location, float* f2, char** err);
 
 /* ---- Hogbom minor cycle --------------------------------------------------
  * run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883): one

@@ -238,6 +238,22 @@ int oc_std_plan(const oc_std_gridder* g, double u, double v, int64_t* x0, int64_
     return 1;
 }
 
+/* oc_std_plan over arrays: start cells and tap rows, -1 when rejected. */
+void oc_std_plan_many(const oc_std_gridder* g, int64_t n, const double* u, const double* v,
+                      int32_t* x0, int32_t* y0, int32_t* wx, int32_t* wy) {
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t a, b, c, d;
+        if (oc_std_plan(g, u[i], v[i], &a, &b, &c, &d)) {
+            x0[i] = (int32_t)a;
+            y0[i] = (int32_t)b;
+            wx[i] = (int32_t)c;
+            wy[i] = (int32_t)d;
+        } else {
+            x0[i] = y0[i] = wx[i] = wy[i] = -1;
+        }
+    }
+}
+
 static int oc_finite_f(float a) { return isfinite(a); }
 
 typedef struct {
@@ -1132,19 +1148,27 @@ int oc_density_cell(int64_t nx, int64_t ny, double cell_x, double cell_y, double
 }
 
 /* build_density_grid_serial / accumulate_density_sample_serial
- * (weighting.rs:1747-1854) with the Hermitian mirror. */
-void oc_density_grid(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
-                     const double* u, const double* v, const float* weight, float* density) {
+ * (weighting.rs:1747-1854) with the Hermitian mirror, at the cells of
+ * `convention` (0 VisImagingWeight, 1 the cube PerPlane rounding of
+ * density_build_cell_convention, weighting.rs:1470-1483). */
+void oc_density_grid_conv(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                          const double* u, const double* v, const float* weight, int convention,
+                          float* density) {
     memset(density, 0, (size_t)(nx * ny) * sizeof(float));
     for (int64_t i = 0; i < n; ++i) {
         float w = weight[i];
         if (!(isfinite(w) && w > 0.0f)) continue;
         int64_t x, y;
-        if (oc_density_cell(nx, ny, cell_x, cell_y, u[i], v[i], 0, &x, &y))
+        if (oc_density_cell(nx, ny, cell_x, cell_y, u[i], v[i], convention, &x, &y))
             density[x * ny + y] = density[x * ny + y] + w;
-        if (oc_density_cell(nx, ny, cell_x, cell_y, -u[i], -v[i], 0, &x, &y))
+        if (oc_density_cell(nx, ny, cell_x, cell_y, -u[i], -v[i], convention, &x, &y))
             density[x * ny + y] = density[x * ny + y] + w;
     }
+}
+
+void oc_density_grid(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                     const double* u, const double* v, const float* weight, float* density) {
+    oc_density_grid_conv(nx, ny, cell_x, cell_y, n, u, v, weight, 0, density);
 }
 
 /* Briggs f2 of apply_weighting_with_density_source (weighting.rs:1108-1121):
@@ -1166,10 +1190,11 @@ float oc_briggs_denominator(float density, float f2) {
 }
 
 /* reweight_batch (weighting.rs:2094-2150): mode 0 natural, 1 uniform,
- * 2 Briggs. */
-void oc_reweight(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
-                 const double* u, const double* v, const float* weight, const float* density,
-                 int mode, float f2, float* out_weight) {
+ * 2 Briggs; density looked up at the cells of `convention`. */
+void oc_reweight_conv(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                      const double* u, const double* v, const float* weight,
+                      const float* density, int mode, float f2, int convention,
+                      float* out_weight) {
     for (int64_t i = 0; i < n; ++i) {
         float w = weight[i];
         if (mode == 0) {
@@ -1177,7 +1202,7 @@ void oc_reweight(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n
             continue;
         }
         int64_t x, y;
-        if (!oc_density_cell(nx, ny, cell_x, cell_y, u[i], v[i], 0, &x, &y)) {
+        if (!oc_density_cell(nx, ny, cell_x, cell_y, u[i], v[i], convention, &x, &y)) {
             out_weight[i] = 0.0f;
             continue;
         }
@@ -1188,6 +1213,12 @@ void oc_reweight(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n
         }
         out_weight[i] = mode == 1 ? w / d : w / oc_briggs_denominator(d, f2);
     }
+}
+
+void oc_reweight(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                 const double* u, const double* v, const float* weight, const float* density,
+                 int mode, float f2, float* out_weight) {
+    oc_reweight_conv(nx, ny, cell_x, cell_y, n, u, v, weight, density, mode, f2, 0, out_weight);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -62,6 +62,8 @@ int oc_std_tap_span(const oc_std_gridder* g, double coordinate, int64_t size,
                     int64_t* start, int64_t* weight_index);
 int oc_std_plan(const oc_std_gridder* g, double u, double v, int64_t* x0, int64_t* y0,
                 int64_t* wx, int64_t* wy);
+void oc_std_plan_many(const oc_std_gridder* g, int64_t n, const double* u, const double* v,
+                      int32_t* x0, int32_t* y0, int32_t* wx, int32_t* wy);
 void oc_std_grid_dirty(const oc_std_gridder* g, int64_t n, const double* u, const double* v,
                        const float* weight, const float* sumwt_factor, const uint8_t* gridable,
                        const float* vis, double* psf_grid, double* dirty_grid, oc_accum* acc,
@@ -118,11 +120,18 @@ int oc_density_cell(int64_t nx, int64_t ny, double cell_x, double cell_y, double
                     int convention, int64_t* cx, int64_t* cy);
 void oc_density_grid(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
                      const double* u, const double* v, const float* weight, float* density);
+void oc_density_grid_conv(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                          const double* u, const double* v, const float* weight, int convention,
+                          float* density);
 float oc_briggs_f2(const float* density, int64_t cells, float robust);
 float oc_briggs_denominator(float density, float f2);
 void oc_reweight(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
                  const double* u, const double* v, const float* weight, const float* density,
                  int mode, float f2, float* out_weight);
+void oc_reweight_conv(int64_t nx, int64_t ny, double cell_x, double cell_y, int64_t n,
+                      const double* u, const double* v, const float* weight,
+                      const float* density, int mode, float f2, int convention,
+                      float* out_weight);
 
 /* ---- Hogbom ------------------------------------------------------------- */
 int oc_peak_location(const float* image, const uint8_t* mask, int64_t nx, int64_t ny,

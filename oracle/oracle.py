@@ -92,6 +92,10 @@ def _declare(L):
         "oc_density_cell": (C.c_int, [_i64, _i64, _d, _d, _d, _d, C.c_int, C.POINTER(_i64),
                                       C.POINTER(_i64)]),
         "oc_density_grid": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, _p]),
+        "oc_density_grid_conv": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, C.c_int, _p]),
+        "oc_reweight_conv": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, _p, C.c_int, _f,
+                                    C.c_int, _p]),
+        "oc_std_plan_many": (None, [C.POINTER(StdParams), _i64, _p, _p, _p, _p, _p, _p]),
         "oc_briggs_f2": (_f, [_p, _i64, _f]),
         "oc_briggs_denominator": (_f, [_f, _f]),
         "oc_reweight": (None, [_i64, _i64, _d, _d, _i64, _p, _p, _p, _p, C.c_int, _f, _p]),
@@ -209,6 +213,14 @@ class StdGridder:
         ok = lib().oc_std_plan(C.byref(self._p), u, v, C.byref(x0), C.byref(y0), C.byref(wx),
                                C.byref(wy))
         return (int(x0.value), int(y0.value), int(wx.value), int(wy.value)) if ok else None
+
+    def plan_many(self, u, v):
+        """sample_tap_span over arrays: (start x, start y, x tap row, y tap row),
+        -1 where the sample is rejected."""
+        u, v = _c(u, np.float64), _c(v, np.float64)
+        out = [np.zeros(len(u), np.int32) for _ in range(4)]
+        lib().oc_std_plan_many(C.byref(self._p), len(u), _ptr(u), _ptr(v), *[_ptr(o) for o in out])
+        return out
 
     def grid_dirty(self, u, v, weight, vis, sumwt_factor=None, gridable=None, threads=1):
         """accumulate_dirty_psf_and_residual_standard_streaming_grid (lib.rs:68306-68500)."""
@@ -457,12 +469,13 @@ def density_cell(geom: Geometry, u: float, v: float, convention: int = 0):
     return (int(cx.value), int(cy.value)) if ok else None
 
 
-def density_grid(geom: Geometry, u, v, weight):
-    """build_density_grid_serial (weighting.rs:1729-1854)."""
+def density_grid(geom: Geometry, u, v, weight, convention: int = 0):
+    """build_density_grid_serial (weighting.rs:1729-1854); convention 1 is the
+    cube PerPlane rounding (weighting.rs:1470-1483)."""
     u, v, weight = _c(u, np.float64), _c(v, np.float64), _c(weight, np.float32)
     d = np.zeros((geom.nx, geom.ny), np.float32)
-    lib().oc_density_grid(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u), _ptr(v),
-                          _ptr(weight), _ptr(d))
+    lib().oc_density_grid_conv(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u),
+                               _ptr(v), _ptr(weight), convention, _ptr(d))
     return d
 
 
@@ -475,17 +488,19 @@ def briggs_denominator(density: float, f2: float) -> float:
     return float(lib().oc_briggs_denominator(density, f2))
 
 
-def apply_weighting(geom: Geometry, u, v, weight, mode: str = "natural", robust: float = 0.0):
-    """apply_weighting_with_density_source, Combined mode (weighting.rs:1055-1180)."""
+def apply_weighting(geom: Geometry, u, v, weight, mode: str = "natural", robust: float = 0.0,
+                    convention: int = 0):
+    """apply_weighting_with_density_source (weighting.rs:1055-1180): Combined
+    density (convention 0) or the cube's PerPlane density (convention 1)."""
     u, v, weight = _c(u, np.float64), _c(v, np.float64), _c(weight, np.float32)
     if mode == "natural":
         return weight.copy(), None, 0.0
-    d = density_grid(geom, u, v, weight)
+    d = density_grid(geom, u, v, weight, convention)
     m = {"uniform": 1, "briggs": 2}[mode]
     f2 = briggs_f2(d, robust) if m == 2 else 0.0
     out = np.zeros_like(weight)
-    lib().oc_reweight(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u), _ptr(v),
-                      _ptr(weight), _ptr(d), m, f2, _ptr(out))
+    lib().oc_reweight_conv(geom.nx, geom.ny, geom.cell_x, geom.cell_y, len(u), _ptr(u), _ptr(v),
+                           _ptr(weight), _ptr(d), m, f2, convention, _ptr(out))
     return out, d, f2
 
 
