@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--no-cube", action="store_true",
                     help="skip the batched-cube versus per-channel-loop comparison")
     ap.add_argument("--cube-channels", type=int, default=256)
+    ap.add_argument("--cube-only", action="store_true",
+                    help="run only the cube comparison (profiling runs)")
+    ap.add_argument("--cube-no-plain", action="store_true",
+                    help="time only the batched cube path (profiling runs)")
     return ap.parse_args()
 
 
@@ -237,7 +241,7 @@ def run_cube(args, ctx, dev, peak):
         cc.cube_grid_degrid(gg, cube, model, "briggs", 0.5)
         last["t2"] = ctx.last_timings()
 
-    steps = max(3, min(args.steps, 10))
+    steps = max(1, min(args.steps, 10))
     ms_grid = timed(batched_grid, steps, 2)
     t_grid = last["t"]
     ms_both = timed(batched_both, steps, 2)
@@ -266,8 +270,11 @@ def run_cube(args, ctx, dev, peak):
                 cc.grid_dirty(gg, b1)
 
     psteps = 2
-    ms_plain = timed(lambda: plain(False), psteps, 1)
-    ms_plain_both = timed(lambda: plain(True), psteps, 1)
+    if args.cube_no_plain:
+        ms_plain = ms_plain_both = float("nan")
+    else:
+        ms_plain = timed(lambda: plain(False), psteps, 1)
+        ms_plain_both = timed(lambda: plain(True), psteps, 1)
     cells = gs[1] * gs[2]
     S_all = C * R
     b_grid = R * 24 + S_all * 13 + C * cells * 12
@@ -367,9 +374,12 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
+    ctx = cc.Context(local)
+    if args.cube_only:
+        print(json.dumps({"cube": run_cube(args, ctx, dev, measured_peaks()[0])}), flush=True)
+        return
     obs = workload(args.rows_fraction)
     n = obs.rows
-    ctx = cc.Context(local)
     gg = cc.StandardGridder(ctx, cc.ImageGeometry(obs.nx, obs.ny, obs.cell, obs.cell), 100)
     gw = cc.WProjector(gg, float(np.abs(obs.w).max()), planes=PLANES, sampling=SAMPLING,
                        support_law=SUPPORT_LAW)

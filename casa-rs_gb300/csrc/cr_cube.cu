@@ -43,6 +43,11 @@ namespace {
 constexpr int kCubeThreads = 256;
 constexpr int kRowsPerBlock = 4096;   // rows of one channel per planning block
 constexpr int kSmemBins = 8192;       // home tiles histogrammed in shared memory
+// Shared-memory tile rows are 39 floats apart (39 = 7 mod 32): the 49 taps
+// t = 7 ix + iy of one record then fall in 49 consecutive banks mod 32, so
+// each warp-wide atomic touches 32 distinct banks.
+constexpr int kRow = 39;
+constexpr int kMaxTapRows = 513;      // oversampling up to 512
 
 struct CubeChan {
     double lscale;       // f / c
@@ -79,6 +84,11 @@ struct CubeArgs {
     unsigned long long* counts;// [C][2]: gridded, skipped
     uint4* rec;                // {meta, c R + r, w vis.re, w vis.im}
     float* rec_w;
+    // per-sample results kept between the passes ([C][R])
+    uint32_t* dcell;           // density cell x ny + y of (u, v), ~0 when none
+    uint32_t* ev_tile;         // home tile, ~0 when the sample is not gridded
+    uint32_t* ev_meta;         // cell in tile | tap rows
+    float* ev_w;               // imaging weight
 };
 
 // weight_density_cell_anchor with the cube (rounded) conventions.
@@ -120,49 +130,84 @@ struct Eval {
     float w;
 };
 
-// One sample of channel c: flags, reweighting, validity and taps.
-__device__ __forceinline__ Eval eval_sample(const CubeArgs& a, const CubeChan& ch, float f2,
-                                            int c, int64_t r) {
-    Eval e{false, 0u, 0u, 0.0f};
-    const int64_t i = (int64_t)c * a.R + r;
-    if (a.flags && a.flags[i]) return e;
-    float w = a.weight ? a.weight[i] : 1.0f;
-    const double um = a.u[r], vm = a.v[r];
+// Samples are evaluated kVec at a time per thread (rows row0 + 32 j): their
+// loads are issued together, so each thread keeps kVec gathers in flight.
+constexpr int kVec = 4;
+constexpr int kWarpRows = 32 * kVec;
+
+// kVec samples of channel c: flags, reweighting, validity and taps.
+__device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& ch, float f2,
+                                             int c, int64_t row0, int64_t r1,
+                                             Eval (&e)[kVec]) {
+    float w[kVec];
+    double um[kVec], vm[kVec];
+    bool live[kVec];
+#pragma unroll
+    for (int j = 0; j < kVec; ++j) {
+        const int64_t r = row0 + 32 * j;
+        e[j] = Eval{false, 0u, 0u, 0.0f};
+        live[j] = r < r1;
+        const int64_t i = (int64_t)c * a.R + (live[j] ? r : 0);
+        if (live[j] && a.flags) live[j] = a.flags[i] == 0;
+        w[j] = a.weight ? a.weight[i] : 1.0f;
+        um[j] = a.u[live[j] ? r : 0];
+        vm[j] = a.v[live[j] ? r : 0];
+    }
     if (a.mode != CR_WEIGHT_NATURAL) {
-        int x, y;
-        float nw = 0.0f;
-        if (density_cell(a, ch, um, vm, false, &x, &y)) {
-            const float d = a.density[((int64_t)c * a.nx + x) * a.ny + y];
-            if (finite_f(w) && w > 0.0f && finite_f(d) && d > 0.0f)
-                nw = a.mode == CR_WEIGHT_UNIFORM ? __fdiv_rn(w, d)
-                                                 : __fdiv_rn(w, __fadd_rn(__fmul_rn(d, f2), 1.0f));
+        float d[kVec];
+        const float* dens = a.density + (int64_t)c * a.nx * a.ny;
+        if (a.dcell) {
+            uint32_t cell[kVec];
+#pragma unroll
+            for (int j = 0; j < kVec; ++j)
+                cell[j] = live[j] ? a.dcell[(int64_t)c * a.R + row0 + 32 * j] : ~0u;
+#pragma unroll
+            for (int j = 0; j < kVec; ++j) d[j] = cell[j] != ~0u ? dens[cell[j]] : 0.0f;
+        } else {
+#pragma unroll
+            for (int j = 0; j < kVec; ++j) {
+                int x, y;
+                d[j] = 0.0f;
+                if (live[j] && density_cell(a, ch, um[j], vm[j], false, &x, &y))
+                    d[j] = dens[(int64_t)x * a.ny + y];
+            }
         }
-        w = nw;
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            float nw = 0.0f;
+            if (finite_f(w[j]) && w[j] > 0.0f && finite_f(d[j]) && d[j] > 0.0f)
+                nw = a.mode == CR_WEIGHT_UNIFORM
+                         ? __fdiv_rn(w[j], d[j])
+                         : __fdiv_rn(w[j], __fadd_rn(__fmul_rn(d[j], f2), 1.0f));
+            w[j] = nw;
+        }
     }
-    if (!(finite_f(w) && w > 0.0f)) return e;
-    int64_t x0 = 0, y0 = 0;
-    int32_t rx = 0, ry = 0;
-    int sx = -1, sy = -1;
-    long long tx, ty;
-    if (fix_mul(um, ch.kx, &tx) && fix_mul(vm, ch.ky, &ty)) {
-        sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
-        if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
-        if (sx == 0 || sy == 0) return e;
+#pragma unroll
+    for (int j = 0; j < kVec; ++j) {
+        if (!live[j] || !(finite_f(w[j]) && w[j] > 0.0f)) continue;
+        int64_t x0 = 0, y0 = 0;
+        int32_t rx = 0, ry = 0;
+        int sx = -1, sy = -1;
+        long long tx, ty;
+        if (fix_mul(um[j], ch.kx, &tx) && fix_mul(vm[j], ch.ky, &ty)) {
+            sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
+            if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
+            if (sx == 0 || sy == 0) continue;
+        }
+        if (sx < 0 || sy < 0) {
+            const double u = __dmul_rn(um[j], ch.lscale), v = __dmul_rn(vm[j], ch.lscale);
+            const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+            const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+            if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
+                !f64_tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry))
+                continue;
+        }
+        e[j].ok = true;
+        e[j].tile = (uint32_t)((x0 >> 5) * a.nty + (y0 >> 5));
+        e[j].meta = ((uint32_t)(x0 & 31) << 27) | ((uint32_t)(y0 & 31) << 22) |
+                    ((uint32_t)rx << 11) | (uint32_t)ry;
+        e[j].w = w[j];
     }
-    if (sx < 0 || sy < 0) {
-        const double u = __dmul_rn(um, ch.lscale), v = __dmul_rn(vm, ch.lscale);
-        const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
-        const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
-        if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
-            !f64_tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry))
-            return e;
-    }
-    e.ok = true;
-    e.tile = (uint32_t)((x0 >> 5) * a.nty + (y0 >> 5));
-    e.meta = ((uint32_t)(x0 & 31) << 27) | ((uint32_t)(y0 & 31) << 22) |
-             ((uint32_t)rx << 11) | (uint32_t)ry;
-    e.w = w;
-    return e;
 }
 
 __global__ void __launch_bounds__(kCubeThreads) cube_density_kernel(CubeArgs a) {
@@ -170,17 +215,36 @@ __global__ void __launch_bounds__(kCubeThreads) cube_density_kernel(CubeArgs a) 
     const CubeChan ch = a.ch[c];
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* dens = a.density + (int64_t)c * a.nx * a.ny;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
-        const int64_t i = (int64_t)c * a.R + r;
-        if (a.flags && a.flags[i]) continue;
-        const float w = a.weight ? a.weight[i] : 1.0f;
-        if (!(finite_f(w) && w > 0.0f)) continue;
-        int x, y;
-        if (density_cell(a, ch, a.u[r], a.v[r], false, &x, &y))
-            atomicAdd(&dens[(int64_t)x * a.ny + y], w);
-        if (density_cell(a, ch, a.u[r], a.v[r], true, &x, &y))
-            atomicAdd(&dens[(int64_t)x * a.ny + y], w);
+    for (int64_t base = r0 + warp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
+        float w[kVec];
+        double um[kVec], vm[kVec];
+        bool live[kVec];
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const int64_t r = base + lane + 32 * j;
+            live[j] = r < r1;
+            const int64_t i = (int64_t)c * a.R + (live[j] ? r : 0);
+            if (live[j] && a.flags) live[j] = a.flags[i] == 0;
+            w[j] = a.weight ? a.weight[i] : 1.0f;
+            um[j] = a.u[live[j] ? r : 0];
+            vm[j] = a.v[live[j] ? r : 0];
+        }
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const int64_t r = base + lane + 32 * j;
+            uint32_t cell = ~0u;
+            int x, y;
+            if (live[j] && density_cell(a, ch, um[j], vm[j], false, &x, &y)) {
+                cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
+                if (finite_f(w[j]) && w[j] > 0.0f) atomicAdd(&dens[cell], w[j]);
+            }
+            if (live[j] && finite_f(w[j]) && w[j] > 0.0f &&
+                density_cell(a, ch, um[j], vm[j], true, &x, &y))
+                atomicAdd(&dens[(int64_t)x * a.ny + y], w[j]);
+            if (r < r1) a.dcell[(int64_t)c * a.R + r] = cell;
+        }
     }
 }
 
@@ -201,9 +265,21 @@ __global__ void __launch_bounds__(kCubeThreads) cube_density_sums(const float* d
         s += __shfl_xor_sync(0xffffffffu, s, o);
         s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&sums[2 * c], s);
-        atomicAdd(&sums[2 * c + 1], s2);
+    __shared__ double sh[2][kCubeThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][warp] = s;
+        sh[1][warp] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, t2 = 0.0;
+        for (int k = 0; k < kCubeThreads / 32; ++k) {
+            t += sh[0][k];
+            t2 += sh[1][k];
+        }
+        atomicAdd(&sums[2 * c], t);
+        atomicAdd(&sums[2 * c + 1], t2);
     }
 }
 
@@ -244,18 +320,29 @@ __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
     double sw = 0.0;
     unsigned long long n_ok = 0, n_skip = 0;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
-        if (a.flags && a.flags[(int64_t)c * a.R + r]) continue;
-        const Eval e = eval_sample(a, ch, f2, c, r);
-        if (e.ok) {
-            ++n_ok;
-            sw += (double)e.w;
-            if (smem)
-                atomicAdd(&s_hist[e.tile], 1u);
-            else
-                atomicAdd(&ghist[e.tile], 1u);
-        } else {
-            ++n_skip;
+    const int wl = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
+        Eval e[kVec];
+        eval_samples(a, ch, f2, c, base + wl, r1, e);
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const int64_t r = base + wl + 32 * j;
+            if (r >= r1) continue;
+            const int64_t i = (int64_t)c * a.R + r;
+            a.ev_tile[i] = e[j].ok ? e[j].tile : ~0u;
+            a.ev_meta[i] = e[j].meta;
+            a.ev_w[i] = e[j].w;
+            if (a.flags && a.flags[i]) continue;
+            if (e[j].ok) {
+                ++n_ok;
+                sw += (double)e[j].w;
+                if (smem)
+                    atomicAdd(&s_hist[e[j].tile], 1u);
+                else
+                    atomicAdd(&ghist[e[j].tile], 1u);
+            } else {
+                ++n_skip;
+            }
         }
     }
     sw = warp_sum(sw);
@@ -285,39 +372,108 @@ __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
             if (s_hist[k]) atomicAdd(&ghist[k], s_hist[k]);
 }
 
-// Pass 2: scatter records into (channel, home tile) bins.
+// Pass 2: scatter records into (channel, home tile) bins from pass 1's
+// per-sample results.
 __global__ void __launch_bounds__(kCubeThreads) cube_scatter_kernel(CubeArgs a) {
     const int c = blockIdx.y;
-    const CubeChan ch = a.ch[c];
-    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
     const int64_t ntiles = a.ntx * a.nty;
     const int lane = threadIdx.x & 31;
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
-    // warp-uniform trip count so that the warp-aggregated atomics see whole warps
-    for (int64_t base = r0 + (threadIdx.x & ~31); base < r1; base += kCubeThreads) {
-        const int64_t r = base + lane;
-        Eval e{false, 0u, 0u, 0.0f};
-        if (r < r1) e = eval_sample(a, ch, f2, c, r);
-        const unsigned act = __ballot_sync(0xffffffffu, e.ok);
-        if (!e.ok) continue;
-        const uint32_t bin = (uint32_t)((int64_t)c * ntiles + e.tile);
-        const unsigned peers = __match_any_sync(act, bin);
-        const int leader = __ffs(peers) - 1;
-        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-        uint32_t pos0 = 0;
-        if (lane == leader) pos0 = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers));
-        pos0 = __shfl_sync(peers, pos0, leader);
-        const uint32_t pos = pos0 + rank;
-        const float2 vv = a.vis[(int64_t)c * a.R + r];
-        float vr = 0.0f, vi = 0.0f;
-        if (finite_f(vv.x) && finite_f(vv.y)) {
-            vr = __fmul_rn(vv.x, e.w);
-            vi = __fmul_rn(vv.y, e.w);
+    // warp-uniform trip counts so that the warp-aggregated atomics see whole warps
+    const int wp = threadIdx.x >> 5;
+    for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
+        uint32_t tile[kVec];
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const int64_t r = base + lane + 32 * j;
+            tile[j] = r < r1 ? a.ev_tile[(int64_t)c * a.R + r] : ~0u;
         }
-        a.rec[pos] = make_uint4(e.meta, (uint32_t)((int64_t)c * a.R + r), __float_as_uint(vr),
-                                __float_as_uint(vi));
-        a.rec_w[pos] = e.w;
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const bool ok = tile[j] != ~0u;
+            const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (!ok) continue;
+            const uint32_t bin = (uint32_t)((int64_t)c * ntiles + tile[j]);
+            const unsigned peers = __match_any_sync(act, bin);
+            const int leader = __ffs(peers) - 1;
+            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+            uint32_t pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers));
+            pos0 = __shfl_sync(peers, pos0, leader);
+            const uint32_t pos = pos0 + rank;
+            const float w = a.ev_w[i];
+            const float2 vv = a.vis[i];
+            float vr = 0.0f, vi = 0.0f;
+            if (finite_f(vv.x) && finite_f(vv.y)) {
+                vr = __fmul_rn(vv.x, w);
+                vi = __fmul_rn(vv.y, w);
+            }
+            a.rec[pos] = make_uint4(a.ev_meta[i], (uint32_t)i, __float_as_uint(vr),
+                                    __float_as_uint(vi));
+            a.rec_w[pos] = w;
+        }
+    }
+}
+
+constexpr uint32_t kGridChunk = 2048;   // source records per gridding work item
+constexpr uint32_t kDegridChunk = 4096; // records per degridding work item
+
+// Work lists.  Gridding: an output tile (channel, tx, ty) gathers the bins
+// (tx, ty), (tx-1, ty), (tx, ty-1), (tx-1, ty-1); their records, taken in
+// that order, are cut into chunks of kGridChunk.  A tile with one chunk is
+// written with plain stores; the chunks of a heavier tile add into the grid
+// with atomics after cube_work_fill zeroed it.  Degridding: each bin's
+// records in chunks of kDegridChunk.
+__device__ __forceinline__ uint32_t bin_count(const uint32_t* bin_start, int64_t bin) {
+    return bin_start[bin + 1] - bin_start[bin];
+}
+
+__device__ __forceinline__ uint32_t tile_sources(const uint32_t* bin_start, int64_t c,
+                                                 int64_t ntiles, int64_t nty, int64_t tx,
+                                                 int64_t ty) {
+    uint32_t n = 0;
+    for (int s = 0; s < 4; ++s) {
+        const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
+        if (sx >= 0 && sy >= 0) n += bin_count(bin_start, c * ntiles + sx * nty + sy);
+    }
+    return n;
+}
+
+__global__ void cube_work_count(const uint32_t* bin_start, int64_t nbins, int64_t ntiles,
+                                int64_t nty, uint32_t* grid_chunks, uint32_t* degrid_chunks) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = b / ntiles, T = b % ntiles;
+        const uint32_t n = tile_sources(bin_start, c, ntiles, nty, T / nty, T % nty);
+        grid_chunks[b] = n == 0 ? 1u : (n + kGridChunk - 1) / kGridChunk;
+        degrid_chunks[b] = (bin_count(bin_start, b) + kDegridChunk - 1) / kDegridChunk;
+    }
+}
+
+__global__ void cube_work_fill(const uint32_t* grid_chunks, const uint32_t* grid_first,
+                               const uint32_t* degrid_chunks, const uint32_t* degrid_first,
+                               int64_t nbins, int64_t ntiles, int64_t nty, int64_t gnx,
+                               int64_t gny, uint2* grid_items, uint2* degrid_items, float* psf,
+                               float2* dirty) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = grid_chunks[b], f = grid_first[b];
+        for (uint32_t k = 0; k < n; ++k) grid_items[f + k] = make_uint2((uint32_t)b, k);
+        const uint32_t nd = degrid_chunks[b], fd = degrid_first[b];
+        for (uint32_t k = 0; k < nd; ++k) degrid_items[fd + k] = make_uint2((uint32_t)b, k);
+        if (n > 1 && psf) {
+            const int64_t c = b / ntiles, T = b % ntiles;
+            const int64_t x0 = (T / nty) * kTile, y0 = (T % nty) * kTile;
+            float* pc = psf + c * gnx * gny;
+            float2* dc = dirty + c * gnx * gny;
+            for (int64_t x = x0; x < min(x0 + kTile, gnx); ++x)
+                for (int64_t y = y0; y < min(y0 + kTile, gny); ++y) {
+                    pc[x * gny + y] = 0.0f;
+                    dc[x * gny + y] = make_float2(0.0f, 0.0f);
+                }
+        }
     }
 }
 
@@ -326,59 +482,83 @@ struct CubeGridArgs {
     const float* rec_w;
     const uint32_t* bin_start;   // [C * ntiles + 1]
     const float* taps;           // [tap_rows][7]
+    int32_t tap_rows;
     int64_t ntx, nty, gnx, gny;
-    int64_t n_items;             // C * ntiles
+    const uint2* items;          // (output tile bin, chunk)
+    const uint32_t* grid_chunks; // chunks of each output tile
+    const unsigned long long* n_items;
     unsigned int* item_counter;
     float* psf;                  // [C][gnx][gny] real part of the PSF grid
     float2* dirty;               // [C][gnx][gny]
 };
 
-// One block per (channel, output tile): gather the footprints of the home
-// tiles (tx, ty), (tx-1, ty), (tx, ty-1), (tx-1, ty-1) that reach it.
-__global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a) {
-    __shared__ float s_psf[kTile * kTile];
-    __shared__ float s_re[kTile * kTile];
-    __shared__ float s_im[kTile * kTile];
+// A block per work item: the chunk's records (from the four source bins)
+// accumulate into a shared-memory copy of the output tile, which is then
+// stored (single-chunk tile) or added (heavier tile) to the grid.  A warp
+// loads 32 records, keeps those whose footprint reaches the tile and runs
+// them in turn, one lane per tap; tile rows are kRow floats apart so that a
+// record's 49 taps hit distinct banks.  (A variant with a private tile per
+// warp and plain read-modify-writes ran 1.5x slower: 8 warps per SM could
+// not hide the dependent shared-memory chain of consecutive records.)
+constexpr int kGridThreads = kCubeThreads;
+
+__global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a) {
+    __shared__ float s_psf[kTile * kRow];
+    __shared__ float s_re[kTile * kRow];
+    __shared__ float s_im[kTile * kRow];
+    __shared__ float s_taps[kMaxTapRows * 7];
     __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t ntiles = a.ntx * a.nty;
+    const unsigned long long n_items = *a.n_items;
+    for (int k = tid; k < a.tap_rows * 7; k += kGridThreads) s_taps[k] = a.taps[k];
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
         __syncthreads();
         const int64_t item = s_item;
-        if (item >= a.n_items) break;
-        const int64_t c = item / ntiles, T = item % ntiles;
+        if ((unsigned long long)item >= n_items) break;
+        const uint2 it = a.items[item];
+        const int64_t bin = it.x;
+        const int64_t c = bin / ntiles, T = bin % ntiles;
         const int64_t tx = T / a.nty, ty = T % a.nty;
+        const bool shared_tile = a.grid_chunks[bin] > 1;
+        const uint32_t clo = it.y * kGridChunk, chi = clo + kGridChunk;
         uint32_t b0[4], b1[4];
         int ox[4], oy[4];
         int nsrc = 0;
+        uint32_t off = 0;   // position of this source in the concatenated order
         for (int s = 0; s < 4; ++s) {
             const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
             if (sx < 0 || sy < 0) continue;
-            const int64_t bin = c * ntiles + sx * a.nty + sy;
-            const uint32_t lo = a.bin_start[bin], hi = a.bin_start[bin + 1];
-            if (lo == hi) continue;
-            b0[nsrc] = lo;
-            b1[nsrc] = hi;
-            ox[nsrc] = -(s & 1) * kTile;
-            oy[nsrc] = -(s >> 1) * kTile;
-            ++nsrc;
+            const int64_t sb = c * ntiles + sx * a.nty + sy;
+            const uint32_t lo = a.bin_start[sb], hi = a.bin_start[sb + 1];
+            const uint32_t n = hi - lo;
+            const uint32_t a0 = max(off, clo), a1 = min(off + n, chi);
+            if (a0 < a1) {
+                b0[nsrc] = lo + (a0 - off);
+                b1[nsrc] = lo + (a1 - off);
+                ox[nsrc] = -(s & 1) * kTile;
+                oy[nsrc] = -(s >> 1) * kTile;
+                ++nsrc;
+            }
+            off += n;
         }
         const int64_t gx0 = tx * kTile, gy0 = ty * kTile;
         float* psf_c = a.psf + c * a.gnx * a.gny;
         float2* dirty_c = a.dirty + c * a.gnx * a.gny;
         if (nsrc == 0) {
-            for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
-                const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
-                if (x < a.gnx && y < a.gny) {
-                    psf_c[x * a.gny + y] = 0.0f;
-                    dirty_c[x * a.gny + y] = make_float2(0.0f, 0.0f);
+            if (!shared_tile)
+                for (int k = tid; k < kTile * kTile; k += kGridThreads) {
+                    const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
+                    if (x < a.gnx && y < a.gny) {
+                        psf_c[x * a.gny + y] = 0.0f;
+                        dirty_c[x * a.gny + y] = make_float2(0.0f, 0.0f);
+                    }
                 }
-            }
             __syncthreads();
             continue;
         }
-        for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
+        for (int k = tid; k < kTile * kRow; k += kGridThreads) {
             s_psf[k] = 0.0f;
             s_re[k] = 0.0f;
             s_im[k] = 0.0f;
@@ -386,13 +566,14 @@ __global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a)
         __syncthreads();
         for (int s = 0; s < nsrc; ++s) {
             const int sox = ox[s], soy = oy[s];
-            for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kCubeThreads) {
-                // lanes look at 32 records; the warp then runs the relevant ones
+            for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kGridThreads) {
                 const uint32_t rr = base + lane;
                 uint4 q = make_uint4(0u, 0u, 0u, 0u);
+                float qw = 0.0f;
                 bool rel = false;
                 if (rr < b1[s]) {
                     q = a.rec[rr];
+                    qw = a.rec_w[rr];
                     const int lx = sox + (int)(q.x >> 27), ly = soy + (int)((q.x >> 22) & 31);
                     rel = lx + 6 >= 0 && ly + 6 >= 0;
                 }
@@ -403,10 +584,10 @@ __global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a)
                     const uint32_t meta = __shfl_sync(0xffffffffu, q.x, src);
                     const float vr = __uint_as_float(__shfl_sync(0xffffffffu, q.z, src));
                     const float vi = __uint_as_float(__shfl_sync(0xffffffffu, q.w, src));
-                    const float pw = a.rec_w[base + src];
+                    const float pw = __shfl_sync(0xffffffffu, qw, src);
                     const int lx = sox + (int)(meta >> 27), ly = soy + (int)((meta >> 22) & 31);
-                    const float* wx = a.taps + ((meta >> 11) & 2047u) * 7;
-                    const float* wy = a.taps + (meta & 2047u) * 7;
+                    const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
+                    const float* wy = s_taps + (meta & 2047u) * 7;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         const int t = lane + 32 * h;
@@ -414,8 +595,8 @@ __global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a)
                             const int ix = t / 7, iy = t - 7 * (t / 7);
                             const int cx = lx + ix, cy = ly + iy;
                             if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
-                                const float wgt = __fmul_rn(__ldg(&wx[ix]), __ldg(&wy[iy]));
-                                const int cell = cx * kTile + cy;
+                                const float wgt = __fmul_rn(wx[ix], wy[iy]);
+                                const int cell = cx * kRow + cy;
                                 atomicAdd(&s_psf[cell], pw * wgt);
                                 atomicAdd(&s_re[cell], vr * wgt);
                                 atomicAdd(&s_im[cell], vi * wgt);
@@ -426,11 +607,19 @@ __global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a)
             }
         }
         __syncthreads();
-        for (int k = tid; k < kTile * kTile; k += kCubeThreads) {
-            const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
+        for (int k = tid; k < kTile * kTile; k += kGridThreads) {
+            const int cx = k / kTile, cy = k % kTile;
+            const int64_t x = gx0 + cx, y = gy0 + cy;
             if (x < a.gnx && y < a.gny) {
-                psf_c[x * a.gny + y] = s_psf[k];
-                dirty_c[x * a.gny + y] = make_float2(s_re[k], s_im[k]);
+                const int cell = cx * kRow + cy;
+                if (!shared_tile) {
+                    psf_c[x * a.gny + y] = s_psf[cell];
+                    dirty_c[x * a.gny + y] = make_float2(s_re[cell], s_im[cell]);
+                } else {
+                    if (s_psf[cell] != 0.0f) atomicAdd(&psf_c[x * a.gny + y], s_psf[cell]);
+                    if (s_re[cell] != 0.0f || s_im[cell] != 0.0f)
+                        atomicAdd(&dirty_c[x * a.gny + y], make_float2(s_re[cell], s_im[cell]));
+                }
             }
         }
         __syncthreads();
@@ -440,56 +629,79 @@ __global__ void __launch_bounds__(kCubeThreads) cube_grid_kernel(CubeGridArgs a)
 struct CubeDegridArgs {
     const uint4* rec;
     const uint32_t* bin_start;   // [C * ntiles + 1]
+    int32_t tap_rows;
     int64_t ntiles, nty, gnx, gny, R;
-    int64_t n_items;             // C * ntiles
+    const uint2* items;          // (bin, chunk)
+    const unsigned long long* n_items;
     unsigned int* item_counter;
     const float* taps;
     const float2* grid;          // [C][gnx][gny]
     float2* pred;                // [C][R]
 };
 
-// Bins in turn; a warp per record: pred = sum grid * (wx wy) in float32,
-// written at the record's sample (channel-major index).
+// Bins in turn.  The block stages the 38 x 38 model footprint of its home
+// tile in shared memory; a warp takes 4 records at a time, 7 lanes per
+// record, lane ix forming wx[ix] * sum_iy wy[iy] g[x0 + ix][y0 + iy]
+// (float32), and the 7 lanes' sums are reduced with shuffles.
 __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArgs a) {
+    constexpr int kFoot = kTile + 6;
+    __shared__ float s_re[kFoot * kRow];
+    __shared__ float s_im[kFoot * kRow];
+    __shared__ float s_taps[kMaxTapRows * 7];
     __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int sub = lane >> 3, ix = lane & 7;   // record slot, tap column (7 = idle)
+    const unsigned long long n_items = *a.n_items;
+    for (int k = tid; k < a.tap_rows * 7; k += kCubeThreads) s_taps[k] = a.taps[k];
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
         __syncthreads();
         const int64_t item = s_item;
-        __syncthreads();
-        if (item >= a.n_items) break;
-        const uint32_t lo = a.bin_start[item], hi = a.bin_start[item + 1];
-        if (lo == hi) continue;
-        const int64_t c = item / a.ntiles, T = item % a.ntiles;
+        if ((unsigned long long)item >= n_items) break;
+        const uint2 it = a.items[item];
+        const int64_t bin = it.x;
+        const uint32_t lo = a.bin_start[bin] + it.y * kDegridChunk;
+        const uint32_t hi = min(a.bin_start[bin + 1], lo + kDegridChunk);
+        const int64_t c = bin / a.ntiles, T = bin % a.ntiles;
         const int64_t gx0 = (T / a.nty) * kTile, gy0 = (T % a.nty) * kTile;
         const float2* g = a.grid + c * a.gnx * a.gny;
-        for (uint32_t k = lo + warp; k < hi; k += kCubeThreads / 32) {
-            const uint4 q = a.rec[k];
-            const uint32_t meta = q.x;
-            const float* wx = a.taps + ((meta >> 11) & 2047u) * 7;
-            const float* wy = a.taps + (meta & 2047u) * 7;
-            const float2* g0 = g + (gx0 + (int64_t)(meta >> 27)) * a.gny + gy0 +
-                               (int64_t)((meta >> 22) & 31);
+        for (int k = tid; k < kFoot * kFoot; k += kCubeThreads) {
+            const int fx = k / kFoot, fy = k % kFoot;
+            const int64_t x = gx0 + fx, y = gy0 + fy;
+            float2 v = make_float2(0.0f, 0.0f);
+            if (x < a.gnx && y < a.gny) v = __ldg(&g[x * a.gny + y]);
+            s_re[fx * kRow + fy] = v.x;
+            s_im[fx * kRow + fy] = v.y;
+        }
+        __syncthreads();
+        for (uint32_t base = lo + warp * 4; base < hi; base += kCubeThreads / 8) {
+            const uint32_t k = base + sub;
             float re = 0.0f, im = 0.0f;
+            uint32_t sample = 0;
+            if (k < hi) {
+                const uint4 q = a.rec[k];
+                sample = q.y;
+                if (ix < 7) {
+                    const uint32_t meta = q.x;
+                    const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
+                    const float* wy = s_taps + (meta & 2047u) * 7;
+                    const int row = ((int)(meta >> 27) + ix) * kRow + (int)((meta >> 22) & 31);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int t = lane + 32 * h;
-                if (t < 49) {
-                    const int ix = t / 7, iy = t - 7 * (t / 7);
-                    const float wgt = __fmul_rn(__ldg(&wx[ix]), __ldg(&wy[iy]));
-                    const float2 gv = __ldg(&g0[(int64_t)ix * a.gny + iy]);
-                    re = fmaf(gv.x, wgt, re);
-                    im = fmaf(gv.y, wgt, im);
+                    for (int iy = 0; iy < 7; ++iy) {
+                        const float wgt = __fmul_rn(wx[ix], wy[iy]);
+                        re = fmaf(s_re[row + iy], wgt, re);
+                        im = fmaf(s_im[row + iy], wgt, im);
+                    }
                 }
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
+            for (int o = 4; o > 0; o >>= 1) {
                 re += __shfl_xor_sync(0xffffffffu, re, o);
                 im += __shfl_xor_sync(0xffffffffu, im, o);
             }
-            if (lane == 0) a.pred[q.y] = make_float2(re, im);
+            if (ix == 0 && k < hi) a.pred[sample] = make_float2(re, im);
         }
+        __syncthreads();
     }
 }
 
@@ -500,19 +712,27 @@ __global__ void __launch_bounds__(kCubeThreads) cube_taps_kernel(CubeArgs a, Cub
     const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += kCubeThreads) {
-        const int64_t i = (int64_t)c * a.R + r;
-        const Eval e = eval_sample(a, ch, f2, c, r);
-        if (e.ok) {
-            const int64_t tx = e.tile / a.nty, ty = e.tile % a.nty;
-            t.start_x[i] = (int32_t)(tx * kTile + (e.meta >> 27));
-            t.start_y[i] = (int32_t)(ty * kTile + ((e.meta >> 22) & 31));
-            t.row_x[i] = (int32_t)((e.meta >> 11) & 2047u);
-            t.row_y[i] = (int32_t)(e.meta & 2047u);
-            t.weight[i] = e.w;
-        } else {
-            t.start_x[i] = t.start_y[i] = t.row_x[i] = t.row_y[i] = -1;
-            t.weight[i] = 0.0f;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
+        Eval ev[kVec];
+        eval_samples(a, ch, f2, c, base + lane, r1, ev);
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            const int64_t r = base + lane + 32 * j;
+            if (r >= r1) continue;
+            const int64_t i = (int64_t)c * a.R + r;
+            const Eval e = ev[j];
+            if (e.ok) {
+                const int64_t tx = e.tile / a.nty, ty = e.tile % a.nty;
+                t.start_x[i] = (int32_t)(tx * kTile + (e.meta >> 27));
+                t.start_y[i] = (int32_t)(ty * kTile + ((e.meta >> 22) & 31));
+                t.row_x[i] = (int32_t)((e.meta >> 11) & 2047u);
+                t.row_y[i] = (int32_t)(e.meta & 2047u);
+                t.weight[i] = e.w;
+            } else {
+                t.start_x[i] = t.start_y[i] = t.row_x[i] = t.row_y[i] = -1;
+                t.weight[i] = 0.0f;
+            }
         }
     }
 }
@@ -528,7 +748,7 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     if ((uint64_t)in.C * (uint64_t)in.R >= (1ull << 32))
         fail(CR_INVALID, "cube larger than 2^32 samples");
     const cr_grid_info& gi = g->info;
-    if (gi.oversampling > 2046) fail(CR_INVALID, "oversampling above 2046");
+    if (gi.oversampling > kMaxTapRows - 1) fail(CR_INVALID, "cube oversampling above 512");
     CubeRecords cr{};
     cr.R = in.R;
     cr.C = in.C;
@@ -600,9 +820,13 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     a.rec_w = cr.rec_w;
     const dim3 grid((unsigned)std::max<int64_t>((in.R + kRowsPerBlock - 1) / kRowsPerBlock, 1),
                     (unsigned)in.C);
+    a.ev_tile = (uint32_t*)workspace(ctx, "cube_ev_tile", ns * 4);
+    a.ev_meta = (uint32_t*)workspace(ctx, "cube_ev_meta", ns * 4);
+    a.ev_w = (float*)workspace(ctx, "cube_ev_w", ns * 4);
     if (mode != CR_WEIGHT_NATURAL) {
         const int64_t cells = (int64_t)g->geom.nx * g->geom.ny;
         a.density = (float*)workspace(ctx, "cube_density", (size_t)(in.C * cells) * 4);
+        a.dcell = (uint32_t*)workspace(ctx, "cube_dcell", ns * 4);
         CR_CUDA_CHECK(cudaMemsetAsync(a.density, 0, (size_t)(in.C * cells) * 4, ctx->stream));
         if (in.R > 0) {
             cube_density_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
@@ -641,31 +865,67 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
         cube_scatter_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "cube_scatter_kernel");
     }
+    // work lists (their output-zeroing part runs in cube_grid)
+    cr.grid_chunks = (uint32_t*)workspace(ctx, "cube_gchunks", (size_t)nbins * 4);
+    cr.degrid_chunks = (uint32_t*)workspace(ctx, "cube_dchunks", (size_t)nbins * 4);
+    cube_work_count<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
+        cr.bin_start, nbins, cr.ntiles, cr.nty, cr.grid_chunks, cr.degrid_chunks);
+    note_launch(ctx, "cube_work_count");
+    cr.grid_first = (uint32_t*)workspace(ctx, "cube_gfirst", (size_t)nbins * 4);
+    cr.degrid_first = (uint32_t*)workspace(ctx, "cube_dfirst", (size_t)nbins * 4);
+    cr.n_items = (unsigned long long*)workspace(ctx, "cube_nitems", 16);
+    exclusive_scan_u32(ctx, cr.grid_chunks, cr.grid_first, nbins, cr.n_items);
+    exclusive_scan_u32(ctx, cr.degrid_chunks, cr.degrid_first, nbins, cr.n_items + 1);
+    // sum over tiles of ceil(n / K) <= tiles + (sum n) / K, and each record is a
+    // source of at most four output tiles
+    const size_t max_grid_items = (size_t)nbins + 4 * ns / kGridChunk + 1;
+    const size_t max_degrid_items = (size_t)nbins + ns / kDegridChunk + 1;
+    cr.grid_items = (uint2*)workspace(ctx, "cube_gitems", max_grid_items * 8);
+    cr.degrid_items = (uint2*)workspace(ctx, "cube_ditems", max_degrid_items * 8);
     return cr;
 }
 
-void cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf, float2* dirty) {
+void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty) {
     const cr_grid_info& gi = g->info;
+    const int64_t nbins = (int64_t)cr.C * cr.ntiles;
+    cube_work_fill<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
+        cr.grid_chunks, cr.grid_first, cr.degrid_chunks, cr.degrid_first, nbins, cr.ntiles,
+        cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.degrid_items, psf, dirty);
+    note_launch(ctx, "cube_work_fill");
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, g->taps_d, cr.ntx, cr.nty, gi.grid_nx,
-                   gi.grid_ny, (int64_t)cr.C * cr.ntiles, counter, psf, dirty};
+    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, g->taps_d, g->tap_rows, cr.ntx, cr.nty,
+                   gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunks, cr.n_items, counter,
+                   psf, dirty};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    int per_sm = 0;
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_grid_kernel,
+                                                                kGridThreads, 0));
     kernel_mark(ctx, 0, false);
-    cube_grid_kernel<<<sms * 6, kCubeThreads, 0, ctx->stream>>>(a);
+    cube_grid_kernel<<<sms * std::max(per_sm, 1), kGridThreads, 0, ctx->stream>>>(a);
     note_launch(ctx, "cube_grid_kernel");
     kernel_mark(ctx, 0, true);
+    cr.fill_done = true;
 }
 
 void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
                  float2* pred) {
     const cr_grid_info& gi = g->info;
     CR_CUDA_CHECK(cudaMemsetAsync(pred, 0, (size_t)cr.C * cr.R * 8, ctx->stream));
+    if (!cr.fill_done) {
+        // the degridding work list without a gridding pass before it
+        const int64_t nbins = (int64_t)cr.C * cr.ntiles;
+        cube_work_fill<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
+            cr.grid_chunks, cr.grid_first, cr.degrid_chunks, cr.degrid_first, nbins, cr.ntiles,
+            cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.degrid_items, nullptr, nullptr);
+        note_launch(ctx, "cube_work_fill");
+    }
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeDegridArgs a{cr.rec, cr.bin_start, cr.ntiles, cr.nty, gi.grid_nx, gi.grid_ny, cr.R,
-                     (int64_t)cr.C * cr.ntiles, counter, g->taps_d, grid, pred};
+    CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
+                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d, grid,
+                     pred};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     kernel_mark(ctx, 1, false);

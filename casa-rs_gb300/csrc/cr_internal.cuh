@@ -217,6 +217,12 @@ struct CubeRecords {
     double* sumwt = nullptr;           // [C]
     unsigned long long* counts = nullptr;  // [C][2] gridded, skipped
     unsigned long long* n_rec = nullptr;
+    // work lists: chunks per bin, their scan, (bin, chunk) items, item totals
+    uint32_t *grid_chunks = nullptr, *grid_first = nullptr;
+    uint32_t *degrid_chunks = nullptr, *degrid_first = nullptr;
+    uint2 *grid_items = nullptr, *degrid_items = nullptr;
+    unsigned long long* n_items = nullptr;   // [0] gridding, [1] degridding
+    bool fill_done = false;                  // set once cube_grid has filled the lists
 };
 // Per-sample outputs of cube_sample_taps ([C][R], -1 / 0 when not gridded).
 struct CubeTaps {
@@ -227,7 +233,7 @@ struct CubeTaps {
 CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
                       float robust, const CubeTaps* taps = nullptr);
 // psf [C][gnx][gny] float32 (real part), dirty [C][gnx][gny] complex64
-void cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf, float2* dirty);
+void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty);
 // pred [C][R] complex64, zero for samples that are not gridded
 void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
                  float2* pred);

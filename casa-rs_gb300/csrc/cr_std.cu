@@ -17,6 +17,9 @@ namespace {
 
 constexpr int kStdThreads = 256;
 constexpr int kFoot = kTile + 6;   // 38
+// footprint rows 39 floats apart (= 7 mod 32): the 49 taps of a record hit
+// distinct banks within each warp-wide atomic
+constexpr int kFootRow = 39;
 constexpr int kStdChunk = 2048;    // records per work item
 
 struct StdGridArgs {
@@ -38,15 +41,15 @@ struct StdGridArgs {
 
 template <bool RESIDUAL>
 __global__ void __launch_bounds__(kStdThreads) std_grid_kernel(StdGridArgs a) {
-    __shared__ float s_psf[kFoot * kFoot];
-    __shared__ float s_dr[kFoot * kFoot];
-    __shared__ float s_di[kFoot * kFoot];
+    __shared__ float s_psf[kFoot * kFootRow];
+    __shared__ float s_dr[kFoot * kFootRow];
+    __shared__ float s_di[kFoot * kFootRow];
     __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned long long n_items = *a.n_items;
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
-        for (int c = tid; c < kFoot * kFoot; c += kStdThreads) {
+        for (int c = tid; c < kFoot * kFootRow; c += kStdThreads) {
             s_psf[c] = 0.0f;
             s_dr[c] = 0.0f;
             s_di[c] = 0.0f;
@@ -58,38 +61,55 @@ __global__ void __launch_bounds__(kStdThreads) std_grid_kernel(StdGridArgs a) {
         const uint32_t r0 = a.tile_start[T] + a.item_begin[item];
         const uint32_t r1 = min(a.tile_start[T + 1], r0 + (uint32_t)kStdChunk);
         const int x0 = (int)((T / a.nty) * kTile), y0 = (int)((T % a.nty) * kTile);
-        for (uint32_t r = r0 + warp; r < r1; r += kStdThreads / 32) {
-            const int lx = a.rx[r] - x0, ly = a.ry[r] - y0;
-            const float* wx = a.taps + a.ra[r] * 7;
-            const float* wy = a.taps + a.rb[r] * 7;
-            const double2 vs = a.vsum[r];
-            const double ws = a.wsum[r];
-            float vr, vi;
-            if (RESIDUAL) {
-                const float2 p = a.pred[r];
-                vr = (float)(vs.x - (double)p.x * ws);
-                vi = (float)(vs.y - (double)p.y * ws);
-            } else {
-                vr = (float)vs.x;
-                vi = (float)vs.y;
+        // lanes load 32 records at once; the warp then scatters them in turn
+        for (uint32_t rb0 = r0 + warp * 32; rb0 < r1; rb0 += kStdThreads) {
+            const uint32_t r = rb0 + lane;
+            int lx = 0, ly = 0, ia = 0, ib = 0;
+            float vr = 0.0f, vi = 0.0f, pw = 0.0f;
+            if (r < r1) {
+                lx = a.rx[r] - x0;
+                ly = a.ry[r] - y0;
+                ia = a.ra[r] * 7;
+                ib = a.rb[r] * 7;
+                const double2 vs = a.vsum[r];
+                const double ws = a.wsum[r];
+                if (RESIDUAL) {
+                    const float2 p = a.pred[r];
+                    vr = (float)(vs.x - (double)p.x * ws);
+                    vi = (float)(vs.y - (double)p.y * ws);
+                } else {
+                    vr = (float)vs.x;
+                    vi = (float)vs.y;
+                }
+                pw = (float)ws;
             }
-            const float pw = (float)ws;
+            const int nrec = (int)min(32u, r1 - rb0);
+            for (int k = 0; k < nrec; ++k) {
+                const int klx = __shfl_sync(0xffffffffu, lx, k);
+                const int kly = __shfl_sync(0xffffffffu, ly, k);
+                const float* wx = a.taps + __shfl_sync(0xffffffffu, ia, k);
+                const float* wy = a.taps + __shfl_sync(0xffffffffu, ib, k);
+                const float kvr = __shfl_sync(0xffffffffu, vr, k);
+                const float kvi = __shfl_sync(0xffffffffu, vi, k);
+                const float kpw = __shfl_sync(0xffffffffu, pw, k);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                int t = lane + 32 * h;
-                if (t < 49) {
-                    int tx = t / 7, ty = t - 7 * (t / 7);
-                    float wgt = __fmul_rn(__ldg(&wx[tx]), __ldg(&wy[ty]));
-                    int c = (lx + tx) * kFoot + (ly + ty);
-                    if (!RESIDUAL) atomicAdd(&s_psf[c], pw * wgt);
-                    atomicAdd(&s_dr[c], vr * wgt);
-                    atomicAdd(&s_di[c], vi * wgt);
+                for (int h = 0; h < 2; ++h) {
+                    int t = lane + 32 * h;
+                    if (t < 49) {
+                        int tx = t / 7, ty = t - 7 * (t / 7);
+                        float wgt = __fmul_rn(__ldg(&wx[tx]), __ldg(&wy[ty]));
+                        int c = (klx + tx) * kFootRow + (kly + ty);
+                        if (!RESIDUAL) atomicAdd(&s_psf[c], kpw * wgt);
+                        atomicAdd(&s_dr[c], kvr * wgt);
+                        atomicAdd(&s_di[c], kvi * wgt);
+                    }
                 }
             }
         }
         __syncthreads();
-        for (int c = tid; c < kFoot * kFoot; c += kStdThreads) {
-            int64_t x = x0 + c / kFoot, y = y0 + c % kFoot;
+        for (int k = tid; k < kFoot * kFoot; k += kStdThreads) {
+            const int fx = k / kFoot, fy = k % kFoot, c = fx * kFootRow + fy;
+            int64_t x = x0 + fx, y = y0 + fy;
             if (x < a.gnx && y < a.gny) {
                 int64_t cell = x * a.gny + y;
                 if (!RESIDUAL && s_psf[c] != 0.0f) atomicAdd(&a.psf[cell].x, s_psf[c]);
