@@ -248,3 +248,53 @@ def cube_device_inputs(obs: CubeObservation, device="cuda"):
         ph = (-2.0 * math.pi * float(obs.lambda_scale[c])) * (U @ L)
         vis[c] = torch.complex(torch.cos(ph) @ Fx, torch.sin(ph) @ Fx)
     return flags, vis
+
+
+def gaussian_model(rng, n: int, nx: int, ny: int, fmin: float, fmax: float,
+                   fwhm_min: float = 1.0, fwhm_max: float = 5.0) -> np.ndarray:
+    """float32 [nx][ny] image of n circular Gaussians (integrated flux
+    log-uniform in [fmin, fmax], FWHM uniform in [fwhm_min, fwhm_max] pixels,
+    centres uniform in the inner half of the field)."""
+    img = np.zeros((nx, ny), np.float64)
+    flux = np.exp(rng.uniform(np.log(fmin), np.log(fmax), n))
+    fwhm = rng.uniform(fwhm_min, fwhm_max, n)
+    cx = rng.uniform(nx / 4, 3 * nx / 4, n)
+    cy = rng.uniform(ny / 4, 3 * ny / 4, n)
+    for s, f, x0, y0 in zip(flux, fwhm, cx, cy):
+        sig = f / (2.0 * math.sqrt(2.0 * math.log(2.0)))
+        h = int(math.ceil(5 * sig)) + 1
+        xs = np.arange(max(int(x0) - h, 0), min(int(x0) + h + 1, nx))
+        ys = np.arange(max(int(y0) - h, 0), min(int(y0) + h + 1, ny))
+        g = np.exp(-((xs[:, None] - x0) ** 2 + (ys[None, :] - y0) ** 2) / (2 * sig * sig))
+        img[np.ix_(xs, ys)] += s * g / g.sum()
+    return img.astype(np.float32)
+
+
+def config3(seed: int = 3) -> Observation:
+    """Differentiable-imaging workload: 27 antennas to 5 km, 8 h of 5 s dumps
+    at 1.4 GHz (2,021,760 rows), 2048 x 2048 image; the sky is a Gaussian
+    model image (gaussian_model, 50 components 0.01-1 Jy, FWHM 1-5 px)."""
+    return observation(5000.0, 8.0, 5.0, 1.4e9, 2048, 0, 0.01, 1.0, seed, "config3")
+
+
+def config5(seed: int = 5):
+    """Major/minor-loop workload: 27 antennas to 21 km, 8 h of 4 s dumps
+    (2,527,200 rows) at 4 channels over 1.3-1.5 GHz gridded together (MFS:
+    10,108,800 visibilities), 2048 x 2048 image with the cell 1/3 of the beam
+    at 1.5 GHz, sky of 300 points (1 mJy-1 Jy, on pixel centres) and 5
+    Gaussians (0.1-0.5 Jy, FWHM 3-10 px).  Returns (observation with u, v, w
+    in wavelengths for all channels, model image)."""
+    um, vm, wm = uvw_metres(21000.0, 8.0, 4.0)
+    freqs = np.linspace(1.3e9, 1.5e9, 4)
+    ls = freqs / C_LIGHT
+    u = np.concatenate([um * s for s in ls])
+    v = np.concatenate([vm * s for s in ls])
+    w = np.concatenate([wm * s for s in ls])
+    nx = 2048
+    cell = 1.0 / (3.0 * float(np.sqrt(um * um + vm * vm).max()) * ls[-1])
+    rng = np.random.default_rng(seed)
+    sky = point_sky(rng, 300, nx, nx, 1e-3, 1.0)
+    sky.x_pix, sky.y_pix = np.round(sky.x_pix), np.round(sky.y_pix)
+    model = model_image(sky, nx, nx) + gaussian_model(rng, 5, nx, nx, 0.1, 0.5, 3.0, 10.0)
+    obs = Observation("config5", nx, nx, cell, float(freqs.mean()), u, v, w, sky, seed)
+    return obs, model
