@@ -42,7 +42,6 @@ namespace {
 
 constexpr int kCubeThreads = 256;
 constexpr int kRowsPerBlock = 4096;   // rows of one channel per planning block
-constexpr int kSmemBins = 8192;       // home tiles histogrammed in shared memory
 // Shared-memory tile rows are 39 floats apart (39 = 7 mod 32): the 49 taps
 // t = 7 ix + iy of one record then fall in 49 consecutive banks mod 32, so
 // each warp-wide atomic touches 32 distinct banks.
@@ -302,20 +301,30 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     return v;
 }
 
-// Pass 1: histogram of (channel, home tile), per-channel sumwt and counts.
+// Records are binned by (channel, home tile, start cell in the tile), so that
+// within a home tile they follow the cell order and records with one start
+// cell are adjacent.
+__device__ __forceinline__ int64_t cell_bin(int c, int64_t ntiles, uint32_t tile,
+                                            uint32_t meta) {
+    return (((int64_t)c * ntiles + tile) << 10) | (int64_t)(meta >> 22);
+}
+
+// Tile-level starts from the cell-level exclusive scan.
+__global__ void tile_starts_from_cells(const uint32_t* cell_start, int64_t nbins,
+                                       uint32_t* bin_start) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= nbins;
+         b += (int64_t)gridDim.x * blockDim.x)
+        bin_start[b] = cell_start[b << 10];
+}
+
+// Pass 1: histogram of (channel, home tile, cell), per-channel sumwt and counts.
 __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
-    extern __shared__ uint32_t s_hist[];
     __shared__ double s_sum[kCubeThreads / 32];
     __shared__ unsigned long long s_ok[kCubeThreads / 32], s_skip[kCubeThreads / 32];
     const int c = blockIdx.y;
     const CubeChan ch = a.ch[c];
     const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
     const int64_t ntiles = a.ntx * a.nty;
-    const bool smem = ntiles <= kSmemBins;
-    uint32_t* ghist = a.hist + (int64_t)c * ntiles;
-    if (smem)
-        for (int64_t k = threadIdx.x; k < ntiles; k += kCubeThreads) s_hist[k] = 0u;
-    __syncthreads();
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
     double sw = 0.0;
@@ -336,10 +345,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
             if (e[j].ok) {
                 ++n_ok;
                 sw += (double)e[j].w;
-                if (smem)
-                    atomicAdd(&s_hist[e[j].tile], 1u);
-                else
-                    atomicAdd(&ghist[e[j].tile], 1u);
+                atomicAdd(&a.hist[cell_bin(c, ntiles, e[j].tile, e[j].meta)], 1u);
             } else {
                 ++n_skip;
             }
@@ -367,9 +373,6 @@ __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
         if (o) atomicAdd(&a.counts[2 * c], o);
         if (s) atomicAdd(&a.counts[2 * c + 1], s);
     }
-    if (smem)
-        for (int64_t k = threadIdx.x; k < ntiles; k += kCubeThreads)
-            if (s_hist[k]) atomicAdd(&ghist[k], s_hist[k]);
 }
 
 // Pass 2: scatter records into (channel, home tile) bins from pass 1's
@@ -395,8 +398,8 @@ __global__ void __launch_bounds__(kCubeThreads) cube_scatter_kernel(CubeArgs a) 
             const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
             const unsigned act = __ballot_sync(0xffffffffu, ok);
             if (!ok) continue;
-            const uint32_t bin = (uint32_t)((int64_t)c * ntiles + tile[j]);
-            const unsigned peers = __match_any_sync(act, bin);
+            const int64_t bin = cell_bin(c, ntiles, tile[j], a.ev_meta[i]);
+            const unsigned peers = __match_any_sync(act, (unsigned long long)bin);
             const int leader = __ffs(peers) - 1;
             const unsigned rank = __popc(peers & ((1u << lane) - 1u));
             uint32_t pos0 = 0;
@@ -564,6 +567,32 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
             s_im[k] = 0.0f;
         }
         __syncthreads();
+        // Records of a home tile arrive in start-cell order, so a warp's
+        // consecutive records often share a start cell: lane t sums tap t of
+        // such a run in registers and adds it to the tile once per run.
+        const int ix0 = lane / 7, iy0 = lane % 7;
+        const int ix1 = (lane + 32) / 7, iy1 = (lane + 32) % 7;
+        const bool has1 = lane + 32 < 49;
+        int cur_lx = 0, cur_ly = 0;
+        bool open = false;
+        float p0 = 0.f, r0 = 0.f, i0 = 0.f, p1 = 0.f, r1 = 0.f, i1 = 0.f;
+        auto flush = [&]() {
+            int cx = cur_lx + ix0, cy = cur_ly + iy0;
+            if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
+                const int cell = cx * kRow + cy;
+                atomicAdd(&s_psf[cell], p0);
+                atomicAdd(&s_re[cell], r0);
+                atomicAdd(&s_im[cell], i0);
+            }
+            cx = cur_lx + ix1;
+            cy = cur_ly + iy1;
+            if (has1 && cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
+                const int cell = cx * kRow + cy;
+                atomicAdd(&s_psf[cell], p1);
+                atomicAdd(&s_re[cell], r1);
+                atomicAdd(&s_im[cell], i1);
+            }
+        };
         for (int s = 0; s < nsrc; ++s) {
             const int sox = ox[s], soy = oy[s];
             for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kGridThreads) {
@@ -586,26 +615,29 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
                     const float vi = __uint_as_float(__shfl_sync(0xffffffffu, q.w, src));
                     const float pw = __shfl_sync(0xffffffffu, qw, src);
                     const int lx = sox + (int)(meta >> 27), ly = soy + (int)((meta >> 22) & 31);
+                    if (!open || lx != cur_lx || ly != cur_ly) {
+                        if (open) flush();
+                        open = true;
+                        cur_lx = lx;
+                        cur_ly = ly;
+                        p0 = r0 = i0 = p1 = r1 = i1 = 0.f;
+                    }
                     const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
                     const float* wy = s_taps + (meta & 2047u) * 7;
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int t = lane + 32 * h;
-                        if (t < 49) {
-                            const int ix = t / 7, iy = t - 7 * (t / 7);
-                            const int cx = lx + ix, cy = ly + iy;
-                            if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
-                                const float wgt = __fmul_rn(wx[ix], wy[iy]);
-                                const int cell = cx * kRow + cy;
-                                atomicAdd(&s_psf[cell], pw * wgt);
-                                atomicAdd(&s_re[cell], vr * wgt);
-                                atomicAdd(&s_im[cell], vi * wgt);
-                            }
-                        }
+                    const float w0 = __fmul_rn(wx[ix0], wy[iy0]);
+                    p0 = fmaf(pw, w0, p0);
+                    r0 = fmaf(vr, w0, r0);
+                    i0 = fmaf(vi, w0, i0);
+                    if (has1) {
+                        const float w1 = __fmul_rn(wx[ix1], wy[iy1]);
+                        p1 = fmaf(pw, w1, p1);
+                        r1 = fmaf(vr, w1, r1);
+                        i1 = fmaf(vi, w1, i1);
                     }
                 }
             }
         }
+        if (open) flush();
         __syncthreads();
         for (int k = tid; k < kTile * kTile; k += kGridThreads) {
             const int cx = k / kTile, cy = k % kTile;
@@ -776,11 +808,13 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     cr.rec = (uint4*)workspace(ctx, "cube_rec", ns * 16);
     cr.rec_w = (float*)workspace(ctx, "cube_rec_w", ns * 4);
     cr.bin_start = (uint32_t*)workspace(ctx, "cube_bin_start", (size_t)(nbins + 1) * 4);
-    uint32_t* hist = (uint32_t*)workspace(ctx, "cube_hist", (size_t)(nbins + 1) * 4);
+    const int64_t ncells = (nbins << 10) + 1;   // (channel, tile, cell) bins + total
+    if (ncells >= (1ll << 32)) fail(CR_INVALID, "cube has too many (channel, tile, cell) bins");
+    uint32_t* hist = (uint32_t*)workspace(ctx, "cube_hist", (size_t)ncells * 4);
     cr.sumwt = (double*)workspace(ctx, "cube_sumwt", (size_t)in.C * 8);
     cr.counts = (unsigned long long*)workspace(ctx, "cube_counts", (size_t)in.C * 16 + 8);
     cr.n_rec = cr.counts + 2 * in.C;
-    CR_CUDA_CHECK(cudaMemsetAsync(hist, 0, (size_t)(nbins + 1) * 4, ctx->stream));
+    CR_CUDA_CHECK(cudaMemsetAsync(hist, 0, (size_t)ncells * 4, ctx->stream));
     CR_CUDA_CHECK(cudaMemsetAsync(cr.sumwt, 0, (size_t)in.C * 8, ctx->stream));
     CR_CUDA_CHECK(cudaMemsetAsync(cr.counts, 0, (size_t)in.C * 16 + 8, ctx->stream));
 
@@ -853,14 +887,14 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
         return cr;
     }
     if (in.R > 0) {
-        const size_t smem = cr.ntiles <= kSmemBins ? (size_t)cr.ntiles * 4 : 0;
-        cube_hist_kernel<<<grid, kCubeThreads, smem, ctx->stream>>>(a);
+        cube_hist_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "cube_hist_kernel");
     }
-    exclusive_scan_u32(ctx, hist, cr.bin_start, nbins + 1, nullptr);
-    // the cursor starts at each bin's first slot; the total lands in n_rec
-    CR_CUDA_CHECK(cudaMemcpyAsync(hist, cr.bin_start, (size_t)(nbins + 1) * 4,
-                                  cudaMemcpyDeviceToDevice, ctx->stream));
+    // in place: hist becomes each cell bin's first slot, the scatter's cursor
+    exclusive_scan_u32(ctx, hist, hist, ncells, nullptr);
+    tile_starts_from_cells<<<grid_blocks(nbins + 1, 256), 256, 0, ctx->stream>>>(hist, nbins,
+                                                                                 cr.bin_start);
+    note_launch(ctx, "tile_starts_from_cells");
     if (in.R > 0) {
         cube_scatter_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "cube_scatter_kernel");
