@@ -90,6 +90,12 @@ struct CubeArgs {
     float* ev_w;               // imaging weight
 };
 
+// Both density cells of a sample, of (u, v) and of the mirror (-u, -v),
+// from one pair of fixed-point products (FP64 fallback per cell).
+__device__ __forceinline__ void density_cells(const CubeArgs& a, const CubeChan& ch, double um,
+                                              double vm, int* x, int* y, bool* ok, int* xm,
+                                              int* ym, bool* okm);
+
 // weight_density_cell_anchor with the cube (rounded) conventions.
 __device__ __forceinline__ bool density_cell(const CubeArgs& a, const CubeChan& ch, double um,
                                              double vm, bool mirror, int* ox, int* oy) {
@@ -118,6 +124,35 @@ __device__ __forceinline__ bool density_cell(const CubeArgs& a, const CubeChan& 
     *ox = (int)rx;
     *oy = (int)ry;
     return true;
+}
+
+__device__ __forceinline__ void density_cells(const CubeArgs& a, const CubeChan& ch, double um,
+                                              double vm, int* x, int* y, bool* ok, int* xm,
+                                              int* ym, bool* okm) {
+    long long tx, ty;
+    if (fix_mul(um, ch.kdx, &tx) && fix_mul(vm, ch.kdy, &ty)) {
+        long long ax, ay;
+        // (u, v): x = u s + c, y = -v s + c; mirror: x = -u s + c, y = v s + c
+        if (fix_round(tx + a.dcx_fix, kFixMargin, &ax) &&
+            fix_round(a.dcy_fix - ty, kFixMargin, &ay)) {
+            *ok = !(ax <= 0 || ay <= 0 || ax >= a.nx || ay >= a.ny);
+            *x = (int)ax;
+            *y = (int)ay;
+        } else {
+            *ok = density_cell(a, ch, um, vm, false, x, y);
+        }
+        if (fix_round(a.dcx_fix - tx, kFixMargin, &ax) &&
+            fix_round(a.dcy_fix + ty, kFixMargin, &ay)) {
+            *okm = !(ax <= 0 || ay <= 0 || ax >= a.nx || ay >= a.ny);
+            *xm = (int)ax;
+            *ym = (int)ay;
+        } else {
+            *okm = density_cell(a, ch, um, vm, true, xm, ym);
+        }
+        return;
+    }
+    *ok = density_cell(a, ch, um, vm, false, x, y);
+    *okm = density_cell(a, ch, um, vm, true, xm, ym);
 }
 
 __device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
@@ -209,7 +244,7 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
     }
 }
 
-__global__ void __launch_bounds__(kCubeThreads) cube_density_kernel(CubeArgs a) {
+__global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs a) {
     const int c = blockIdx.y;
     const CubeChan ch = a.ch[c];
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
@@ -234,17 +269,29 @@ __global__ void __launch_bounds__(kCubeThreads) cube_density_kernel(CubeArgs a) 
         for (int j = 0; j < kVec; ++j) {
             const int64_t r = base + lane + 32 * j;
             uint32_t cell = ~0u;
-            int x, y;
-            if (live[j] && density_cell(a, ch, um[j], vm[j], false, &x, &y)) {
-                cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
-                if (finite_f(w[j]) && w[j] > 0.0f) atomicAdd(&dens[cell], w[j]);
+            if (live[j]) {
+                int x = 0, y = 0, xm = 0, ym = 0;
+                bool ok = false, okm = false;
+                density_cells(a, ch, um[j], vm[j], &x, &y, &ok, &xm, &ym, &okm);
+                const bool pos = finite_f(w[j]) && w[j] > 0.0f;
+                if (ok) {
+                    cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
+                    if (pos) atomicAdd(&dens[cell], w[j]);
+                }
+                if (okm && pos) atomicAdd(&dens[(int64_t)xm * a.ny + ym], w[j]);
             }
-            if (live[j] && finite_f(w[j]) && w[j] > 0.0f &&
-                density_cell(a, ch, um[j], vm[j], true, &x, &y))
-                atomicAdd(&dens[(int64_t)x * a.ny + y], w[j]);
             if (r < r1) a.dcell[(int64_t)c * a.R + r] = cell;
         }
     }
+}
+
+// hi + lo += x without rounding error (Knuth's two-sum; lo collects errors)
+__device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
 }
 
 // Per channel: sum d and sum d^2 (d > 0) in FP64, then f2 (weighting.rs:1108-1121).
@@ -252,13 +299,20 @@ __global__ void __launch_bounds__(kCubeThreads) cube_density_sums(const float* d
                                                                   int64_t cells, double* sums) {
     const int c = blockIdx.y;
     const float* d = density + (int64_t)c * cells;
-    double s = 0.0, s2 = 0.0;
+    // per thread in float32 pairs (error-free sums and products: exact for
+    // sums below 2^48 of integer-valued densities), FP64 only to combine
+    float s_hi = 0.f, s_lo = 0.f, q_hi = 0.f, q_lo = 0.f;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cells;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const double v = (double)d[k];
-        s += v;
-        if (v > 0.0) s2 += v * v;
+        const float v = d[k];
+        two_sum(s_hi, s_lo, v);
+        if (v > 0.0f) {
+            const float p = __fmul_rn(v, v);
+            two_sum(q_hi, q_lo, p);
+            q_lo = __fadd_rn(q_lo, fmaf(v, v, -p));
+        }
     }
+    double s = (double)s_hi + (double)s_lo, s2 = (double)q_hi + (double)q_lo;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -318,7 +372,7 @@ __global__ void tile_starts_from_cells(const uint32_t* cell_start, int64_t nbins
 }
 
 // Pass 1: histogram of (channel, home tile, cell), per-channel sumwt and counts.
-__global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
+__global__ void __launch_bounds__(kCubeThreads, 3) cube_hist_kernel(CubeArgs a) {
     __shared__ double s_sum[kCubeThreads / 32];
     __shared__ unsigned long long s_ok[kCubeThreads / 32], s_skip[kCubeThreads / 32];
     const int c = blockIdx.y;
@@ -377,7 +431,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_hist_kernel(CubeArgs a) {
 
 // Pass 2: scatter records into (channel, home tile) bins from pass 1's
 // per-sample results.
-__global__ void __launch_bounds__(kCubeThreads) cube_scatter_kernel(CubeArgs a) {
+__global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs a) {
     const int c = blockIdx.y;
     const int64_t ntiles = a.ntx * a.nty;
     const int lane = threadIdx.x & 31;
@@ -526,22 +580,23 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
         const int64_t tx = T / a.nty, ty = T % a.nty;
         const bool shared_tile = a.grid_chunks[bin] > 1;
         const uint32_t clo = it.y * kGridChunk, chi = clo + kGridChunk;
+        // source s = home tile (tx - (s & 1), ty - (s >> 1)); [b0, b1) its records
+        // inside this chunk (empty when none)
         uint32_t b0[4], b1[4];
-        int ox[4], oy[4];
         int nsrc = 0;
         uint32_t off = 0;   // position of this source in the concatenated order
+#pragma unroll
         for (int s = 0; s < 4; ++s) {
             const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
+            b0[s] = b1[s] = 0;
             if (sx < 0 || sy < 0) continue;
             const int64_t sb = c * ntiles + sx * a.nty + sy;
             const uint32_t lo = a.bin_start[sb], hi = a.bin_start[sb + 1];
             const uint32_t n = hi - lo;
             const uint32_t a0 = max(off, clo), a1 = min(off + n, chi);
             if (a0 < a1) {
-                b0[nsrc] = lo + (a0 - off);
-                b1[nsrc] = lo + (a1 - off);
-                ox[nsrc] = -(s & 1) * kTile;
-                oy[nsrc] = -(s >> 1) * kTile;
+                b0[s] = lo + (a0 - off);
+                b1[s] = lo + (a1 - off);
                 ++nsrc;
             }
             off += n;
@@ -593,8 +648,9 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
                 atomicAdd(&s_im[cell], i1);
             }
         };
-        for (int s = 0; s < nsrc; ++s) {
-            const int sox = ox[s], soy = oy[s];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const int sox = -(s & 1) * kTile, soy = -(s >> 1) * kTile;
             for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kGridThreads) {
                 const uint32_t rr = base + lane;
                 uint4 q = make_uint4(0u, 0u, 0u, 0u);
