@@ -487,23 +487,42 @@ __device__ __forceinline__ uint32_t bin_count(const uint32_t* bin_start, int64_t
     return bin_start[bin + 1] - bin_start[bin];
 }
 
-__device__ __forceinline__ uint32_t tile_sources(const uint32_t* bin_start, int64_t c,
-                                                 int64_t ntiles, int64_t nty, int64_t tx,
-                                                 int64_t ty) {
-    uint32_t n = 0;
-    for (int s = 0; s < 4; ++s) {
-        const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
-        if (sx >= 0 && sy >= 0) n += bin_count(bin_start, c * ntiles + sx * nty + sy);
-    }
-    return n;
+// Start of cell bin cb: cell_end holds each cell bin's end (= the next
+// bin's start) once the scatter has advanced the cursors.
+__device__ __forceinline__ uint32_t cell_start(const uint32_t* cell_end, int64_t cb) {
+    return cb == 0 ? 0u : cell_end[cb - 1];
 }
 
-__global__ void cube_work_count(const uint32_t* bin_start, int64_t nbins, int64_t ntiles,
-                                int64_t nty, uint32_t* grid_chunks, uint32_t* degrid_chunks) {
+// The records of output tile (c, tx, ty)'s four sources that can reach it:
+// all of the home tile; of (tx-1, ty) and (tx-1, ty-1) only start cells with
+// x >= 26 (a contiguous suffix, records being in cell order); all of
+// (tx, ty-1) (its reaching cells, y >= 26, are not contiguous).
+__device__ __forceinline__ void source_ranges(const uint32_t* bin_start,
+                                              const uint32_t* cell_end, int64_t c,
+                                              int64_t ntiles, int64_t nty, int64_t tx,
+                                              int64_t ty, uint32_t (&lo)[4],
+                                              uint32_t (&hi)[4]) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
+        lo[s] = hi[s] = 0u;
+        if (sx < 0 || sy < 0) continue;
+        const int64_t sb = c * ntiles + sx * nty + sy;
+        hi[s] = bin_start[sb + 1];
+        lo[s] = (s & 1) ? cell_start(cell_end, (sb << 10) + (kTile - 6) * kTile)
+                        : bin_start[sb];
+    }
+}
+
+__global__ void cube_work_count(const uint32_t* bin_start, const uint32_t* cell_end,
+                                int64_t nbins, int64_t ntiles, int64_t nty,
+                                uint32_t* grid_chunks, uint32_t* degrid_chunks) {
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins;
          b += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = b / ntiles, T = b % ntiles;
-        const uint32_t n = tile_sources(bin_start, c, ntiles, nty, T / nty, T % nty);
+        uint32_t lo[4], hi[4];
+        source_ranges(bin_start, cell_end, c, ntiles, nty, T / nty, T % nty, lo, hi);
+        const uint32_t n = (hi[0] - lo[0]) + (hi[1] - lo[1]) + (hi[2] - lo[2]) + (hi[3] - lo[3]);
         grid_chunks[b] = n == 0 ? 1u : (n + kGridChunk - 1) / kGridChunk;
         degrid_chunks[b] = (bin_count(bin_start, b) + kDegridChunk - 1) / kDegridChunk;
     }
@@ -538,6 +557,7 @@ struct CubeGridArgs {
     const uint4* rec;
     const float* rec_w;
     const uint32_t* bin_start;   // [C * ntiles + 1]
+    const uint32_t* cell_end;    // [C * ntiles * 1024] end of each cell bin
     const float* taps;           // [tap_rows][7]
     int32_t tap_rows;
     int64_t ntx, nty, gnx, gny;
@@ -583,17 +603,14 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
         // source s = home tile (tx - (s & 1), ty - (s >> 1)); [b0, b1) its records
         // inside this chunk (empty when none)
         uint32_t b0[4], b1[4];
+        source_ranges(a.bin_start, a.cell_end, c, ntiles, a.nty, tx, ty, b0, b1);
         int nsrc = 0;
         uint32_t off = 0;   // position of this source in the concatenated order
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const int64_t sx = tx - (s & 1), sy = ty - (s >> 1);
-            b0[s] = b1[s] = 0;
-            if (sx < 0 || sy < 0) continue;
-            const int64_t sb = c * ntiles + sx * a.nty + sy;
-            const uint32_t lo = a.bin_start[sb], hi = a.bin_start[sb + 1];
-            const uint32_t n = hi - lo;
+            const uint32_t lo = b0[s], n = b1[s] - b0[s];
             const uint32_t a0 = max(off, clo), a1 = min(off + n, chi);
+            b0[s] = b1[s] = 0;
             if (a0 < a1) {
                 b0[s] = lo + (a0 - off);
                 b1[s] = lo + (a1 - off);
@@ -958,8 +975,9 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     // work lists (their output-zeroing part runs in cube_grid)
     cr.grid_chunks = (uint32_t*)workspace(ctx, "cube_gchunks", (size_t)nbins * 4);
     cr.degrid_chunks = (uint32_t*)workspace(ctx, "cube_dchunks", (size_t)nbins * 4);
+    cr.cell_end = hist;
     cube_work_count<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
-        cr.bin_start, nbins, cr.ntiles, cr.nty, cr.grid_chunks, cr.degrid_chunks);
+        cr.bin_start, cr.cell_end, nbins, cr.ntiles, cr.nty, cr.grid_chunks, cr.degrid_chunks);
     note_launch(ctx, "cube_work_count");
     cr.grid_first = (uint32_t*)workspace(ctx, "cube_gfirst", (size_t)nbins * 4);
     cr.degrid_first = (uint32_t*)workspace(ctx, "cube_dfirst", (size_t)nbins * 4);
@@ -984,7 +1002,7 @@ void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* 
     note_launch(ctx, "cube_work_fill");
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, g->taps_d, g->tap_rows, cr.ntx, cr.nty,
+    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows, cr.ntx, cr.nty,
                    gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunks, cr.n_items, counter,
                    psf, dirty};
     int sms = 0;

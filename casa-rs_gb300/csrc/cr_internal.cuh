@@ -214,6 +214,7 @@ struct CubeRecords {
     uint4* rec = nullptr;              // {cell | tap rows, c R + r, w vis}
     float* rec_w = nullptr;
     uint32_t* bin_start = nullptr;     // [C ntiles + 1]
+    uint32_t* cell_end = nullptr;      // [C ntiles 1024] end of each (tile, cell) bin
     double* sumwt = nullptr;           // [C]
     unsigned long long* counts = nullptr;  // [C][2] gridded, skipped
     unsigned long long* n_rec = nullptr;
