@@ -47,6 +47,10 @@ class CubeBatch(C.Structure):
                 ("location", _i32)]
 
 
+class Beam(C.Structure):
+    _fields_ = [("major_fwhm_rad", _d), ("minor_fwhm_rad", _d), ("position_angle_rad", _d)]
+
+
 class Sums(C.Structure):
     _fields_ = [("normalization_sumwt", _d), ("reported_sumwt", _d), ("gridded", _i64),
                 ("skipped", _i64), ("unique_records", _i64), ("taps", _i64)]
@@ -99,6 +103,12 @@ SIGNATURES = {
                                       _p, _i32, _p, _err]),
     "cr_cube_sample_taps": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _p, _p,
                                       _p, _i32, _err]),
+    "cr_fit_beam": (C.c_int, [_p, _p, _i32, _i32, _i32, _d, _d, _f, C.POINTER(Beam),
+                              C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_f), _err]),
+    "cr_restore": (C.c_int, [_p, _p, _p, _i32, _i32, _i32, _d, _d, C.POINTER(Beam), _p, _i32,
+                             _err]),
+    "cr_psf_sidelobe": (C.c_int, [_p, _p, _i32, _i32, _i32, _d, _d, C.POINTER(Beam),
+                                  C.POINTER(_f), _err]),
     "cr_plan_residual_image": (C.c_int, [_p, _p, _p, _i32, C.POINTER(PsfState), _p, _i32,
                                          _err]),
     "cr_grid_to_image": (C.c_int, [_p, _p, _p, _p, _i32, _f, _p, _i32, _err]),

@@ -692,6 +692,71 @@ def cube_sample_taps(gridder, cube: CubeBatch, weighting: str = "natural", robus
 
 
 # ----------------------------------------------------------------------------
+# restoring beam
+# ----------------------------------------------------------------------------
+@dataclass
+class BeamFit:
+    """BeamFit: FWHM axes and position angle in radians."""
+    major_fwhm_rad: float
+    minor_fwhm_rad: float
+    position_angle_rad: float
+
+    def to_c(self) -> _lib.Beam:
+        return _lib.Beam(self.major_fwhm_rad, self.minor_fwhm_rad, self.position_angle_rad)
+
+
+def fit_beam(psf, cell_rad, cutoff: float = 0.35, ctx: Optional[Context] = None):
+    """fit_beam_from_psf (beam.rs:27-103): (BeamFit or None, attempts,
+    cutoff used).  A host PSF needs no context."""
+    arrs = _Arrays()
+    pp = arrs.ptr(psf, np.float32, torch.float32 if torch else None)
+    nx, ny = int(psf.shape[0]), int(psf.shape[1])
+    if arrs.location == CR_DEVICE and ctx is None:
+        raise ValueError("a device PSF needs a Context")
+    b = _lib.Beam()
+    fitted, attempts, used = C.c_int32(), C.c_int32(), C.c_float()
+    call("cr_fit_beam", ctx.handle if ctx is not None else None, pp, nx, ny, arrs.location,
+         float(cell_rad[0]), float(cell_rad[1]), float(cutoff), C.byref(b), C.byref(fitted),
+         C.byref(attempts), C.byref(used))
+    beam = BeamFit(b.major_fwhm_rad, b.minor_fwhm_rad, b.position_angle_rad) if fitted.value else None
+    return beam, int(attempts.value), (float(used.value) if fitted.value else None)
+
+
+def restore(ctx: Context, model, residual, cell_rad, beam: BeamFit):
+    """restore_model (beam.rs:105-120) plus the residual (None: model only)."""
+    arrs = _Arrays()
+    nx, ny = int(model.shape[0]), int(model.shape[1])
+    mp = arrs.ptr(model, np.float32, torch.float32 if torch else None, (nx, ny))
+    rp = arrs.ptr(residual, np.float32, torch.float32 if torch else None, (nx, ny))
+    if arrs.location == CR_DEVICE:
+        ctx.use_torch_stream()
+    else:
+        ctx.use_own_stream()
+    out, op, loc = arrs.out((nx, ny), np.float32, torch.float32 if torch else None,
+                            _device_of(model))
+    b = beam.to_c()
+    call("cr_restore", ctx.handle, mp, rp, nx, ny, arrs.location, float(cell_rad[0]),
+         float(cell_rad[1]), C.byref(b), op, loc)
+    return out
+
+
+def psf_sidelobe(ctx: Context, psf, cell_rad, beam: BeamFit) -> float:
+    """estimate_psf_sidelobe_level_with_beam (beam.rs:319-328)."""
+    arrs = _Arrays()
+    nx, ny = int(psf.shape[0]), int(psf.shape[1])
+    pp = arrs.ptr(psf, np.float32, torch.float32 if torch else None, (nx, ny))
+    if arrs.location == CR_DEVICE:
+        ctx.use_torch_stream()
+    else:
+        ctx.use_own_stream()
+    lvl = C.c_float()
+    b = beam.to_c()
+    call("cr_psf_sidelobe", ctx.handle, pp, nx, ny, arrs.location, float(cell_rad[0]),
+         float(cell_rad[1]), C.byref(b), C.byref(lvl))
+    return float(lvl.value)
+
+
+# ----------------------------------------------------------------------------
 # Hogbom
 # ----------------------------------------------------------------------------
 @dataclass

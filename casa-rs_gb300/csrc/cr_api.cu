@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "cr_internal.cuh"
 
@@ -866,6 +867,65 @@ int cr_cube_sample_taps(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
             copy_out(ctx, imaging_weight, t.weight, S * 4, CR_HOST);
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_fit_beam(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32_t location,
+                double cell_x_rad, double cell_y_rad, float cutoff, cr_beam* beam,
+                int32_t* fitted, int32_t* attempts, float* cutoff_used, char** err) {
+    return guarded(err, [&] {
+        need(psf && beam && fitted, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        const size_t n = (size_t)nx * (size_t)ny;
+        std::vector<float> host;
+        const float* p = psf;
+        if (location == CR_DEVICE) {
+            need(ctx != nullptr, "a device PSF needs a context");
+            bind(ctx);
+            host.resize(n);
+            CR_CUDA_CHECK(cudaMemcpyAsync(host.data(), psf, n * 4, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+            p = host.data();
+        } else {
+            need(location == CR_HOST, "location must be CR_HOST or CR_DEVICE");
+        }
+        int32_t at = 0;
+        float cu = 0.0f;
+        *beam = cr_beam{0.0, 0.0, 0.0};
+        *fitted = fit_beam(p, nx, ny, cell_x_rad, cell_y_rad, cutoff, beam, &at, &cu) ? 1 : 0;
+        if (attempts) *attempts = at;
+        if (cutoff_used) *cutoff_used = cu;
+    });
+}
+
+int cr_restore(cr_ctx* ctx, const float* model, const float* residual, int32_t nx, int32_t ny,
+               int32_t location, double cell_x_rad, double cell_y_rad, const cr_beam* beam,
+               float* restored, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        need(ctx && model && beam, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        bind(ctx);
+        const size_t n = (size_t)nx * (size_t)ny;
+        const float* m = (const float*)device_input(ctx, model, n * 4, location, "rs_in_model");
+        const float* r = (const float*)device_input(ctx, residual, n * 4, location, "rs_in_res");
+        float* out = out_ptr<float>(ctx, restored, out_location, n * 4, "restored");
+        restore(ctx, m, r, nx, ny, cell_x_rad, cell_y_rad, *beam, out);
+        if (out_location == CR_HOST) copy_out(ctx, restored, out, n * 4, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32_t location,
+                    double cell_x_rad, double cell_y_rad, const cr_beam* beam, float* level,
+                    char** err) {
+    return guarded(err, [&] {
+        need(ctx && psf && beam && level, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        bind(ctx);
+        const size_t n = (size_t)nx * (size_t)ny;
+        const float* p = (const float*)device_input(ctx, psf, n * 4, location, "sl_psf");
+        *level = psf_sidelobe(ctx, p, nx, ny, cell_x_rad, cell_y_rad, *beam);
     });
 }
 

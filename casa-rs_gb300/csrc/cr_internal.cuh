@@ -240,6 +240,14 @@ void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2
                  float2* pred);
 void cube_read_sums(cr_ctx* ctx, const CubeRecords& cr, cr_sums* out);
 
+// ---- restoring beam (cr_beam.cu) -------------------------------------------------
+bool fit_beam(const float* psf_host, int64_t nx, int64_t ny, double cell_x, double cell_y,
+              float cutoff, cr_beam* beam, int32_t* attempts, float* cutoff_used);
+void restore(cr_ctx* ctx, const float* model, const float* residual, int32_t nx, int32_t ny,
+             double cell_x, double cell_y, const cr_beam& beam, float* out);
+float psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, double cell_x,
+                   double cell_y, const cr_beam& beam);
+
 // ---- W-projection build ----------------------------------------------------------
 void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
                  int32_t sampling, int32_t support_min, int32_t support_max);

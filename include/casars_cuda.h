@@ -299,6 +299,31 @@ int cr_cube_sample_taps(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                         int32_t* row_x, int32_t* row_y, float* imaging_weight,
                         int32_t out_location, char** err);
 
+/* ---- restoring beam ---------------------------------------------------------
+ * fit_beam_from_psf (beam.rs:27-103): the main lobe above `cutoff` (clamped
+ * to [0.01, 0.99], lowered by 1.5x per failed attempt, at most 50 attempts),
+ * resampled bicubically and fitted by Levenberg-Marquardt; FWHM and position
+ * angle in radians, quantised through float32 arcsec / degrees.  *fitted is
+ * 0 when no attempt converged.  The fit runs on the host (a device PSF is
+ * copied back first; ctx may be NULL for a host PSF). */
+typedef struct {
+    double major_fwhm_rad, minor_fwhm_rad, position_angle_rad;
+} cr_beam;
+int cr_fit_beam(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32_t location,
+                double cell_x_rad, double cell_y_rad, float cutoff, cr_beam* beam,
+                int32_t* fitted, int32_t* attempts, float* cutoff_used, char** err);
+/* restore_model (beam.rs:105-120) plus the residual: restored = model (*)
+ * Gaussian (the analytic beam of make_casa_gaussian_psf_image, full-plane
+ * circular FFT convolution) + residual (NULL: model only).  Even sides. */
+int cr_restore(cr_ctx* ctx, const float* model, const float* residual, int32_t nx, int32_t ny,
+               int32_t location, double cell_x_rad, double cell_y_rad, const cr_beam* beam,
+               float* restored, int32_t out_location, char** err);
+/* estimate_psf_sidelobe_level_with_beam (beam.rs:319-328):
+ * max(|min psf|, |max(psf - Gaussian)|); 0 for an unusable beam. */
+int cr_psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32_t location,
+                    double cell_x_rad, double cell_y_rad, const cr_beam* beam, float* level,
+                    char** err);
+
 /* ---- weighting -----------------------------------------------------------
  * apply_weighting_with_density_source, Combined density
  * (weighting.rs:1055-1180): natural passes weights through; uniform and
