@@ -38,6 +38,7 @@ class CleanConfig:
     max_psf_fraction: float = 0.8
     major_cycle_limit: Optional[int] = None
     inclusive: bool = True
+    psf_cutoff: float = 0.35
 
 
 @dataclass
@@ -52,6 +53,9 @@ class CleanResult:
     stop_reason: Optional[str]
     components: list = field(default_factory=list)
     cycle_thresholds: list = field(default_factory=list)
+    beam: Optional[im.BeamFit] = None
+    restored: object = None
+    max_psf_sidelobe: float = 0.0
 
 
 def clean_cycle_threshold(peak: float, max_psf_sidelobe: float, cfg: CleanConfig) -> float:
@@ -86,23 +90,13 @@ def tolerant_clean_stop_reason(peak_abs: float, threshold: float,
 _HANDOFF = ("CycleThresholdReached", "NsigmaThresholdReached")
 
 
-def psf_sidelobe_level(psf) -> float:
-    """Largest |PSF| outside the main lobe: the lobe is the box around the
-    centre out to the first samples below 0.35 on each axis (a simple
-    stand-in for beam.rs's fitted-beam estimate)."""
-    p = psf.detach().cpu().numpy() if (torch is not None and isinstance(psf, torch.Tensor)) else np.asarray(psf)
-    nx, ny = p.shape
-    cx, cy = nx // 2, ny // 2
-    def reach(line, c):
-        k = 0
-        while c + k + 1 < len(line) and abs(line[c + k + 1]) >= 0.35:
-            k += 1
-        return k + 1
-    rx = max(reach(p[:, cy], cx), reach(p[::-1, cy], nx - 1 - cx))
-    ry = max(reach(p[cx, :], cy), reach(p[cx, ::-1], ny - 1 - cy))
-    m = np.abs(p).copy()
-    m[max(cx - rx, 0):cx + rx + 1, max(cy - ry, 0):cy + ry + 1] = 0.0
-    return float(m.max())
+def psf_beam_and_sidelobe(ctx, psf, cell_rad, cutoff: float = 0.35):
+    """The fitted beam and estimate_psf_sidelobe_level (beam.rs:292-304):
+    max(|min psf|, |max(psf - fitted Gaussian)|), 0 when no beam fits."""
+    beam, _, _ = im.fit_beam(psf, cell_rad, cutoff, ctx=ctx)
+    if beam is None:
+        return None, 0.0
+    return beam, im.psf_sidelobe(ctx, psf, cell_rad, beam)
 
 
 def _absmax(a) -> float:
@@ -125,7 +119,10 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
     CUDA tensors for a device batch, numpy arrays for a host batch."""
     psf, residual, state, _ = im.dirty_image(gridder, batch, wproj)
     plan = im.Plan(gridder, batch, wproj)
-    sidelobe = psf_sidelobe_level(psf) if max_psf_sidelobe is None else max_psf_sidelobe
+    geom = gridder.geometry
+    cell = (geom.cell_x_rad, geom.cell_y_rad)
+    beam, fitted_sidelobe = psf_beam_and_sidelobe(gridder.ctx, psf, cell, cfg.psf_cutoff)
+    sidelobe = fitted_sidelobe if max_psf_sidelobe is None else max_psf_sidelobe
     model = _zeros_like(residual)
     ctx = gridder.ctx
     actual = reported = major = 0
@@ -189,5 +186,6 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
             residual = plan.residual_image(model, state)
     finally:
         plan.close()
+    restored = im.restore(gridder.ctx, model, residual, cell, beam) if beam is not None else None
     return CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
-                       thresholds)
+                       thresholds, beam, restored, sidelobe)

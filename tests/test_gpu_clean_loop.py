@@ -5,7 +5,8 @@ cr_plan_residual_image refreshes) and the oracle loop (oracle.cotton_schwab:
 the C Hogbom and the FP64 residual) run on the same noise-free point-source
 observation.  Every component position matches, fluxes agree within 1e-5
 relative, the cycle thresholds, major-cycle count and stop reason agree, and
-the final residual is within 1e-5 of the oracle's peak.
+the final residual is within 1e-5 of the oracle's peak; the restored image
+(fitted beam, model convolved plus residual) agrees with the oracle's.
 """
 import math
 
@@ -81,8 +82,20 @@ def test_standard_loop_matches_oracle(ctx, host):
     if not host:
         out.residual = out.residual.cpu().numpy()
         out.model = out.model.cpu().numpy()
+        out.restored = out.restored.cpu().numpy()
     assert ref["major_cycles"] >= 3
     _compare(out, ref)
+    # the restored image: the oracle's beam fit of its PSF, restoration of its
+    # model plus residual
+    from oracle import beam as OB
+    cell = (obs.cell, obs.cell)
+    ob, _, _ = OB.fit_beam(psf_o.astype(np.float32), cell, 0.35)
+    assert out.beam is not None
+    for a, b2 in ((out.beam.major_fwhm_rad, ob.major_fwhm_rad),
+                  (out.beam.minor_fwhm_rad, ob.minor_fwhm_rad)):
+        assert abs(a - b2) <= 1e-4 * b2
+    rest = OB.restore(ref["model"], ref["residual"], cell, ob)
+    assert peak_norm_err(out.restored, rest) <= 1e-4
 
 
 def test_wproj_loop_matches_oracle(ctx):
