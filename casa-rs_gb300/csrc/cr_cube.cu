@@ -440,36 +440,47 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
     // warp-uniform trip counts so that the warp-aggregated atomics see whole warps
     const int wp = threadIdx.x >> 5;
     for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
-        uint32_t tile[kVec];
+        // loads first, then every cursor atomic, then the stores: the kVec
+        // atomics of a thread are in flight together
+        uint32_t tile[kVec], meta[kVec], pos0[kVec];
+        unsigned peers[kVec];
+        float w[kVec];
+        float2 vv[kVec];
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
             const int64_t r = base + lane + 32 * j;
-            tile[j] = r < r1 ? a.ev_tile[(int64_t)c * a.R + r] : ~0u;
+            const int64_t i = (int64_t)c * a.R + (r < r1 ? r : r0);
+            tile[j] = r < r1 ? a.ev_tile[i] : ~0u;
+            meta[j] = a.ev_meta[i];
+            w[j] = a.ev_w[i];
+            vv[j] = a.vis[i];
         }
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
             const bool ok = tile[j] != ~0u;
-            const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
             const unsigned act = __ballot_sync(0xffffffffu, ok);
+            peers[j] = 0u;
+            pos0[j] = 0u;
             if (!ok) continue;
-            const int64_t bin = cell_bin(c, ntiles, tile[j], a.ev_meta[i]);
-            const unsigned peers = __match_any_sync(act, (unsigned long long)bin);
-            const int leader = __ffs(peers) - 1;
-            const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-            uint32_t pos0 = 0;
-            if (lane == leader) pos0 = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers));
-            pos0 = __shfl_sync(peers, pos0, leader);
-            const uint32_t pos = pos0 + rank;
-            const float w = a.ev_w[i];
-            const float2 vv = a.vis[i];
+            const int64_t bin = cell_bin(c, ntiles, tile[j], meta[j]);
+            peers[j] = __match_any_sync(act, (unsigned long long)bin);
+            if (lane == __ffs(peers[j]) - 1)
+                pos0[j] = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers[j]));
+        }
+#pragma unroll
+        for (int j = 0; j < kVec; ++j) {
+            if (tile[j] == ~0u) continue;
+            const int leader = __ffs(peers[j]) - 1;
+            const uint32_t pos = __shfl_sync(peers[j], pos0[j], leader) +
+                                 __popc(peers[j] & ((1u << lane) - 1u));
+            const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
             float vr = 0.0f, vi = 0.0f;
-            if (finite_f(vv.x) && finite_f(vv.y)) {
-                vr = __fmul_rn(vv.x, w);
-                vi = __fmul_rn(vv.y, w);
+            if (finite_f(vv[j].x) && finite_f(vv[j].y)) {
+                vr = __fmul_rn(vv[j].x, w[j]);
+                vi = __fmul_rn(vv[j].y, w[j]);
             }
-            a.rec[pos] = make_uint4(a.ev_meta[i], (uint32_t)i, __float_as_uint(vr),
-                                    __float_as_uint(vi));
-            a.rec_w[pos] = w;
+            a.rec[pos] = make_uint4(meta[j], (uint32_t)i, __float_as_uint(vr), __float_as_uint(vi));
+            a.rec_w[pos] = w[j];
         }
     }
 }

@@ -147,3 +147,32 @@ def test_cube_boundary_samples_take_the_oracle_decisions(ctx):
         np.testing.assert_array_equal(sy[c], oy)
         np.testing.assert_array_equal(rx[c], orx)
         np.testing.assert_array_equal(ry[c], ory)
+
+
+@pytest.mark.parametrize("nx,os_,cell", [(100, 100, 3.1e-5), (150, 100, 2.2e-5), (96, 64, 4.4e-5)])
+def test_cube_plan_other_oversampling_and_sizes(ctx, nx, os_, cell):
+    """Oversampling 100 (offset boundaries that are not dyadic) and grids whose
+    halves are not whole multiples of the tile: the integer path still takes
+    the oracle's decisions for every sample."""
+    rng = np.random.default_rng(nx)
+    geom = O.Geometry(nx, nx, cell, cell)
+    og = O.StdGridder(geom, os_)
+    ls = np.array([1.0e9, 1.23e9, 1.7e9, 2.0e9]) / S.C_LIGHT
+    half = (og.gnx / 2 - 4) * og.du / ls[-1]
+    um = rng.uniform(-half, half, 30000)
+    vm = rng.uniform(-half, half, 30000)
+    vis = np.ones((len(ls), len(um)), np.complex64)
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(nx, nx, cell, cell), os_)
+    for mode in ("natural", "uniform"):
+        sx, sy, rx, ry, wt = cc.cube_sample_taps(gg, cc.CubeBatch(um, vm, ls, vis), mode)
+        for c in range(len(ls)):
+            u, v = um * ls[c], vm * ls[c]
+            wo, _, _ = O.apply_weighting(geom, u, v, np.ones(len(u), np.float32), mode,
+                                         convention=1)
+            ox, oy, orx, ory = og.plan_many(u, v)
+            ok = (ox >= 0) & (wo > 0)
+            np.testing.assert_array_equal(sx[c], np.where(ok, ox, -1))
+            np.testing.assert_array_equal(sy[c], np.where(ok, oy, -1))
+            np.testing.assert_array_equal(rx[c], np.where(ok, orx, -1))
+            np.testing.assert_array_equal(ry[c], np.where(ok, ory, -1))
+            np.testing.assert_array_equal(wt[c], np.where(ok, wo, 0.0).astype(np.float32))
