@@ -39,7 +39,7 @@ constexpr int kGridThreads = 256;
 constexpr int kRowsPerWarp = kTile / (kGridThreads / 32);  // 4
 constexpr int kMaxSegRadius = 4;
 constexpr int kMaxSeg = (2 * kMaxSegRadius + 1) * (2 * kMaxSegRadius + 1);
-constexpr int kChunk = 1024;  // candidate records per work item
+constexpr int kChunk = 512;  // candidate records per work item
 
 // ---- construction ----------------------------------------------------------------
 __global__ void screen_kernel(float2* buf, int64_t conv, int64_t inner, int planes_in_batch,
