@@ -128,6 +128,12 @@ class Context:
     def synchronize(self):
         call("cr_ctx_synchronize", self._h)
 
+    def set_cube_graphs(self, enable: bool):
+        """All-device cube calls are captured into a CUDA graph on their second
+        occurrence and replayed afterwards; False runs every call eagerly."""
+        if self._lib.cr_ctx_set_cube_graphs(self._h, 1 if enable else 0) != 0:
+            raise ValueError("null context")
+
     @property
     def launch_count(self) -> int:
         return int(self._lib.cr_ctx_launch_count(self._h))
@@ -620,7 +626,25 @@ class CubeBatch:
         return b
 
 
-def _cube_call(gridder, cube, weighting, robust, grids, model_grids):
+def _out_or_new(arrs, given, shape, np_dtype, torch_dtype, dev):
+    """A caller-supplied output (contiguous, of the call's shape, type and
+    location) or a new one."""
+    if given is None:
+        return arrs.out(shape, np_dtype, torch_dtype, dev)
+    if _is_torch(given):
+        ok = given.is_cuda and given.dtype == torch_dtype and given.is_contiguous()
+        loc = CR_DEVICE
+    else:
+        ok = isinstance(given, np.ndarray) and given.dtype == np_dtype and \
+            given.flags.c_contiguous
+        loc = CR_HOST
+    if not ok or tuple(given.shape) != tuple(shape):
+        raise ValueError(f"output must be a contiguous {np_dtype.__name__} array of shape {shape}")
+    arrs._loc(loc)
+    return given, (given.data_ptr() if loc == CR_DEVICE else given.ctypes.data), loc
+
+
+def _cube_call(gridder, cube, weighting, robust, grids, model_grids, out=(None, None, None)):
     ctx = gridder.ctx
     arrs = _Arrays()
     b = cube._bind(arrs)
@@ -635,11 +659,13 @@ def _cube_call(gridder, cube, weighting, robust, grids, model_grids):
     pp = dp = prp = None
     loc = CR_HOST if arrs.location is None else arrs.location
     if grids:
-        psf, pp, loc = arrs.out(gs, np.float32, torch.float32 if torch else None, dev)
-        dirty, dp, _ = arrs.out(gs, np.complex64, torch.complex64 if torch else None, dev)
+        psf, pp, loc = _out_or_new(arrs, out[0], gs, np.float32,
+                                   torch.float32 if torch else None, dev)
+        dirty, dp, _ = _out_or_new(arrs, out[1], gs, np.complex64,
+                                   torch.complex64 if torch else None, dev)
     if model_grids is not None:
-        pred, prp, loc = arrs.out((cube.channels, cube.rows), np.complex64,
-                                  torch.complex64 if torch else None, dev)
+        pred, prp, loc = _out_or_new(arrs, out[2], (cube.channels, cube.rows), np.complex64,
+                                     torch.complex64 if torch else None, dev)
     sums = (_lib.Sums * cube.channels)()
     mode = WEIGHTING_MODES[weighting]
     if grids and model_grids is not None:
@@ -655,23 +681,31 @@ def _cube_call(gridder, cube, weighting, robust, grids, model_grids):
     return psf, dirty, pred, ([GridSums.from_c(s) for s in sums] if sums is not None else None)
 
 
-def cube_grid_dirty(gridder, cube: CubeBatch, weighting: str = "natural", robust: float = 0.0):
+def cube_grid_dirty(gridder, cube: CubeBatch, weighting: str = "natural", robust: float = 0.0,
+                    out=None):
     """Every channel's PSF grid (float32, real part) and dirty grid
-    (complex64), [C][gnx][gny], with per-channel sums."""
-    psf, dirty, _, sums = _cube_call(gridder, cube, weighting, robust, True, None)
+    (complex64), [C][gnx][gny], with per-channel sums.  ``out`` = (psf,
+    dirty) writes into given arrays; device calls that repeat their arrays
+    and parameters are replayed from a captured CUDA graph."""
+    psf, dirty, _, sums = _cube_call(gridder, cube, weighting, robust, True, None,
+                                     tuple(out or (None, None)) + (None,))
     return psf, dirty, sums
 
 
 def cube_degrid(gridder, cube: CubeBatch, model_grids, weighting: str = "natural",
-                robust: float = 0.0):
-    """Model visibilities [C][R] of per-channel model grids [C][gnx][gny]."""
-    return _cube_call(gridder, cube, weighting, robust, False, model_grids)[2]
+                robust: float = 0.0, out=None):
+    """Model visibilities [C][R] of per-channel model grids [C][gnx][gny]
+    (written into ``out`` when given)."""
+    return _cube_call(gridder, cube, weighting, robust, False, model_grids,
+                      (None, None, out))[2]
 
 
 def cube_grid_degrid(gridder, cube: CubeBatch, model_grids, weighting: str = "natural",
-                     robust: float = 0.0):
-    """One plan, then both: (psf grids, dirty grids, model visibilities, sums)."""
-    return _cube_call(gridder, cube, weighting, robust, True, model_grids)
+                     robust: float = 0.0, out=None):
+    """One plan, then both: (psf grids, dirty grids, model visibilities, sums);
+    ``out`` = (psf, dirty, pred) writes into given arrays."""
+    return _cube_call(gridder, cube, weighting, robust, True, model_grids,
+                      tuple(out) if out is not None else (None, None, None))
 
 
 def cube_sample_taps(gridder, cube: CubeBatch, weighting: str = "natural", robust: float = 0.0):

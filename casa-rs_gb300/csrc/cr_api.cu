@@ -133,6 +133,61 @@ CubeInput cube_input(cr_ctx* ctx, const cr_cube_batch* b) {
     return in;
 }
 
+// A call signature of the cube path: every pointer, size and parameter the
+// captured pipeline depends on.
+std::string cube_key(const cr_gridder* g, const cr_cube_batch* b, int32_t weighting, float robust,
+                     const void* psf, const void* dirty, const void* model, const void* pred) {
+    std::string k;
+    auto put = [&](const void* p, size_t n) { k.append((const char*)p, n); };
+    put(&g, sizeof g);
+    put(&b->rows, sizeof b->rows);
+    put(&b->channels, sizeof b->channels);
+    put(&b->u_m, sizeof b->u_m);
+    put(&b->v_m, sizeof b->v_m);
+    put(&b->vis, sizeof b->vis);
+    put(&b->weight, sizeof b->weight);
+    put(&b->flags, sizeof b->flags);
+    put(&weighting, sizeof weighting);
+    put(&robust, sizeof robust);
+    put(&psf, sizeof psf);
+    put(&dirty, sizeof dirty);
+    put(&model, sizeof model);
+    put(&pred, sizeof pred);
+    put(b->lambda_scale, (size_t)b->channels * sizeof(double));
+    return k;
+}
+
+// Replays a captured cube pipeline on the context's own stream, ordered
+// after and before the caller's stream by events; times it as one stage.
+void cube_replay(cr_ctx* ctx, CubeGraph& G, cr_sums* sums) {
+    cudaStream_t caller = ctx->stream, own = ctx->own_stream;
+    if (caller != own) {
+        CR_CUDA_CHECK(cudaEventRecord(ctx->ev[4], caller));
+        CR_CUDA_CHECK(cudaStreamWaitEvent(own, ctx->ev[4], 0));
+    }
+    CR_CUDA_CHECK(cudaEventRecord(ctx->ev[0], own));
+    CR_CUDA_CHECK(cudaGraphLaunch(G.exec, own));
+    ctx->launches += G.launches;
+    CR_CUDA_CHECK(cudaEventRecord(ctx->ev[1], own));
+    if (caller != own) {
+        CR_CUDA_CHECK(cudaEventRecord(ctx->ev[5], own));
+        CR_CUDA_CHECK(cudaStreamWaitEvent(caller, ctx->ev[5], 0));
+    }
+    ctx->stream = own;
+    try {
+        cube_read_sums(ctx, G.cr, sums);
+        CR_CUDA_CHECK(cudaEventSynchronize(ctx->ev[1]));
+    } catch (...) {
+        ctx->stream = caller;
+        throw;
+    }
+    ctx->stream = caller;
+    float ms = 0.0f;
+    CR_CUDA_CHECK(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    ctx->kev_used = 0;
+    set_timings(ctx, cr_timings{0.f, ms, 0.f, 0.f, 0.f});
+}
+
 int cube_run(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t weighting,
              float robust, float* psf_grids, float* dirty_grids, const float* model_grids,
              int32_t grid_location, float* pred, int32_t out_location, cr_sums* sums,
@@ -140,6 +195,87 @@ int cube_run(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t wei
     return guarded(err, [&] {
         need(ctx != nullptr && g != nullptr, "null argument");
         bind(ctx);
+        // All-device calls are captured into a CUDA graph on their second
+        // occurrence (the first runs eagerly: it sizes the workspaces and
+        // tunes the gridding chunk) and replayed from then on, until a
+        // workspace is reallocated.
+        const bool on_device = batch != nullptr && batch->location == CR_DEVICE &&
+                               out_location == CR_DEVICE &&
+                               (!model_grids || grid_location == CR_DEVICE) &&
+                               !psf_grids == !dirty_grids && (!model_grids || pred);
+        if (on_device && ctx->cube_graphs_enabled) {
+            const std::string key = cube_key(g, batch, weighting, robust, psf_grids,
+                                             dirty_grids, model_grids, pred);
+            // callers that never repeat a signature must not grow the table
+            if (ctx->cube_graphs.size() >= 32 && !ctx->cube_graphs.count(key))
+                ctx->cube_graphs.clear();
+            auto& slot = ctx->cube_graphs[key];
+            if (!slot) slot = std::make_shared<CubeGraph>();
+            CubeGraph& G = *slot;
+            if (G.exec && G.epoch != ctx->ws_epoch) {
+                CR_CUDA_CHECK(cudaGraphExecDestroy(G.exec));
+                G.exec = nullptr;
+                G.eager_runs = 0;
+            }
+            if (G.exec) {
+                cube_replay(ctx, G, sums);
+                return;
+            }
+            if (G.eager_runs >= 1 && !G.failed) {
+                CubeInput in = cube_input(ctx, batch);
+                cudaStream_t caller = ctx->stream, own = ctx->own_stream;
+                if (caller != own) {
+                    CR_CUDA_CHECK(cudaEventRecord(ctx->ev[4], caller));
+                    CR_CUDA_CHECK(cudaStreamWaitEvent(own, ctx->ev[4], 0));
+                }
+                ctx->stream = own;
+                try {
+                    cube_upload_channels(ctx, g, in);
+                } catch (...) {
+                    ctx->stream = caller;
+                    throw;
+                }
+                cudaGraph_t graph = nullptr;
+                const int64_t launches0 = ctx->launches;
+                try {
+                    CR_CUDA_CHECK(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
+                    ctx->capturing = true;
+                    CubeRecords cr = cube_plan(ctx, g, in, weighting, robust);
+                    if (psf_grids)
+                        cube_grid(ctx, g, cr, psf_grids, (float2*)dirty_grids);
+                    if (model_grids)
+                        cube_degrid(ctx, g, cr, (const float2*)model_grids, (float2*)pred);
+                    ctx->capturing = false;
+                    CR_CUDA_CHECK(cudaStreamEndCapture(own, &graph));
+                    CR_CUDA_CHECK(cudaGraphInstantiate(&G.exec, graph, 0));
+                    CR_CUDA_CHECK(cudaGraphDestroy(graph));
+                    G.cr = cr;
+                    G.epoch = ctx->ws_epoch;
+                    G.launches = ctx->launches - launches0;
+                    ctx->launches = launches0;
+                } catch (...) {
+                    // a call that cannot be captured (say, a workspace that
+                    // must grow) runs eagerly, now and from then on
+                    if (ctx->capturing) {
+                        ctx->capturing = false;
+                        graph = nullptr;
+                        cudaStreamEndCapture(own, &graph);
+                    }
+                    if (graph) cudaGraphDestroy(graph);
+                    if (G.exec) cudaGraphExecDestroy(G.exec);
+                    G.exec = nullptr;
+                    cudaGetLastError();
+                    ctx->launches = launches0;
+                    G.failed = true;
+                }
+                ctx->stream = caller;
+                if (G.exec) {
+                    cube_replay(ctx, G, sums);
+                    return;
+                }
+            }
+            G.eager_runs++;
+        }
         StageTimer tm(ctx);
         tm.mark();
         CubeInput in = cube_input(ctx, batch);
@@ -294,6 +430,7 @@ void cr_gridder_destroy(cr_gridder* g) {
     if (!g) return;
     cudaSetDevice(g->ctx->device);
     cudaStreamSynchronize(g->ctx->stream);
+    g->ctx->cube_graphs.clear();   // captured pipelines may read this gridder's tables
     cudaFree(g->taps_d);
     cudaFree(g->corr_x_d);
     cudaFree(g->corr_y_d);
@@ -927,6 +1064,13 @@ int cr_psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32
         const float* p = (const float*)device_input(ctx, psf, n * 4, location, "sl_psf");
         *level = psf_sidelobe(ctx, p, nx, ny, cell_x_rad, cell_y_rad, *beam);
     });
+}
+
+int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable) {
+    if (!ctx) return CR_INVALID;
+    ctx->cube_graphs_enabled = enable != 0;
+    if (!enable) ctx->cube_graphs.clear();
+    return CR_OK;
 }
 
 }  // extern "C"

@@ -23,6 +23,8 @@ void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes)
     if (bytes == 0) bytes = 16;
     DevBuf& b = pool[name];
     if (b.bytes >= bytes) return b.ptr;
+    if (ctx->capturing) fail(CR_CUDA, "workspace '" + name + "' grew during graph capture");
+    ctx->ws_epoch++;
     if (b.ptr) CR_CUDA_CHECK(cudaFreeAsync(b.ptr, ctx->stream));
     size_t want = bytes + bytes / 8;
     want = (want + 255) & ~size_t(255);
@@ -48,6 +50,7 @@ void note_launch(cr_ctx* ctx, const char* what) {
 }
 
 void kernel_mark(cr_ctx* ctx, int which, bool end) {
+    if (ctx->capturing) return;   // a captured graph is timed as a whole
     CR_CUDA_CHECK(cudaEventRecord(ctx->kev[which * 2 + (end ? 1 : 0)], ctx->stream));
     if (end) ctx->kev_used |= 1 << which;
 }

@@ -485,12 +485,16 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
     }
 }
 
-constexpr uint32_t kGridChunk = 2048;   // source records per gridding work item
+// Source records per gridding work item: chosen per cube shape by a
+// first-use tuning pass over these candidates (the default before tuning).
+constexpr uint32_t kGridChunkCandidates[3] = {1024, 2048, 4096};
+constexpr uint32_t kGridChunkDefault = 2048;
+constexpr uint32_t kGridChunkMin = 1024;
 constexpr uint32_t kDegridChunk = 4096; // records per degridding work item
 
 // Work lists.  Gridding: an output tile (channel, tx, ty) gathers the bins
 // (tx, ty), (tx-1, ty), (tx, ty-1), (tx-1, ty-1); their records, taken in
-// that order, are cut into chunks of kGridChunk.  A tile with one chunk is
+// that order, are cut into chunks (of the tuned size).  A tile with one chunk is
 // written with plain stores; the chunks of a heavier tile add into the grid
 // with atomics after cube_work_fill zeroed it.  Degridding: each bin's
 // records in chunks of kDegridChunk.
@@ -526,7 +530,7 @@ __device__ __forceinline__ void source_ranges(const uint32_t* bin_start,
 }
 
 __global__ void cube_work_count(const uint32_t* bin_start, const uint32_t* cell_end,
-                                int64_t nbins, int64_t ntiles, int64_t nty,
+                                int64_t nbins, int64_t ntiles, int64_t nty, uint32_t grid_chunk,
                                 uint32_t* grid_chunks, uint32_t* degrid_chunks) {
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins;
          b += (int64_t)gridDim.x * blockDim.x) {
@@ -534,7 +538,7 @@ __global__ void cube_work_count(const uint32_t* bin_start, const uint32_t* cell_
         uint32_t lo[4], hi[4];
         source_ranges(bin_start, cell_end, c, ntiles, nty, T / nty, T % nty, lo, hi);
         const uint32_t n = (hi[0] - lo[0]) + (hi[1] - lo[1]) + (hi[2] - lo[2]) + (hi[3] - lo[3]);
-        grid_chunks[b] = n == 0 ? 1u : (n + kGridChunk - 1) / kGridChunk;
+        grid_chunks[b] = n == 0 ? 1u : (n + grid_chunk - 1) / grid_chunk;
         degrid_chunks[b] = (bin_count(bin_start, b) + kDegridChunk - 1) / kDegridChunk;
     }
 }
@@ -573,6 +577,7 @@ struct CubeGridArgs {
     int32_t tap_rows;
     int64_t ntx, nty, gnx, gny;
     const uint2* items;          // (output tile bin, chunk)
+    uint32_t grid_chunk;         // records per chunk
     const uint32_t* grid_chunks; // chunks of each output tile
     const unsigned long long* n_items;
     unsigned int* item_counter;
@@ -610,7 +615,7 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
         const int64_t c = bin / ntiles, T = bin % ntiles;
         const int64_t tx = T / a.nty, ty = T % a.nty;
         const bool shared_tile = a.grid_chunks[bin] > 1;
-        const uint32_t clo = it.y * kGridChunk, chi = clo + kGridChunk;
+        const uint32_t clo = it.y * a.grid_chunk, chi = clo + a.grid_chunk;
         // source s = home tile (tx - (s & 1), ty - (s >> 1)); [b0, b1) its records
         // inside this chunk (empty when none)
         uint32_t b0[4], b1[4];
@@ -855,6 +860,27 @@ __global__ void __launch_bounds__(kCubeThreads) cube_taps_kernel(CubeArgs a, Cub
 
 }  // namespace
 
+void cube_upload_channels(cr_ctx* ctx, cr_gridder* g, const CubeInput& in) {
+    const cr_grid_info& gi = g->info;
+    const double dus = (double)g->geom.nx * g->geom.cell_x_rad;
+    const double dvs = (double)g->geom.ny * g->geom.cell_y_rad;
+    std::vector<CubeChan> chh((size_t)in.C);
+    for (int c = 0; c < in.C; ++c) {
+        const double s = in.lambda_scale[c];
+        if (!(std::isfinite(s) && s > 0.0)) fail(CR_INVALID, "lambda_scale must be finite and > 0");
+        chh[c].lscale = s;
+        chh[c].kx = fix_scale_of(s, gi.du, false);
+        chh[c].ky = fix_scale_of(s, gi.dv, false);
+        chh[c].kdx = fix_scale_of(s, dus, true);
+        chh[c].kdy = fix_scale_of(s, dvs, true);
+    }
+    CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", chh.size() * sizeof(CubeChan));
+    CR_CUDA_CHECK(cudaMemcpyAsync(chd, chh.data(), chh.size() * sizeof(CubeChan),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    // the pageable source must outlive the copy
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+}
+
 CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
                       float robust, const CubeTaps* taps) {
     if (mode != CR_WEIGHT_NATURAL && mode != CR_WEIGHT_UNIFORM && mode != CR_WEIGHT_BRIGGS)
@@ -873,22 +899,11 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     cr.ntiles = cr.ntx * cr.nty;
     const int64_t nbins = (int64_t)in.C * cr.ntiles;
     const size_t ns = (size_t)std::max<int64_t>((int64_t)in.C * in.R, 1);
-    // per-channel constants
+    // per-channel constants (uploaded before a capture by the caller)
     const double dus = (double)g->geom.nx * g->geom.cell_x_rad;
     const double dvs = (double)g->geom.ny * g->geom.cell_y_rad;
-    std::vector<CubeChan> chh((size_t)in.C);
-    for (int c = 0; c < in.C; ++c) {
-        const double s = in.lambda_scale[c];
-        if (!(std::isfinite(s) && s > 0.0)) fail(CR_INVALID, "lambda_scale must be finite and > 0");
-        chh[c].lscale = s;
-        chh[c].kx = fix_scale_of(s, gi.du, false);
-        chh[c].ky = fix_scale_of(s, gi.dv, false);
-        chh[c].kdx = fix_scale_of(s, dus, true);
-        chh[c].kdy = fix_scale_of(s, dvs, true);
-    }
-    CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", chh.size() * sizeof(CubeChan));
-    CR_CUDA_CHECK(cudaMemcpyAsync(chd, chh.data(), chh.size() * sizeof(CubeChan),
-                                  cudaMemcpyHostToDevice, ctx->stream));
+    if (!ctx->capturing) cube_upload_channels(ctx, g, in);
+    CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", (size_t)in.C * sizeof(CubeChan));
     cr.rec = (uint4*)workspace(ctx, "cube_rec", ns * 16);
     cr.rec_w = (float*)workspace(ctx, "cube_rec_w", ns * 4);
     cr.bin_start = (uint32_t*)workspace(ctx, "cube_bin_start", (size_t)(nbins + 1) * 4);
@@ -983,63 +998,98 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
         cube_scatter_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
         note_launch(ctx, "cube_scatter_kernel");
     }
-    // work lists (their output-zeroing part runs in cube_grid)
+    // work-list buffers (the lists are made by cube_grid / cube_degrid)
     cr.grid_chunks = (uint32_t*)workspace(ctx, "cube_gchunks", (size_t)nbins * 4);
     cr.degrid_chunks = (uint32_t*)workspace(ctx, "cube_dchunks", (size_t)nbins * 4);
     cr.cell_end = hist;
-    cube_work_count<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
-        cr.bin_start, cr.cell_end, nbins, cr.ntiles, cr.nty, cr.grid_chunks, cr.degrid_chunks);
-    note_launch(ctx, "cube_work_count");
     cr.grid_first = (uint32_t*)workspace(ctx, "cube_gfirst", (size_t)nbins * 4);
     cr.degrid_first = (uint32_t*)workspace(ctx, "cube_dfirst", (size_t)nbins * 4);
     cr.n_items = (unsigned long long*)workspace(ctx, "cube_nitems", 16);
-    exclusive_scan_u32(ctx, cr.grid_chunks, cr.grid_first, nbins, cr.n_items);
-    exclusive_scan_u32(ctx, cr.degrid_chunks, cr.degrid_first, nbins, cr.n_items + 1);
     // sum over tiles of ceil(n / K) <= tiles + (sum n) / K, and each record is a
     // source of at most four output tiles
-    const size_t max_grid_items = (size_t)nbins + 4 * ns / kGridChunk + 1;
+    const size_t max_grid_items = (size_t)nbins + 4 * ns / kGridChunkMin + 1;
     const size_t max_degrid_items = (size_t)nbins + ns / kDegridChunk + 1;
     cr.grid_items = (uint2*)workspace(ctx, "cube_gitems", max_grid_items * 8);
     cr.degrid_items = (uint2*)workspace(ctx, "cube_ditems", max_degrid_items * 8);
     return cr;
 }
 
-void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty) {
+// Work lists for one gridding chunk size; with psf/dirty, heavy output tiles
+// are zeroed for their atomic chunks.
+static void make_work_lists(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, uint32_t chunk,
+                            float* psf, float2* dirty) {
     const cr_grid_info& gi = g->info;
     const int64_t nbins = (int64_t)cr.C * cr.ntiles;
+    cube_work_count<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
+        cr.bin_start, cr.cell_end, nbins, cr.ntiles, cr.nty, chunk, cr.grid_chunks,
+        cr.degrid_chunks);
+    note_launch(ctx, "cube_work_count");
+    exclusive_scan_u32(ctx, cr.grid_chunks, cr.grid_first, nbins, cr.n_items);
+    exclusive_scan_u32(ctx, cr.degrid_chunks, cr.degrid_first, nbins, cr.n_items + 1);
     cube_work_fill<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
         cr.grid_chunks, cr.grid_first, cr.degrid_chunks, cr.degrid_first, nbins, cr.ntiles,
         cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.degrid_items, psf, dirty);
     note_launch(ctx, "cube_work_fill");
+    cr.grid_chunk = chunk;
+    cr.fill_done = true;
+}
+
+static void launch_cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf,
+                             float2* dirty) {
+    const cr_grid_info& gi = g->info;
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows, cr.ntx, cr.nty,
-                   gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunks, cr.n_items, counter,
-                   psf, dirty};
+    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows, cr.ntx,
+                   cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunk, cr.grid_chunks,
+                   cr.n_items, counter, psf, dirty};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int per_sm = 0;
     CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_grid_kernel,
                                                                 kGridThreads, 0));
-    kernel_mark(ctx, 0, false);
     cube_grid_kernel<<<sms * std::max(per_sm, 1), kGridThreads, 0, ctx->stream>>>(a);
     note_launch(ctx, "cube_grid_kernel");
-    kernel_mark(ctx, 0, true);
-    cr.fill_done = true;
 }
 
-void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
+void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty) {
+    const std::string key = std::to_string(cr.C) + "x" + std::to_string(cr.ntx) + "x" +
+                            std::to_string(cr.nty) + "/" + std::to_string(g->info.oversampling);
+    auto tuned = ctx->cube_chunk.find(key);
+    if (tuned == ctx->cube_chunk.end() && !ctx->capturing) {
+        // first use of this cube shape: time the gridding pass (work lists
+        // and kernel) for every candidate chunk size and keep the fastest
+        cudaEvent_t e0 = ctx->kev[0], e1 = ctx->kev[1];
+        float best_ms = 0.0f;
+        uint32_t best = kGridChunkDefault;
+        for (uint32_t chunk : kGridChunkCandidates) {
+            CR_CUDA_CHECK(cudaEventRecord(e0, ctx->stream));
+            make_work_lists(ctx, g, cr, chunk, psf, dirty);
+            launch_cube_grid(ctx, g, cr, psf, dirty);
+            CR_CUDA_CHECK(cudaEventRecord(e1, ctx->stream));
+            CR_CUDA_CHECK(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            CR_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+            if (chunk == kGridChunkCandidates[0] || ms < best_ms) {
+                best_ms = ms;
+                best = chunk;
+            }
+        }
+        ctx->cube_chunk[key] = best;
+        tuned = ctx->cube_chunk.find(key);
+    }
+    const uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    make_work_lists(ctx, g, cr, chunk, psf, dirty);
+    kernel_mark(ctx, 0, false);
+    launch_cube_grid(ctx, g, cr, psf, dirty);
+    kernel_mark(ctx, 0, true);
+}
+
+void cube_degrid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* grid,
                  float2* pred) {
     const cr_grid_info& gi = g->info;
     CR_CUDA_CHECK(cudaMemsetAsync(pred, 0, (size_t)cr.C * cr.R * 8, ctx->stream));
-    if (!cr.fill_done) {
-        // the degridding work list without a gridding pass before it
-        const int64_t nbins = (int64_t)cr.C * cr.ntiles;
-        cube_work_fill<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
-            cr.grid_chunks, cr.grid_first, cr.degrid_chunks, cr.degrid_first, nbins, cr.ntiles,
-            cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.degrid_items, nullptr, nullptr);
-        note_launch(ctx, "cube_work_fill");
-    }
+    // the degridding work list without a gridding pass before it
+    if (!cr.fill_done) make_work_lists(ctx, g, cr, kGridChunkDefault, nullptr, nullptr);
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
     CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -35,6 +36,8 @@ struct DevBuf {
 // A named set of grow-only device buffers.
 using Pool = std::map<std::string, DevBuf>;
 
+struct CubeGraph;   // a captured cube pipeline (cr_cube.cu)
+
 }  // namespace cr
 
 // A context: one device, one stream, grow-only device workspaces, cached
@@ -51,6 +54,14 @@ struct cr_ctx {
     int kev_used = 0;
     cr_timings timings = {};
     int64_t launches = 0;
+    // cube path: tuned gridding chunk per cube shape, captured pipelines per
+    // call signature; ws_epoch changes whenever a workspace is (re)allocated,
+    // which retires the captured graphs (they hold workspace addresses)
+    std::map<std::string, uint32_t> cube_chunk;
+    std::map<std::string, std::shared_ptr<cr::CubeGraph>> cube_graphs;
+    bool cube_graphs_enabled = true;
+    bool capturing = false;
+    uint64_t ws_epoch = 0;
     // small pinned host buffer for device->host scalars
     void* pinned = nullptr;
 };
@@ -223,7 +234,8 @@ struct CubeRecords {
     uint32_t *degrid_chunks = nullptr, *degrid_first = nullptr;
     uint2 *grid_items = nullptr, *degrid_items = nullptr;
     unsigned long long* n_items = nullptr;   // [0] gridding, [1] degridding
-    bool fill_done = false;                  // set once cube_grid has filled the lists
+    uint32_t grid_chunk = 0;                 // records per gridding work item
+    bool fill_done = false;                  // set once the work lists are made
 };
 // Per-sample outputs of cube_sample_taps ([C][R], -1 / 0 when not gridded).
 struct CubeTaps {
@@ -236,9 +248,24 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
 // psf [C][gnx][gny] float32 (real part), dirty [C][gnx][gny] complex64
 void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty);
 // pred [C][R] complex64, zero for samples that are not gridded
-void cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, const float2* grid,
+void cube_degrid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* grid,
                  float2* pred);
 void cube_read_sums(cr_ctx* ctx, const CubeRecords& cr, cr_sums* out);
+// Host-side constants of the cube plan, uploaded outside any graph capture.
+void cube_upload_channels(cr_ctx* ctx, cr_gridder* g, const CubeInput& in);
+
+// One captured planning + gridding (+ degridding) pipeline of the cube.
+struct CubeGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t epoch = 0;
+    int eager_runs = 0;
+    bool failed = false;     // capture failed: this signature runs eagerly
+    int64_t launches = 0;   // kernels in the graph
+    CubeRecords cr;
+    ~CubeGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
 
 // ---- restoring beam (cr_beam.cu) -------------------------------------------------
 bool fit_beam(const float* psf_host, int64_t nx, int64_t ny, double cell_x, double cell_y,

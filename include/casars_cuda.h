@@ -277,6 +277,11 @@ typedef struct {
 
 /* psf_grids [channels][gnx][gny] float32 (real part of each channel's PSF
  * grid), dirty_grids [channels][gnx][gny] complex64, sums[channels]. */
+/* Calls whose arrays are all device memory are captured into a CUDA graph
+ * on their second occurrence with the same pointers and parameters and
+ * replayed afterwards (cr_timings.grid_ms then times the whole pipeline);
+ * this switches that off (0) or on (nonzero, the default). */
+int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable);
 int cr_cube_grid_dirty(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                        int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
                        int32_t out_location, cr_sums* sums, char** err);
