@@ -102,6 +102,15 @@ SIGNATURES = {
                                  _err]),
     "cr_cube_grid_degrid": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _p, _i32,
                                       _p, _i32, _p, _err]),
+    "cr_cube_plan_create": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, C.POINTER(_p),
+                                       _p, _err]),
+    "cr_cube_plan_destroy": (None, [_p]),
+    "cr_cube_plan_channels": (_i32, [_p]),
+    "cr_cube_plan_grid_dirty": (C.c_int, [_p, _p, _p, _p, _i32, _err]),
+    "cr_cube_plan_degrid": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
+    "cr_cube_plan_grid_residual": (C.c_int, [_p, _p, _p, _i32, _p, _p, _i32, _err]),
+    "cr_cube_plan_dirty_images": (C.c_int, [_p, _p, _p, _p, _i32, _p, _err]),
+    "cr_cube_plan_residual_images": (C.c_int, [_p, _p, _p, _i32, _p, _p, _p, _i32, _err]),
     "cr_cube_sample_taps": (C.c_int, [_p, _p, C.POINTER(CubeBatch), _i32, _f, _p, _p, _p, _p,
                                       _p, _i32, _err]),
     "cr_fit_beam": (C.c_int, [_p, _p, _i32, _i32, _i32, _d, _d, _f, C.POINTER(Beam),

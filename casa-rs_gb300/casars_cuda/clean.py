@@ -189,3 +189,212 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
     restored = im.restore(gridder.ctx, model, residual, cell, beam) if beam is not None else None
     return CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
                        thresholds, beam, restored, sidelobe)
+
+
+# ----------------------------------------------------------------------------
+# cube CLEAN
+# ----------------------------------------------------------------------------
+@dataclass
+class CubeCleanResult:
+    """StandardMfsCubeCleanResult (lib.rs:2995-3013) plus the plane images."""
+    models: object
+    residuals: object
+    psfs: object
+    states: list
+    beams: list
+    restored: object
+    sidelobes: list
+    initial_peak: float
+    max_psf_sidelobe: float
+    final_cycle_threshold: float
+    minor_iterations: int
+    major_cycles: int
+    planes_at_or_below_initial_threshold: int
+    plane_iterations: list
+    plane_stop_reasons: list
+    components: list
+    cycle_thresholds: list
+    active_planes: list
+
+
+def _f32max(values) -> np.float32:
+    """The finite maximum of values, 0 when none (fold with f32::max)."""
+    m = np.float32(0.0)
+    for v in values:
+        v = np.float32(v)
+        if np.isfinite(v) and v > m:
+            m = v
+    return m
+
+
+def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom, refresh):
+    """The control of run_standard_mfs_cube_clean (lib.rs:3026-3210).
+
+    Planes advance in ascending order; per synchronized pass every plane whose
+    residual peak is above the cube-wide cycle threshold (clean_cycle_threshold
+    of the cube's peak and largest PSF sidelobe) runs one major cycle of its
+    own Cotton-Schwab controller with the remaining global budget, one major
+    cycle allowed and the cube threshold as override
+    (run_standard_mfs_prepared_clean_plane_one_major_cycle, lib.rs:46465-46520).
+    The residual refreshes of a pass are batched: a plane's refresh depends on
+    its own model only, so refreshing every updated plane after the pass's
+    minor cycles gives the same residuals as refreshing each in turn.
+
+    residuals / models / psfs are indexable by plane (arrays [C][nx][ny]);
+    hogbom(model, residual, psf, niter, threshold, cycle_threshold) returns a
+    HogbomOutcome-like object; refresh(planes) recomputes residuals[c] for
+    the listed planes from models[c] in place.  Returns a dict of the loop's
+    results."""
+    f32 = np.float32
+    n = len(sidelobes)
+    absmax = lambda c: f32(_absmax(residuals[c]))
+    cyc = lambda peak, sl: clean_cycle_threshold(float(peak), float(sl), cfg)
+    initial_peak = _f32max(absmax(c) for c in range(n))
+    max_sidelobe = _f32max(sidelobes)
+    at_or_below = sum(1 for c in range(n) if absmax(c) <= f32(cyc(initial_peak, max_sidelobe)))
+    plane_iters, plane_stop = [0] * n, [None] * n
+    comps = [[] for _ in range(n)]
+    completed = major = 0
+    thresholds, actives = [], []
+    t = f32(cfg.threshold_jy_per_beam)
+    while True:
+        peak = _f32max(absmax(c) for c in range(n))
+        thr = cyc(peak, max_sidelobe)
+        if peak <= t or (t > 0 and abs(peak - t) / t < f32(0.01)) or completed >= cfg.niter:
+            break
+        if cfg.major_cycle_limit is not None and major >= cfg.major_cycle_limit:
+            break
+        active = [c for c in range(n) if absmax(c) > f32(thr)]
+        if not active:
+            break
+        major += 1
+        cycle_niter = cfg.niter - completed
+        thresholds.append(thr)
+        actives.append(active)
+        pass_iters = 0
+        pending = {}   # plane -> (stop set before the refresh, stop_after, refreshed in loop)
+        for c in active:
+            # the plane's controller (run_hogbom_cotton_schwab, niter =
+            # cycle_niter, major_cycle_limit = 1) up to its residual refresh
+            stop = None
+            min_peak = absmax(c)
+            p = absmax(c)
+            s = tolerant_clean_stop_reason(p, cfg.threshold_jy_per_beam)
+            if s is not None:
+                plane_stop[c] = s
+                continue
+            out = hogbom(models[c], residuals[c], psfs[c],
+                         min(cycle_niter, cfg.minor_cycle_length),
+                         cfg.threshold_jy_per_beam, thr)
+            models[c], residuals[c] = out.model, out.residual
+            comps[c].extend(zip(map(tuple, np.asarray(out.positions).tolist()),
+                                np.asarray(out.fluxes).tolist()))
+            plane_iters[c] += out.reported_updates
+            pass_iters += out.reported_updates
+            updated = out.actual_updates > 0
+            stop_after = None
+            if out.stop_reason is not None:
+                if updated and out.stop_reason in _HANDOFF:
+                    pass
+                elif out.stop_reason in _HANDOFF:
+                    stop = out.stop_reason
+                else:
+                    stop = stop_after = out.stop_reason
+            if not updated:
+                plane_stop[c] = stop if stop is not None else "IterationLimitReached"
+                continue
+            minor_peak = absmax(c)
+            if not minor_peak < min_peak and min_peak > 0 and \
+                    (minor_peak - min_peak) / min_peak > f32(0.1):
+                pending[c] = ("DivergenceDetected", None, False)
+            elif out.reported_updates >= cycle_niter:
+                pending[c] = ("IterationLimitReached", None, False)
+            else:
+                pending[c] = (stop, stop_after, True)
+        if pending:
+            refresh(sorted(pending))
+        for c, (stop, stop_after, in_loop) in pending.items():
+            if in_loop and stop_after is None:
+                s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam)
+                # otherwise the next turn of the plane's loop meets its
+                # one-major-cycle limit
+                stop = s if s is not None else "MajorCycleLimitReached"
+            elif in_loop:
+                stop = stop_after
+            plane_stop[c] = stop
+        completed += pass_iters
+        if pass_iters == 0:
+            break
+    final_thr = cyc(_f32max(absmax(c) for c in range(n)), max_sidelobe)
+    stops = []
+    for c in range(n):
+        if plane_iters[c] >= cfg.niter:
+            stops.append("IterationLimitReached")
+            continue
+        s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam)
+        if s is None:
+            s = plane_stop[c]
+            if s in (None, "MajorCycleLimitReached"):
+                s = "CycleThresholdReached"
+        stops.append(s)
+    return dict(plane_iterations=plane_iters, plane_stops=stops, components=comps,
+                minor_iterations=completed, major_cycles=major, thresholds=thresholds,
+                active=actives, initial_peak=float(initial_peak),
+                max_sidelobe=float(max_sidelobe), final_cycle_threshold=final_thr,
+                planes_at_or_below_initial_threshold=at_or_below)
+
+
+def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
+                   robust: float = 0.0, max_psf_sidelobe: Optional[float] = None,
+                   restore: bool = True) -> CubeCleanResult:
+    """run_standard_mfs_cube_clean (lib.rs:3026-3210) on the device: one
+    persistent cube plan (im.CubePlan) gives every plane's PSF and residual
+    and replays the records for each pass's residual refresh (all updated
+    planes in one batched degrid + grid); the minor cycles are cr_hogbom per
+    plane; each plane's beam is fitted to its PSF and its sidelobe level
+    estimated (beam.rs:292-304) unless max_psf_sidelobe is given."""
+    plan = im.CubePlan(gridder, cube, weighting, robust)
+    ctx = gridder.ctx
+    geom = gridder.geometry
+    cell = (geom.cell_x_rad, geom.cell_y_rad)
+    try:
+        psfs, residuals, states = plan.dirty_images()
+        n = plan.channels
+        beams, sidelobes = [], []
+        for c in range(n):
+            if states[c].psf_peak > 0:
+                b, sl = psf_beam_and_sidelobe(ctx, psfs[c], cell, cfg.psf_cutoff)
+            else:
+                b, sl = None, 0.0
+            beams.append(b)
+            sidelobes.append(sl if max_psf_sidelobe is None else max_psf_sidelobe)
+        models = _zeros_like(residuals)
+
+        def hogbom(model, residual, psf, niter, threshold, cycle_threshold):
+            return im.run_hogbom_minor_cycle(ctx, model, residual, psf, cfg.gain, niter,
+                                             threshold=threshold,
+                                             cycle_threshold=cycle_threshold,
+                                             inclusive=cfg.inclusive)
+
+        def refresh(planes):
+            mask = np.zeros(n, np.uint8)
+            mask[planes] = 1
+            plan.residual_images(models, states, planes=mask, out=residuals)
+
+        out = cube_clean_loop(residuals, psfs, models, sidelobes, cfg, hogbom, refresh)
+    finally:
+        plan.close()
+    restored = None
+    if restore:
+        restored = _zeros_like(residuals)
+        for c in range(n):
+            if beams[c] is not None and _absmax(models[c]) > 0:
+                restored[c] = im.restore(ctx, models[c], residuals[c], cell, beams[c])
+            else:
+                restored[c] = residuals[c]
+    return CubeCleanResult(models, residuals, psfs, states, beams, restored, sidelobes,
+                           out["initial_peak"], out["max_sidelobe"],
+                           out["final_cycle_threshold"], out["minor_iterations"],
+                           out["major_cycles"], out["planes_at_or_below_initial_threshold"],
+                           out["plane_iterations"], out["plane_stops"], out["components"],
+                           out["thresholds"], out["active"])

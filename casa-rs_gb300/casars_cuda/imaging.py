@@ -725,6 +725,123 @@ def cube_sample_taps(gridder, cube: CubeBatch, weighting: str = "natural", robus
     return tuple(o[0] for o in outs) + (wt[0],)
 
 
+class CubePlan:
+    """A persistent cube plan (cr_cube_plan): the cube's weighting and records
+    made once and replayed by gridding, degridding and residual calls -- the
+    planned-sample replay of run_standard_mfs_cube_clean (lib.rs:3026-3210).
+    Arrays live where the cube batch is (torch CUDA tensors or numpy)."""
+
+    def __init__(self, gridder, cube: CubeBatch, weighting: str = "natural",
+                 robust: float = 0.0):
+        ctx = gridder.ctx
+        arrs = _Arrays()
+        b = cube._bind(arrs)
+        _prepare(gridder, arrs)
+        self.gridder = gridder
+        self.channels, self.rows = cube.channels, cube.rows
+        self.device = _device_of(cube.u_m, cube.visibility)
+        self.location = CR_HOST if arrs.location is None else arrs.location
+        h = C.c_void_p()
+        sums = (_lib.Sums * self.channels)()
+        call("cr_cube_plan_create", ctx.handle, gridder.handle, C.byref(b),
+             WEIGHTING_MODES[weighting], float(robust), C.byref(h), sums)
+        self._h = h
+        self.sums = [GridSums.from_c(s) for s in sums]
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().cr_cube_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _arrays(self):
+        arrs = _Arrays()
+        arrs.location = self.location
+        if self.location == CR_DEVICE:
+            self.gridder.ctx.use_torch_stream()
+        else:
+            self.gridder.ctx.use_own_stream()
+        return arrs
+
+    def _grid_shape(self):
+        return (self.channels,) + tuple(self.gridder.grid_shape())
+
+    def _image_shape(self):
+        g = self.gridder.geometry
+        return (self.channels, g.nx, g.ny)
+
+    @staticmethod
+    def _planes(planes):
+        if planes is None:
+            return None, None
+        m = np.ascontiguousarray(np.asarray(
+            planes.cpu() if _is_torch(planes) else planes).astype(np.uint8))
+        return m, m.ctypes.data
+
+    def grid_dirty(self, out=None):
+        """PSF grids (float32, real part) and dirty grids (complex64)."""
+        arrs = self._arrays()
+        gs = self._grid_shape()
+        o = out or (None, None)
+        psf, pp, loc = _out_or_new(arrs, o[0], gs, np.float32, torch.float32 if torch else None,
+                                   self.device)
+        dirty, dp, _ = _out_or_new(arrs, o[1], gs, np.complex64,
+                                   torch.complex64 if torch else None, self.device)
+        call("cr_cube_plan_grid_dirty", self.gridder.ctx.handle, self._h, pp, dp, loc)
+        return psf, dirty
+
+    def degrid(self, model_grids, out=None):
+        arrs = self._arrays()
+        mp = arrs.ptr(model_grids, np.complex64, torch.complex64 if torch else None,
+                      self._grid_shape())
+        pred, op, loc = _out_or_new(arrs, out, (self.channels, self.rows), np.complex64,
+                                    torch.complex64 if torch else None, self.device)
+        call("cr_cube_plan_degrid", self.gridder.ctx.handle, self._h, mp, self.location, op, loc)
+        return pred
+
+    def grid_residual(self, model_grids, planes=None, out=None):
+        """Residual grids of the selected planes (others left as in ``out``)."""
+        arrs = self._arrays()
+        mp = arrs.ptr(model_grids, np.complex64, torch.complex64 if torch else None,
+                      self._grid_shape())
+        mask, mk = self._planes(planes)
+        res, rp, loc = _out_or_new(arrs, out, self._grid_shape(), np.complex64,
+                                   torch.complex64 if torch else None, self.device)
+        call("cr_cube_plan_grid_residual", self.gridder.ctx.handle, self._h, mp, self.location,
+             mk, rp, loc)
+        return res
+
+    def dirty_images(self):
+        """(psf images, residual images, [PsfState] per plane); a plane with
+        no usable samples has zero images and a zero state."""
+        arrs = self._arrays()
+        shape = self._image_shape()
+        psf, pp, loc = arrs.out(shape, np.float32, torch.float32 if torch else None, self.device)
+        res, rp, _ = arrs.out(shape, np.float32, torch.float32 if torch else None, self.device)
+        states = (_lib.PsfState * self.channels)()
+        call("cr_cube_plan_dirty_images", self.gridder.ctx.handle, self._h, pp, rp, loc, states)
+        return psf, res, [PsfState(s.psf_peak, s.normalization_sumwt, s.reported_sumwt)
+                          for s in states]
+
+    def residual_images(self, models, states, planes=None, out=None):
+        """Residual images of the selected planes from model images
+        [C][nx][ny] (the major-cycle refresh); others left as in ``out``."""
+        arrs = self._arrays()
+        mp = arrs.ptr(models, np.float32, torch.float32 if torch else None, self._image_shape())
+        mask, mk = self._planes(planes)
+        cs = (_lib.PsfState * self.channels)(*[s.to_c() for s in states])
+        res, rp, loc = _out_or_new(arrs, out, self._image_shape(), np.float32,
+                                   torch.float32 if torch else None, self.device)
+        call("cr_cube_plan_residual_images", self.gridder.ctx.handle, self._h, mp, self.location,
+             mk, cs, rp, loc)
+        return res
+
+
 # ----------------------------------------------------------------------------
 # restoring beam
 # ----------------------------------------------------------------------------

@@ -2,6 +2,8 @@
 //
 // Every entry point catches internal errors and turns them into the
 // reference shims' convention: an int status and a heap message in *err.
+#include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -1071,6 +1073,253 @@ int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable) {
     ctx->cube_graphs_enabled = enable != 0;
     if (!enable) ctx->cube_graphs.clear();
     return CR_OK;
+}
+
+// ---- persistent cube plans --------------------------------------------------
+
+int cr_cube_plan_create(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, cr_cube_plan** out, cr_sums* sums,
+                        char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr && out != nullptr, "null argument");
+        *out = nullptr;
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        CubeInput in = cube_input(ctx, batch);
+        cr_cube_plan* p = new cr_cube_plan();
+        p->ctx = ctx;
+        p->g = g;
+        try {
+            p->rec = cube_plan(ctx, g, in, weighting, robust, nullptr, &p->pool);
+            tm.mark();
+            p->sums.resize((size_t)in.C);
+            cube_read_sums(ctx, p->rec, p->sums.data());
+        } catch (...) {
+            cr_cube_plan_destroy(p);
+            throw;
+        }
+        int64_t n = 0;
+        for (const cr_sums& s : p->sums) n += s.gridded;
+        p->rec.n_records = n;
+        if (sums) std::copy(p->sums.begin(), p->sums.end(), sums);
+        set_timings(ctx, cr_timings{tm.between(0, 1), 0.f, 0.f, 0.f, 0.f});
+        *out = p;
+    });
+}
+
+void cr_cube_plan_destroy(cr_cube_plan* p) {
+    if (!p) return;
+    cudaSetDevice(p->ctx->device);
+    pool_free(p->ctx, p->pool);
+    cudaStreamSynchronize(p->ctx->stream);
+    delete p;
+}
+
+int32_t cr_cube_plan_channels(const cr_cube_plan* p) { return p ? p->rec.C : 0; }
+
+namespace {
+
+void check_cube_plan(cr_ctx* ctx, cr_cube_plan* p) {
+    need(ctx != nullptr && p != nullptr && p->ctx == ctx, "plan belongs to another context");
+}
+
+// A host plane mask [C] on the device (NULL: every plane), and the planes it
+// selects.
+const uint8_t* cube_mask(cr_ctx* ctx, const cr_cube_plan* p, const uint8_t* planes,
+                         std::vector<int>* chosen) {
+    const int C = p->rec.C;
+    chosen->clear();
+    for (int c = 0; c < C; ++c)
+        if (!planes || planes[c]) chosen->push_back(c);
+    if (!planes) return nullptr;
+    uint8_t* d = (uint8_t*)workspace(ctx, "cube_mask", (size_t)C);
+    CR_CUDA_CHECK(cudaMemcpyAsync(d, planes, (size_t)C, cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));   // pageable source
+    return d;
+}
+
+}  // namespace
+
+int cr_cube_plan_grid_dirty(cr_ctx* ctx, cr_cube_plan* p, float* psf_grids, float* dirty_grids,
+                            int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        check_cube_plan(ctx, p);
+        need(psf_grids != nullptr && dirty_grids != nullptr, "null argument");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        const size_t cells = grid_bytes(p->g) / 8, C = (size_t)p->rec.C;
+        float* psf = out_ptr<float>(ctx, psf_grids, out_location, C * cells * 4, "cube_psf");
+        float2* dirty = out_ptr<float2>(ctx, dirty_grids, out_location, C * cells * 8,
+                                        "cube_dirty");
+        cube_grid(ctx, p->g, p->rec, psf, dirty);
+        tm.mark();
+        if (out_location == CR_HOST) {
+            copy_out(ctx, psf_grids, psf, C * cells * 4, CR_HOST);
+            copy_out(ctx, dirty_grids, dirty, C * cells * 8, CR_HOST);
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f});
+    });
+}
+
+int cr_cube_plan_degrid(cr_ctx* ctx, cr_cube_plan* p, const float* model_grids,
+                        int32_t grid_location, float* pred, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        check_cube_plan(ctx, p);
+        need(model_grids != nullptr && pred != nullptr, "null argument");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        const size_t cells = grid_bytes(p->g) / 8, C = (size_t)p->rec.C;
+        const float2* mg = (const float2*)device_input(ctx, model_grids, C * cells * 8,
+                                                       grid_location, "cube_model");
+        float2* pr = out_ptr<float2>(ctx, pred, out_location, C * (size_t)p->rec.R * 8 + 8,
+                                     "cube_pred");
+        cube_degrid(ctx, p->g, p->rec, mg, pr);
+        tm.mark();
+        if (out_location == CR_HOST) copy_out(ctx, pred, pr, C * (size_t)p->rec.R * 8, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, 0.f, tm.between(0, 1), 0.f, 0.f});
+    });
+}
+
+int cr_cube_plan_grid_residual(cr_ctx* ctx, cr_cube_plan* p, const float* model_grids,
+                               int32_t grid_location, const uint8_t* planes,
+                               float* residual_grids, int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        check_cube_plan(ctx, p);
+        need(model_grids != nullptr && residual_grids != nullptr, "null argument");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        const size_t cells = grid_bytes(p->g) / 8, C = (size_t)p->rec.C;
+        std::vector<int> chosen;
+        const uint8_t* mask = cube_mask(ctx, p, planes, &chosen);
+        const float2* mg = (const float2*)device_input(ctx, model_grids, C * cells * 8,
+                                                       grid_location, "cube_model");
+        float2* res = out_ptr<float2>(ctx, residual_grids, out_location, C * cells * 8,
+                                      "cube_residual");
+        cube_grid_residual(ctx, p->g, p->rec, mg, res, mask);
+        tm.mark();
+        if (out_location == CR_HOST)
+            for (int c : chosen)
+                copy_out(ctx, (float2*)residual_grids + (size_t)c * cells, res + (size_t)c * cells,
+                         cells * 8, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f});
+    });
+}
+
+int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
+                              float* residual_images, int32_t out_location,
+                              cr_psf_state* states, char** err) {
+    return guarded(err, [&] {
+        check_cube_plan(ctx, p);
+        need(psf_images != nullptr && residual_images != nullptr, "null argument");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        cr_gridder* g = p->g;
+        const size_t cells = grid_bytes(g) / 8, C = (size_t)p->rec.C, np = image_pixels(g);
+        float* psf = (float*)workspace(ctx, "cpi_psf", C * cells * 4);
+        float2* dirty = (float2*)workspace(ctx, "cpi_dirty", C * cells * 8);
+        cube_grid(ctx, g, p->rec, psf, dirty);
+        tm.mark();
+        float* pi = out_ptr<float>(ctx, psf_images, out_location, C * np * 4, "cpi_psf_img");
+        float* ri = out_ptr<float>(ctx, residual_images, out_location, C * np * 4, "cpi_res_img");
+        unsigned int* peaks = (unsigned int*)workspace(ctx, "cpi_peaks", C * 4);
+        CR_CUDA_CHECK(cudaMemsetAsync(peaks, 0, C * 4, ctx->stream));
+        std::vector<float> sumwt(C);
+        for (size_t c = 0; c < C; ++c) {
+            sumwt[c] = (float)p->sums[c].normalization_sumwt;
+            float* pc = pi + c * np;
+            float* rc = ri + c * np;
+            if (!(p->sums[c].normalization_sumwt > 0.0 && p->sums[c].reported_sumwt > 0.0)) {
+                CR_CUDA_CHECK(cudaMemsetAsync(pc, 0, np * 4, ctx->stream));
+                CR_CUDA_CHECK(cudaMemsetAsync(rc, 0, np * 4, ctx->stream));
+                continue;
+            }
+            // the normalisation of dirty_grids_to_psf_and_residual_owned,
+            // as the single-plane cr_dirty_image
+            grid_to_image_real(ctx, g, psf + c * cells, 1.0f / sumwt[c], pc);
+            abs_peak(ctx, pc, (int64_t)np, peaks + c);
+            scale_image(ctx, pc, (int64_t)np, 1.0f, peaks + c);
+            grid_to_image(ctx, g, nullptr, dirty + c * cells, 1.0f / sumwt[c], rc);
+            scale_image(ctx, rc, (int64_t)np, 1.0f, peaks + c);
+        }
+        tm.mark();
+        std::vector<unsigned int> pk(C);
+        CR_CUDA_CHECK(cudaMemcpyAsync(pk.data(), peaks, C * 4, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        for (size_t c = 0; c < C; ++c) {
+            float peak;
+            std::memcpy(&peak, &pk[c], 4);
+            const bool ok = p->sums[c].normalization_sumwt > 0.0 &&
+                            p->sums[c].reported_sumwt > 0.0 && std::isfinite(peak) &&
+                            peak > 0.0f;
+            if (!ok) {
+                // a plane with no usable samples or a zero PSF: empty images
+                CR_CUDA_CHECK(cudaMemsetAsync(pi + c * np, 0, np * 4, ctx->stream));
+                CR_CUDA_CHECK(cudaMemsetAsync(ri + c * np, 0, np * 4, ctx->stream));
+            }
+            if (states)
+                states[c] = ok ? cr_psf_state{peak, sumwt[c], (float)p->sums[c].reported_sumwt}
+                               : cr_psf_state{0.0f, 0.0f, 0.0f};
+        }
+        if (out_location == CR_HOST) {
+            copy_out(ctx, psf_images, pi, C * np * 4, CR_HOST);
+            copy_out(ctx, residual_images, ri, C * np * 4, CR_HOST);
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, tm.between(1, 2), 0.f});
+    });
+}
+
+int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* models,
+                                 int32_t model_location, const uint8_t* planes,
+                                 const cr_psf_state* states, float* residual_images,
+                                 int32_t out_location, char** err) {
+    return guarded(err, [&] {
+        check_cube_plan(ctx, p);
+        need(models != nullptr && states != nullptr && residual_images != nullptr,
+             "null argument");
+        bind(ctx);
+        cr_gridder* g = p->g;
+        const size_t cells = grid_bytes(g) / 8, C = (size_t)p->rec.C, np = image_pixels(g);
+        std::vector<int> chosen;
+        for (size_t c = 0; c < C; ++c)
+            if (!planes || planes[c])
+                need(states[c].normalization_sumwt > 0.0f && states[c].psf_peak > 0.0f,
+                     "invalid PSF state for a selected plane");
+        StageTimer tm(ctx);
+        tm.mark();
+        const uint8_t* mask = cube_mask(ctx, p, planes, &chosen);
+        const float* m = (const float*)device_input(ctx, models, C * np * 4, model_location,
+                                                    "cube_models");
+        float2* mg = (float2*)workspace(ctx, "cpr_model_grids", C * cells * 8);
+        for (int c : chosen) image_to_grid(ctx, g, nullptr, m + (size_t)c * np, mg + c * cells);
+        tm.mark();
+        float2* res = (float2*)workspace(ctx, "cpr_residual_grids", C * cells * 8);
+        cube_grid_residual(ctx, g, p->rec, mg, res, mask);
+        tm.mark();
+        float* img = out_ptr<float>(ctx, residual_images, out_location, C * np * 4, "cpr_image");
+        for (int c : chosen) {
+            grid_to_image(ctx, g, nullptr, res + (size_t)c * cells,
+                          1.0f / states[c].normalization_sumwt, img + (size_t)c * np);
+            scale_image(ctx, img + (size_t)c * np, (int64_t)np, 1.0f / states[c].psf_peak,
+                        nullptr);
+            if (out_location == CR_HOST)
+                copy_out(ctx, residual_images + (size_t)c * np, img + (size_t)c * np, np * 4,
+                         CR_HOST);
+        }
+        tm.mark();
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, tm.between(1, 2), 0.f,
+                                  tm.between(0, 1) + tm.between(2, 3), 0.f});
+    });
 }
 
 }  // extern "C"

@@ -529,12 +529,18 @@ __device__ __forceinline__ void source_ranges(const uint32_t* bin_start,
     }
 }
 
+// Channels whose plane_mask entry is 0 get no work items.
 __global__ void cube_work_count(const uint32_t* bin_start, const uint32_t* cell_end,
                                 int64_t nbins, int64_t ntiles, int64_t nty, uint32_t grid_chunk,
-                                uint32_t* grid_chunks, uint32_t* degrid_chunks) {
+                                const uint8_t* plane_mask, uint32_t* grid_chunks,
+                                uint32_t* degrid_chunks) {
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbins;
          b += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = b / ntiles, T = b % ntiles;
+        if (plane_mask && !plane_mask[c]) {
+            grid_chunks[b] = degrid_chunks[b] = 0u;
+            continue;
+        }
         uint32_t lo[4], hi[4];
         source_ranges(bin_start, cell_end, c, ntiles, nty, T / nty, T % nty, lo, hi);
         const uint32_t n = (hi[0] - lo[0]) + (hi[1] - lo[1]) + (hi[2] - lo[2]) + (hi[3] - lo[3]);
@@ -554,14 +560,14 @@ __global__ void cube_work_fill(const uint32_t* grid_chunks, const uint32_t* grid
         for (uint32_t k = 0; k < n; ++k) grid_items[f + k] = make_uint2((uint32_t)b, k);
         const uint32_t nd = degrid_chunks[b], fd = degrid_first[b];
         for (uint32_t k = 0; k < nd; ++k) degrid_items[fd + k] = make_uint2((uint32_t)b, k);
-        if (n > 1 && psf) {
+        if (n > 1 && dirty) {
             const int64_t c = b / ntiles, T = b % ntiles;
             const int64_t x0 = (T / nty) * kTile, y0 = (T % nty) * kTile;
-            float* pc = psf + c * gnx * gny;
+            float* pc = psf ? psf + c * gnx * gny : nullptr;
             float2* dc = dirty + c * gnx * gny;
             for (int64_t x = x0; x < min(x0 + kTile, gnx); ++x)
                 for (int64_t y = y0; y < min(y0 + kTile, gny); ++y) {
-                    pc[x * gny + y] = 0.0f;
+                    if (pc) pc[x * gny + y] = 0.0f;
                     dc[x * gny + y] = make_float2(0.0f, 0.0f);
                 }
         }
@@ -582,7 +588,8 @@ struct CubeGridArgs {
     const unsigned long long* n_items;
     unsigned int* item_counter;
     float* psf;                  // [C][gnx][gny] real part of the PSF grid
-    float2* dirty;               // [C][gnx][gny]
+    float2* dirty;               // [C][gnx][gny] (the residual grid with RESIDUAL)
+    const float2* res;           // RESIDUAL: w (vis - pred) per record
 };
 
 // A block per work item: the chunk's records (from the four source bins)
@@ -595,6 +602,9 @@ struct CubeGridArgs {
 // not hide the dependent shared-memory chain of consecutive records.)
 constexpr int kGridThreads = kCubeThreads;
 
+// With RESIDUAL the records carry w (vis - pred) from `res` and no PSF is
+// formed.
+template <bool RESIDUAL>
 __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a) {
     __shared__ float s_psf[kTile * kRow];
     __shared__ float s_re[kTile * kRow];
@@ -635,14 +645,14 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
             off += n;
         }
         const int64_t gx0 = tx * kTile, gy0 = ty * kTile;
-        float* psf_c = a.psf + c * a.gnx * a.gny;
+        float* psf_c = RESIDUAL ? nullptr : a.psf + c * a.gnx * a.gny;
         float2* dirty_c = a.dirty + c * a.gnx * a.gny;
         if (nsrc == 0) {
             if (!shared_tile)
                 for (int k = tid; k < kTile * kTile; k += kGridThreads) {
                     const int64_t x = gx0 + k / kTile, y = gy0 + k % kTile;
                     if (x < a.gnx && y < a.gny) {
-                        psf_c[x * a.gny + y] = 0.0f;
+                        if (!RESIDUAL) psf_c[x * a.gny + y] = 0.0f;
                         dirty_c[x * a.gny + y] = make_float2(0.0f, 0.0f);
                     }
                 }
@@ -668,7 +678,7 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
             int cx = cur_lx + ix0, cy = cur_ly + iy0;
             if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
                 const int cell = cx * kRow + cy;
-                atomicAdd(&s_psf[cell], p0);
+                if (!RESIDUAL) atomicAdd(&s_psf[cell], p0);
                 atomicAdd(&s_re[cell], r0);
                 atomicAdd(&s_im[cell], i0);
             }
@@ -676,7 +686,7 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
             cy = cur_ly + iy1;
             if (has1 && cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
                 const int cell = cx * kRow + cy;
-                atomicAdd(&s_psf[cell], p1);
+                if (!RESIDUAL) atomicAdd(&s_psf[cell], p1);
                 atomicAdd(&s_re[cell], r1);
                 atomicAdd(&s_im[cell], i1);
             }
@@ -691,7 +701,13 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
                 bool rel = false;
                 if (rr < b1[s]) {
                     q = a.rec[rr];
-                    qw = a.rec_w[rr];
+                    if (RESIDUAL) {
+                        const float2 rv = a.res[rr];
+                        q.z = __float_as_uint(rv.x);
+                        q.w = __float_as_uint(rv.y);
+                    } else {
+                        qw = a.rec_w[rr];
+                    }
                     const int lx = sox + (int)(q.x >> 27), ly = soy + (int)((q.x >> 22) & 31);
                     rel = lx + 6 >= 0 && ly + 6 >= 0;
                 }
@@ -714,12 +730,12 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
                     const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
                     const float* wy = s_taps + (meta & 2047u) * 7;
                     const float w0 = __fmul_rn(wx[ix0], wy[iy0]);
-                    p0 = fmaf(pw, w0, p0);
+                    if (!RESIDUAL) p0 = fmaf(pw, w0, p0);
                     r0 = fmaf(vr, w0, r0);
                     i0 = fmaf(vi, w0, i0);
                     if (has1) {
                         const float w1 = __fmul_rn(wx[ix1], wy[iy1]);
-                        p1 = fmaf(pw, w1, p1);
+                        if (!RESIDUAL) p1 = fmaf(pw, w1, p1);
                         r1 = fmaf(vr, w1, r1);
                         i1 = fmaf(vi, w1, i1);
                     }
@@ -734,10 +750,11 @@ __global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a)
             if (x < a.gnx && y < a.gny) {
                 const int cell = cx * kRow + cy;
                 if (!shared_tile) {
-                    psf_c[x * a.gny + y] = s_psf[cell];
+                    if (!RESIDUAL) psf_c[x * a.gny + y] = s_psf[cell];
                     dirty_c[x * a.gny + y] = make_float2(s_re[cell], s_im[cell]);
                 } else {
-                    if (s_psf[cell] != 0.0f) atomicAdd(&psf_c[x * a.gny + y], s_psf[cell]);
+                    if (!RESIDUAL && s_psf[cell] != 0.0f)
+                        atomicAdd(&psf_c[x * a.gny + y], s_psf[cell]);
                     if (s_re[cell] != 0.0f || s_im[cell] != 0.0f)
                         atomicAdd(&dirty_c[x * a.gny + y], make_float2(s_re[cell], s_im[cell]));
                 }
@@ -758,12 +775,17 @@ struct CubeDegridArgs {
     const float* taps;
     const float2* grid;          // [C][gnx][gny]
     float2* pred;                // [C][R]
+    const float* rec_w;          // RESIDUAL: imaging weight per record
+    float2* res;                 // RESIDUAL: w vis - w pred per record
 };
 
 // Bins in turn.  The block stages the 38 x 38 model footprint of its home
 // tile in shared memory; a warp takes 4 records at a time, 7 lanes per
 // record, lane ix forming wx[ix] * sum_iy wy[iy] g[x0 + ix][y0 + iy]
 // (float32), and the 7 lanes' sums are reduced with shuffles.
+// With RESIDUAL each record's w vis - w pred goes to res (record order)
+// instead of pred (sample order).
+template <bool RESIDUAL>
 __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArgs a) {
     constexpr int kFoot = kTile + 6;
     __shared__ float s_re[kFoot * kRow];
@@ -799,8 +821,9 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
             const uint32_t k = base + sub;
             float re = 0.0f, im = 0.0f;
             uint32_t sample = 0;
+            uint4 q = make_uint4(0u, 0u, 0u, 0u);
             if (k < hi) {
-                const uint4 q = a.rec[k];
+                q = a.rec[k];
                 sample = q.y;
                 if (ix < 7) {
                     const uint32_t meta = q.x;
@@ -820,7 +843,15 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
                 re += __shfl_xor_sync(0xffffffffu, re, o);
                 im += __shfl_xor_sync(0xffffffffu, im, o);
             }
-            if (ix == 0 && k < hi) a.pred[sample] = make_float2(re, im);
+            if (ix == 0 && k < hi) {
+                if (RESIDUAL) {
+                    const float w = a.rec_w[k];
+                    a.res[k] = make_float2(__fsub_rn(__uint_as_float(q.z), __fmul_rn(w, re)),
+                                           __fsub_rn(__uint_as_float(q.w), __fmul_rn(w, im)));
+                } else {
+                    a.pred[sample] = make_float2(re, im);
+                }
+            }
         }
         __syncthreads();
     }
@@ -882,7 +913,12 @@ void cube_upload_channels(cr_ctx* ctx, cr_gridder* g, const CubeInput& in) {
 }
 
 CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
-                      float robust, const CubeTaps* taps) {
+                      float robust, const CubeTaps* taps, Pool* keep) {
+    // buffers the records and work lists live in: the plan's own pool when
+    // given (a persistent plan), else the context's workspaces
+    auto kept = [&](const char* name, size_t bytes) {
+        return keep ? pool_alloc(ctx, *keep, name, bytes) : workspace(ctx, name, bytes);
+    };
     if (mode != CR_WEIGHT_NATURAL && mode != CR_WEIGHT_UNIFORM && mode != CR_WEIGHT_BRIGGS)
         fail(CR_INVALID, "unknown weighting mode");
     if (in.C <= 0 || in.C > 65535) fail(CR_INVALID, "channels must lie in [1, 65535]");
@@ -904,14 +940,14 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     const double dvs = (double)g->geom.ny * g->geom.cell_y_rad;
     if (!ctx->capturing) cube_upload_channels(ctx, g, in);
     CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", (size_t)in.C * sizeof(CubeChan));
-    cr.rec = (uint4*)workspace(ctx, "cube_rec", ns * 16);
-    cr.rec_w = (float*)workspace(ctx, "cube_rec_w", ns * 4);
-    cr.bin_start = (uint32_t*)workspace(ctx, "cube_bin_start", (size_t)(nbins + 1) * 4);
+    cr.rec = (uint4*)kept("cube_rec", ns * 16);
+    cr.rec_w = (float*)kept("cube_rec_w", ns * 4);
+    cr.bin_start = (uint32_t*)kept("cube_bin_start", (size_t)(nbins + 1) * 4);
     const int64_t ncells = (nbins << 10) + 1;   // (channel, tile, cell) bins + total
     if (ncells >= (1ll << 32)) fail(CR_INVALID, "cube has too many (channel, tile, cell) bins");
-    uint32_t* hist = (uint32_t*)workspace(ctx, "cube_hist", (size_t)ncells * 4);
-    cr.sumwt = (double*)workspace(ctx, "cube_sumwt", (size_t)in.C * 8);
-    cr.counts = (unsigned long long*)workspace(ctx, "cube_counts", (size_t)in.C * 16 + 8);
+    uint32_t* hist = (uint32_t*)kept("cube_hist", (size_t)ncells * 4);
+    cr.sumwt = (double*)kept("cube_sumwt", (size_t)in.C * 8);
+    cr.counts = (unsigned long long*)kept("cube_counts", (size_t)in.C * 16 + 8);
     cr.n_rec = cr.counts + 2 * in.C;
     CR_CUDA_CHECK(cudaMemsetAsync(hist, 0, (size_t)ncells * 4, ctx->stream));
     CR_CUDA_CHECK(cudaMemsetAsync(cr.sumwt, 0, (size_t)in.C * 8, ctx->stream));
@@ -999,29 +1035,29 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
         note_launch(ctx, "cube_scatter_kernel");
     }
     // work-list buffers (the lists are made by cube_grid / cube_degrid)
-    cr.grid_chunks = (uint32_t*)workspace(ctx, "cube_gchunks", (size_t)nbins * 4);
-    cr.degrid_chunks = (uint32_t*)workspace(ctx, "cube_dchunks", (size_t)nbins * 4);
+    cr.grid_chunks = (uint32_t*)kept("cube_gchunks", (size_t)nbins * 4);
+    cr.degrid_chunks = (uint32_t*)kept("cube_dchunks", (size_t)nbins * 4);
     cr.cell_end = hist;
-    cr.grid_first = (uint32_t*)workspace(ctx, "cube_gfirst", (size_t)nbins * 4);
-    cr.degrid_first = (uint32_t*)workspace(ctx, "cube_dfirst", (size_t)nbins * 4);
-    cr.n_items = (unsigned long long*)workspace(ctx, "cube_nitems", 16);
+    cr.grid_first = (uint32_t*)kept("cube_gfirst", (size_t)nbins * 4);
+    cr.degrid_first = (uint32_t*)kept("cube_dfirst", (size_t)nbins * 4);
+    cr.n_items = (unsigned long long*)kept("cube_nitems", 16);
     // sum over tiles of ceil(n / K) <= tiles + (sum n) / K, and each record is a
     // source of at most four output tiles
     const size_t max_grid_items = (size_t)nbins + 4 * ns / kGridChunkMin + 1;
     const size_t max_degrid_items = (size_t)nbins + ns / kDegridChunk + 1;
-    cr.grid_items = (uint2*)workspace(ctx, "cube_gitems", max_grid_items * 8);
-    cr.degrid_items = (uint2*)workspace(ctx, "cube_ditems", max_degrid_items * 8);
+    cr.grid_items = (uint2*)kept("cube_gitems", max_grid_items * 8);
+    cr.degrid_items = (uint2*)kept("cube_ditems", max_degrid_items * 8);
     return cr;
 }
 
 // Work lists for one gridding chunk size; with psf/dirty, heavy output tiles
 // are zeroed for their atomic chunks.
 static void make_work_lists(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, uint32_t chunk,
-                            float* psf, float2* dirty) {
+                            float* psf, float2* dirty, const uint8_t* plane_mask = nullptr) {
     const cr_grid_info& gi = g->info;
     const int64_t nbins = (int64_t)cr.C * cr.ntiles;
     cube_work_count<<<grid_blocks(nbins, 256), 256, 0, ctx->stream>>>(
-        cr.bin_start, cr.cell_end, nbins, cr.ntiles, cr.nty, chunk, cr.grid_chunks,
+        cr.bin_start, cr.cell_end, nbins, cr.ntiles, cr.nty, chunk, plane_mask, cr.grid_chunks,
         cr.degrid_chunks);
     note_launch(ctx, "cube_work_count");
     exclusive_scan_u32(ctx, cr.grid_chunks, cr.grid_first, nbins, cr.n_items);
@@ -1032,28 +1068,34 @@ static void make_work_lists(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, uint32_
     note_launch(ctx, "cube_work_fill");
     cr.grid_chunk = chunk;
     cr.fill_done = true;
+    cr.lists_masked = plane_mask != nullptr;
 }
 
+template <bool RESIDUAL>
 static void launch_cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, float* psf,
-                             float2* dirty) {
+                             float2* dirty, const float2* res = nullptr) {
     const cr_grid_info& gi = g->info;
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
     CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows, cr.ntx,
                    cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunk, cr.grid_chunks,
-                   cr.n_items, counter, psf, dirty};
+                   cr.n_items, counter, psf, dirty, res};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int per_sm = 0;
-    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_grid_kernel,
-                                                                kGridThreads, 0));
-    cube_grid_kernel<<<sms * std::max(per_sm, 1), kGridThreads, 0, ctx->stream>>>(a);
-    note_launch(ctx, "cube_grid_kernel");
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, cube_grid_kernel<RESIDUAL>, kGridThreads, 0));
+    cube_grid_kernel<RESIDUAL><<<sms * std::max(per_sm, 1), kGridThreads, 0, ctx->stream>>>(a);
+    note_launch(ctx, RESIDUAL ? "cube_grid_kernel_residual" : "cube_grid_kernel");
+}
+
+static std::string cube_shape_key(const cr_gridder* g, const CubeRecords& cr) {
+    return std::to_string(cr.C) + "x" + std::to_string(cr.ntx) + "x" + std::to_string(cr.nty) +
+           "/" + std::to_string(g->info.oversampling);
 }
 
 void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty) {
-    const std::string key = std::to_string(cr.C) + "x" + std::to_string(cr.ntx) + "x" +
-                            std::to_string(cr.nty) + "/" + std::to_string(g->info.oversampling);
+    const std::string key = cube_shape_key(g, cr);
     auto tuned = ctx->cube_chunk.find(key);
     if (tuned == ctx->cube_chunk.end() && !ctx->capturing) {
         // first use of this cube shape: time the gridding pass (work lists
@@ -1064,7 +1106,7 @@ void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* 
         for (uint32_t chunk : kGridChunkCandidates) {
             CR_CUDA_CHECK(cudaEventRecord(e0, ctx->stream));
             make_work_lists(ctx, g, cr, chunk, psf, dirty);
-            launch_cube_grid(ctx, g, cr, psf, dirty);
+            launch_cube_grid<false>(ctx, g, cr, psf, dirty);
             CR_CUDA_CHECK(cudaEventRecord(e1, ctx->stream));
             CR_CUDA_CHECK(cudaEventSynchronize(e1));
             float ms = 0.0f;
@@ -1080,26 +1122,51 @@ void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* 
     const uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
     make_work_lists(ctx, g, cr, chunk, psf, dirty);
     kernel_mark(ctx, 0, false);
-    launch_cube_grid(ctx, g, cr, psf, dirty);
+    launch_cube_grid<false>(ctx, g, cr, psf, dirty);
+    kernel_mark(ctx, 0, true);
+}
+
+template <bool RESIDUAL>
+static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr,
+                               const float2* grid, float2* pred, float2* res) {
+    const cr_grid_info& gi = g->info;
+    unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
+    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
+    CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
+                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d, grid,
+                     pred, cr.rec_w, res};
+    int sms = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    cube_degrid_kernel<RESIDUAL><<<sms * 8, kCubeThreads, 0, ctx->stream>>>(a);
+    note_launch(ctx, RESIDUAL ? "cube_degrid_kernel_residual" : "cube_degrid_kernel");
+}
+
+void cube_grid_residual(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* model,
+                        float2* residual, const uint8_t* plane_mask) {
+    auto tuned = ctx->cube_chunk.find(cube_shape_key(g, cr));
+    const uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    // the lists skip masked planes and zero the heavy tiles of the others
+    make_work_lists(ctx, g, cr, chunk, nullptr, residual, plane_mask);
+    const size_t nrec = cr.n_records >= 0 ? (size_t)std::max<int64_t>(cr.n_records, 1)
+                                          : (size_t)std::max<int64_t>((int64_t)cr.C * cr.R, 1);
+    float2* res = (float2*)workspace(ctx, "cube_res", nrec * 8);
+    kernel_mark(ctx, 1, false);
+    launch_cube_degrid<true>(ctx, g, cr, model, nullptr, res);
+    kernel_mark(ctx, 1, true);
+    kernel_mark(ctx, 0, false);
+    launch_cube_grid<true>(ctx, g, cr, nullptr, residual, res);
     kernel_mark(ctx, 0, true);
 }
 
 void cube_degrid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* grid,
                  float2* pred) {
-    const cr_grid_info& gi = g->info;
     CR_CUDA_CHECK(cudaMemsetAsync(pred, 0, (size_t)cr.C * cr.R * 8, ctx->stream));
     // the degridding work list without a gridding pass before it
-    if (!cr.fill_done) make_work_lists(ctx, g, cr, kGridChunkDefault, nullptr, nullptr);
-    unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
-    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
-                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d, grid,
-                     pred};
-    int sms = 0;
-    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    if (!cr.fill_done || cr.lists_masked)
+        make_work_lists(ctx, g, cr, cr.fill_done ? cr.grid_chunk : kGridChunkDefault, nullptr,
+                        nullptr);
     kernel_mark(ctx, 1, false);
-    cube_degrid_kernel<<<sms * 8, kCubeThreads, 0, ctx->stream>>>(a);
-    note_launch(ctx, "cube_degrid_kernel");
+    launch_cube_degrid<false>(ctx, g, cr, grid, pred, nullptr);
     kernel_mark(ctx, 1, true);
 }
 

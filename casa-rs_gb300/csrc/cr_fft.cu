@@ -28,6 +28,18 @@ __global__ void widen_checker_kernel(const float2* g, int64_t gnx, int64_t gny, 
     }
 }
 
+// The real part alone (a PSF grid kept as float32).
+__global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t gny,
+                                          double2* out) {
+    const int64_t n = gnx * gny;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t x = t / gny, y = t - x * gny;
+        double s = ((x + y) & 1) ? -1.0 : 1.0;
+        out[t] = make_double2(s * (double)g[t], 0.0);
+    }
+}
+
 // image(x, y) = Re(raw[blc + (x, y)]) * sign * scale * corr_x * corr_y.
 // sinc_mode 1 (W-projection image correction) further divides by
 // sinc_x * sinc_y with the reference's 1e-6 guard; sinc_mode 2 multiplies by
@@ -113,12 +125,20 @@ __global__ void scale_image_kernel(float* img, int64_t n, float scale, const uns
 }  // namespace
 
 static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float2* grid,
-                               float scale, float* image, bool adjoint) {
+                               float scale, float* image, bool adjoint,
+                               const float* real_grid = nullptr) {
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
     double2* work = (double2*)workspace(ctx, "fft_z", (size_t)gnx * gny * 16);
-    widen_checker_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(grid, gnx, gny, work);
-    note_launch(ctx, "widen_checker_kernel");
+    if (real_grid) {
+        widen_checker_real_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
+            real_grid, gnx, gny, work);
+        note_launch(ctx, "widen_checker_real_kernel");
+    } else {
+        widen_checker_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(grid, gnx,
+                                                                                  gny, work);
+        note_launch(ctx, "widen_checker_kernel");
+    }
     cufftHandle plan = fft_plan(ctx, gnx, gny);
     check_cufft(cufftExecZ2Z(plan, (cufftDoubleComplex*)work, (cufftDoubleComplex*)work, CUFFT_INVERSE),
                 "cufftExecZ2Z");
@@ -142,6 +162,11 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
 void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                    float* image) {
     grid_to_image_impl(ctx, g, wp, grid, scale, image, false);
+}
+
+void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float scale,
+                        float* image) {
+    grid_to_image_impl(ctx, g, nullptr, nullptr, scale, image, false, grid);
 }
 
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,

@@ -199,6 +199,9 @@ void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* gri
                            float* image);
 // model image (device) -> centred model grid (device)
 void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid);
+// grid_to_image of a real grid (the real part of a PSF grid), standard gridder
+void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float scale,
+                        float* image);
 // max |image| into *peak_dev (float bits as uint32)
 void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev);
 // image *= scale, then / *peak_dev when peak_dev != null
@@ -236,6 +239,8 @@ struct CubeRecords {
     unsigned long long* n_items = nullptr;   // [0] gridding, [1] degridding
     uint32_t grid_chunk = 0;                 // records per gridding work item
     bool fill_done = false;                  // set once the work lists are made
+    bool lists_masked = false;               // the lists skip some planes
+    int64_t n_records = -1;                  // total records, when read back
 };
 // Per-sample outputs of cube_sample_taps ([C][R], -1 / 0 when not gridded).
 struct CubeTaps {
@@ -244,12 +249,17 @@ struct CubeTaps {
 };
 // With `taps`, only the weighting and the per-sample plan run.
 CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t mode,
-                      float robust, const CubeTaps* taps = nullptr);
+                      float robust, const CubeTaps* taps = nullptr, Pool* keep = nullptr);
 // psf [C][gnx][gny] float32 (real part), dirty [C][gnx][gny] complex64
 void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty);
 // pred [C][R] complex64, zero for samples that are not gridded
 void cube_degrid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* grid,
                  float2* pred);
+// Residual grids of every plane with plane_mask[c] != 0 (device, NULL = all):
+// degrid the model grids per record, w vis - w pred, grid that; the psf is
+// not formed.  Other planes' grids are left as they are.
+void cube_grid_residual(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* model,
+                        float2* residual, const uint8_t* plane_mask);
 void cube_read_sums(cr_ctx* ctx, const CubeRecords& cr, cr_sums* out);
 // Host-side constants of the cube plan, uploaded outside any graph capture.
 void cube_upload_channels(cr_ctx* ctx, cr_gridder* g, const CubeInput& in);
@@ -300,6 +310,14 @@ inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) 
 // A materialised plan of one batch (the device form of the reference's
 // planned taps): its records outlive the call that made them, in the plan's
 // own pool, and serve any number of gridding and degridding calls.
+struct cr_cube_plan {
+    cr_ctx* ctx = nullptr;
+    cr_gridder* g = nullptr;
+    cr::Pool pool;
+    cr::CubeRecords rec;
+    std::vector<cr_sums> sums;
+};
+
 struct cr_plan {
     cr_ctx* ctx = nullptr;
     cr_gridder* g = nullptr;

@@ -59,6 +59,7 @@ typedef struct cr_ctx cr_ctx;
 typedef struct cr_gridder cr_gridder;
 typedef struct cr_wproj cr_wproj;
 typedef struct cr_plan cr_plan;
+typedef struct cr_cube_plan cr_cube_plan;
 
 /* ImageGeometry (types.rs:885-930). */
 typedef struct {
@@ -303,6 +304,45 @@ int cr_cube_sample_taps(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                         int32_t weighting, float robust, int32_t* start_x, int32_t* start_y,
                         int32_t* row_x, int32_t* row_y, float* imaging_weight,
                         int32_t out_location, char** err);
+
+/* ---- persistent cube plans -------------------------------------------------
+ * The cube's weighting and records made once (cr_cube_plan_create, the
+ * weighting and planning of cr_cube_grid_dirty) and reused by gridding,
+ * degridding and residual calls: the planned-sample replay that
+ * run_standard_mfs_cube_clean (casa-imaging lib.rs:3026-3210) drives once per
+ * plane and major cycle.  The plan copies what it needs (weighted
+ * visibilities in record order); the batch may be released afterwards.
+ * `sums` receives one cr_sums per channel.
+ *
+ * planes (host, [channels], NULL = all) selects the planes a residual call
+ * refreshes; the others' outputs are left as they are.  The image calls
+ * use the single-plane normalisation per channel (cr_dirty_image /
+ * cr_plan_residual_image); a plane without usable samples gets zero images
+ * and a zero cr_psf_state instead of an error. */
+int cr_cube_plan_create(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
+                        int32_t weighting, float robust, cr_cube_plan** out, cr_sums* sums,
+                        char** err);
+void cr_cube_plan_destroy(cr_cube_plan* plan);
+int32_t cr_cube_plan_channels(const cr_cube_plan* plan);
+int cr_cube_plan_grid_dirty(cr_ctx* ctx, cr_cube_plan* plan, float* psf_grids,
+                            float* dirty_grids, int32_t out_location, char** err);
+int cr_cube_plan_degrid(cr_ctx* ctx, cr_cube_plan* plan, const float* model_grids,
+                        int32_t grid_location, float* pred, int32_t out_location, char** err);
+/* Residual grids: degrid the model grids, (vis - pred) weighted, gridded. */
+int cr_cube_plan_grid_residual(cr_ctx* ctx, cr_cube_plan* plan, const float* model_grids,
+                               int32_t grid_location, const uint8_t* planes,
+                               float* residual_grids, int32_t out_location, char** err);
+/* Normalised PSF and residual images [channels][nx][ny] with each plane's
+ * PSF state. */
+int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* plan, float* psf_images,
+                              float* residual_images, int32_t out_location,
+                              cr_psf_state* states, char** err);
+/* Model images [channels][nx][ny] -> residual images of the selected
+ * planes (the major-cycle refresh of each plane). */
+int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* plan, const float* models,
+                                 int32_t model_location, const uint8_t* planes,
+                                 const cr_psf_state* states, float* residual_images,
+                                 int32_t out_location, char** err);
 
 /* ---- restoring beam ---------------------------------------------------------
  * fit_beam_from_psf (beam.rs:27-103): the main lobe above `cutoff` (clamped

@@ -583,14 +583,18 @@ _STOP_NAMES = {0: None, 1: "GlobalThresholdReached", 2: "CycleThresholdReached",
 
 def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000,
                   cyclefactor=1.0, min_psf_fraction=0.05, max_psf_fraction=0.8,
-                  major_cycle_limit=None, sidelobe=0.0, inclusive=True):
+                  major_cycle_limit=None, sidelobe=0.0, inclusive=True, model=None,
+                  cycle_threshold_override=None):
     """run_hogbom_cotton_schwab (lib.rs:59354-59636) without mask and n-sigma
     threshold.  `refresh(model) -> residual` is the measured major cycle.
-    Returns a dict with model, residual, major cycles, iterations, the stop
-    reason, the per-cycle thresholds and the component list."""
+    `model` continues from an earlier model; `cycle_threshold_override`
+    replaces the per-cycle threshold (the cube-wide threshold of
+    run_standard_mfs_cube_clean).  Returns a dict with model, residual,
+    major cycles, iterations, the stop reason, the per-cycle thresholds and
+    the component list."""
     f32 = np.float32
     res = np.array(residual, np.float32, copy=True)
-    model = np.zeros_like(res)
+    model = np.zeros_like(res) if model is None else np.array(model, np.float32, copy=True)
     actual = reported = major = 0
     stop = None
     min_peak = f32(np.max(np.abs(res)))
@@ -612,6 +616,8 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
         cyc_niter = min(niter - reported, minor_cycle_length)
         thr = clean_cycle_threshold(peak, sidelobe, cyclefactor, min_psf_fraction,
                                     max_psf_fraction, threshold)
+        if cycle_threshold_override is not None:
+            thr = float(cycle_threshold_override)
         thresholds.append(thr)
         out = hogbom(res, psf, gain, cyc_niter, threshold=threshold, cycle_threshold=thr,
                      model=model, inclusive=inclusive)
@@ -657,3 +663,84 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
         res = np.asarray(refresh(model), np.float32)
     return dict(model=model, residual=res, major_cycles=major, actual=actual, reported=reported,
                 stop_reason=stop, thresholds=thresholds, components=comps)
+
+
+def cube_clean(planes, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000, cyclefactor=1.0,
+               min_psf_fraction=0.05, max_psf_fraction=0.8, major_cycle_limit=None,
+               inclusive=True):
+    """run_standard_mfs_cube_clean (casa-imaging lib.rs:3026-3210) over
+    planes in ascending order.  Each plane is a dict with residual, psf,
+    refresh(model) -> residual and sidelobe (its PSF sidelobe level).  Per
+    synchronized pass every active plane (residual peak above the cube-wide
+    cycle threshold) runs one major cycle of its own controller
+    (run_standard_mfs_prepared_clean_plane_one_major_cycle, lib.rs:46465-46520:
+    niter = the remaining global budget, one major cycle, the cube threshold
+    as override).  Then the plane results of
+    complete_standard_mfs_prepared_clean_plane (lib.rs:46343-46460)."""
+    f32 = np.float32
+    n = len(planes)
+    res = [np.array(p["residual"], np.float32, copy=True) for p in planes]
+    model = [np.zeros_like(r) for r in res]
+    absmax = lambda a: f32(np.max(np.abs(a))) if a.size else f32(0)
+    finite_max = lambda vals: max([f32(v) for v in vals if np.isfinite(v)] + [f32(0)])
+    cyc = lambda peak, sl: clean_cycle_threshold(peak, sl, cyclefactor, min_psf_fraction,
+                                                 max_psf_fraction, threshold)
+    initial_peak = finite_max([absmax(r) for r in res])
+    max_sidelobe = finite_max([p["sidelobe"] for p in planes])
+    first_thr = cyc(initial_peak, max_sidelobe)
+    at_or_below = sum(1 for r in res if absmax(r) <= f32(first_thr))
+    plane_iters = [0] * n
+    plane_stop = [None] * n
+    comps = [[] for _ in range(n)]
+    completed = major = 0
+    thresholds, actives = [], []
+    while True:
+        peak = finite_max([absmax(r) for r in res])
+        thr = cyc(peak, max_sidelobe)
+        t = f32(threshold)
+        reached = peak <= t or (t > 0 and abs(peak - t) / t < f32(0.01))
+        if reached or completed >= niter:
+            break
+        if major_cycle_limit is not None and major >= major_cycle_limit:
+            break
+        active = [i for i in range(n) if absmax(res[i]) > f32(thr)]
+        if not active:
+            break
+        major += 1
+        cycle_niter = niter - completed
+        thresholds.append(thr)
+        actives.append(active)
+        pass_iters = 0
+        for i in active:
+            out = cotton_schwab(res[i], planes[i]["psf"], planes[i]["refresh"], cycle_niter,
+                                gain=gain, threshold=threshold,
+                                minor_cycle_length=minor_cycle_length, cyclefactor=cyclefactor,
+                                min_psf_fraction=min_psf_fraction,
+                                max_psf_fraction=max_psf_fraction, major_cycle_limit=1,
+                                sidelobe=max_sidelobe, inclusive=inclusive, model=model[i],
+                                cycle_threshold_override=thr)
+            model[i], res[i] = out["model"], out["residual"]
+            comps[i].extend(out["components"])
+            plane_iters[i] += out["reported"]
+            plane_stop[i] = out["stop_reason"]
+            pass_iters += out["reported"]
+        completed += pass_iters
+        if pass_iters == 0:
+            break
+    final_thr = cyc(finite_max([absmax(r) for r in res]), max_sidelobe)
+    stops = []
+    for i in range(n):
+        if plane_iters[i] >= niter:
+            stops.append("IterationLimitReached")
+            continue
+        s = tolerant_clean_stop_reason(absmax(res[i]), threshold, 0.0)
+        if s is None:
+            s = plane_stop[i]
+            if s in (None, "MajorCycleLimitReached"):
+                s = "CycleThresholdReached"
+        stops.append(s)
+    return dict(models=model, residuals=res, plane_iterations=plane_iters, plane_stops=stops,
+                components=comps, minor_iterations=completed, major_cycles=major,
+                thresholds=thresholds, active=actives, initial_peak=float(initial_peak),
+                max_sidelobe=float(max_sidelobe), final_cycle_threshold=final_thr,
+                planes_at_or_below_initial_threshold=at_or_below)
