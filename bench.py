@@ -275,6 +275,40 @@ def run_cube(args, ctx, dev, peak):
     ctx.set_cube_graphs(True)
     n_vis = sum(s.gridded_samples for s in last["sums"])
 
+    # a resident plan (the cube CLEAN's major cycle): weighting and records
+    # once, then per pass the batched residual refresh (degrid the model
+    # grids, grid w (vis - pred)) and the image stage around it
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    plan = cc.CubePlan(gg, cube, "briggs", 0.5)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_plan_create = ev0.elapsed_time(ev1)
+    res_grids = torch.empty(gs, dtype=torch.complex64, device=dev)
+    ms_refresh = timed(lambda: plan.grid_residual(model, out=res_grids), steps, 2)
+    t_refresh = ctx.last_timings()
+    pg = torch.empty(gs, dtype=torch.float32, device=dev)
+    dg = torch.empty(gs, dtype=torch.complex64, device=dev)
+    ms_plan_grid = timed(lambda: plan.grid_dirty(out=(pg, dg)), steps, 2)
+    del pg, dg
+    _, _, states = plan.dirty_images()
+    models = torch.zeros((C, obs.nx, obs.nx), dtype=torch.float32, device=dev)
+    models[:, obs.nx // 2, obs.nx // 2] = 1.0
+    res_imgs = torch.empty_like(models)
+    ms_refresh_img = timed(lambda: plan.residual_images(models, states, out=res_imgs), 2, 1)
+    t_img = ctx.last_timings()
+    # the same refresh with FP64 transforms, and how far the float32 images
+    # are from it (peak-normalised, worst plane)
+    plan.set_fft_precision(64)
+    res64 = torch.empty_like(models)
+    ms_refresh_img64 = timed(lambda: plan.residual_images(models, states, out=res64), 1, 1)
+    t_img64 = ctx.last_timings()
+    plan.set_fft_precision(32)
+    img_err = float(torch.max(torch.amax(torch.abs(res_imgs - res64), dim=(1, 2)) /
+                              torch.amax(torch.abs(res64), dim=(1, 2)).clamp_min(1e-30)))
+    plan.close()
+    del res_grids, res_imgs, res64, models
+
     # the plain loop: per channel, the single-channel API on that channel's
     # batch (flagged samples carry gridable = 0 and weight 0)
     lsd = torch.as_tensor(obs.lambda_scale, device=dev)
@@ -320,6 +354,19 @@ def run_cube(args, ctx, dev, peak):
                                   "cube_grid_kernel": gk,
                                   "degrid": t_both["degrid_ms"],
                                   "cube_degrid_kernel": t_both["degrid_kernel_ms"]}},
+        "resident_plan": {"create_ms": ms_plan_create, "grid_ms": ms_plan_grid,
+                          "grid_mvis_s": n_vis / (ms_plan_grid * 1e-3) / 1e6,
+                          "residual_refresh_ms": ms_refresh,
+                          "residual_refresh_mvis_s": n_vis / (ms_refresh * 1e-3) / 1e6,
+                          "refresh_kernels_ms": {"cube_degrid_kernel_residual":
+                                                 t_refresh["degrid_kernel_ms"],
+                                                 "cube_grid_kernel_residual":
+                                                 t_refresh["grid_kernel_ms"]},
+                          "residual_images_ms": ms_refresh_img,
+                          "residual_images_fft_ms": t_img["fft_ms"],
+                          "residual_images_fp64_ms": ms_refresh_img64,
+                          "residual_images_fp64_fft_ms": t_img64["fft_ms"],
+                          "float32_vs_fp64_image_err": img_err},
         "plain_loop": {"grid_ms": ms_plain, "grid_degrid_ms": ms_plain_both,
                        "grid_mvis_s": n_vis / (ms_plain * 1e-3) / 1e6,
                        "grid_degrid_mvis_s": n_vis / (ms_plain_both * 1e-3) / 1e6},

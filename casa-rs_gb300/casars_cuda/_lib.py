@@ -106,6 +106,7 @@ SIGNATURES = {
                                        _p, _err]),
     "cr_cube_plan_destroy": (None, [_p]),
     "cr_cube_plan_channels": (_i32, [_p]),
+    "cr_cube_plan_set_fft_precision": (C.c_int, [_p, _i32]),
     "cr_cube_plan_grid_dirty": (C.c_int, [_p, _p, _p, _p, _i32, _err]),
     "cr_cube_plan_degrid": (C.c_int, [_p, _p, _p, _i32, _p, _i32, _err]),
     "cr_cube_plan_grid_residual": (C.c_int, [_p, _p, _p, _i32, _p, _p, _i32, _err]),

@@ -346,14 +346,15 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
 
 def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
                    robust: float = 0.0, max_psf_sidelobe: Optional[float] = None,
-                   restore: bool = True) -> CubeCleanResult:
+                   restore: bool = True, fft_bits: int = 32) -> CubeCleanResult:
     """run_standard_mfs_cube_clean (lib.rs:3026-3210) on the device: one
     persistent cube plan (im.CubePlan) gives every plane's PSF and residual
     and replays the records for each pass's residual refresh (all updated
     planes in one batched degrid + grid); the minor cycles are cr_hogbom per
     plane; each plane's beam is fitted to its PSF and its sidelobe level
-    estimated (beam.rs:292-304) unless max_psf_sidelobe is given."""
-    plan = im.CubePlan(gridder, cube, weighting, robust)
+    estimated (beam.rs:292-304) unless max_psf_sidelobe is given.  fft_bits
+    picks the image-stage transforms (im.CubePlan.set_fft_precision)."""
+    plan = im.CubePlan(gridder, cube, weighting, robust, fft_bits)
     ctx = gridder.ctx
     geom = gridder.geometry
     cell = (geom.cell_x_rad, geom.cell_y_rad)

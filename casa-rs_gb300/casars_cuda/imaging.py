@@ -732,7 +732,7 @@ class CubePlan:
     Arrays live where the cube batch is (torch CUDA tensors or numpy)."""
 
     def __init__(self, gridder, cube: CubeBatch, weighting: str = "natural",
-                 robust: float = 0.0):
+                 robust: float = 0.0, fft_bits: int = 32):
         ctx = gridder.ctx
         arrs = _Arrays()
         b = cube._bind(arrs)
@@ -747,6 +747,13 @@ class CubePlan:
              WEIGHTING_MODES[weighting], float(robust), C.byref(h), sums)
         self._h = h
         self.sums = [GridSums.from_c(s) for s in sums]
+        self.set_fft_precision(fft_bits)
+
+    def set_fft_precision(self, bits: int):
+        """Image-stage transforms: 32 (float32, default) or 64 (FP64)."""
+        if _lib.load().cr_cube_plan_set_fft_precision(self._h, int(bits)) != 0:
+            raise ValueError("fft precision must be 32 or 64")
+        self.fft_bits = int(bits)
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

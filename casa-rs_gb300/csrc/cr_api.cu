@@ -351,6 +351,7 @@ void cr_ctx_destroy(cr_ctx* ctx) {
         if (kv.second.ptr) cudaFreeAsync(kv.second.ptr, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->fft_plans) cufftDestroy(kv.second);
+    for (auto& kv : ctx->fft_plans_c2c) cufftDestroy(kv.second);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->kev)
@@ -1118,6 +1119,12 @@ void cr_cube_plan_destroy(cr_cube_plan* p) {
 
 int32_t cr_cube_plan_channels(const cr_cube_plan* p) { return p ? p->rec.C : 0; }
 
+int cr_cube_plan_set_fft_precision(cr_cube_plan* p, int32_t bits) {
+    if (!p || (bits != 32 && bits != 64)) return CR_INVALID;
+    p->fft_bits = bits;
+    return CR_OK;
+}
+
 namespace {
 
 void check_cube_plan(cr_ctx* ctx, cr_cube_plan* p) {
@@ -1230,6 +1237,7 @@ int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
         float* pi = out_ptr<float>(ctx, psf_images, out_location, C * np * 4, "cpi_psf_img");
         float* ri = out_ptr<float>(ctx, residual_images, out_location, C * np * 4, "cpi_res_img");
         unsigned int* peaks = (unsigned int*)workspace(ctx, "cpi_peaks", C * 4);
+        const bool single = p->fft_bits == 32;
         CR_CUDA_CHECK(cudaMemsetAsync(peaks, 0, C * 4, ctx->stream));
         std::vector<float> sumwt(C);
         for (size_t c = 0; c < C; ++c) {
@@ -1243,10 +1251,10 @@ int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
             }
             // the normalisation of dirty_grids_to_psf_and_residual_owned,
             // as the single-plane cr_dirty_image
-            grid_to_image_real(ctx, g, psf + c * cells, 1.0f / sumwt[c], pc);
+            grid_to_image_real(ctx, g, psf + c * cells, 1.0f / sumwt[c], pc, single);
             abs_peak(ctx, pc, (int64_t)np, peaks + c);
             scale_image(ctx, pc, (int64_t)np, 1.0f, peaks + c);
-            grid_to_image(ctx, g, nullptr, dirty + c * cells, 1.0f / sumwt[c], rc);
+            grid_to_image(ctx, g, nullptr, dirty + c * cells, 1.0f / sumwt[c], rc, single);
             scale_image(ctx, rc, (int64_t)np, 1.0f, peaks + c);
         }
         tm.mark();
@@ -1300,7 +1308,9 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
         const float* m = (const float*)device_input(ctx, models, C * np * 4, model_location,
                                                     "cube_models");
         float2* mg = (float2*)workspace(ctx, "cpr_model_grids", C * cells * 8);
-        for (int c : chosen) image_to_grid(ctx, g, nullptr, m + (size_t)c * np, mg + c * cells);
+        const bool single = p->fft_bits == 32;
+        for (int c : chosen)
+            image_to_grid(ctx, g, nullptr, m + (size_t)c * np, mg + c * cells, single);
         tm.mark();
         float2* res = (float2*)workspace(ctx, "cpr_residual_grids", C * cells * 8);
         cube_grid_residual(ctx, g, p->rec, mg, res, mask);
@@ -1308,7 +1318,7 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
         float* img = out_ptr<float>(ctx, residual_images, out_location, C * np * 4, "cpr_image");
         for (int c : chosen) {
             grid_to_image(ctx, g, nullptr, res + (size_t)c * cells,
-                          1.0f / states[c].normalization_sumwt, img + (size_t)c * np);
+                          1.0f / states[c].normalization_sumwt, img + (size_t)c * np, single);
             scale_image(ctx, img + (size_t)c * np, (int64_t)np, 1.0f / states[c].psf_peak,
                         nullptr);
             if (out_location == CR_HOST)

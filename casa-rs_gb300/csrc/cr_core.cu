@@ -55,18 +55,28 @@ void kernel_mark(cr_ctx* ctx, int which, bool end) {
     if (end) ctx->kev_used |= 1 << which;
 }
 
-cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny) {
+static cufftHandle cached_plan(cr_ctx* ctx,
+                               std::map<std::pair<int64_t, int64_t>, cufftHandle>& plans,
+                               int64_t nx, int64_t ny, cufftType type) {
     auto key = std::make_pair(nx, ny);
-    auto it = ctx->fft_plans.find(key);
-    if (it != ctx->fft_plans.end()) {
+    auto it = plans.find(key);
+    if (it != plans.end()) {
         check_cufft(cufftSetStream(it->second, ctx->stream), "cufftSetStream");
         return it->second;
     }
     cufftHandle h;
-    check_cufft(cufftPlan2d(&h, (int)nx, (int)ny, CUFFT_Z2Z), "cufftPlan2d");
+    check_cufft(cufftPlan2d(&h, (int)nx, (int)ny, type), "cufftPlan2d");
     check_cufft(cufftSetStream(h, ctx->stream), "cufftSetStream");
-    ctx->fft_plans[key] = h;
+    plans[key] = h;
     return h;
+}
+
+cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny) {
+    return cached_plan(ctx, ctx->fft_plans, nx, ny, CUFFT_Z2Z);
+}
+
+cufftHandle fft_plan_c2c(cr_ctx* ctx, int64_t nx, int64_t ny) {
+    return cached_plan(ctx, ctx->fft_plans_c2c, nx, ny, CUFFT_C2C);
 }
 
 // ---- host tables --------------------------------------------------------------

@@ -17,26 +17,38 @@ namespace cr {
 
 namespace {
 
-__global__ void widen_checker_kernel(const float2* g, int64_t gnx, int64_t gny, double2* out) {
+// The FP64 transforms work on double2, the float32 ones (cube images) on
+// float2; sign flips are exact in either.
+__device__ __forceinline__ double2 make_work(double re, double im, double2*) {
+    return make_double2(re, im);
+}
+__device__ __forceinline__ float2 make_work(float re, float im, float2*) {
+    return make_float2(re, im);
+}
+
+template <typename W>
+__global__ void widen_checker_kernel(const float2* g, int64_t gnx, int64_t gny, W* out) {
+    using S = decltype(out->x);
     const int64_t n = gnx * gny;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / gny, y = t - x * gny;
         float2 v = g[t];
-        double s = ((x + y) & 1) ? -1.0 : 1.0;
-        out[t] = make_double2(s * (double)v.x, s * (double)v.y);
+        S s = ((x + y) & 1) ? S(-1) : S(1);
+        out[t] = make_work(s * (S)v.x, s * (S)v.y, out);
     }
 }
 
 // The real part alone (a PSF grid kept as float32).
-__global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t gny,
-                                          double2* out) {
+template <typename W>
+__global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t gny, W* out) {
+    using S = decltype(out->x);
     const int64_t n = gnx * gny;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / gny, y = t - x * gny;
-        double s = ((x + y) & 1) ? -1.0 : 1.0;
-        out[t] = make_double2(s * (double)g[t], 0.0);
+        S s = ((x + y) & 1) ? S(-1) : S(1);
+        out[t] = make_work(s * (S)g[t], S(0), out);
     }
 }
 
@@ -44,7 +56,8 @@ __global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t g
 // sinc_mode 1 (W-projection image correction) further divides by
 // sinc_x * sinc_y with the reference's 1e-6 guard; sinc_mode 2 multiplies by
 // it, which is the transpose of the W-projection model apodisation.
-__global__ void crop_correct_kernel(const double2* raw, int64_t gny, int32_t nx, int32_t ny,
+template <typename W>
+__global__ void crop_correct_kernel(const W* raw, int64_t gny, int32_t nx, int32_t ny,
                                     int64_t blc_x, int64_t blc_y, int parity, double scale,
                                     const float* corr_x, const float* corr_y, const float* sx,
                                     const float* sy, int sinc_mode, float* image) {
@@ -53,7 +66,7 @@ __global__ void crop_correct_kernel(const double2* raw, int64_t gny, int32_t nx,
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / ny, y = t - x * ny;
         int64_t gx = blc_x + x, gy = blc_y + y;
-        double r = raw[gx * gny + gy].x;
+        double r = (double)raw[gx * gny + gy].x;
         if ((gx + gy + parity) & 1) r = -r;
         float v = (float)(r * scale);
         float factor = __fmul_rn(corr_x[gx], corr_y[gy]);
@@ -71,10 +84,12 @@ __global__ void crop_correct_kernel(const double2* raw, int64_t gny, int32_t nx,
 
 // apodize_model / apodize_w_project_model (gridder.rs:1554-1592) into a
 // zeroed grid, with the input checkerboard of the centred forward FFT.
+template <typename W>
 __global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64_t gny,
                                int64_t blc_x, int64_t blc_y, const float* corr_x,
                                const float* corr_y, const float* sinc_x, const float* sinc_y,
-                               double2* grid) {
+                               W* grid) {
+    using S = decltype(grid->x);
     const int64_t n = (int64_t)nx * ny;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -84,19 +99,24 @@ __global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64
         if (sinc_x) f = __fmul_rn(__fmul_rn(f, sinc_x[gx]), sinc_y[gy]);
         float v = model[t] * f;
         if ((gx + gy) & 1) v = -v;
-        grid[gx * gny + gy] = make_double2((double)v, 0.0);
+        grid[gx * gny + gy] = make_work((S)v, S(0), grid);
     }
 }
 
-__global__ void narrow_sign_kernel(const double2* g, int64_t gnx, int64_t gny, int parity,
+template <typename W>
+__global__ void narrow_sign_kernel(const W* g, int64_t gnx, int64_t gny, int parity,
                                    float2* out) {
     const int64_t n = gnx * gny;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / gny, y = t - x * gny;
-        double2 v = g[t];
-        if ((x + y + parity) & 1) v = make_double2(-v.x, -v.y);
-        out[t] = make_float2((float)v.x, (float)v.y);
+        W v = g[t];
+        float re = (float)v.x, im = (float)v.y;
+        if ((x + y + parity) & 1) {
+            re = -re;
+            im = -im;
+        }
+        out[t] = make_float2(re, im);
     }
 }
 
@@ -124,24 +144,35 @@ __global__ void scale_image_kernel(float* img, int64_t n, float scale, const uns
 
 }  // namespace
 
+// The bare transform in place: cuFFT Z2Z (FP64) or C2C (float32).
+static void exec_fft(cr_ctx* ctx, int64_t gnx, int64_t gny, double2* work, int dir) {
+    check_cufft(cufftExecZ2Z(fft_plan(ctx, gnx, gny), (cufftDoubleComplex*)work,
+                             (cufftDoubleComplex*)work, dir),
+                "cufftExecZ2Z");
+}
+static void exec_fft(cr_ctx* ctx, int64_t gnx, int64_t gny, float2* work, int dir) {
+    check_cufft(cufftExecC2C(fft_plan_c2c(ctx, gnx, gny), (cufftComplex*)work,
+                             (cufftComplex*)work, dir),
+                "cufftExecC2C");
+}
+
+template <typename W>
 static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float2* grid,
-                               float scale, float* image, bool adjoint,
-                               const float* real_grid = nullptr) {
+                               float scale, float* image, bool adjoint, const float* real_grid) {
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
-    double2* work = (double2*)workspace(ctx, "fft_z", (size_t)gnx * gny * 16);
+    W* work = (W*)workspace(ctx, sizeof(W) == 16 ? "fft_z" : "fft_c",
+                            (size_t)gnx * gny * sizeof(W));
     if (real_grid) {
-        widen_checker_real_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
+        widen_checker_real_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
             real_grid, gnx, gny, work);
         note_launch(ctx, "widen_checker_real_kernel");
     } else {
-        widen_checker_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(grid, gnx,
-                                                                                  gny, work);
+        widen_checker_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
+            grid, gnx, gny, work);
         note_launch(ctx, "widen_checker_kernel");
     }
-    cufftHandle plan = fft_plan(ctx, gnx, gny);
-    check_cufft(cufftExecZ2Z(plan, (cufftDoubleComplex*)work, (cufftDoubleComplex*)work, CUFFT_INVERSE),
-                "cufftExecZ2Z");
+    exec_fft(ctx, gnx, gny, work, CUFFT_INVERSE);
     int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
     double inv = 1.0 / ((double)gnx * (double)gny);
     const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
@@ -153,43 +184,59 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
         sx = adjoint ? wp->sinc_gx_d : wp->sinc_x_d;
         sy = adjoint ? wp->sinc_gy_d : wp->sinc_x_d;
     }
-    crop_correct_kernel<<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
+    crop_correct_kernel<W><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
         work, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity,
         inv * (double)scale, g->corr_x_d, g->corr_y_d, sx, sy, mode, image);
     note_launch(ctx, "crop_correct_kernel");
 }
 
+template <typename W>
+static void image_to_grid_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
+                               float2* grid) {
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
+    W* work = (W*)workspace(ctx, sizeof(W) == 16 ? "fft_z" : "fft_c",
+                            (size_t)gnx * gny * sizeof(W));
+    CR_CUDA_CHECK(cudaMemsetAsync(work, 0, (size_t)gnx * gny * sizeof(W), ctx->stream));
+    const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
+    apodize_kernel<W><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
+        model, g->geom.nx, g->geom.ny, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d,
+        g->corr_y_d, wp ? wp->sinc_gx_d : nullptr, wp ? wp->sinc_gy_d : nullptr, work);
+    note_launch(ctx, "apodize_kernel");
+    exec_fft(ctx, gnx, gny, work, CUFFT_FORWARD);
+    int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
+    narrow_sign_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(work, gnx, gny,
+                                                                               parity, grid);
+    note_launch(ctx, "narrow_sign_kernel");
+}
+
 void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
-                   float* image) {
-    grid_to_image_impl(ctx, g, wp, grid, scale, image, false);
+                   float* image, bool single) {
+    if (single)
+        grid_to_image_impl<float2>(ctx, g, wp, grid, scale, image, false, nullptr);
+    else
+        grid_to_image_impl<double2>(ctx, g, wp, grid, scale, image, false, nullptr);
 }
 
 void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float scale,
-                        float* image) {
-    grid_to_image_impl(ctx, g, nullptr, nullptr, scale, image, false, grid);
+                        float* image, bool single) {
+    if (single)
+        grid_to_image_impl<float2>(ctx, g, nullptr, nullptr, scale, image, false, grid);
+    else
+        grid_to_image_impl<double2>(ctx, g, nullptr, nullptr, scale, image, false, grid);
 }
 
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                            float* image) {
-    grid_to_image_impl(ctx, g, wp, grid, scale, image, true);
+    grid_to_image_impl<double2>(ctx, g, wp, grid, scale, image, true, nullptr);
 }
 
-void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid) {
-    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
-    if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
-    double2* work = (double2*)workspace(ctx, "fft_z", (size_t)gnx * gny * 16);
-    CR_CUDA_CHECK(cudaMemsetAsync(work, 0, (size_t)gnx * gny * 16, ctx->stream));
-    const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
-    apodize_kernel<<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
-        model, g->geom.nx, g->geom.ny, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d,
-        g->corr_y_d, wp ? wp->sinc_gx_d : nullptr, wp ? wp->sinc_gy_d : nullptr, work);
-    note_launch(ctx, "apodize_kernel");
-    cufftHandle plan = fft_plan(ctx, gnx, gny);
-    check_cufft(cufftExecZ2Z(plan, (cufftDoubleComplex*)work, (cufftDoubleComplex*)work, CUFFT_FORWARD),
-                "cufftExecZ2Z");
-    int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
-    narrow_sign_kernel<<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(work, gnx, gny, parity, grid);
-    note_launch(ctx, "narrow_sign_kernel");
+void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid,
+                   bool single) {
+    if (single)
+        image_to_grid_impl<float2>(ctx, g, wp, model, grid);
+    else
+        image_to_grid_impl<double2>(ctx, g, wp, model, grid);
 }
 
 void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev) {

@@ -48,6 +48,7 @@ struct cr_ctx {
     cudaStream_t stream = nullptr;
     cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
+    std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans_c2c;
     cudaEvent_t ev[8] = {};
     // [0,1] bracket the last gridding kernel, [2,3] the last degridding kernel
     cudaEvent_t kev[4] = {};
@@ -111,6 +112,7 @@ void note_launch(cr_ctx* ctx, const char* what);
 // Event pair around one gridding (which = 0) or degridding (which = 1) kernel.
 void kernel_mark(cr_ctx* ctx, int which, bool end);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
+cufftHandle fft_plan_c2c(cr_ctx* ctx, int64_t nx, int64_t ny);
 
 // ---- host-side tables (restated from gridder.rs) ----------------------------
 int64_t casa_composite_padded_len(int64_t image_len, double padding);
@@ -192,16 +194,18 @@ void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
 
 // ---- FFT stage -------------------------------------------------------------------
 // grid (device, modified in place) -> image * scale (device)
+// single: float32 C2C transforms instead of FP64 Z2Z (the cube image stage)
 void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
-                   float* image);
+                   float* image, bool single = false);
 // the exact adjoint of image_to_grid's image-side factor (no sinc division)
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                            float* image);
 // model image (device) -> centred model grid (device)
-void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid);
+void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid,
+                   bool single = false);
 // grid_to_image of a real grid (the real part of a PSF grid), standard gridder
 void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float scale,
-                        float* image);
+                        float* image, bool single = false);
 // max |image| into *peak_dev (float bits as uint32)
 void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev);
 // image *= scale, then / *peak_dev when peak_dev != null
@@ -316,6 +320,7 @@ struct cr_cube_plan {
     cr::Pool pool;
     cr::CubeRecords rec;
     std::vector<cr_sums> sums;
+    int32_t fft_bits = 32;   // image-stage transforms: 32 (C2C) or 64 (Z2Z)
 };
 
 struct cr_plan {

@@ -324,6 +324,10 @@ int cr_cube_plan_create(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                         char** err);
 void cr_cube_plan_destroy(cr_cube_plan* plan);
 int32_t cr_cube_plan_channels(const cr_cube_plan* plan);
+/* Transforms of the image calls: 32 = float32 C2C (the default; FP64 runs
+ * at a small fraction of the float32 rate on this GPU), 64 = FP64 Z2Z as in
+ * the single-plane calls.  Returns CR_INVALID for other values. */
+int cr_cube_plan_set_fft_precision(cr_cube_plan* plan, int32_t bits);
 int cr_cube_plan_grid_dirty(cr_ctx* ctx, cr_cube_plan* plan, float* psf_grids,
                             float* dirty_grids, int32_t out_location, char** err);
 int cr_cube_plan_degrid(cr_ctx* ctx, cr_cube_plan* plan, const float* model_grids,

@@ -9,7 +9,8 @@ seeded per-channel flags) is planned once (cr_cube_plan_create) and replayed:
   1e-5 of each channel's peak, and unselected planes are left untouched;
 * PSF and residual images with their PSF states agree with the oracle's
   dirty products per channel, and model -> residual images with the
-  oracle's major-cycle refresh, within 1e-5 of the peak;
+  oracle's major-cycle refresh, within 1e-5 of the peak, with float32 or
+  FP64 image transforms;
 * run_cube_clean (batched refreshes, cr_hogbom per plane) agrees with the
   oracle's run_standard_mfs_cube_clean restatement (each plane refreshed in
   turn): component positions exactly, fluxes within 1e-5 relative, the same
@@ -119,12 +120,14 @@ def test_cube_plan_residual_grids_match_oracle(ctx, cube):
     plan.close()
 
 
-@pytest.mark.parametrize("mode,robust", [("natural", 0.0), ("briggs", 0.5)])
-def test_cube_plan_images_match_oracle(ctx, cube, mode, robust):
+@pytest.mark.parametrize("mode,robust,bits", [("natural", 0.0, 32), ("briggs", 0.5, 32),
+                                              ("briggs", 0.5, 64)])
+def test_cube_plan_images_match_oracle(ctx, cube, mode, robust, bits):
+    """Float32 (default) and FP64 image-stage transforms."""
     obs, flags, vis = cube
     gg = _gridder(ctx, obs)
     cb = cc.CubeBatch(obs.u_m, obs.v_m, obs.lambda_scale, vis, None, flags)
-    plan = cc.CubePlan(gg, cb, mode, robust)
+    plan = cc.CubePlan(gg, cb, mode, robust, fft_bits=bits)
     ref = _oracle_planes(obs, flags, vis, mode, robust)
     psf, res, states = plan.dirty_images()
     models = np.zeros((obs.channels, obs.nx, obs.nx), np.float32)
