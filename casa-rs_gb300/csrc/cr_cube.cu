@@ -372,7 +372,7 @@ __global__ void tile_starts_from_cells(const uint32_t* cell_start, int64_t nbins
 }
 
 // Pass 1: histogram of (channel, home tile, cell), per-channel sumwt and counts.
-__global__ void __launch_bounds__(kCubeThreads, 3) cube_hist_kernel(CubeArgs a) {
+__global__ void __launch_bounds__(kCubeThreads, 4) cube_hist_kernel(CubeArgs a) {
     __shared__ double s_sum[kCubeThreads / 32];
     __shared__ unsigned long long s_ok[kCubeThreads / 32], s_skip[kCubeThreads / 32];
     const int c = blockIdx.y;
@@ -605,7 +605,7 @@ constexpr int kGridThreads = kCubeThreads;
 // With RESIDUAL the records carry w (vis - pred) from `res` and no PSF is
 // formed.
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kGridThreads) cube_grid_kernel(CubeGridArgs a) {
+__global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs a) {
     __shared__ float s_psf[kTile * kRow];
     __shared__ float s_re[kTile * kRow];
     __shared__ float s_im[kTile * kRow];

@@ -230,7 +230,7 @@ struct __align__(16) Entry {
 constexpr int kCand = 128;  // candidate records examined per batch
 
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kGridThreads) wp_grid_kernel(GridArgs a) {
+__global__ void __launch_bounds__(kGridThreads, 5) wp_grid_kernel(GridArgs a) {
     __shared__ int s_item;
     __shared__ uint32_t s_seg_start[kMaxSeg];
     __shared__ uint32_t s_seg_pref[kMaxSeg + 1];
