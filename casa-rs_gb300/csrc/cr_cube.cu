@@ -610,11 +610,17 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
     __shared__ float s_re[kTile * kRow];
     __shared__ float s_im[kTile * kRow];
     __shared__ float s_taps[kMaxTapRows * 7];
+    // per warp, the decoded records of its current batch of 32:
+    // {run key, x tap row * 7, y tap row * 7, weight} and {w vis}
+    __shared__ int4 s_ra[kGridThreads];
+    __shared__ float2 s_rb[kGridThreads];
     __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t ntiles = a.ntx * a.nty;
     const unsigned long long n_items = *a.n_items;
     for (int k = tid; k < a.tap_rows * 7; k += kGridThreads) s_taps[k] = a.taps[k];
+    int4* w_ra = s_ra + warp * 32;
+    float2* w_rb = s_rb + warp * 32;
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
         __syncthreads();
@@ -668,13 +674,33 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
         // Records of a home tile arrive in start-cell order, so a warp's
         // consecutive records often share a start cell: lane t sums tap t of
         // such a run in registers and adds it to the tile once per run.
+        // Lane t holds taps t (slot 0) and t + 32 (slot 1, lanes 0-16; the
+        // other lanes form a dummy product that is never added).  A run is
+        // keyed by (source, start cell); a run whose footprint lies inside
+        // the tile adds at run base + a per-lane offset without bounds tests.
         const int ix0 = lane / 7, iy0 = lane % 7;
         const int ix1 = (lane + 32) / 7, iy1 = (lane + 32) % 7;
         const bool has1 = lane + 32 < 49;
-        int cur_lx = 0, cur_ly = 0;
-        bool open = false;
+        const int jx1 = has1 ? ix1 : 0, jy1 = has1 ? iy1 : 0;
+        const int off0 = ix0 * kRow + iy0, off1 = ix1 * kRow + iy1;
+        uint32_t cur_key = ~0u;
+        int cur_lx = 0, cur_ly = 0, cur_base = 0;
+        bool cur_inside = false;
         float p0 = 0.f, r0 = 0.f, i0 = 0.f, p1 = 0.f, r1 = 0.f, i1 = 0.f;
         auto flush = [&]() {
+            if (cur_inside) {
+                const int c0 = cur_base + off0;
+                if (!RESIDUAL) atomicAdd(&s_psf[c0], p0);
+                atomicAdd(&s_re[c0], r0);
+                atomicAdd(&s_im[c0], i0);
+                if (has1) {
+                    const int c1 = cur_base + off1;
+                    if (!RESIDUAL) atomicAdd(&s_psf[c1], p1);
+                    atomicAdd(&s_re[c1], r1);
+                    atomicAdd(&s_im[c1], i1);
+                }
+                return;
+            }
             int cx = cur_lx + ix0, cy = cur_ly + iy0;
             if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
                 const int cell = cx * kRow + cy;
@@ -695,54 +721,67 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
         for (int s = 0; s < 4; ++s) {
             const int sox = -(s & 1) * kTile, soy = -(s >> 1) * kTile;
             for (uint32_t base = b0[s] + warp * 32; base < b1[s]; base += kGridThreads) {
+                // lanes load and decode 32 records; those that reach the
+                // tile are packed into the warp's staging slots
                 const uint32_t rr = base + lane;
-                uint4 q = make_uint4(0u, 0u, 0u, 0u);
-                float qw = 0.0f;
                 bool rel = false;
+                int4 ra = make_int4(0, 0, 0, 0);
+                float2 rb = make_float2(0.0f, 0.0f);
                 if (rr < b1[s]) {
-                    q = a.rec[rr];
+                    const uint4 q = a.rec[rr];
+                    float qw = 0.0f;
                     if (RESIDUAL) {
-                        const float2 rv = a.res[rr];
-                        q.z = __float_as_uint(rv.x);
-                        q.w = __float_as_uint(rv.y);
+                        rb = a.res[rr];
                     } else {
                         qw = a.rec_w[rr];
+                        rb = make_float2(__uint_as_float(q.z), __uint_as_float(q.w));
                     }
                     const int lx = sox + (int)(q.x >> 27), ly = soy + (int)((q.x >> 22) & 31);
                     rel = lx + 6 >= 0 && ly + 6 >= 0;
+                    ra = make_int4((int)((q.x >> 22) | ((uint32_t)s << 10)),
+                                   (int)((q.x >> 11) & 2047u) * 7, (int)(q.x & 2047u) * 7,
+                                   __float_as_int(qw));
                 }
-                unsigned m = __ballot_sync(0xffffffffu, rel);
-                while (m) {
-                    const int src = __ffs(m) - 1;
-                    m &= m - 1;
-                    const uint32_t meta = __shfl_sync(0xffffffffu, q.x, src);
-                    const float vr = __uint_as_float(__shfl_sync(0xffffffffu, q.z, src));
-                    const float vi = __uint_as_float(__shfl_sync(0xffffffffu, q.w, src));
-                    const float pw = __shfl_sync(0xffffffffu, qw, src);
-                    const int lx = sox + (int)(meta >> 27), ly = soy + (int)((meta >> 22) & 31);
-                    if (!open || lx != cur_lx || ly != cur_ly) {
-                        if (open) flush();
-                        open = true;
-                        cur_lx = lx;
-                        cur_ly = ly;
+                const unsigned m = __ballot_sync(0xffffffffu, rel);
+                if (rel) {
+                    const int pos = __popc(m & ((1u << lane) - 1u));
+                    w_ra[pos] = ra;
+                    w_rb[pos] = rb;
+                }
+                __syncwarp();
+                const int nrel = __popc(m);
+                for (int k = 0; k < nrel; ++k) {
+                    const int4 A = w_ra[k];
+                    const float2 B = w_rb[k];
+                    const float vr = B.x, vi = B.y, pw = __int_as_float(A.w);
+                    const uint32_t key = (uint32_t)A.x;
+                    if (key != cur_key) {
+                        if (cur_key != ~0u) flush();
+                        cur_key = key;
+                        cur_lx = sox + (int)((key >> 5) & 31);
+                        cur_ly = soy + (int)(key & 31);
+                        cur_base = cur_lx * kRow + cur_ly;
+                        cur_inside = cur_lx >= 0 && cur_ly >= 0 && cur_lx <= kTile - 7 &&
+                                     cur_ly <= kTile - 7;
                         p0 = r0 = i0 = p1 = r1 = i1 = 0.f;
                     }
-                    const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
-                    const float* wy = s_taps + (meta & 2047u) * 7;
+                    const float* wx = s_taps + A.y;
+                    const float* wy = s_taps + A.z;
                     const float w0 = __fmul_rn(wx[ix0], wy[iy0]);
-                    if (!RESIDUAL) p0 = fmaf(pw, w0, p0);
+                    const float w1 = __fmul_rn(wx[jx1], wy[jy1]);
+                    if (!RESIDUAL) {
+                        p0 = fmaf(pw, w0, p0);
+                        p1 = fmaf(pw, w1, p1);
+                    }
                     r0 = fmaf(vr, w0, r0);
                     i0 = fmaf(vi, w0, i0);
-                    if (has1) {
-                        const float w1 = __fmul_rn(wx[ix1], wy[iy1]);
-                        if (!RESIDUAL) p1 = fmaf(pw, w1, p1);
-                        r1 = fmaf(vr, w1, r1);
-                        i1 = fmaf(vi, w1, i1);
-                    }
+                    r1 = fmaf(vr, w1, r1);
+                    i1 = fmaf(vi, w1, i1);
                 }
+                __syncwarp();   // the slots are refilled by the next batch
             }
         }
-        if (open) flush();
+        if (cur_key != ~0u) flush();
         __syncthreads();
         for (int k = tid; k < kTile * kTile; k += kGridThreads) {
             const int cx = k / kTile, cy = k % kTile;
