@@ -686,35 +686,37 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
         uint32_t cur_key = ~0u;
         int cur_lx = 0, cur_ly = 0, cur_base = 0;
         bool cur_inside = false;
-        float p0 = 0.f, r0 = 0.f, i0 = 0.f, p1 = 0.f, r1 = 0.f, i1 = 0.f;
+        // (psf slot 0, psf slot 1), (re, im) slot 0, (re, im) slot 1: paired
+        // float32 FMAs (FFMA2) update two sums per instruction
+        float2 pp = make_float2(0.f, 0.f), ri0 = pp, ri1 = pp;
         auto flush = [&]() {
             if (cur_inside) {
                 const int c0 = cur_base + off0;
-                if (!RESIDUAL) atomicAdd(&s_psf[c0], p0);
-                atomicAdd(&s_re[c0], r0);
-                atomicAdd(&s_im[c0], i0);
+                if (!RESIDUAL) atomicAdd(&s_psf[c0], pp.x);
+                atomicAdd(&s_re[c0], ri0.x);
+                atomicAdd(&s_im[c0], ri0.y);
                 if (has1) {
                     const int c1 = cur_base + off1;
-                    if (!RESIDUAL) atomicAdd(&s_psf[c1], p1);
-                    atomicAdd(&s_re[c1], r1);
-                    atomicAdd(&s_im[c1], i1);
+                    if (!RESIDUAL) atomicAdd(&s_psf[c1], pp.y);
+                    atomicAdd(&s_re[c1], ri1.x);
+                    atomicAdd(&s_im[c1], ri1.y);
                 }
                 return;
             }
             int cx = cur_lx + ix0, cy = cur_ly + iy0;
             if (cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
                 const int cell = cx * kRow + cy;
-                if (!RESIDUAL) atomicAdd(&s_psf[cell], p0);
-                atomicAdd(&s_re[cell], r0);
-                atomicAdd(&s_im[cell], i0);
+                if (!RESIDUAL) atomicAdd(&s_psf[cell], pp.x);
+                atomicAdd(&s_re[cell], ri0.x);
+                atomicAdd(&s_im[cell], ri0.y);
             }
             cx = cur_lx + ix1;
             cy = cur_ly + iy1;
             if (has1 && cx >= 0 && cx < kTile && cy >= 0 && cy < kTile) {
                 const int cell = cx * kRow + cy;
-                if (!RESIDUAL) atomicAdd(&s_psf[cell], p1);
-                atomicAdd(&s_re[cell], r1);
-                atomicAdd(&s_im[cell], i1);
+                if (!RESIDUAL) atomicAdd(&s_psf[cell], pp.y);
+                atomicAdd(&s_re[cell], ri1.x);
+                atomicAdd(&s_im[cell], ri1.y);
             }
         };
 #pragma unroll
@@ -753,7 +755,7 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
                 for (int k = 0; k < nrel; ++k) {
                     const int4 A = w_ra[k];
                     const float2 B = w_rb[k];
-                    const float vr = B.x, vi = B.y, pw = __int_as_float(A.w);
+                    const float pw = __int_as_float(A.w);
                     const uint32_t key = (uint32_t)A.x;
                     if (key != cur_key) {
                         if (cur_key != ~0u) flush();
@@ -763,20 +765,17 @@ __global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs
                         cur_base = cur_lx * kRow + cur_ly;
                         cur_inside = cur_lx >= 0 && cur_ly >= 0 && cur_lx <= kTile - 7 &&
                                      cur_ly <= kTile - 7;
-                        p0 = r0 = i0 = p1 = r1 = i1 = 0.f;
+                        pp = ri0 = ri1 = make_float2(0.f, 0.f);
                     }
                     const float* wx = s_taps + A.y;
                     const float* wy = s_taps + A.z;
-                    const float w0 = __fmul_rn(wx[ix0], wy[iy0]);
-                    const float w1 = __fmul_rn(wx[jx1], wy[jy1]);
-                    if (!RESIDUAL) {
-                        p0 = fmaf(pw, w0, p0);
-                        p1 = fmaf(pw, w1, p1);
-                    }
-                    r0 = fmaf(vr, w0, r0);
-                    i0 = fmaf(vi, w0, i0);
-                    r1 = fmaf(vr, w1, r1);
-                    i1 = fmaf(vi, w1, i1);
+                    // w0 = wx[ix0] wy[iy0], w1 = wx[jx1] wy[jy1] (float32
+                    // products), then one fused multiply-add per sum as before
+                    const float2 w = __fmul2_rn(make_float2(wx[ix0], wx[jx1]),
+                                                make_float2(wy[iy0], wy[jy1]));
+                    if (!RESIDUAL) pp = __ffma2_rn(make_float2(pw, pw), w, pp);
+                    ri0 = __ffma2_rn(B, make_float2(w.x, w.x), ri0);
+                    ri1 = __ffma2_rn(B, make_float2(w.y, w.y), ri1);
                 }
                 __syncwarp();   // the slots are refilled by the next batch
             }
@@ -827,8 +826,7 @@ struct CubeDegridArgs {
 template <bool RESIDUAL>
 __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArgs a) {
     constexpr int kFoot = kTile + 6;
-    __shared__ float s_re[kFoot * kRow];
-    __shared__ float s_im[kFoot * kRow];
+    __shared__ float2 s_g[kFoot * kRow];   // model footprint, (re, im) pairs
     __shared__ float s_taps[kMaxTapRows * 7];
     __shared__ int s_item;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -852,13 +850,12 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
             const int64_t x = gx0 + fx, y = gy0 + fy;
             float2 v = make_float2(0.0f, 0.0f);
             if (x < a.gnx && y < a.gny) v = __ldg(&g[x * a.gny + y]);
-            s_re[fx * kRow + fy] = v.x;
-            s_im[fx * kRow + fy] = v.y;
+            s_g[fx * kRow + fy] = v;
         }
         __syncthreads();
         for (uint32_t base = lo + warp * 4; base < hi; base += kCubeThreads / 8) {
             const uint32_t k = base + sub;
-            float re = 0.0f, im = 0.0f;
+            float2 acc = make_float2(0.0f, 0.0f);   // (re, im), paired FMAs
             uint32_t sample = 0;
             uint4 q = make_uint4(0u, 0u, 0u, 0u);
             if (k < hi) {
@@ -869,14 +866,15 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
                     const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
                     const float* wy = s_taps + (meta & 2047u) * 7;
                     const int row = ((int)(meta >> 27) + ix) * kRow + (int)((meta >> 22) & 31);
+                    const float wxi = wx[ix];
 #pragma unroll
                     for (int iy = 0; iy < 7; ++iy) {
-                        const float wgt = __fmul_rn(wx[ix], wy[iy]);
-                        re = fmaf(s_re[row + iy], wgt, re);
-                        im = fmaf(s_im[row + iy], wgt, im);
+                        const float wgt = __fmul_rn(wxi, wy[iy]);
+                        acc = __ffma2_rn(s_g[row + iy], make_float2(wgt, wgt), acc);
                     }
                 }
             }
+            float re = acc.x, im = acc.y;
 #pragma unroll
             for (int o = 4; o > 0; o >>= 1) {
                 re += __shfl_xor_sync(0xffffffffu, re, o);
