@@ -52,6 +52,7 @@ struct CubeChan {
     double lscale;       // f / c
     FixScale kx, ky;     // lscale / du, lscale / dv
     FixScale kdx, kdy;   // lscale * nx cell_x, lscale * ny cell_y
+    DfScale fx, fy, fdx, fdy;   // the same four as float32 pairs
 };
 
 struct CubeArgs {
@@ -59,6 +60,7 @@ struct CubeArgs {
     int32_t C;
     const double* u;
     const double* v;
+    const float4* uvdf;        // per row (u_hi, u_lo, v_hi, v_lo); NaN u_hi: exact path only
     const CubeChan* ch;
     const float2* vis;
     const float* weight;
@@ -89,6 +91,39 @@ struct CubeArgs {
     uint32_t* ev_meta;         // cell in tile | tap rows
     float* ev_w;               // imaging weight
 };
+
+// Rows' u, v as float32 pairs for the fast path.  Rows whose coordinates are
+// not finite, exceed 2^60 or are below 2^-60 (but not zero) get a NaN u_hi
+// and always take the integer path.
+__global__ void cube_rows_df_kernel(const double* u, const double* v, int64_t R, float4* out) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < R;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const double um = u[r], vm = v[r];
+        const bool ok = isfinite(um) && isfinite(vm) && fabs(um) < 0x1p60 &&
+                        fabs(vm) < 0x1p60 && (um == 0.0 || fabs(um) > 0x1p-60) &&
+                        (vm == 0.0 || fabs(vm) > 0x1p-60);
+        const float uh = __double2float_rn(um), vh = __double2float_rn(vm);
+        const float ul = __double2float_rn(__dsub_rn(um, (double)uh));
+        const float vl = __double2float_rn(__dsub_rn(vm, (double)vh));
+        out[r] = ok ? make_float4(uh, ul, vh, vl) : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+    }
+}
+
+// The density cell (x, y) of x = s_x p_x + e_x + nx/2 (valid when 1 <= x <
+// nx, likewise y) on the float32-pair path; false when undecided.
+__device__ __forceinline__ bool df_density_cell(float px, float ex, float py, float ey,
+                                                int32_t nx, int32_t ny, int* x, int* y,
+                                                bool* ok) {
+    float ax, ay, dh;
+    if (!df_nearest(px, ex, (nx & 1) ? 0.5f : 0.0f, &ax, &dh) ||
+        !df_nearest(py, ey, (ny & 1) ? 0.5f : 0.0f, &ay, &dh))
+        return false;
+    const int cx = (nx >> 1) + (int)ax, cy = (ny >> 1) + (int)ay;
+    *ok = !(cx <= 0 || cy <= 0 || cx >= nx || cy >= ny);
+    *x = cx;
+    *y = cy;
+    return true;
+}
 
 // Both density cells of a sample, of (u, v) and of the mirror (-u, -v),
 // from one pair of fixed-point products (FP64 fallback per cell).
@@ -174,7 +209,7 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
                                              int c, int64_t row0, int64_t r1,
                                              Eval (&e)[kVec]) {
     float w[kVec];
-    double um[kVec], vm[kVec];
+    float4 uv[kVec];
     bool live[kVec];
 #pragma unroll
     for (int j = 0; j < kVec; ++j) {
@@ -184,8 +219,7 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
         const int64_t i = (int64_t)c * a.R + (live[j] ? r : 0);
         if (live[j] && a.flags) live[j] = a.flags[i] == 0;
         w[j] = a.weight ? a.weight[i] : 1.0f;
-        um[j] = a.u[live[j] ? r : 0];
-        vm[j] = a.v[live[j] ? r : 0];
+        uv[j] = a.uvdf[live[j] ? r : 0];
     }
     if (a.mode != CR_WEIGHT_NATURAL) {
         float d[kVec];
@@ -202,7 +236,8 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
             for (int j = 0; j < kVec; ++j) {
                 int x, y;
                 d[j] = 0.0f;
-                if (live[j] && density_cell(a, ch, um[j], vm[j], false, &x, &y))
+                const int64_t r = row0 + 32 * j;
+                if (live[j] && density_cell(a, ch, a.u[r], a.v[r], false, &x, &y))
                     d[j] = dens[(int64_t)x * a.ny + y];
             }
         }
@@ -221,15 +256,22 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
         if (!live[j] || !(finite_f(w[j]) && w[j] > 0.0f)) continue;
         int64_t x0 = 0, y0 = 0;
         int32_t rx = 0, ry = 0;
-        int sx = -1, sy = -1;
+        // float32 pairs first: x = u K_x + G/2, y = -v K_y + G/2
+        float px, ex, py, ey;
+        df_product(uv[j].x, uv[j].y, ch.fx, &px, &ex);
+        df_product(-uv[j].z, -uv[j].w, ch.fy, &py, &ey);
+        int sx = df_tap_span(px, ex, a.gnx, a.os, a.tap_rows, &x0, &rx);
+        int sy = sx == 0 ? 0 : df_tap_span(py, ey, a.gny, a.os, a.tap_rows, &y0, &ry);
+        if (sx == 0 || sy == 0) continue;
+        const int64_t r = row0 + 32 * j;
         long long tx, ty;
-        if (fix_mul(um[j], ch.kx, &tx) && fix_mul(vm[j], ch.ky, &ty)) {
+        if ((sx < 0 || sy < 0) && fix_mul(a.u[r], ch.kx, &tx) && fix_mul(a.v[r], ch.ky, &ty)) {
             sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
             if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
             if (sx == 0 || sy == 0) continue;
         }
         if (sx < 0 || sy < 0) {
-            const double u = __dmul_rn(um[j], ch.lscale), v = __dmul_rn(vm[j], ch.lscale);
+            const double u = __dmul_rn(a.u[r], ch.lscale), v = __dmul_rn(a.v[r], ch.lscale);
             const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
             const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
             if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
@@ -253,7 +295,7 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs 
     float* dens = a.density + (int64_t)c * a.nx * a.ny;
     for (int64_t base = r0 + warp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
         float w[kVec];
-        double um[kVec], vm[kVec];
+        float4 uv[kVec];
         bool live[kVec];
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
@@ -262,8 +304,7 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs 
             const int64_t i = (int64_t)c * a.R + (live[j] ? r : 0);
             if (live[j] && a.flags) live[j] = a.flags[i] == 0;
             w[j] = a.weight ? a.weight[i] : 1.0f;
-            um[j] = a.u[live[j] ? r : 0];
-            vm[j] = a.v[live[j] ? r : 0];
+            uv[j] = a.uvdf[live[j] ? r : 0];
         }
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
@@ -272,7 +313,14 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs 
             if (live[j]) {
                 int x = 0, y = 0, xm = 0, ym = 0;
                 bool ok = false, okm = false;
-                density_cells(a, ch, um[j], vm[j], &x, &y, &ok, &xm, &ym, &okm);
+                // float32 pairs first: (u, v) -> x = u s_x + nx/2, y = -v s_y + ny/2;
+                // the mirror negates both products
+                float px, ex, py, ey;
+                df_product(uv[j].x, uv[j].y, ch.fdx, &px, &ex);
+                df_product(-uv[j].z, -uv[j].w, ch.fdy, &py, &ey);
+                if (!df_density_cell(px, ex, py, ey, a.nx, a.ny, &x, &y, &ok) ||
+                    !df_density_cell(-px, -ex, -py, -ey, a.nx, a.ny, &xm, &ym, &okm))
+                    density_cells(a, ch, a.u[r], a.v[r], &x, &y, &ok, &xm, &ym, &okm);
                 const bool pos = finite_f(w[j]) && w[j] > 0.0f;
                 if (ok) {
                     cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
@@ -941,6 +989,10 @@ void cube_upload_channels(cr_ctx* ctx, cr_gridder* g, const CubeInput& in) {
         chh[c].ky = fix_scale_of(s, gi.dv, false);
         chh[c].kdx = fix_scale_of(s, dus, true);
         chh[c].kdy = fix_scale_of(s, dvs, true);
+        chh[c].fx = df_scale_of(s, gi.du, false);
+        chh[c].fy = df_scale_of(s, gi.dv, false);
+        chh[c].fdx = df_scale_of(s, dus, true);
+        chh[c].fdy = df_scale_of(s, dvs, true);
     }
     CubeChan* chd = (CubeChan*)workspace(ctx, "cube_chan", chh.size() * sizeof(CubeChan));
     CR_CUDA_CHECK(cudaMemcpyAsync(chd, chh.data(), chh.size() * sizeof(CubeChan),
@@ -1026,6 +1078,13 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     a.rec_w = cr.rec_w;
     const dim3 grid((unsigned)std::max<int64_t>((in.R + kRowsPerBlock - 1) / kRowsPerBlock, 1),
                     (unsigned)in.C);
+    float4* uvdf = (float4*)workspace(ctx, "cube_uvdf", (size_t)std::max<int64_t>(in.R, 1) * 16);
+    if (in.R > 0) {
+        cube_rows_df_kernel<<<grid_blocks(in.R, 256), 256, 0, ctx->stream>>>(in.u, in.v, in.R,
+                                                                             uvdf);
+        note_launch(ctx, "cube_rows_df_kernel");
+    }
+    a.uvdf = uvdf;
     a.ev_tile = (uint32_t*)workspace(ctx, "cube_ev_tile", ns * 4);
     a.ev_meta = (uint32_t*)workspace(ctx, "cube_ev_meta", ns * 4);
     a.ev_w = (float*)workspace(ctx, "cube_ev_w", ns * 4);

@@ -111,6 +111,82 @@ __device__ __forceinline__ int fix_tap_span(long long X, int64_t size, int32_t o
     return 1;
 }
 
+// ---- float32-pair fast path ---------------------------------------------------
+// Before the integer path, the same decisions are tried in float32 pairs:
+// a = ah + al (ah = RN32(a), al = RN32(a - ah)) and K = kh + kl, both to
+// about 2^-48 relative; the product a K is then p + e with p = RN(ah kh),
+// e = fma(ah, kh, -p) + ah kl + al kh (three FMAs), about 2^-44 |a K| from
+// the exact value.  A decision is taken only when the exact value lies more
+// than kDfMargin (in the decision's own units: cells for the anchor,
+// oversampled cells for the offset) from its boundaries.  With |x| < 2^20
+// the pair's error (below 2^-14 after the offset's scaling by os <= 512)
+// and the reference's own FP64 error (below 2^-38) are far inside the
+// margin, so the decision equals the FP64 one.  Otherwise (about one
+// decision in 2^11) the caller takes the integer path.
+constexpr float kDfMargin = 1.0f / 4096.0f;
+constexpr float kDfLimit = 1048576.0f;   // |p| < 2^20
+
+struct DfScale {
+    float hi, lo;
+};
+
+// K = num / den (or num * den), as a float32 pair.
+inline DfScale df_scale_of(double num, double den, bool multiply) {
+    long double k = multiply ? (long double)num * (long double)den
+                             : (long double)num / (long double)den;
+    DfScale s{0.0f, 0.0f};
+    if (!std::isfinite((double)k)) return s;
+    s.hi = (float)k;
+    s.lo = (float)(k - (long double)s.hi);
+    return s;
+}
+
+__device__ __forceinline__ void df_product(float ah, float al, DfScale k, float* p, float* e) {
+    const float ph = __fmul_rn(ah, k.hi);
+    float er = __fmaf_rn(ah, k.hi, -ph);
+    er = __fmaf_rn(ah, k.lo, er);
+    er = __fmaf_rn(al, k.hi, er);
+    *p = ph;
+    *e = er;
+}
+
+// The integer a nearest to x = p + e + h (h = 0 or 1/2) and dh = RN(p + h) - a
+// (exact), or false when x is within the margin of a half-integer, is
+// large, or is not finite.
+__device__ __forceinline__ bool df_nearest(float p, float e, float h, float* a, float* dh) {
+    if (!(fabsf(p) < kDfLimit)) return false;
+    const float q = __fadd_rn(p, h);
+    const float r = rintf(q);
+    const float d = __fadd_rn(__fsub_rn(q, r), e);
+    if (!(fabsf(fabsf(d) - 0.5f) > kDfMargin)) return false;
+    float n = r;
+    if (d > 0.5f) n = r + 1.0f;
+    if (d < -0.5f) n = r - 1.0f;
+    *a = n;
+    *dh = __fsub_rn(q, n);
+    return true;
+}
+
+// sample_tap_span of x = p + e + size / 2 (the grid coordinate): 1 =
+// accepted, 0 = rejected, -1 = undecided (take the integer path).
+__device__ __forceinline__ int df_tap_span(float p, float e, int64_t size, int32_t os,
+                                           int32_t rows, int64_t* start, int32_t* row) {
+    float a, dh;
+    if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return -1;
+    const int64_t anchor = (size >> 1) + (int64_t)a;
+    if (anchor - 3 < 0 || anchor + 3 >= size) return 0;
+    // offset round((anchor - x) os) = round(-(dh + e) os)
+    const float osf = (float)os;
+    const float v = -__fmaf_rn(dh, osf, __fmul_rn(e, osf));
+    const float o = rintf(v);
+    if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return -1;
+    const int64_t idx = (int64_t)o + os / 2;
+    if (idx < 0 || idx >= rows) return 0;
+    *start = anchor - 3;
+    *row = (int32_t)idx;
+    return 1;
+}
+
 // sample_tap_span in the reference's FP64 operations.
 __device__ __forceinline__ bool f64_tap_span(double coord, int64_t size, int32_t os,
                                              int32_t rows, int64_t* start, int32_t* row) {
