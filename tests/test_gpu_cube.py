@@ -235,3 +235,37 @@ def test_cube_graph_replay_matches_eager_calls(ctx, cube):
         assert t["grid_ms"] > 0
     gg_e.close()
     ctx_e.close()
+
+
+def test_cube_density_boundary_samples_take_the_oracle_cells(ctx):
+    """Samples on and one ulp around density-cell boundaries (odd image
+    size, so the centre is a half-integer): uniform weights, which divide by
+    each sample's density cell, agree bit-exactly with the oracle."""
+    nx = 129
+    cell = 2.0e-5
+    geom = O.Geometry(nx, nx, cell, cell)
+    ls = np.array([1.0e9, 1.37e9, 1.9e9]) / S.C_LIGHT
+    dus = nx * cell
+    xs = [b + k * 2.0 ** -20 for k in (-1, 0, 1) for b in (5.5, 40.5, 64.0, 90.5, nx - 1.5)]
+    um = []
+    for x in xs:
+        base = (x - nx / 2.0) / (ls[1] * dus)
+        for _ in range(3):
+            um.append(base)
+            base = np.nextafter(base, np.inf)
+    um = np.array(um)
+    rng = np.random.default_rng(2)
+    um = np.concatenate([um, rng.uniform(-0.4, 0.4, 200) / (ls[1] * cell)])
+    vm = np.random.default_rng(3).permutation(um)
+    R = len(um)
+    vis = np.ones((len(ls), R), np.complex64)
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(nx, nx, cell, cell), OS)
+    sx, sy, rx, ry, wt = cc.cube_sample_taps(gg, cc.CubeBatch(um, vm, ls, vis), "uniform")
+    og = O.StdGridder(geom, OS)
+    for c in range(len(ls)):
+        u, v = um * ls[c], vm * ls[c]
+        wo, _, _ = O.apply_weighting(geom, u, v, np.ones(R, np.float32), "uniform", 0.0,
+                                     convention=1)
+        ox, _, _, _ = og.plan_many(u, v)
+        np.testing.assert_array_equal(wt[c], np.where((ox >= 0) & (wo > 0), wo, 0.0)
+                                      .astype(np.float32))
