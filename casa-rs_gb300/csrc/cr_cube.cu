@@ -485,13 +485,14 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
     const int lane = threadIdx.x & 31;
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
-    // warp-uniform trip counts so that the warp-aggregated atomics see whole warps
     const int wp = threadIdx.x >> 5;
     for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
         // loads first, then every cursor atomic, then the stores: the kVec
-        // atomics of a thread are in flight together
-        uint32_t tile[kVec], meta[kVec], pos0[kVec];
-        unsigned peers[kVec];
+        // atomics of a thread are in flight together.  (The samples of a
+        // warp -- consecutive rows of one channel, different baselines --
+        // almost never share a cell bin, so the atomics are not aggregated:
+        // a warp match cost more than it saved.)
+        uint32_t tile[kVec], meta[kVec], pos[kVec];
         float w[kVec];
         float2 vv[kVec];
 #pragma unroll
@@ -505,30 +506,22 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
         }
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
-            const bool ok = tile[j] != ~0u;
-            const unsigned act = __ballot_sync(0xffffffffu, ok);
-            peers[j] = 0u;
-            pos0[j] = 0u;
-            if (!ok) continue;
-            const int64_t bin = cell_bin(c, ntiles, tile[j], meta[j]);
-            peers[j] = __match_any_sync(act, (unsigned long long)bin);
-            if (lane == __ffs(peers[j]) - 1)
-                pos0[j] = atomicAdd(&a.cursor[bin], (uint32_t)__popc(peers[j]));
+            pos[j] = 0u;
+            if (tile[j] != ~0u)
+                pos[j] = atomicAdd(&a.cursor[cell_bin(c, ntiles, tile[j], meta[j])], 1u);
         }
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
             if (tile[j] == ~0u) continue;
-            const int leader = __ffs(peers[j]) - 1;
-            const uint32_t pos = __shfl_sync(peers[j], pos0[j], leader) +
-                                 __popc(peers[j] & ((1u << lane) - 1u));
             const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
             float vr = 0.0f, vi = 0.0f;
             if (finite_f(vv[j].x) && finite_f(vv[j].y)) {
                 vr = __fmul_rn(vv[j].x, w[j]);
                 vi = __fmul_rn(vv[j].y, w[j]);
             }
-            a.rec[pos] = make_uint4(meta[j], (uint32_t)i, __float_as_uint(vr), __float_as_uint(vi));
-            a.rec_w[pos] = w[j];
+            a.rec[pos[j]] = make_uint4(meta[j], (uint32_t)i, __float_as_uint(vr),
+                                       __float_as_uint(vi));
+            a.rec_w[pos[j]] = w[j];
         }
     }
 }
