@@ -47,6 +47,17 @@ class CubeBatch(C.Structure):
                 ("location", _i32)]
 
 
+class RowRuns(C.Structure):
+    _fields_ = [("rows", _i64), ("channels", _i32), ("correlations", _i32), ("uvw_m", _p),
+                ("lambda_scale", _p), ("data", _p), ("flag", _p), ("weight", _p),
+                ("weight_spectrum", _p), ("gridable", _p), ("location", _i32)]
+
+
+class Polarization(C.Structure):
+    _fields_ = [("mode", _i32), ("corr0", _i32), ("corr1", _i32), ("transform", _i32),
+                ("sumwt_factor", _f)]
+
+
 class Beam(C.Structure):
     _fields_ = [("major_fwhm_rad", _d), ("minor_fwhm_rad", _d), ("position_angle_rad", _d)]
 
@@ -132,6 +143,11 @@ SIGNATURES = {
     "cr_adjoint": (C.c_int, [_p, _p, _p, C.POINTER(VisBatch), _p, _i32, _err]),
     "cr_apply_weighting": (C.c_int, [_p, _p, C.POINTER(VisBatch), _i32, _f, _p, _i32,
                                      C.POINTER(_f), _err]),
+    "cr_row_runs_prepare": (C.c_int, [_p, C.POINTER(RowRuns), C.POINTER(Polarization), _p, _p, _p,
+                                       _p, _p, _p, _p, _p, _p, _i32, C.POINTER(_i64), _err]),
+    "cr_polarization_for_plane": (C.c_int, [_i32, _p, _i32, C.POINTER(Polarization), _err]),
+    "cr_apply_weighting_rows": (C.c_int, [_p, _p, C.POINTER(VisBatch), _p, _p, _i32, _f, _p, _i32,
+                                          _p, _err]),
     "cr_apply_weighting_plane": (C.c_int, [_p, _p, C.POINTER(VisBatch), _i32, _f, _p, _i32,
                                      C.POINTER(_f), _err]),
     "cr_hogbom": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64, _i32,

@@ -574,6 +574,138 @@ def apply_weighting(gridder, batch: VisibilityBatch, mode: str = "natural",
 
 
 # ----------------------------------------------------------------------------
+# row runs (MeasurementSet-shaped rows)
+# ----------------------------------------------------------------------------
+PLANES = {"I": 0, "Q": 1, "U": 2, "V": 3, "XX": 4, "YY": 5, "RR": 6, "LL": 7}
+PAIR_TRANSFORMS = {"half_sum": 0, "half_difference": 1, "positive_half_imag_difference": 2,
+                   "negative_half_imag_difference": 3}
+
+
+@dataclass
+class Polarization:
+    """StandardMfsVisibilityPolarization (types.rs:1612-1632): one explicit
+    correlation (corr1 None) or a collapsed pair with a transform."""
+    corr0: int
+    corr1: Optional[int] = None
+    transform: str = "half_sum"
+    sumwt_factor: float = 1.0
+
+    def to_c(self) -> _lib.Polarization:
+        if self.corr1 is None:
+            return _lib.Polarization(0, self.corr0, self.corr0, 0, self.sumwt_factor)
+        return _lib.Polarization(1, self.corr0, self.corr1, PAIR_TRANSFORMS[self.transform],
+                                 self.sumwt_factor)
+
+    @staticmethod
+    def for_plane(plane: str, corr_types) -> "Polarization":
+        """derive_pair_selection / paired_sumwt_factor (types.rs:62-138) from
+        CASA correlation codes (RR=5 .. LL=8, XX=9 .. YY=12)."""
+        ct = np.ascontiguousarray(np.asarray(corr_types, np.int32))
+        out = _lib.Polarization()
+        call("cr_polarization_for_plane", PLANES[plane], ct.ctypes.data, len(ct), C.byref(out))
+        inv = {v: k for k, v in PAIR_TRANSFORMS.items()}
+        if out.mode == 0:
+            return Polarization(int(out.corr0), None, "half_sum", float(out.sumwt_factor))
+        return Polarization(int(out.corr0), int(out.corr1), inv[int(out.transform)],
+                            float(out.sumwt_factor))
+
+
+@dataclass
+class RowRuns:
+    """StandardMfsVisibilityRow (types.rs:1639-1662) for many rows: uvw in
+    metres [R][3], DATA / FLAG / WEIGHT_SPECTRUM [R][C][corr], WEIGHT
+    [R][corr], optional per-row gridable; lambda_scale[c] = f_c / c."""
+    uvw_m: object
+    lambda_scale: object
+    data: object
+    flag: object = None
+    weight: object = None
+    weight_spectrum: object = None
+    gridable: object = None
+
+    def _bind(self, arrs: _Arrays) -> _lib.RowRuns:
+        r = _lib.RowRuns()
+        shape = tuple(self.data.shape)
+        if len(shape) != 3:
+            raise ValueError("data must be [rows][channels][correlations]")
+        r.rows, r.channels, r.correlations = shape
+        r.uvw_m = arrs.ptr(self.uvw_m, np.float64, torch.float64 if torch else None,
+                           (shape[0], 3))
+        ls = np.ascontiguousarray(np.asarray(
+            self.lambda_scale.cpu() if _is_torch(self.lambda_scale) else self.lambda_scale,
+            np.float64))
+        if ls.shape != (shape[1],):
+            raise ValueError("lambda_scale must have one entry per channel")
+        arrs.keep.append(ls)
+        r.lambda_scale = ls.ctypes.data
+        r.data = arrs.ptr(self.data, np.complex64, torch.complex64 if torch else None, shape)
+        flag = self.flag
+        if flag is not None and _is_torch(flag) and flag.dtype == torch.bool:
+            flag = flag.to(torch.uint8)
+        r.flag = arrs.ptr(flag, np.uint8, torch.uint8 if torch else None, shape)
+        r.weight = arrs.ptr(self.weight, np.float32, torch.float32 if torch else None,
+                            (shape[0], shape[2]))
+        r.weight_spectrum = arrs.ptr(self.weight_spectrum, np.float32,
+                                     torch.float32 if torch else None, shape)
+        g = self.gridable
+        if g is not None and _is_torch(g) and g.dtype == torch.bool:
+            g = g.to(torch.uint8)
+        r.gridable = arrs.ptr(g, np.uint8, torch.uint8 if torch else None, (shape[0],))
+        r.location = CR_HOST if arrs.location is None else arrs.location
+        return r
+
+
+def prepare_row_runs(ctx: Context, runs: RowRuns, pol: Polarization):
+    """The row path's samples (routed_weighted_grid_sample_from_run,
+    lib.rs:880-1062) as (VisibilityBatch, density_u, density_v): kept
+    (row, channel) samples in that order, with the VisImagingWeight density
+    coordinates of the row path (weighting.rs:748-756)."""
+    arrs = _Arrays()
+    rr = runs._bind(arrs)
+    dev = _device_of(runs.data, runs.uvw_m)
+    if arrs.location == CR_DEVICE:
+        ctx.use_torch_stream()
+    else:
+        ctx.use_own_stream()
+    n = rr.rows * rr.channels
+    outs = {}
+    for name, npdt, tdt in (("u", np.float64, "float64"), ("v", np.float64, "float64"),
+                            ("w", np.float64, "float64"), ("weight", np.float32, "float32"),
+                            ("sumwt_factor", np.float32, "float32"), ("gridable", np.uint8, "uint8"),
+                            ("vis", np.complex64, "complex64"), ("du", np.float64, "float64"),
+                            ("dv", np.float64, "float64")):
+        outs[name] = arrs.out((n,), npdt, getattr(torch, tdt) if torch else None, dev)
+    k = C.c_int64()
+    p = pol.to_c()
+    call("cr_row_runs_prepare", ctx.handle, C.byref(rr), C.byref(p),
+         *[outs[x][1] for x in ("u", "v", "w", "weight", "sumwt_factor", "gridable", "vis",
+                                "du", "dv")], outs["u"][2], C.byref(k))
+    m = int(k.value)
+    a = {x: outs[x][0][:m] for x in outs}
+    batch = VisibilityBatch(a["u"], a["v"], a["vis"], a["weight"], a["w"], a["sumwt_factor"],
+                            a["gridable"])
+    return batch, a["du"], a["dv"]
+
+
+def apply_weighting_rows(gridder, batch: VisibilityBatch, density_u, density_v,
+                         mode: str = "natural", robust: float = 0.0):
+    """Weighting of a row-path batch: density built at (density_u,
+    density_v), looked up at the batch's u, v (the streaming weighting plan,
+    weighting.rs:333-380, 646-746).  Returns the imaging weights and f2."""
+    arrs = _Arrays()
+    b = batch._bind(arrs, False)
+    du = arrs.ptr(density_u, np.float64, torch.float64 if torch else None)
+    dv = arrs.ptr(density_v, np.float64, torch.float64 if torch else None)
+    _prepare(gridder, arrs)
+    out, op, loc = arrs.out((len(batch),), np.float32, torch.float32 if torch else None,
+                            _device_of(batch.u_lambda))
+    f2 = C.c_float()
+    call("cr_apply_weighting_rows", gridder.ctx.handle, gridder.handle, C.byref(b), du, dv,
+         WEIGHTING_MODES[mode], float(robust), op, loc, C.byref(f2))
+    return out, float(f2.value)
+
+
+# ----------------------------------------------------------------------------
 # batched spectral cube
 # ----------------------------------------------------------------------------
 SPEED_OF_LIGHT_M_PER_S = 299_792_458.0

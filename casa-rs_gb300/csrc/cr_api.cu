@@ -914,6 +914,110 @@ int cr_apply_weighting_plane(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* bat
                                 err);
 }
 
+int cr_apply_weighting_rows(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch,
+                            const double* density_u, const double* density_v, int32_t mode,
+                            float robust, float* out_weight, int32_t out_location, float* f2,
+                            char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr, "null argument");
+        bind(ctx);
+        DeviceBatch b = device_batch(ctx, batch, false);
+        const size_t n = (size_t)b.n;
+        need(b.n == 0 || (density_u && density_v), "density coordinates are null");
+        const double* du = (const double*)device_input(ctx, density_u, n * 8, batch->location,
+                                                       "density_u");
+        const double* dv = (const double*)device_input(ctx, density_v, n * 8, batch->location,
+                                                       "density_v");
+        float* out = out_ptr<float>(ctx, out_weight, out_location, n * 4 + 4, "weights");
+        apply_weighting(ctx, g, b, mode, robust, out, f2, 0, du, dv);
+        if (out_location == CR_HOST) copy_out(ctx, out_weight, out, n * 4, CR_HOST);
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int cr_row_runs_prepare(cr_ctx* ctx, const cr_row_runs* runs, const cr_polarization* pol,
+                        double* u, double* v, double* w, float* weight, float* sumwt_factor,
+                        uint8_t* gridable, float* vis, double* density_u, double* density_v,
+                        int32_t out_location, int64_t* n_out, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && runs != nullptr && pol != nullptr && n_out != nullptr,
+             "null argument");
+        bind(ctx);
+        need(runs->rows >= 0 && runs->channels > 0, "row runs need rows >= 0 and channels > 0");
+        const size_t n = (size_t)runs->rows * (size_t)runs->channels;
+        StageTimer tm(ctx);
+        tm.mark();
+        RowsOut o;
+        o.u = out_ptr<double>(ctx, u, out_location, n * 8 + 8, "rr_u");
+        o.v = out_ptr<double>(ctx, v, out_location, n * 8 + 8, "rr_v");
+        o.w = out_ptr<double>(ctx, w, out_location, n * 8 + 8, "rr_w");
+        o.du = out_ptr<double>(ctx, density_u, out_location, n * 8 + 8, "rr_du");
+        o.dv = out_ptr<double>(ctx, density_v, out_location, n * 8 + 8, "rr_dv");
+        o.weight = out_ptr<float>(ctx, weight, out_location, n * 4 + 4, "rr_wt");
+        o.sumwt_factor = out_ptr<float>(ctx, sumwt_factor, out_location, n * 4 + 4, "rr_sf");
+        o.gridable = out_ptr<uint8_t>(ctx, gridable, out_location, n + 1, "rr_grd");
+        o.vis = out_ptr<float2>(ctx, vis, out_location, n * 8 + 8, "rr_vis");
+        const int64_t k = prepare_rows(ctx, runs, pol, o);
+        tm.mark();
+        if (out_location == CR_HOST) {
+            const size_t m = (size_t)k;
+            copy_out(ctx, u, o.u, m * 8, CR_HOST);
+            copy_out(ctx, v, o.v, m * 8, CR_HOST);
+            copy_out(ctx, w, o.w, m * 8, CR_HOST);
+            copy_out(ctx, density_u, o.du, m * 8, CR_HOST);
+            copy_out(ctx, density_v, o.dv, m * 8, CR_HOST);
+            copy_out(ctx, weight, o.weight, m * 4, CR_HOST);
+            copy_out(ctx, sumwt_factor, o.sumwt_factor, m * 4, CR_HOST);
+            copy_out(ctx, gridable, o.gridable, m, CR_HOST);
+            copy_out(ctx, vis, o.vis, m * 8, CR_HOST);
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        }
+        *n_out = k;
+        set_timings(ctx, cr_timings{tm.between(0, 1), 0.f, 0.f, 0.f, 0.f});
+    });
+}
+
+int cr_polarization_for_plane(int32_t plane, const int32_t* corr_types, int32_t correlations,
+                              cr_polarization* out, char** err) {
+    return guarded(err, [&] {
+        need(out != nullptr && (correlations == 0 || corr_types != nullptr), "null argument");
+        need(plane >= 0 && plane <= 7, "plane must be 0..7");
+        auto find = [&](int32_t code) {
+            for (int32_t k = 0; k < correlations; ++k)
+                if (corr_types[k] == code) return k;
+            return -1;
+        };
+        // the pairs of derive_pair_selection: (first, second) codes
+        const int32_t xx = find(9), yy = find(12), xy = find(10), yx = find(11);
+        const int32_t rr = find(5), ll = find(8), rl = find(6), lr = find(7);
+        cr_polarization p{1, -1, -1, 0, plane == 0 ? 2.0f : 1.0f};
+        auto pick = [&](int32_t a, int32_t b, int32_t transform) {
+            if (a < 0 || b < 0) return false;
+            p.corr0 = a;
+            p.corr1 = b;
+            p.transform = transform;
+            return true;
+        };
+        bool ok = false;
+        switch (plane) {
+            case 0: ok = pick(xx, yy, 0) || pick(rr, ll, 0); break;
+            case 1: ok = pick(xx, yy, 1) || pick(rl, lr, 0); break;
+            case 2: ok = pick(xy, yx, 0) || pick(rl, lr, 2); break;
+            case 3: ok = pick(xy, yx, 3) || pick(rr, ll, 1); break;
+            default: {
+                const int32_t codes[4] = {9, 12, 5, 8};   // XX, YY, RR, LL
+                const int32_t k = find(codes[plane - 4]);
+                if (k >= 0) {
+                    p = cr_polarization{0, k, k, 0, 1.0f};
+                    ok = true;
+                }
+            }
+        }
+        if (!ok) fail(CR_INVALID, "the correlations cannot form this plane");
+        *out = p;
+    });
+}
+
 int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
               int32_t nx, int32_t ny, int32_t location, float gain, float threshold,
               float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,

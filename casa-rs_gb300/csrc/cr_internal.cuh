@@ -151,6 +151,19 @@ const void* device_input(cr_ctx* ctx, const void* p, size_t bytes, int32_t locat
                          const char* name);
 void copy_out(cr_ctx* ctx, void* dst, const void* src_dev, size_t bytes, int32_t location);
 
+// ---- row runs -------------------------------------------------------------------
+struct RowsOut {
+    double *u, *v, *w, *du, *dv;
+    float* weight;
+    float* sumwt_factor;
+    uint8_t* gridable;
+    float2* vis;
+};
+// Kept samples of the row runs into `out` (device arrays of rows x channels
+// entries); returns their count (synchronises).
+int64_t prepare_rows(cr_ctx* ctx, const cr_row_runs* rr, const cr_polarization* pol,
+                     const RowsOut& out);
+
 // ---- records: the deduplicated sample plan ------------------------------------
 // Samples with identical (cell, kernel offset, w-plane, conjugation) get
 // identical taps; they are summed into one record before gridding.
@@ -294,8 +307,11 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
                  int32_t sampling, int32_t support_min, int32_t support_max);
 
 // ---- weighting / Hogbom ----------------------------------------------------------
+// build_u / build_v (device, optional): where the density is built, when
+// that differs from the lookup coordinates u, v (the row path).
 void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t mode,
-                     float robust, float* out_weight, float* f2_out, int32_t convention = 0);
+                     float robust, float* out_weight, float* f2_out, int32_t convention = 0,
+                     const double* build_u = nullptr, const double* build_v = nullptr);
 void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
             int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,

@@ -109,7 +109,8 @@ __global__ void reweight_kernel(const double* u, const double* v, const float* w
 }  // namespace
 
 void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t mode,
-                     float robust, float* out_weight, float* f2_out, int32_t convention) {
+                     float robust, float* out_weight, float* f2_out, int32_t convention,
+                     const double* build_u, const double* build_v) {
     if (mode != CR_WEIGHT_NATURAL && mode != CR_WEIGHT_UNIFORM && mode != CR_WEIGHT_BRIGGS)
         fail(CR_INVALID, "unknown weighting mode");
     const int32_t nx = g->geom.nx, ny = g->geom.ny;
@@ -131,8 +132,10 @@ void apply_weighting(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, int32_t m
         density = (float*)workspace(ctx, "wt_density", (size_t)nx * ny * 4);
         CR_CUDA_CHECK(cudaMemsetAsync(density, 0, (size_t)nx * ny * 4, ctx->stream));
         if (b.n > 0) {
-            density_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(b.u, b.v, b.weight, b.n,
-                                                                           p, density);
+            // the density is built at build_u, build_v when given (the row
+            // path's VisImagingWeight coordinates), looked up at u, v
+            density_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(
+                build_u ? build_u : b.u, build_v ? build_v : b.v, b.weight, b.n, p, density);
             note_launch(ctx, "density_kernel");
         }
         if (mode == CR_WEIGHT_BRIGGS) {

@@ -100,6 +100,37 @@ typedef struct {
     int32_t location;         /* CR_HOST or CR_DEVICE */
 } cr_vis_batch;
 
+/* Row-shaped visibilities (StandardMfsVisibilityRow, types.rs:1639-1662):
+ * per row its uvw in metres and [channels][correlations] DATA, FLAG and
+ * (optional) WEIGHT_SPECTRUM, plus [correlations] WEIGHT and an optional
+ * per-row gridable flag.  lambda_scale[c] = channel frequency / c is host
+ * memory; the other arrays are at `location`.  Arrays are row-major:
+ * data[(row * channels + channel) * correlations + corr]. */
+typedef struct {
+    int64_t rows;
+    int32_t channels;
+    int32_t correlations;
+    const double* uvw_m;            /* [rows][3] */
+    const double* lambda_scale;     /* host [channels] */
+    const float* data;              /* complex64 [rows][channels][correlations] */
+    const uint8_t* flag;            /* [rows][channels][correlations] or NULL */
+    const float* weight;            /* [rows][correlations] (unused with a spectrum) */
+    const float* weight_spectrum;   /* [rows][channels][correlations] or NULL */
+    const uint8_t* gridable;        /* [rows] or NULL */
+    int32_t location;
+} cr_row_runs;
+
+/* StandardMfsVisibilityPolarization (types.rs:1612-1632): mode 0 = one
+ * explicit correlation corr0; mode 1 = the pair (corr0, corr1) collapsed by
+ * `transform` (StandardMfsPairCollapseTransform, types.rs:1582-1608): 0 half
+ * sum, 1 half difference, 2 (a - b) * (0, 1/2), 3 (a - b) * (0, -1/2). */
+typedef struct {
+    int32_t mode;
+    int32_t corr0, corr1;
+    int32_t transform;
+    float sumwt_factor;
+} cr_polarization;
+
 /* WProjectGridAccumulation / DirtyGridAccumulation (lib.rs:70973-70988). */
 typedef struct {
     double normalization_sumwt;
@@ -347,6 +378,41 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* plan, const float* m
                                  int32_t model_location, const uint8_t* planes,
                                  const cr_psf_state* states, float* residual_images,
                                  int32_t out_location, char** err);
+
+/* ---- row runs ---------------------------------------------------------------
+ * The row path's sample preparation on the device
+ * (routed_weighted_grid_sample_from_run, lib.rs:880-1062): every kept
+ * (row, channel) sample, in that order, as a visibility batch -- u, v, w in
+ * wavelengths (uvw_m * lambda_scale, FP64), the natural weight, the plane's
+ * sumwt factor, the row's gridable flag, the (collapsed) visibility -- plus
+ * the VisImagingWeight density coordinates of the row path
+ * (casa_vis_imaging_weight_uv_lambda, weighting.rs:748-756:
+ * float32(u_m * float32(f/c))).  A sample is dropped when a used correlation
+ * is flagged, its visibility is not finite, a hand's weight or the natural
+ * weight is not finite and positive, or the sumwt factor is not.  Outputs
+ * hold rows * channels entries at out_location; *n_out receives the count.
+ * vis is complex64 interleaved. */
+int cr_row_runs_prepare(cr_ctx* ctx, const cr_row_runs* runs, const cr_polarization* pol,
+                        double* u, double* v, double* w, float* weight, float* sumwt_factor,
+                        uint8_t* gridable, float* vis, double* density_u, double* density_v,
+                        int32_t out_location, int64_t* n_out, char** err);
+/* PlaneStokes::derive_pair_selection and paired_sumwt_factor
+ * (types.rs:62-138): the polarization of plane 0 I, 1 Q, 2 U, 3 V (a pair of
+ * CASA correlation codes RR=5, RL=6, LR=7, LL=8, XX=9, XY=10, YX=11, YY=12,
+ * collapsed; sumwt factor 2 for I, 1 otherwise) or of the raw planes 4 XX,
+ * 5 YY, 6 RR, 7 LL (that correlation, explicit, sumwt factor 1).
+ * CR_INVALID when the correlations cannot form the plane. */
+int cr_polarization_for_plane(int32_t plane, const int32_t* corr_types, int32_t correlations,
+                              cr_polarization* out, char** err);
+/* Weighting of a row-path batch: the density is built at the density
+ * coordinates (density_u, density_v, at the batch's location) and looked up
+ * at the batch's u, v, as the streaming weighting plan does
+ * (accumulate_standard_mfs_density_row_with_accessors, weighting.rs:646-746;
+ * weight_sample, weighting.rs:333-380). */
+int cr_apply_weighting_rows(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batch,
+                            const double* density_u, const double* density_v, int32_t mode,
+                            float robust, float* out_weight, int32_t out_location, float* f2,
+                            char** err);
 
 /* ---- restoring beam ---------------------------------------------------------
  * fit_beam_from_psf (beam.rs:27-103): the main lobe above `cutoff` (clamped

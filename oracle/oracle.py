@@ -489,13 +489,16 @@ def briggs_denominator(density: float, f2: float) -> float:
 
 
 def apply_weighting(geom: Geometry, u, v, weight, mode: str = "natural", robust: float = 0.0,
-                    convention: int = 0):
+                    convention: int = 0, build_u=None, build_v=None):
     """apply_weighting_with_density_source (weighting.rs:1055-1180): Combined
-    density (convention 0) or the cube's PerPlane density (convention 1)."""
+    density (convention 0) or the cube's PerPlane density (convention 1).
+    build_u / build_v: the density is built there and looked up at u, v (the
+    streaming row path, weighting.rs:646-756 and 333-380)."""
     u, v, weight = _c(u, np.float64), _c(v, np.float64), _c(weight, np.float32)
     if mode == "natural":
         return weight.copy(), None, 0.0
-    d = density_grid(geom, u, v, weight, convention)
+    d = density_grid(geom, u if build_u is None else build_u,
+                     v if build_v is None else build_v, weight, convention)
     m = {"uniform": 1, "briggs": 2}[mode]
     f2 = briggs_f2(d, robust) if m == 2 else 0.0
     out = np.zeros_like(weight)
