@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cube", action="store_true",
                     help="skip the batched-cube versus per-channel-loop comparison")
     ap.add_argument("--cube-channels", type=int, default=256)
+    ap.add_argument("--no-rows", action="store_true", help="skip the row-runs measurement")
     ap.add_argument("--no-major-minor", action="store_true",
                     help="skip the device-resident major/minor CLEAN loop")
     ap.add_argument("--cube-only", action="store_true",
@@ -382,6 +383,46 @@ def run_cube(args, ctx, dev, peak):
     }
 
 
+def run_rows(args, ctx, dev, peak):
+    """Row runs to samples on the device (cr_row_runs_prepare): the cube's
+    rows (1,263,600 of them, 27 antennas to 1 km, 10 h of 10 s dumps) with 64
+    channels over 1.0-2.0 GHz and 4 correlations (XX, XY, YX, YY), 10 %
+    flags, a weight spectrum, Stokes I (XX + YY collapsed).  Inputs in HBM;
+    GB/s counts the bytes the kernels must move once: per (row, channel) the
+    two used correlations' data, flags and spectrum weights, per row its
+    uvw, and per kept sample the batch written (57 B)."""
+    import torch
+    import casars_cuda as cc
+    from casars_cuda import synthetic as S
+    obs = S.cube_observation(channels=64)
+    R, C, K = obs.rows, obs.channels, 4
+    g = torch.Generator(device=dev).manual_seed(11)
+    data = torch.randn((R, C, K), dtype=torch.complex64, device=dev, generator=g)
+    flag = (torch.rand((R, C, K), device=dev, generator=g) < 0.1).to(torch.uint8)
+    spec = torch.rand((R, C, K), device=dev, generator=g) + 0.5
+    uvw = torch.as_tensor(np.stack([obs.u_m, obs.v_m, np.zeros_like(obs.u_m)], 1), device=dev)
+    runs = cc.RowRuns(uvw, obs.lambda_scale, data, flag, None, spec, None)
+    pol = cc.Polarization.for_plane("I", [9, 10, 11, 12])
+    for _ in range(2):
+        b, _, _ = cc.prepare_row_runs(ctx, runs, pol)
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 10))
+    t_ms = []
+    for _ in range(steps):
+        b, _, _ = cc.prepare_row_runs(ctx, runs, pol)
+        t_ms.append(ctx.last_timings()["plan_ms"])
+    ms = float(np.median(t_ms))
+    kept = len(b)
+    algo = R * C * 2 * (8 + 1 + 4) + R * 24 + kept * 57
+    del data, flag, spec, b
+    torch.cuda.empty_cache()
+    return {"workload": f"{R} rows x {C} channels x {K} correlations, Stokes I from XX+YY, "
+                        "10 % flags, weight spectrum",
+            "samples": R * C, "kept": kept, "ms": ms, "msamples_s": R * C / (ms * 1e-3) / 1e6,
+            "algorithmic_bytes": algo, "achieved_gbs": algo / (ms * 1e-3) / 1e9,
+            "frac_of_measured_hbm": algo / (ms * 1e-3) / 1e9 / peak}
+
+
 def run_major_minor(args, ctx, dev):
     """The device-resident major/minor loop: 2048^2 Stokes I, 10,108,800
     visibilities (21 km layout, 4 channels 1.3-1.5 GHz gridded together), 64
@@ -638,6 +679,8 @@ def main():
 
     if not args.no_cube:
         result["cube"] = run_cube(args, ctx, dev, peak)
+    if not args.no_rows:
+        result["row_runs"] = run_rows(args, ctx, dev, peak)
     if not args.no_major_minor:
         result["major_minor"] = run_major_minor(args, ctx, dev)
 
