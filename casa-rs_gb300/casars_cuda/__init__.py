@@ -7,6 +7,7 @@ from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, Psf
                       image_to_grid, predict, residual_image, run_hogbom_minor_cycle,
                       CubeBatch, cube_degrid, cube_grid_degrid, cube_grid_dirty,
                       cube_sample_taps, CubePlan, BeamFit, fit_beam, restore, psf_sidelobe,
-                      RowRuns, Polarization, prepare_row_runs, apply_weighting_rows)
+                      RowRuns, Polarization, prepare_row_runs, apply_weighting_rows,
+                      run_hogbom_planes)
 from .clean import (CleanConfig, CleanResult, clean_cycle_threshold, run_cotton_schwab,  # noqa: F401
                     CubeCleanResult, cube_clean_loop, run_cube_clean)

@@ -227,7 +227,8 @@ def _f32max(values) -> np.float32:
     return m
 
 
-def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom, refresh):
+def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom, refresh,
+                    hogbom_many=None):
     """The control of run_standard_mfs_cube_clean (lib.rs:3026-3210).
 
     Planes advance in ascending order; per synchronized pass every plane whose
@@ -243,11 +244,24 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
     residuals / models / psfs are indexable by plane (arrays [C][nx][ny]);
     hogbom(model, residual, psf, niter, threshold, cycle_threshold) returns a
     HogbomOutcome-like object; refresh(planes) recomputes residuals[c] for
-    the listed planes from models[c] in place.  Returns a dict of the loop's
-    results."""
+    the listed planes from models[c] in place.  hogbom_many(planes, niter,
+    threshold, cycle_threshold), when given, runs the listed planes' minor
+    cycles together (in place; outcomes in list order) -- the planes are
+    independent, so this equals running them in turn.  Returns a dict of the
+    loop's results."""
     f32 = np.float32
     n = len(sidelobes)
-    absmax = lambda c: f32(_absmax(residuals[c]))
+
+    def plane_peaks():
+        # every plane's |residual| peak at once (one reduction, one copy)
+        if torch is not None and isinstance(residuals, torch.Tensor):
+            return residuals.abs().amax(dim=(1, 2)).float().cpu().numpy()
+        if isinstance(residuals, np.ndarray):
+            return np.abs(residuals).max(axis=(1, 2)).astype(np.float32)
+        return np.array([_absmax(residuals[c]) for c in range(n)], np.float32)
+
+    pk = plane_peaks()
+    absmax = lambda c: f32(pk[c])
     cyc = lambda peak, sl: clean_cycle_threshold(float(peak), float(sl), cfg)
     initial_peak = _f32max(absmax(c) for c in range(n))
     max_sidelobe = _f32max(sidelobes)
@@ -273,20 +287,30 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
         actives.append(active)
         pass_iters = 0
         pending = {}   # plane -> (stop set before the refresh, stop_after, refreshed in loop)
+        # the planes' controllers (run_hogbom_cotton_schwab, niter =
+        # cycle_niter, major_cycle_limit = 1) up to their residual refresh
+        todo, start_peak = [], {}
         for c in active:
-            # the plane's controller (run_hogbom_cotton_schwab, niter =
-            # cycle_niter, major_cycle_limit = 1) up to its residual refresh
-            stop = None
-            min_peak = absmax(c)
             p = absmax(c)
             s = tolerant_clean_stop_reason(p, cfg.threshold_jy_per_beam)
             if s is not None:
                 plane_stop[c] = s
                 continue
-            out = hogbom(models[c], residuals[c], psfs[c],
-                         min(cycle_niter, cfg.minor_cycle_length),
-                         cfg.threshold_jy_per_beam, thr)
-            models[c], residuals[c] = out.model, out.residual
+            todo.append(c)
+            start_peak[c] = p
+        budget = min(cycle_niter, cfg.minor_cycle_length)
+        if hogbom_many is not None:
+            outs = hogbom_many(todo, budget, cfg.threshold_jy_per_beam, thr)
+        else:
+            outs = [hogbom(models[c], residuals[c], psfs[c], budget, cfg.threshold_jy_per_beam,
+                           thr) for c in todo]
+        for c, out in zip(todo, outs):
+            if out.model is not None:
+                models[c], residuals[c] = out.model, out.residual
+        pk = plane_peaks()
+        for c, out in zip(todo, outs):
+            stop = None
+            min_peak = start_peak[c]
             comps[c].extend(zip(map(tuple, np.asarray(out.positions).tolist()),
                                 np.asarray(out.fluxes).tolist()))
             plane_iters[c] += out.reported_updates
@@ -313,6 +337,7 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
                 pending[c] = (stop, stop_after, True)
         if pending:
             refresh(sorted(pending))
+            pk = plane_peaks()
         for c, (stop, stop_after, in_loop) in pending.items():
             if in_loop and stop_after is None:
                 s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam)
@@ -362,8 +387,9 @@ def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
         psfs, residuals, states = plan.dirty_images()
         n = plan.channels
         beams, sidelobes = [], []
+        fit = restore or max_psf_sidelobe is None   # beams feed restoration and sidelobes
         for c in range(n):
-            if states[c].psf_peak > 0:
+            if fit and states[c].psf_peak > 0:
                 b, sl = psf_beam_and_sidelobe(ctx, psfs[c], cell, cfg.psf_cutoff)
             else:
                 b, sl = None, 0.0
@@ -382,7 +408,16 @@ def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
             mask[planes] = 1
             plan.residual_images(models, states, planes=mask, out=residuals)
 
-        out = cube_clean_loop(residuals, psfs, models, sidelobes, cfg, hogbom, refresh)
+        hogbom_many = None
+        if torch is not None and isinstance(residuals, torch.Tensor) and residuals.is_cuda:
+            def hogbom_many(planes, niter, threshold, cycle_threshold):
+                return im.run_hogbom_planes(ctx, models, residuals, psfs, planes, cfg.gain,
+                                            niter, threshold=threshold,
+                                            cycle_threshold=cycle_threshold,
+                                            inclusive=cfg.inclusive)
+
+        out = cube_clean_loop(residuals, psfs, models, sidelobes, cfg, hogbom, refresh,
+                              hogbom_many)
     finally:
         plan.close()
     restored = None

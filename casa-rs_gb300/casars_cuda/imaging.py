@@ -1061,6 +1061,49 @@ class HogbomOutcome:
     stop_reason: Optional[str]
 
 
+def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float,
+                      cycle_niter: int, threshold: float = 0.0, cycle_threshold: float = 0.0,
+                      nsigma_threshold: float = 0.0, masks=None, inclusive: bool = True):
+    """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) on the
+    listed planes of [P][nx][ny] device images in one launch
+    (cr_hogbom_planes); models and residuals are updated in place.  Returns
+    one HogbomOutcome per listed plane (model / residual None: in place)."""
+    if not (_is_torch(models) and models.is_cuda):
+        raise ValueError("run_hogbom_planes takes torch CUDA images")
+    for t in (models, residuals, psfs):
+        if t.dtype != torch.float32 or not t.is_contiguous() or t.shape != models.shape:
+            raise ValueError("images must be contiguous float32 [P][nx][ny] of one shape")
+    P, nx, ny = models.shape
+    pl = np.ascontiguousarray(np.asarray(planes, np.int32))
+    n = len(pl)
+    cap = int(cycle_niter) + 1
+    cx = np.zeros(max(n, 1) * cap, np.int32)
+    cy = np.zeros_like(cx)
+    cpk = np.zeros(max(n, 1) * cap, np.float32)
+    cfl = np.zeros_like(cpk)
+    actual = np.zeros(max(n, 1), np.int64)
+    reported = np.zeros_like(actual)
+    stop = np.zeros(max(n, 1), np.int32)
+    mk = None
+    if masks is not None:
+        mk = masks.to(torch.uint8).contiguous()
+    ctx.use_torch_stream()
+    call("cr_hogbom_planes", ctx.handle, models.data_ptr(), residuals.data_ptr(),
+         psfs.data_ptr(), mk.data_ptr() if mk is not None else None, P, nx, ny,
+         pl.ctypes.data, n, float(gain), float(threshold), float(cycle_threshold),
+         float(nsigma_threshold), int(cycle_niter), int(bool(inclusive)), cx.ctypes.data,
+         cy.ctypes.data, cpk.ctypes.data, cfl.ctypes.data, actual.ctypes.data,
+         reported.ctypes.data, stop.ctypes.data)
+    outs = []
+    for s in range(n):
+        k = int(actual[s])
+        o = s * cap
+        outs.append(HogbomOutcome(None, None, np.stack([cx[o:o + k], cy[o:o + k]], 1),
+                                  cpk[o:o + k].copy(), cfl[o:o + k].copy(), k,
+                                  int(reported[s]), STOP_REASONS[int(stop[s])]))
+    return outs
+
+
 def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycle_niter: int,
                            threshold: float = 0.0, cycle_threshold: float = 0.0,
                            nsigma_threshold: float = 0.0, mask=None,

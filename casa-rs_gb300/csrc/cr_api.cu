@@ -1436,4 +1436,26 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
     });
 }
 
+int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                     const uint8_t* mask, int32_t nplanes, int32_t nx, int32_t ny,
+                     const int32_t* planes, int32_t n, float gain, float threshold,
+                     float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                     int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                     float* comp_flux, int64_t* actual, int64_t* reported,
+                     int32_t* stop_reason, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && model != nullptr && residual != nullptr && psf != nullptr,
+             "null argument");
+        need(nplanes >= 0, "nplanes is negative");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        hogbom_planes(ctx, model, residual, psf, mask, nx, ny, nplanes, planes, n, gain,
+                      threshold, cycle_threshold, nsigma_threshold, cycle_niter, inclusive,
+                      comp_x, comp_y, comp_peak, comp_flux, actual, reported, stop_reason);
+        tm.mark();
+        set_timings(ctx, cr_timings{0.f, 0.f, 0.f, 0.f, tm.between(0, 1)});
+    });
+}
+
 }  // extern "C"

@@ -15,8 +15,10 @@
 // block reduces all candidates to the same global peak.  The kernel is
 // launched cooperatively (all blocks resident); the barrier's wait is bounded
 // and reports CR_TIMEOUT instead of spinning forever.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "cr_internal.cuh"
 
@@ -137,10 +139,12 @@ __device__ int stop_reason(float peak_abs, float thr, float cyc, float nsig) {
     return 0;
 }
 
-__global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
+// The minor cycle of one image by `nblocks` co-resident blocks, this one
+// being block `bidx` of them.
+__device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
     const int64_t npix = (int64_t)a.nx * a.ny;
-    const int64_t chunk = (npix + gridDim.x - 1) / gridDim.x;
-    const int64_t p0 = (int64_t)blockIdx.x * chunk;
+    const int64_t chunk = (npix + nblocks - 1) / nblocks;
+    const int64_t p0 = (int64_t)bidx * chunk;
     const int64_t p1 = min(npix, p0 + chunk);
     const int kcx = a.nx / 2, kcy = a.ny / 2;
     __shared__ Cand s_best;
@@ -163,22 +167,22 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
             }
         }
         Cand c = block_argmax(ba, bk, bv);
-        if (threadIdx.x == 0) a.cands[blockIdx.x] = c;
+        if (threadIdx.x == 0) a.cands[bidx] = c;
     }
-    if (!grid_barrier(a.bar, gridDim.x)) {
+    if (!grid_barrier(a.bar, (unsigned)nblocks)) {
         if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
         return;
     }
     long long it = 0;
     int stop = CR_STOP_NONE;
     for (; it < a.budget; ++it) {
-        const Cand* cur = a.cands + (it & 1) * gridDim.x;
-        Cand* nxt = a.cands + ((it + 1) & 1) * gridDim.x;
+        const Cand* cur = a.cands + (it & 1) * nblocks;
+        Cand* nxt = a.cands + ((it + 1) & 1) * nblocks;
         // every block reduces all candidates to the same global peak
         {
             float ba = -1.0f, bv = 0.0f;
             int bk = 0x7fffffff;
-            for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+            for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
                 // other blocks wrote these: read through L2, not a stale L1 line
                 int4 raw = __ldcg(reinterpret_cast<const int4*>(cur) + i);
                 Cand c{__int_as_float(raw.x), raw.y, __int_as_float(raw.z), 0};
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
         const Cand best = s_best;
         const int px = best.key % a.nx, py = best.key / a.nx;
         const float comp = __fmul_rn(a.gain, best.value);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (bidx == 0 && threadIdx.x == 0) {
             int64_t m = (int64_t)px * a.ny + py;
             a.model[m] = __fadd_rn(a.model[m], comp);
             if (a.comp_x) {
@@ -221,34 +225,83 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
         // candidate in the same pass
         float ba = -1.0f, bv = 0.0f;
         int bk = 0x7fffffff;
-        for (int64_t t = p0 + threadIdx.x; t < p1; t += blockDim.x) {
-            int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
-            int kx = x - px + kcx, ky = y - py + kcy;
+        // (x, y) stepped along with t, without a division per pixel; PSF
+        // offsets in 32 bits (npix < 2^31)
+        const int step = (int)blockDim.x, sx = step / a.ny, sy = step - sx * a.ny;
+        int64_t t = p0 + threadIdx.x;
+        int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
+#pragma unroll 4
+        for (; t < p1; t += step) {
+            const int kx = x - px + kcx, ky = y - py + kcy;
             float v = a.residual[t];
             if (kx >= 0 && kx < a.nx && ky >= 0 && ky < a.ny) {
-                v = __fsub_rn(v, __fmul_rn(comp, a.psf[(int64_t)kx * a.ny + ky]));
+                v = __fsub_rn(v, __fmul_rn(comp, a.psf[kx * a.ny + ky]));
                 a.residual[t] = v;
             }
-            if (a.mask && !a.mask[t]) continue;
-            float av = fabsf(v);
-            int key = y * a.nx + x;
-            if (better(av, key, ba, bk)) {
-                ba = av;
-                bk = key;
-                bv = v;
+            if (!a.mask || a.mask[t]) {
+                const float av = fabsf(v);
+                const int key = y * a.nx + x;
+                if (better(av, key, ba, bk)) {
+                    ba = av;
+                    bk = key;
+                    bv = v;
+                }
+            }
+            x += sx;
+            y += sy;
+            if (y >= a.ny) {
+                y -= a.ny;
+                ++x;
             }
         }
         Cand c = block_argmax(ba, bk, bv);
-        if (threadIdx.x == 0) nxt[blockIdx.x] = c;
-        if (!grid_barrier(a.bar, gridDim.x)) {
+        if (threadIdx.x == 0) nxt[bidx] = c;
+        if (!grid_barrier(a.bar, (unsigned)nblocks)) {
             if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
             return;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bidx == 0 && threadIdx.x == 0) {
         *a.out_actual = it;
         *a.out_stop = stop;
     }
+}
+
+__global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
+    hogbom_body(a, (int)gridDim.x, (int)blockIdx.x);
+}
+
+// Several images [P][nx][ny] at once: `per_plane` blocks for each listed
+// plane, each group with its own barrier words, candidates, component list
+// and results (slot s = the plane's position in the list).
+struct HogPlanesArgs {
+    HogArgs base;           // pointers to plane 0; cands / bar / comp / out of slot 0
+    const int* planes;      // [n] plane indices
+    int per_plane;
+    int64_t comp_cap;       // components per slot
+};
+
+__global__ void __launch_bounds__(kHogThreads) hogbom_planes_kernel(HogPlanesArgs pa) {
+    const int slot = (int)blockIdx.x / pa.per_plane;
+    const int bidx = (int)blockIdx.x % pa.per_plane;
+    const int64_t npix = (int64_t)pa.base.nx * pa.base.ny;
+    const int64_t off = (int64_t)pa.planes[slot] * npix;
+    HogArgs a = pa.base;
+    a.model += off;
+    a.residual += off;
+    a.psf += off;
+    if (a.mask) a.mask += off;
+    a.cands += (int64_t)slot * 2 * pa.per_plane;
+    a.bar += 4 * slot;
+    if (a.comp_x) {
+        a.comp_x += slot * pa.comp_cap;
+        a.comp_y += slot * pa.comp_cap;
+        a.comp_peak += slot * pa.comp_cap;
+        a.comp_flux += slot * pa.comp_cap;
+    }
+    a.out_actual += slot;
+    a.out_stop += slot;
+    hogbom_body(a, pa.per_plane, bidx);
 }
 
 }  // namespace
@@ -305,6 +358,100 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
     if (actual) *actual = h.actual;
     if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
     if (stop_reason_out) *stop_reason_out = h.stop;
+}
+
+void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                   const uint8_t* mask, int32_t nx, int32_t ny, int32_t nplanes,
+                   const int32_t* planes, int32_t n, float gain, float threshold,
+                   float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                   int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                   float* comp_flux, int64_t* actual, int64_t* reported,
+                   int32_t* stop_reason_out) {
+    if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
+    if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
+    if (cycle_niter < 0) fail(CR_INVALID, "cycle_niter is negative");
+    if (n < 0 || (n > 0 && !planes)) fail(CR_INVALID, "plane list is null");
+    for (int32_t s = 0; s < n; ++s)
+        if (planes[s] < 0 || planes[s] >= nplanes) fail(CR_INVALID, "plane index out of range");
+    if (n == 0) return;
+    const long long budget = inclusive ? cycle_niter + 1 : cycle_niter;
+    const int64_t cap = budget > 0 ? budget : 1;
+    int sms = 0, per_sm = 0;
+    CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hogbom_planes_kernel,
+                                                                kHogThreads, 0));
+    if (per_sm < 1) fail(CR_CUDA, "Hogbom kernel cannot be resident");
+    const int resident = sms * per_sm;
+    // blocks per plane: as many as keep every listed plane's group resident,
+    // at most 8; planes beyond one launch's room go in further launches
+    const int batch = std::min<int>(n, resident);
+    const int per_plane = std::max(1, std::min(8, resident / batch));
+    const size_t head = 16 * (size_t)batch + 8 * (size_t)batch + 4 * (size_t)batch + 16;
+    const size_t head_al = (head + 255) & ~(size_t)255;
+    const size_t cand_b = (size_t)batch * 2 * per_plane * sizeof(Cand);
+    char* wsp = (char*)workspace(ctx, "hogp_ws", head_al + cand_b + (size_t)batch * cap * 16);
+    unsigned int* bar = (unsigned int*)wsp;
+    long long* out_actual = (long long*)(wsp + 16 * (size_t)batch);
+    int* out_stop = (int*)(wsp + 24 * (size_t)batch);
+    int* out_status = (int*)(wsp + 28 * (size_t)batch);
+    Cand* cands = (Cand*)(wsp + head_al);
+    int* cx = (int*)(wsp + head_al + cand_b);
+    int* cy = cx + (size_t)batch * cap;
+    float* cp = (float*)(cy + (size_t)batch * cap);
+    float* cf = cp + (size_t)batch * cap;
+    int* plist = (int*)workspace(ctx, "hogp_planes", (size_t)batch * 4);
+    std::vector<long long> h_actual((size_t)batch);
+    std::vector<int> h_stop((size_t)batch);
+    for (int32_t s0 = 0; s0 < n; s0 += batch) {
+        const int m = std::min<int>(batch, n - s0);
+        CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, head_al, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(plist, planes + s0, (size_t)m * 4, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        HogPlanesArgs pa;
+        pa.base = HogArgs{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
+                          nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual,
+                          out_stop, out_status};
+        pa.planes = plist;
+        pa.per_plane = per_plane;
+        pa.comp_cap = cap;
+        void* args[] = {&pa};
+        CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_planes_kernel,
+                                                  dim3((unsigned)(m * per_plane)),
+                                                  dim3(kHogThreads), args, 0, ctx->stream));
+        note_launch(ctx, "hogbom_planes_kernel");
+        int status = 0;
+        CR_CUDA_CHECK(cudaMemcpyAsync(h_actual.data(), out_actual, (size_t)m * 8,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(h_stop.data(), out_stop, (size_t)m * 4,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(&status, out_status, 4, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        if (status) fail(CR_TIMEOUT, "Hogbom grid barrier timed out");
+        long long most = 0;
+        for (int s = 0; s < m; ++s) {
+            const int64_t k = s0 + s;
+            const long long got = h_actual[(size_t)s];
+            most = std::max(most, got);
+            if (actual) actual[k] = got;
+            if (reported) reported[k] = std::min<int64_t>(got, cycle_niter);
+            if (stop_reason_out) stop_reason_out[k] = h_stop[(size_t)s];
+        }
+        if (comp_x && most > 0) {
+            // the batch's component lists in one copy per array (the slots
+            // past each plane's count are not read)
+            const size_t ho = (size_t)s0 * cap, len = (size_t)m * cap * 4;
+            CR_CUDA_CHECK(cudaMemcpyAsync(comp_x + ho, cx, len, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(comp_y + ho, cy, len, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(comp_peak + ho, cp, len, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(comp_flux + ho, cf, len, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        }
+    }
 }
 
 }  // namespace cr

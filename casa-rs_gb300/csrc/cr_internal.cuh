@@ -317,6 +317,16 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
             int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
             int64_t* reported, int32_t* stop_reason);
+// The minor cycles of the listed planes of [nplanes][nx][ny] images in one
+// launch (groups of co-resident blocks, one per plane); results per listed
+// plane, component arrays [n][cycle_niter + inclusive] (host, or null).
+void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                   const uint8_t* mask, int32_t nx, int32_t ny, int32_t nplanes,
+                   const int32_t* planes, int32_t n, float gain, float threshold,
+                   float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                   int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                   float* comp_flux, int64_t* actual, int64_t* reported,
+                   int32_t* stop_reason_out);
 
 inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) {
     int64_t b = (n + threads - 1) / threads;

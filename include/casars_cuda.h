@@ -468,6 +468,21 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf,
               float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
               int32_t* stop_reason, char** err);
 
+/* The Hogbom minor cycles of several planes in one launch: model, residual,
+ * psf (and mask, or NULL) are DEVICE arrays [nplanes][nx][ny]; the n planes
+ * listed in `planes` (host) each run run_hogbom_minor_cycle_cpu_with_progress
+ * with the same gain, thresholds and budget, as cr_hogbom would one by one
+ * (each plane's blocks only touch that plane).  actual, reported and
+ * stop_reason are host [n]; the component arrays (host, or NULL) hold
+ * [n][cycle_niter + 1] entries, plane s's first actual[s] of them valid. */
+int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                     const uint8_t* mask, int32_t nplanes, int32_t nx, int32_t ny,
+                     const int32_t* planes, int32_t n, float gain, float threshold,
+                     float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+                     int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                     float* comp_flux, int64_t* actual, int64_t* reported,
+                     int32_t* stop_reason, char** err);
+
 /* ---- allocation-free Hogbom minor cycle ----------------------------------
  * No counterpart in the reference.  The same minor cycle as cr_hogbom for
  * callers that may not allocate device memory once they run: for example a

@@ -193,3 +193,36 @@ def test_cube_clean_matches_oracle(ctx, cube, device):
         assert peak_norm_err(to_np(out.models[c]), ref["models"][c]) <= 1e-5
         assert out.beams[c] is not None
     assert out.restored is not None
+
+
+def test_hogbom_planes_equals_single_plane_calls(ctx, cube):
+    """cr_hogbom_planes on a subset of planes gives each listed plane exactly
+    what cr_hogbom gives it alone, and leaves the other planes untouched."""
+    import torch
+    obs, flags, vis = cube
+    gg = _gridder(ctx, obs)
+    cb = cc.CubeBatch(obs.u_m, obs.v_m, obs.lambda_scale, vis, None, flags)
+    plan = cc.CubePlan(gg, cb)
+    psf, res, states = plan.dirty_images()
+    plan.close()
+    P = obs.channels
+    psf_d = torch.as_tensor(psf).cuda().contiguous()
+    res_d = torch.as_tensor(res).cuda().contiguous()
+    mod_d = torch.zeros_like(res_d)
+    planes = [4, 0, 2, 5]
+    outs = cc.run_hogbom_planes(ctx, mod_d, res_d, psf_d, planes, 0.1, 60,
+                                cycle_threshold=0.05)
+    for s, c in enumerate(planes):
+        one = cc.run_hogbom_minor_cycle(ctx, np.zeros_like(res[c]), res[c], psf[c], 0.1, 60,
+                                        cycle_threshold=0.05)
+        o = outs[s]
+        assert o.actual_updates == one.actual_updates > 0
+        assert o.reported_updates == one.reported_updates
+        assert o.stop_reason == one.stop_reason
+        np.testing.assert_array_equal(o.positions, one.positions)
+        np.testing.assert_array_equal(o.fluxes, one.fluxes)
+        np.testing.assert_array_equal(res_d[c].cpu().numpy(), one.residual)
+        np.testing.assert_array_equal(mod_d[c].cpu().numpy(), one.model)
+    for c in set(range(P)) - set(planes):
+        np.testing.assert_array_equal(res_d[c].cpu().numpy(), res[c])
+        assert float(mod_d[c].abs().max()) == 0.0
