@@ -88,6 +88,8 @@ SIGNATURES = {
     "cr_ctx_last_timings": (C.c_int, [_p, C.POINTER(Timings)]),
     "cr_ctx_launch_count": (_i64, [_p]),
     "cr_ctx_set_cube_graphs": (C.c_int, [_p, _i32]),
+    "cr_clark": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _i32, _f, _f, _f, _f, _i64, _p,
+                           _p, _p, _p, C.POINTER(_i64), C.POINTER(_i32), C.POINTER(_f), _err]),
     "cr_hogbom_planes": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _p, _i32, _f, _f, _f,
                                    _f, _i64, _i32, _p, _p, _p, _p, _p, _p, _p, _err]),
     "cr_gridder_create": (C.c_int, [_p, C.POINTER(Geometry), _d, _i32, C.POINTER(_p),

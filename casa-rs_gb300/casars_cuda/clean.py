@@ -434,3 +434,90 @@ def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
                            out["major_cycles"], out["planes_at_or_below_initial_threshold"],
                            out["plane_iterations"], out["plane_stops"], out["components"],
                            out["thresholds"], out["active"])
+
+
+# ----------------------------------------------------------------------------
+# Clark
+# ----------------------------------------------------------------------------
+def clark_step_niter(cycle_reported_niter: int) -> int:
+    """casa_clark_step_niter (lib.rs:63168-63174)."""
+    return cycle_reported_niter if cycle_reported_niter < 5000 else 2000
+
+
+def run_clark_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
+                            max_psf_sidelobe: Optional[float] = None) -> CleanResult:
+    """run_clark_cotton_schwab (lib.rs:63314-63520): per major cycle a Clark
+    minor cycle on the device (cr_clark; PSF patch from the fitted beam),
+    the residual refreshed whenever the model changed, CASA's stop and
+    hand-off rules and divergence guard.  Images stay where the batch is."""
+    psf, residual, state, _ = im.dirty_image(gridder, batch, wproj)
+    plan = im.Plan(gridder, batch, wproj)
+    geom = gridder.geometry
+    cell = (geom.cell_x_rad, geom.cell_y_rad)
+    beam, fitted_sidelobe = psf_beam_and_sidelobe(gridder.ctx, psf, cell, cfg.psf_cutoff)
+    sidelobe = fitted_sidelobe if max_psf_sidelobe is None else max_psf_sidelobe
+    ncent = im.clark_ncent(beam, cell)
+    model = _zeros_like(residual)
+    ctx = gridder.ctx
+    actual = reported = major = 0
+    stop = None
+    min_peak = np.float32(_absmax(residual))
+    comps, thresholds = [], []
+    try:
+        while reported < cfg.niter:
+            if cfg.major_cycle_limit is not None and major >= cfg.major_cycle_limit:
+                stop = "MajorCycleLimitReached"
+                break
+            peak = _absmax(residual)
+            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam)
+            if s is not None:
+                stop = s
+                break
+            step = clark_step_niter(min(cfg.niter - reported, cfg.minor_cycle_length))
+            thr = clean_cycle_threshold(peak, sidelobe, cfg)
+            thresholds.append(thr)
+            out = im.run_clark_minor_cycle(ctx, model, residual, psf, ncent, cfg.gain, step,
+                                           threshold=cfg.threshold_jy_per_beam,
+                                           cycle_threshold=thr)
+            model, residual = out.model, out.residual
+            comps.extend(zip(map(tuple, out.positions.tolist()), out.fluxes.tolist()))
+            updated = out.actual_updates > 0
+            after = reported + out.reported_updates
+            if updated:
+                residual = plan.residual_image(model, state)
+                if after < cfg.niter:
+                    major += 1
+            actual += out.actual_updates
+            reported = after
+            stop_after = False
+            if out.stop_reason is not None:
+                if updated and out.stop_reason in _HANDOFF:
+                    pass
+                elif out.stop_reason in _HANDOFF:
+                    stop = out.stop_reason
+                else:
+                    stop = out.stop_reason
+                    stop_after = True
+            if not updated or stop_after:
+                break
+            minor_peak = np.float32(_absmax(residual))
+            if minor_peak < min_peak:
+                min_peak = minor_peak
+            elif min_peak > 0 and (minor_peak - min_peak) / min_peak > np.float32(0.1):
+                stop = "DivergenceDetected"
+                break
+            if stop is None and reported >= cfg.niter:
+                stop = "IterationLimitReached"
+                break
+            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam)
+            if s is not None:
+                stop = s
+                break
+        if cfg.niter > 0 and stop is None:
+            stop = "IterationLimitReached"
+    finally:
+        plan.close()
+    restored = im.restore(gridder.ctx, model, residual, cell, beam) if beam is not None else None
+    return CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
+                       thresholds, beam, restored, sidelobe)
+

@@ -1061,6 +1061,57 @@ class HogbomOutcome:
     stop_reason: Optional[str]
 
 
+def clark_ncent(beam, cell_rad) -> int:
+    """ncent of build_clark_psf_patch (lib.rs:64422-64440): max(4, ceil(major /
+    cell_x), ceil(minor / cell_y)) of the fitted beam, 4 without one."""
+    if beam is None:
+        return 4
+    cx, cy = (cell_rad, cell_rad) if np.isscalar(cell_rad) else cell_rad
+    major = max(1, int(np.ceil(beam.major_fwhm_rad / cx)))
+    minor = max(1, int(np.ceil(beam.minor_fwhm_rad / cy)))
+    return max(4, major, minor)
+
+
+def run_clark_minor_cycle(ctx: Context, model, residual, psf, ncent: int, gain: float,
+                          cycle_niter: int, threshold: float = 0.0, cycle_threshold: float = 0.0,
+                          nsigma_threshold: float = 0.0, mask=None):
+    """run_clark_minor_cycle_cpu (lib.rs:62129-62355) on the device (cr_clark).
+    model and residual are updated copies; the outcome's max_exterior_abs is
+    the patch's exterior PSF peak."""
+    arrs = _Arrays()
+    if _is_torch(residual) and residual.is_cuda:
+        m = model.detach().to(torch.float32).clone().contiguous()
+        r = residual.detach().to(torch.float32).clone().contiguous()
+        arrs._loc(CR_DEVICE)
+        arrs.keep += [m, r]
+        mp, rp = m.data_ptr(), r.data_ptr()
+        ctx.use_torch_stream()
+    else:
+        m = np.array(model, np.float32, copy=True, order="C")
+        r = np.array(residual, np.float32, copy=True, order="C")
+        arrs._loc(CR_HOST)
+        mp, rp = m.ctypes.data, r.ctypes.data
+        ctx.use_own_stream()
+    nx, ny = r.shape
+    pp = arrs.ptr(psf, np.float32, torch.float32 if torch else None, (nx, ny))
+    kp = arrs.ptr(mask, np.uint8, torch.uint8 if torch else None, (nx, ny))
+    cap = max(int(cycle_niter), 1)
+    cx = np.zeros(cap, np.int32)
+    cy = np.zeros(cap, np.int32)
+    cpk = np.zeros(cap, np.float32)
+    cfl = np.zeros(cap, np.float32)
+    actual, stop, mea = C.c_int64(), C.c_int32(), C.c_float()
+    call("cr_clark", ctx.handle, mp, rp, pp, kp, nx, ny, arrs.location, int(ncent), float(gain),
+         float(threshold), float(cycle_threshold), float(nsigma_threshold), int(cycle_niter),
+         cx.ctypes.data, cy.ctypes.data, cpk.ctypes.data, cfl.ctypes.data, C.byref(actual),
+         C.byref(stop), C.byref(mea))
+    k = int(actual.value)
+    out = HogbomOutcome(m, r, np.stack([cx[:k], cy[:k]], 1), cpk[:k], cfl[:k], k, k,
+                        STOP_REASONS[int(stop.value)])
+    out.max_exterior_abs = float(mea.value)
+    return out
+
+
 def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float,
                       cycle_niter: int, threshold: float = 0.0, cycle_threshold: float = 0.0,
                       nsigma_threshold: float = 0.0, masks=None, inclusive: bool = True):

@@ -1458,4 +1458,41 @@ int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* ps
     });
 }
 
+int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
+             int32_t nx, int32_t ny, int32_t location, int32_t ncent, float gain,
+             float threshold, float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+             int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+             int64_t* actual, int32_t* stop_reason, float* max_exterior_abs, char** err) {
+    return guarded(err, [&] {
+        need(ctx && model && residual && psf, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        need(location == CR_HOST || location == CR_DEVICE, "bad location");
+        need(!comp_x == !comp_y && !comp_x == !comp_peak && !comp_x == !comp_flux,
+             "component arrays must be all given or all null");
+        bind(ctx);
+        size_t nb = (size_t)nx * ny * 4;
+        float* m = location == CR_DEVICE ? model : (float*)workspace(ctx, "clk_model", nb);
+        float* r = location == CR_DEVICE ? residual : (float*)workspace(ctx, "clk_residual", nb);
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(m, model, nb, cudaMemcpyHostToDevice, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(r, residual, nb, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const float* p = (const float*)device_input(ctx, psf, nb, location, "clk_psf");
+        const uint8_t* mk = (const uint8_t*)device_input(ctx, mask, (size_t)nx * ny, location,
+                                                         "clk_mask");
+        StageTimer tm(ctx);
+        tm.mark();
+        cr::clark_minor_cycle(ctx, m, r, p, mk, nx, ny, ncent, gain, threshold, cycle_threshold,
+                              nsigma_threshold, cycle_niter, comp_x, comp_y, comp_peak,
+                              comp_flux, actual, stop_reason, max_exterior_abs);
+        tm.mark();
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(model, m, nb, cudaMemcpyDeviceToHost, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(residual, r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        set_timings(ctx, cr_timings{0.f, 0.f, 0.f, 0.f, tm.between(0, 1)});
+    });
+}
+
 }  // extern "C"

@@ -317,6 +317,14 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
             int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
             int64_t* reported, int32_t* stop_reason);
+// run_clark_minor_cycle_cpu (lib.rs:62129-62355) on device images; the PSF
+// patch is (3 ncent + 1)^2 about the centre (build_clark_psf_patch).
+void clark_minor_cycle(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                       const uint8_t* mask, int32_t nx, int32_t ny, int32_t ncent, float gain,
+                       float threshold, float cycle_threshold, float nsigma_threshold,
+                       int64_t cycle_niter, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                       float* comp_flux, int64_t* actual, int32_t* stop_out,
+                       float* max_exterior_out);
 // The minor cycles of the listed planes of [nplanes][nx][ny] images in one
 // launch (groups of co-resident blocks, one per plane); results per listed
 // plane, component arrays [n][cycle_niter + inclusive] (host, or null).

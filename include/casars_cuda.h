@@ -483,6 +483,23 @@ int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* ps
                      float* comp_flux, int64_t* actual, int64_t* reported,
                      int32_t* stop_reason, char** err);
 
+/* ---- Clark minor cycle ------------------------------------------------------
+ * run_clark_minor_cycle_cpu (lib.rs:62129-62355): subcycles over the active
+ * pixels (|residual| >= max(peak x max exterior PSF x factor, cycle
+ * threshold)) with a (3 ncent + 1)^2 PSF patch about the centre
+ * (build_clark_psf_patch, lib.rs:64422-64456; ncent = max(4, ceil(major /
+ * cell), ceil(minor / cell)) of the fitted beam), then the residual update by
+ * the PSF convolution of the subcycle's components (fft_convolve_real,
+ * lib.rs:64415-64420).  model and residual are
+ * updated in place at `location`; component arrays (host, capacity
+ * cycle_niter) may be NULL; *max_exterior_abs receives the patch's exterior
+ * PSF peak. */
+int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
+             int32_t nx, int32_t ny, int32_t location, int32_t ncent, float gain,
+             float threshold, float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
+             int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+             int64_t* actual, int32_t* stop_reason, float* max_exterior_abs, char** err);
+
 /* ---- allocation-free Hogbom minor cycle ----------------------------------
  * No counterpart in the reference.  The same minor cycle as cr_hogbom for
  * callers that may not allocate device memory once they run: for example a
