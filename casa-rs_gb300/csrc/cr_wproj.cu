@@ -230,7 +230,7 @@ struct __align__(16) Entry {
 constexpr int kCand = 128;  // candidate records examined per batch
 
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kGridThreads, 5) wp_grid_kernel(GridArgs a) {
+__global__ void __launch_bounds__(kGridThreads, 6) wp_grid_kernel(GridArgs a) {
     __shared__ int s_item;
     __shared__ uint32_t s_seg_start[kMaxSeg];
     __shared__ uint32_t s_seg_pref[kMaxSeg + 1];
@@ -514,7 +514,7 @@ __device__ void degrid_flat(const float2* g, const float2* cube, int gny, int s,
 
 // One warp per record: sum conj(cwt) * grid over the window
 // (degrid_sample_planned, gridder.rs:3726-3747), then warp shuffles.
-__global__ void __launch_bounds__(256) wp_degrid_kernel(DegridArgs a) {
+__global__ void __launch_bounds__(256, 4) wp_degrid_kernel(DegridArgs a) {
     const int lane = threadIdx.x & 31;
     const int half = lane >> 4, hl = lane & 15;
     const int64_t nrec = (int64_t)a.counts[2];
