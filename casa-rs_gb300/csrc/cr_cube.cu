@@ -646,7 +646,7 @@ constexpr int kGridThreads = kCubeThreads;
 // With RESIDUAL the records carry w (vis - pred) from `res` and no PSF is
 // formed.
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kGridThreads, 5) cube_grid_kernel(CubeGridArgs a) {
+__global__ void __launch_bounds__(kGridThreads, 6) cube_grid_kernel(CubeGridArgs a) {
     __shared__ float s_psf[kTile * kRow];
     __shared__ float s_re[kTile * kRow];
     __shared__ float s_im[kTile * kRow];
