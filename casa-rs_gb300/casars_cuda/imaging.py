@@ -857,6 +857,60 @@ def cube_sample_taps(gridder, cube: CubeBatch, weighting: str = "natural", robus
     return tuple(o[0] for o in outs) + (wt[0],)
 
 
+class DirtyAccumulator:
+    """StandardMfsDirtyAccumulator (lib.rs:3259-3380): batches gridded one
+    after another into device-resident PSF and dirty grids (standard
+    gridder, weights already final); finish() gives the normalised PSF and
+    residual images.  Images come back where the last batch was."""
+
+    def __init__(self, gridder):
+        self.gridder = gridder
+        h = C.c_void_p()
+        call("cr_accumulator_create", gridder.ctx.handle, gridder.handle, C.byref(h))
+        self._h = h
+        self.location, self.device = CR_HOST, None
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().cr_accumulator_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, batch: VisibilityBatch) -> GridSums:
+        arrs = _Arrays()
+        b = batch._bind(arrs, False)
+        _prepare(self.gridder, arrs)
+        self.location = b.location
+        self.device = _device_of(batch.u_lambda)
+        s = _lib.Sums()
+        call("cr_accumulator_add", self.gridder.ctx.handle, self._h, C.byref(b), C.byref(s))
+        return GridSums.from_c(s)
+
+    def finish(self):
+        """(psf, residual, PsfState, GridSums of every batch added)."""
+        arrs = _Arrays()
+        arrs.location = self.location
+        if self.location == CR_DEVICE:
+            self.gridder.ctx.use_torch_stream()
+        else:
+            self.gridder.ctx.use_own_stream()
+        g = self.gridder.geometry
+        psf, pp, loc = arrs.out((g.nx, g.ny), np.float32, torch.float32 if torch else None,
+                                self.device)
+        res, rp, _ = arrs.out((g.nx, g.ny), np.float32, torch.float32 if torch else None,
+                              self.device)
+        st, s = _lib.PsfState(), _lib.Sums()
+        call("cr_accumulator_finish", self.gridder.ctx.handle, self._h, pp, rp, loc,
+             C.byref(st), C.byref(s))
+        return psf, res, PsfState(st.psf_peak, st.normalization_sumwt, st.reported_sumwt), \
+            GridSums.from_c(s)
+
+
 class CubePlan:
     """A persistent cube plan (cr_cube_plan): the cube's weighting and records
     made once and replayed by gridding, degridding and residual calls -- the

@@ -623,6 +623,40 @@ int cr_image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* mode
     });
 }
 
+// dirty_grids_to_psf_and_residual_owned (lib.rs:48987-49130): PSF and dirty
+// grids with their sums -> normalised PSF and residual images and the PSF
+// state (synchronises).
+static void dirty_products(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* psf, float2* dirty,
+                           const cr_sums& s, float* psf_out, float* residual_out,
+                           int32_t out_location, cr_psf_state* state) {
+    if (s.normalization_sumwt <= 0.0 || s.reported_sumwt <= 0.0)
+        fail(CR_NO_SAMPLES, "no usable samples");
+    const float k = wp ? 2.0f : 1.0f;
+    const float sumwt_f = (float)s.normalization_sumwt;
+    const size_t np = image_pixels(g);
+    float* psf_img = out_ptr<float>(ctx, psf_out, out_location, np * 4, "psf_image");
+    float* res_img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "res_image");
+    unsigned int* peak_d = (unsigned int*)workspace(ctx, "di_peak", 4);
+    grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img);
+    abs_peak(ctx, psf_img, (int64_t)np, peak_d);
+    unsigned int peak_bits = 0;
+    CR_CUDA_CHECK(cudaMemcpyAsync(&peak_bits, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    float peak;
+    std::memcpy(&peak, &peak_bits, 4);
+    if (!(std::isfinite(peak) && peak > 0.0f))
+        fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
+    scale_image(ctx, psf_img, (int64_t)np, 1.0f, peak_d);
+    grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img);
+    scale_image(ctx, res_img, (int64_t)np, 1.0f, peak_d);
+    if (out_location == CR_HOST) {
+        copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
+        copy_out(ctx, residual_out, res_img, np * 4, CR_HOST);
+    }
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (state) *state = cr_psf_state{peak, sumwt_f, (float)s.reported_sumwt};
+}
+
 int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
                    float* psf_out, float* residual_out, int32_t out_location,
                    cr_psf_state* state, cr_sums* sums, char** err) {
@@ -645,33 +679,8 @@ int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
         cr_sums s{};
         read_sums(ctx, r, &s);
         if (sums) *sums = s;
-        if (s.normalization_sumwt <= 0.0 || s.reported_sumwt <= 0.0)
-            fail(CR_NO_SAMPLES, "no usable samples");
-        const float k = wp ? 2.0f : 1.0f;
-        const float sumwt_f = (float)s.normalization_sumwt;
-        const size_t np = image_pixels(g);
-        float* psf_img = out_ptr<float>(ctx, psf_out, out_location, np * 4, "psf_image");
-        float* res_img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "res_image");
-        unsigned int* peak_d = (unsigned int*)workspace(ctx, "di_peak", 4);
-        grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img);
-        abs_peak(ctx, psf_img, (int64_t)np, peak_d);
-        unsigned int peak_bits = 0;
-        CR_CUDA_CHECK(cudaMemcpyAsync(&peak_bits, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-        float peak;
-        std::memcpy(&peak, &peak_bits, 4);
-        if (!(std::isfinite(peak) && peak > 0.0f))
-            fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
-        scale_image(ctx, psf_img, (int64_t)np, 1.0f, peak_d);
-        grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img);
-        scale_image(ctx, res_img, (int64_t)np, 1.0f, peak_d);
+        dirty_products(ctx, g, wp, psf, dirty, s, psf_out, residual_out, out_location, state);
         tm.mark();
-        if (out_location == CR_HOST) {
-            copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
-            copy_out(ctx, residual_out, res_img, np * 4, CR_HOST);
-        }
-        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-        if (state) *state = cr_psf_state{peak, sumwt_f, (float)s.reported_sumwt};
         set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, tm.between(2, 3), 0.f});
     });
 }
@@ -1492,6 +1501,82 @@ int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         set_timings(ctx, cr_timings{0.f, 0.f, 0.f, 0.f, tm.between(0, 1)});
+    });
+}
+
+// ---- streaming dirty accumulation -----------------------------------------------
+
+int cr_accumulator_create(cr_ctx* ctx, cr_gridder* g, cr_accumulator** out, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && g != nullptr && out != nullptr, "null argument");
+        *out = nullptr;
+        bind(ctx);
+        cr_accumulator* a = new cr_accumulator();
+        a->ctx = ctx;
+        a->g = g;
+        try {
+            const size_t gb = grid_bytes(g);
+            a->psf = (float2*)pool_alloc(ctx, a->pool, "acc_psf", gb);
+            a->dirty = (float2*)pool_alloc(ctx, a->pool, "acc_dirty", gb);
+            CR_CUDA_CHECK(cudaMemsetAsync(a->psf, 0, gb, ctx->stream));
+            CR_CUDA_CHECK(cudaMemsetAsync(a->dirty, 0, gb, ctx->stream));
+            CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        } catch (...) {
+            cr_accumulator_destroy(a);
+            throw;
+        }
+        *out = a;
+    });
+}
+
+void cr_accumulator_destroy(cr_accumulator* a) {
+    if (!a) return;
+    cudaSetDevice(a->ctx->device);
+    pool_free(a->ctx, a->pool);
+    cudaStreamSynchronize(a->ctx->stream);
+    delete a;
+}
+
+int cr_accumulator_add(cr_ctx* ctx, cr_accumulator* a, const cr_vis_batch* batch,
+                       cr_sums* batch_sums, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && a != nullptr && a->ctx == ctx,
+             "accumulator belongs to another context");
+        bind(ctx);
+        StageTimer tm(ctx);
+        tm.mark();
+        DeviceBatch b = device_batch(ctx, batch, false);
+        Records r = plan(ctx, a->g, nullptr, b);
+        tm.mark();
+        grid_records(ctx, a->g, nullptr, r, a->psf, a->dirty, 0);
+        tm.mark();
+        cr_sums s{};
+        read_sums(ctx, r, &s);
+        a->sums.normalization_sumwt += s.normalization_sumwt;
+        a->sums.reported_sumwt += s.reported_sumwt;
+        a->sums.gridded += s.gridded;
+        a->sums.skipped += s.skipped;
+        a->sums.unique_records += s.unique_records;
+        a->sums.taps += s.taps;
+        a->batches++;
+        if (batch_sums) *batch_sums = s;
+        set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), 0.f, 0.f, 0.f});
+    });
+}
+
+int cr_accumulator_finish(cr_ctx* ctx, cr_accumulator* a, float* psf, float* residual,
+                          int32_t out_location, cr_psf_state* state, cr_sums* total, char** err) {
+    return guarded(err, [&] {
+        need(ctx != nullptr && a != nullptr && a->ctx == ctx,
+             "accumulator belongs to another context");
+        bind(ctx);
+        if (total) *total = a->sums;
+        StageTimer tm(ctx);
+        tm.mark();
+        dirty_products(ctx, a->g, nullptr, a->psf, a->dirty, a->sums, psf, residual,
+                       out_location, state);
+        tm.mark();
+        set_timings(ctx, cr_timings{0.f, 0.f, 0.f, tm.between(0, 1), 0.f});
     });
 }
 

@@ -348,6 +348,16 @@ inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) 
 // A materialised plan of one batch (the device form of the reference's
 // planned taps): its records outlive the call that made them, in the plan's
 // own pool, and serve any number of gridding and degridding calls.
+struct cr_accumulator {
+    cr_ctx* ctx = nullptr;
+    cr_gridder* g = nullptr;
+    cr::Pool pool;
+    float2* psf = nullptr;
+    float2* dirty = nullptr;
+    cr_sums sums = {};
+    int64_t batches = 0;
+};
+
 struct cr_cube_plan {
     cr_ctx* ctx = nullptr;
     cr_gridder* g = nullptr;

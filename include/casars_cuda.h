@@ -60,6 +60,7 @@ typedef struct cr_gridder cr_gridder;
 typedef struct cr_wproj cr_wproj;
 typedef struct cr_plan cr_plan;
 typedef struct cr_cube_plan cr_cube_plan;
+typedef struct cr_accumulator cr_accumulator;
 
 /* ImageGeometry (types.rs:885-930). */
 typedef struct {
@@ -281,6 +282,21 @@ int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
  * normalisation: grid, centred inverse FFT scaled by Nx*Ny, crop, correct. */
 int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batch,
                float* image, int32_t out_location, char** err);
+
+/* ---- streaming dirty accumulation ----------------------------------------
+ * StandardMfsDirtyAccumulator (lib.rs:3259-3380): natural-weighted batches
+ * (weights already final) gridded one after another into one pair of
+ * device-resident PSF and dirty grids with the standard gridder, so a caller
+ * can load a MeasurementSet chunk by chunk and release each; finish forms
+ * the normalised PSF and residual images (dirty_grids_to_psf_and_residual_
+ * owned) from the accumulated grids and sums, CR_NO_SAMPLES when nothing
+ * usable was added.  The accumulator can finish more than once. */
+int cr_accumulator_create(cr_ctx* ctx, cr_gridder* g, cr_accumulator** out, char** err);
+void cr_accumulator_destroy(cr_accumulator* acc);
+int cr_accumulator_add(cr_ctx* ctx, cr_accumulator* acc, const cr_vis_batch* batch,
+                       cr_sums* batch_sums, char** err);
+int cr_accumulator_finish(cr_ctx* ctx, cr_accumulator* acc, float* psf, float* residual,
+                          int32_t out_location, cr_psf_state* state, cr_sums* total, char** err);
 
 /* ---- batched spectral cube ------------------------------------------------
  * Channel c's batch is the unflagged samples of rows r = 0..rows-1 with
