@@ -12,3 +12,4 @@ from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, Psf
                       DirtyAccumulator)
 from .clean import (CleanConfig, CleanResult, clean_cycle_threshold, run_cotton_schwab,  # noqa: F401
                     CubeCleanResult, cube_clean_loop, run_cube_clean, run_clark_cotton_schwab)
+from .run import ImagingRequest, ImagingResult, run_imaging  # noqa: F401
