@@ -88,6 +88,7 @@ SIGNATURES = {
     "cr_ctx_last_timings": (C.c_int, [_p, C.POINTER(Timings)]),
     "cr_ctx_launch_count": (_i64, [_p]),
     "cr_ctx_set_cube_graphs": (C.c_int, [_p, _i32]),
+    "cr_ctx_set_image_fft_precision": (C.c_int, [_p, _i32]),
     "cr_accumulator_create": (C.c_int, [_p, _p, C.POINTER(_p), _err]),
     "cr_accumulator_destroy": (None, [_p]),
     "cr_accumulator_add": (C.c_int, [_p, _p, C.POINTER(VisBatch), C.POINTER(Sums), _err]),

@@ -134,6 +134,19 @@ class Context:
         if self._lib.cr_ctx_set_cube_graphs(self._h, 1 if enable else 0) != 0:
             raise ValueError("null context")
 
+    def set_image_fft_precision(self, precision):
+        """Image-stage FFT precision of the single-plane calls, mirroring
+        DirtyProductFftPolicy.precision (casa-imaging/src/lib.rs:1280-1312):
+        "auto" or "f64" (the default, 64) run FP64; "f32" (32) runs FP32."""
+        bits = {"auto": 0, "f32": 32, "f64": 64}.get(precision, precision)
+        if self._lib.cr_ctx_set_image_fft_precision(self._h, int(bits)) != 0:
+            raise ValueError(f"unsupported FFT precision {precision!r}")
+        self._image_fft_bits = 32 if int(bits) == 32 else 64
+
+    @property
+    def image_fft_precision(self) -> str:
+        return "f32" if getattr(self, "_image_fft_bits", 64) == 32 else "f64"
+
     @property
     def launch_count(self) -> int:
         return int(self._lib.cr_ctx_launch_count(self._h))

@@ -33,6 +33,8 @@ class ImagingRequest:
     w_project_planes: Optional[int] = None
     oversampling: int = 100
     padding: float = 1.2
+    # ImagingFftPlan.dirty_products.precision (lib.rs:1314-1319): auto | f32 | f64
+    fft_precision: str = "auto"
 
 
 @dataclass
@@ -92,6 +94,15 @@ def run_imaging(ctx: im.Context, request: ImagingRequest) -> ImagingResult:
     if not request.visibility_batches:
         raise ValueError("no visibility batches")
     batch = _merge(request.visibility_batches)
+    previous = ctx.image_fft_precision
+    ctx.set_image_fft_precision(request.fft_precision)
+    try:
+        return _run(ctx, request, batch)
+    finally:
+        ctx.set_image_fft_precision(previous)
+
+
+def _run(ctx: im.Context, request: ImagingRequest, batch: im.VisibilityBatch) -> ImagingResult:
     gg = im.StandardGridder(ctx, request.geometry, request.oversampling, request.padding)
     wp = None
     if request.w_term_mode == "wproject":

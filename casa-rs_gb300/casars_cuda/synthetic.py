@@ -101,7 +101,7 @@ def visibilities(u, v, w, sky: Sky, nx: int, ny: int, cell: float, noise_sigma: 
 
 def visibilities_torch(u, v, w, sky: Sky, nx: int, ny: int, cell: float, noise_sigma: float,
                        seed: int, device="cuda", chunk: int = 1 << 19):
-    """The same DFT on the GPU with torch (float64 phase), for large configs."""
+    """The same DFT on the GPU with torch (float64 phase), for large observations."""
     import torch
     l, m, nm1 = sky.lmn(nx, ny, cell)
     L = torch.tensor(np.stack([l, m, nm1], 0), dtype=torch.float64, device=device)
@@ -154,20 +154,20 @@ def observation(max_radius_m: float, hours: float, dump_s: float, freq_hz: float
     return Observation(name, image, image, cell, freq_hz, u, v, w, sky, seed)
 
 
-def config1(seed: int = 1) -> Observation:
+def pswf_512_observation(seed: int = 1) -> Observation:
     """27 antennas out to 1 km, 1 h of 10 s dumps at 1.4 GHz (126,360 rows),
     512 x 512 image, 20 points 0.01-1 Jy, noise 0.01 Jy."""
-    obs = observation(1000.0, 1.0, 10.0, 1.4e9, 512, 20, 0.01, 1.0, seed, "config1")
+    obs = observation(1000.0, 1.0, 10.0, 1.4e9, 512, 20, 0.01, 1.0, seed, "pswf_512")
     rng = np.random.default_rng(seed + 1000)
     obs.vis = visibilities(obs.u, obs.v, np.zeros_like(obs.w), obs.sky, 512, 512, obs.cell,
                            0.01, rng, w_term=False)
     return obs
 
 
-def config2_geometry(seed: int = 2) -> Observation:
+def wproj_4096_observation(seed: int = 2) -> Observation:
     """27 antennas out to 21 km, 8 h of 2 s dumps at 1.4 GHz (5,054,400 rows),
     4096 x 4096 image, 200 points 1 mJy-1 Jy; visibilities not yet made."""
-    return observation(21000.0, 8.0, 2.0, 1.4e9, 4096, 200, 1e-3, 1.0, seed, "config2")
+    return observation(21000.0, 8.0, 2.0, 1.4e9, 4096, 200, 1e-3, 1.0, seed, "wproj_4096")
 
 
 # ----------------------------------------------------------------------------
@@ -270,14 +270,14 @@ def gaussian_model(rng, n: int, nx: int, ny: int, fmin: float, fmax: float,
     return img.astype(np.float32)
 
 
-def config3(seed: int = 3) -> Observation:
+def pair_2048_observation(seed: int = 3) -> Observation:
     """Differentiable-imaging workload: 27 antennas to 5 km, 8 h of 5 s dumps
     at 1.4 GHz (2,021,760 rows), 2048 x 2048 image; the sky is a Gaussian
     model image (gaussian_model, 50 components 0.01-1 Jy, FWHM 1-5 px)."""
-    return observation(5000.0, 8.0, 5.0, 1.4e9, 2048, 0, 0.01, 1.0, seed, "config3")
+    return observation(5000.0, 8.0, 5.0, 1.4e9, 2048, 0, 0.01, 1.0, seed, "pair_2048")
 
 
-def config5(seed: int = 5):
+def major_minor_2048_observation(seed: int = 5):
     """Major/minor-loop workload: 27 antennas to 21 km, 8 h of 4 s dumps
     (2,527,200 rows) at 4 channels over 1.3-1.5 GHz gridded together (MFS:
     10,108,800 visibilities), 2048 x 2048 image with the cell 1/3 of the beam
@@ -296,5 +296,5 @@ def config5(seed: int = 5):
     sky = point_sky(rng, 300, nx, nx, 1e-3, 1.0)
     sky.x_pix, sky.y_pix = np.round(sky.x_pix), np.round(sky.y_pix)
     model = model_image(sky, nx, nx) + gaussian_model(rng, 5, nx, nx, 0.1, 0.5, 3.0, 10.0)
-    obs = Observation("config5", nx, nx, cell, float(freqs.mean()), u, v, w, sky, seed)
+    obs = Observation("major_minor_2048", nx, nx, cell, float(freqs.mean()), u, v, w, sky, seed)
     return obs, model

@@ -586,6 +586,10 @@ int cr_grid_residual(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batc
     });
 }
 
+// Whether the image-stage FFTs of single-plane calls run in FP32 (the
+// dirty-product policy's F32 choice, lib.rs:1280-1312 and 2428-2472).
+static bool image_single(const cr_ctx* ctx) { return ctx->image_fft_bits == 32; }
+
 int cr_grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* grid,
                      int32_t grid_location, float scale, float* image, int32_t out_location,
                      char** err) {
@@ -601,7 +605,7 @@ int cr_grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* grid
                                       ctx->stream));
         size_t ib = image_pixels(g) * 4;
         float* img = out_ptr<float>(ctx, image, out_location, ib, "image");
-        grid_to_image(ctx, g, wp, work, scale, img);
+        grid_to_image(ctx, g, wp, work, scale, img, image_single(ctx));
         if (out_location == CR_HOST) copy_out(ctx, image, img, ib, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
@@ -617,7 +621,7 @@ int cr_image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* mode
                                                     model_location, "model");
         size_t gb = grid_bytes(g);
         float2* out = out_ptr<float2>(ctx, grid, out_location, gb, "model_grid");
-        image_to_grid(ctx, g, wp, m, out);
+        image_to_grid(ctx, g, wp, m, out, image_single(ctx));
         if (out_location == CR_HOST) copy_out(ctx, grid, out, gb, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
@@ -637,7 +641,7 @@ static void dirty_products(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* psf
     float* psf_img = out_ptr<float>(ctx, psf_out, out_location, np * 4, "psf_image");
     float* res_img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "res_image");
     unsigned int* peak_d = (unsigned int*)workspace(ctx, "di_peak", 4);
-    grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img);
+    grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img, image_single(ctx));
     abs_peak(ctx, psf_img, (int64_t)np, peak_d);
     unsigned int peak_bits = 0;
     CR_CUDA_CHECK(cudaMemcpyAsync(&peak_bits, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -647,7 +651,7 @@ static void dirty_products(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* psf
     if (!(std::isfinite(peak) && peak > 0.0f))
         fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
     scale_image(ctx, psf_img, (int64_t)np, 1.0f, peak_d);
-    grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img);
+    grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img, image_single(ctx));
     scale_image(ctx, res_img, (int64_t)np, 1.0f, peak_d);
     if (out_location == CR_HOST) {
         copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
@@ -698,7 +702,7 @@ int cr_residual_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_bat
         const size_t np = image_pixels(g);
         const float* m = (const float*)device_input(ctx, model, np * 4, model_location, "model");
         float2* mgrid = (float2*)workspace(ctx, "ri_model_grid", gb);
-        image_to_grid(ctx, g, wp, m, mgrid);
+        image_to_grid(ctx, g, wp, m, mgrid, image_single(ctx));
         Records r = plan(ctx, g, wp, b);
         degrid_records(ctx, g, wp, r, mgrid);
         float2* res = (float2*)workspace(ctx, "ri_residual_grid", gb);
@@ -706,7 +710,7 @@ int cr_residual_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_bat
         grid_records(ctx, g, wp, r, nullptr, res, 1);
         float* img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "ri_image");
         const float k = wp ? 2.0f : 1.0f;
-        grid_to_image(ctx, g, wp, res, k / state->normalization_sumwt, img);
+        grid_to_image(ctx, g, wp, res, k / state->normalization_sumwt, img, image_single(ctx));
         scale_image(ctx, img, (int64_t)np, 1.0f / state->psf_peak, nullptr);
         if (out_location == CR_HOST) copy_out(ctx, residual_out, img, np * 4, CR_HOST);
         cr_sums s{};
@@ -727,7 +731,7 @@ int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         const float* m = (const float*)device_input(ctx, model, image_pixels(g) * 4,
                                                     model_location, "model");
         float2* mgrid = (float2*)workspace(ctx, "pr_model_grid", gb);
-        image_to_grid(ctx, g, wp, m, mgrid);
+        image_to_grid(ctx, g, wp, m, mgrid, image_single(ctx));
         Records r = plan(ctx, g, wp, b);
         degrid_records(ctx, g, wp, r, mgrid);
         float2* out = out_ptr<float2>(ctx, pred, out_location, (size_t)b.n * 8 + 8, "pred");
@@ -755,7 +759,7 @@ int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         // F^H = (Nx Ny) x the scaled inverse; the image-side factor is the
         // forward apodisation's (corr, times sinc for W-projection)
         float n2 = (float)((double)g->info.grid_nx * (double)g->info.grid_ny);
-        grid_to_image_adjoint(ctx, g, wp, grid, n2, img);
+        grid_to_image_adjoint(ctx, g, wp, grid, n2, img, image_single(ctx));
         if (out_location == CR_HOST) copy_out(ctx, image, img, np * 4, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     });
@@ -876,7 +880,7 @@ int cr_plan_residual_image(cr_ctx* ctx, cr_plan* p, const float* model, int32_t 
         const size_t np = image_pixels(p->g);
         const float* m = (const float*)device_input(ctx, model, np * 4, model_location, "model");
         float2* mgrid = (float2*)workspace(ctx, "ri_model_grid", gb);
-        image_to_grid(ctx, p->g, p->wp, m, mgrid);
+        image_to_grid(ctx, p->g, p->wp, m, mgrid, image_single(ctx));
         tm.mark();
         degrid_records(ctx, p->g, p->wp, p->rec, mgrid);
         tm.mark();
@@ -886,7 +890,8 @@ int cr_plan_residual_image(cr_ctx* ctx, cr_plan* p, const float* model, int32_t 
         tm.mark();
         float* img = out_ptr<float>(ctx, residual_out, out_location, np * 4, "ri_image");
         const float k = p->wp ? 2.0f : 1.0f;
-        grid_to_image(ctx, p->g, p->wp, res, k / state->normalization_sumwt, img);
+        grid_to_image(ctx, p->g, p->wp, res, k / state->normalization_sumwt, img,
+                      image_single(ctx));
         scale_image(ctx, img, (int64_t)np, 1.0f / state->psf_peak, nullptr);
         tm.mark();
         if (out_location == CR_HOST) copy_out(ctx, residual_out, img, np * 4, CR_HOST);
@@ -1186,6 +1191,14 @@ int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable) {
     if (!ctx) return CR_INVALID;
     ctx->cube_graphs_enabled = enable != 0;
     if (!enable) ctx->cube_graphs.clear();
+    return CR_OK;
+}
+
+// FftPrecisionChoice {Auto, F32, F64} (fft_backend.rs:61-68) for the image
+// stage of single-plane calls: 0 (Auto) and 64 run FP64, 32 runs FP32.
+int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits) {
+    if (!ctx || (bits != 0 && bits != 32 && bits != 64)) return CR_INVALID;
+    ctx->image_fft_bits = bits == 32 ? 32 : 64;
     return CR_OK;
 }
 

@@ -227,8 +227,11 @@ void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float sca
 }
 
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
-                           float* image) {
-    grid_to_image_impl<double2>(ctx, g, wp, grid, scale, image, true, nullptr);
+                           float* image, bool single) {
+    if (single)
+        grid_to_image_impl<float2>(ctx, g, wp, grid, scale, image, true, nullptr);
+    else
+        grid_to_image_impl<double2>(ctx, g, wp, grid, scale, image, true, nullptr);
 }
 
 void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid,

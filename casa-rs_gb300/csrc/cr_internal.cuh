@@ -61,6 +61,9 @@ struct cr_ctx {
     std::map<std::string, uint32_t> cube_chunk;
     std::map<std::string, std::shared_ptr<cr::CubeGraph>> cube_graphs;
     bool cube_graphs_enabled = true;
+    // Precision of the image-stage FFTs of single-plane calls: 64 (default)
+    // or 32.
+    int image_fft_bits = 64;
     bool capturing = false;
     uint64_t ws_epoch = 0;
     // small pinned host buffer for device->host scalars
@@ -212,7 +215,7 @@ void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float
                    float* image, bool single = false);
 // the exact adjoint of image_to_grid's image-side factor (no sinc division)
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
-                           float* image);
+                           float* image, bool single = false);
 // model image (device) -> centred model grid (device)
 void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model, float2* grid,
                    bool single = false);

@@ -171,6 +171,13 @@ int cr_ctx_synchronize(cr_ctx* ctx, char** err);
 int cr_ctx_last_timings(cr_ctx* ctx, cr_timings* out);
 /* Number of this library's kernel launches since the context was created. */
 int64_t cr_ctx_launch_count(cr_ctx* ctx);
+/* Precision of the image-stage FFTs (grid correction, fftshift, 2-D FFT) of
+ * the single-plane calls: 0 (Auto) or 64 = FP64, the default; 32 = FP32.
+ * Replaces the precision field of DirtyProductFftPolicy
+ * (crates/casa-imaging/src/lib.rs:1280-1312; FftPrecisionChoice at
+ * crates/casa-imaging/src/fft_backend.rs:61-68). Cube plans carry their own
+ * setting (cr_cube_plan_set_fft_precision). */
+int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits);
 const char* cr_version(void);
 
 /* ---- gridders ------------------------------------------------------------

@@ -31,7 +31,7 @@ PLANES = 32
 @pytest.fixture(scope="module")
 def cfg():
     ctx = cc.Context(0)
-    obs = S.config3(3)
+    obs = S.pair_2048_observation(3)
     nx = obs.nx
     dev = torch.device("cuda", 0)
     model = S.gaussian_model(np.random.default_rng(33), 50, nx, nx, 0.01, 1.0)

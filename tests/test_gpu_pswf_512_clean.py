@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def obs():
-    return S.config1(seed=1)
+    return S.pswf_512_observation(seed=1)
 
 
 @pytest.fixture(scope="module")
@@ -33,7 +33,7 @@ def ctx():
 
 
 @pytest.mark.parametrize("os_", [128, 100])
-def test_config1_dirty_and_clean(ctx, obs, os_):
+def test_pswf_512_dirty_and_clean(ctx, obs, os_):
     nx = obs.nx
     geom = O.Geometry(nx, nx, obs.cell, obs.cell)
     og = O.StdGridder(geom, os_)

@@ -25,7 +25,7 @@ def f32_from_bits(b):
 def test_grid_padding():
     assert O.padded_len(512, 1.2) == KATS["grid_padding_512"]["expected"]
     assert O.padded_len(257, 1.3) == KATS["grid_padding_257_casa_1p3"]["expected"]
-    # the BASELINE image sizes
+    # the image sizes of the benchmark workloads
     assert [O.padded_len(n) for n in (512, 1024, 2048, 4096)] == [640, 1250, 2500, 5000]
 
 
