@@ -179,6 +179,7 @@ void cube_replay(cr_ctx* ctx, CubeGraph& G, cr_sums* sums) {
     try {
         cube_read_sums(ctx, G.cr, sums);
         CR_CUDA_CHECK(cudaEventSynchronize(ctx->ev[1]));
+        check_device_status(ctx);
     } catch (...) {
         ctx->stream = caller;
         throw;
@@ -313,6 +314,7 @@ int cube_run(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch, int32_t wei
         set_timings(ctx, cr_timings{tm.between(0, 1), tm.between(1, 2), tm.between(2, 3), 0.f, 0.f});
         cube_read_sums(ctx, cr, sums);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
     });
 }
 
@@ -339,6 +341,9 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
         for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
         for (auto& e : c->kev) CR_CUDA_CHECK(cudaEventCreate(&e));
         CR_CUDA_CHECK(cudaMallocHost(&c->pinned, 4096));
+        CR_CUDA_CHECK(cudaHostAlloc((void**)&c->status_h, 64, cudaHostAllocMapped));
+        *c->status_h = 0;
+        CR_CUDA_CHECK(cudaHostGetDevicePointer((void**)&c->status_d, c->status_h, 0));
         *out = c;
     });
 }
@@ -357,6 +362,7 @@ void cr_ctx_destroy(cr_ctx* ctx) {
     for (auto& e : ctx->kev)
         if (e) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->status_h) cudaFreeHost(ctx->status_h);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -414,7 +420,9 @@ int cr_gridder_create(cr_ctx* ctx, const cr_geometry* geom, double padding, int3
         g->corr_x_h = correction_axis(gnx);
         g->corr_y_h = correction_axis(gny);
         try {
-            CR_CUDA_CHECK(cudaMalloc(&g->taps_d, g->taps_h.size() * 4));
+            g->taps_bytes = (uint32_t)((g->taps_h.size() * 4 + 15) & ~size_t(15));
+            CR_CUDA_CHECK(cudaMalloc(&g->taps_d, g->taps_bytes));
+            CR_CUDA_CHECK(cudaMemset(g->taps_d, 0, g->taps_bytes));
             CR_CUDA_CHECK(cudaMalloc(&g->corr_x_d, (size_t)gnx * 4));
             CR_CUDA_CHECK(cudaMalloc(&g->corr_y_d, (size_t)gny * 4));
             CR_CUDA_CHECK(cudaMemcpy(g->taps_d, g->taps_h.data(), g->taps_h.size() * 4, cudaMemcpyHostToDevice));
@@ -1293,6 +1301,7 @@ int cr_cube_plan_grid_dirty(cr_ctx* ctx, cr_cube_plan* p, float* psf_grids, floa
             copy_out(ctx, dirty_grids, dirty, C * cells * 8, CR_HOST);
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
         set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f});
     });
 }
@@ -1314,6 +1323,7 @@ int cr_cube_plan_degrid(cr_ctx* ctx, cr_cube_plan* p, const float* model_grids,
         tm.mark();
         if (out_location == CR_HOST) copy_out(ctx, pred, pr, C * (size_t)p->rec.R * 8, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
         set_timings(ctx, cr_timings{0.f, 0.f, tm.between(0, 1), 0.f, 0.f});
     });
 }
@@ -1341,6 +1351,7 @@ int cr_cube_plan_grid_residual(cr_ctx* ctx, cr_cube_plan* p, const float* model_
                 copy_out(ctx, (float2*)residual_grids + (size_t)c * cells, res + (size_t)c * cells,
                          cells * 8, CR_HOST);
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
         set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, 0.f, 0.f});
     });
 }
@@ -1408,6 +1419,7 @@ int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
             copy_out(ctx, residual_images, ri, C * np * 4, CR_HOST);
         }
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
         set_timings(ctx, cr_timings{0.f, tm.between(0, 1), 0.f, tm.between(1, 2), 0.f});
     });
 }
@@ -1453,6 +1465,7 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
         }
         tm.mark();
         CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        check_device_status(ctx);
         set_timings(ctx, cr_timings{0.f, tm.between(1, 2), 0.f,
                                   tm.between(0, 1) + tm.between(2, 3), 0.f});
     });

@@ -2,7 +2,10 @@
 #include <cmath>
 #include <cstring>
 
+#include <cudaTypedefs.h>
+
 #include "cr_internal.cuh"
+#include "cr_tma.cuh"
 
 namespace cr {
 
@@ -47,6 +50,15 @@ void note_launch(cr_ctx* ctx, const char* what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) fail(CR_CUDA, std::string("launch of ") + what + ": " + cudaGetErrorString(e));
     ctx->launches++;
+}
+
+void check_device_status(cr_ctx* ctx) {
+    volatile int* st = ctx->status_h;
+    if (!st) return;
+    const int s = *st;
+    if (s == 0) return;
+    *st = 0;
+    fail(s, "a kernel's bounded wait for a bulk copy gave up");
 }
 
 void kernel_mark(cr_ctx* ctx, int which, bool end) {
@@ -425,5 +437,35 @@ DeviceBatch device_batch(cr_ctx* ctx, const cr_vis_batch* b, bool need_w) {
     d.vis = (const float2*)device_input(ctx, b->vis, n * 8, b->location, "vis");
     return d;
 }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+bool encode_tensor_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1,
+                          uint64_t d2, uint64_t stride1, uint64_t stride2, uint32_t b0,
+                          uint32_t b1) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }();
+    if (!encode) return false;
+    if (((uintptr_t)base & 15) || (stride1 & 15) || (stride2 & 15) || ((b0 * 4) & 15) ||
+        b0 == 0 || b1 == 0 || b0 > 256 || b1 > 256 || d0 == 0 || d1 == 0 || d2 == 0)
+        return false;
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {stride1, stride2};
+    const cuuint32_t box[3] = {b0, b1, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
 
 }  // namespace cr

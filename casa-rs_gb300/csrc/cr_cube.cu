@@ -31,10 +31,12 @@
 // no global atomics on the output grids.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "cr_fixed.cuh"
 #include "cr_internal.cuh"
+#include "cr_tma.cuh"
 
 namespace cr {
 
@@ -47,6 +49,8 @@ constexpr int kRowsPerBlock = 4096;   // rows of one channel per planning block
 // each warp-wide atomic touches 32 distinct banks.
 constexpr int kRow = 39;
 constexpr int kMaxTapRows = 513;      // oversampling up to 512
+// the tap table in floats, rounded up to whole 16-byte bulk-copy units
+constexpr int kTapFloats = (kMaxTapRows * 7 + 3) / 4 * 4;
 
 struct CubeChan {
     double lscale;       // f / c
@@ -620,8 +624,10 @@ struct CubeGridArgs {
     const float* rec_w;
     const uint32_t* bin_start;   // [C * ntiles + 1]
     const uint32_t* cell_end;    // [C * ntiles * 1024] end of each cell bin
-    const float* taps;           // [tap_rows][7]
+    const float* taps;           // [tap_rows][7], zero-padded to taps_bytes
     int32_t tap_rows;
+    uint32_t taps_bytes;
+    int* status;                 // set to CR_TIMEOUT when a bounded wait gives up
     int64_t ntx, nty, gnx, gny;
     const uint2* items;          // (output tile bin, chunk)
     uint32_t grid_chunk;         // records per chunk
@@ -650,7 +656,8 @@ __global__ void __launch_bounds__(kGridThreads, 6) cube_grid_kernel(CubeGridArgs
     __shared__ float s_psf[kTile * kRow];
     __shared__ float s_re[kTile * kRow];
     __shared__ float s_im[kTile * kRow];
-    __shared__ float s_taps[kMaxTapRows * 7];
+    __shared__ __align__(16) float s_taps[kTapFloats];
+    __shared__ __align__(8) uint64_t s_bar;
     // per warp, the decoded records of its current batch of 32:
     // {run key, x tap row * 7, y tap row * 7, weight} and {w vis}
     __shared__ int4 s_ra[kGridThreads];
@@ -659,7 +666,21 @@ __global__ void __launch_bounds__(kGridThreads, 6) cube_grid_kernel(CubeGridArgs
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t ntiles = a.ntx * a.nty;
     const unsigned long long n_items = *a.n_items;
-    for (int k = tid; k < a.tap_rows * 7; k += kGridThreads) s_taps[k] = a.taps[k];
+    // the tap table by one bulk copy
+    if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_fence_init();
+        mbar_expect_tx(&s_bar, a.taps_bytes);
+        bulk_load(s_taps, a.taps, a.taps_bytes, &s_bar);
+    }
+    __syncthreads();
+    if (!__syncthreads_and(mbar_wait(&s_bar, 0))) {
+        if (tid == 0) {
+            atomicExch(a.status, CR_TIMEOUT);
+            mbar_wait(&s_bar, 0);   // let the copy land before the block exits
+        }
+        return;
+    }
     int4* w_ra = s_ra + warp * 32;
     float2* w_rb = s_rb + warp * 32;
     for (;;) {
@@ -851,11 +872,13 @@ struct CubeDegridArgs {
     const uint2* items;          // (bin, chunk)
     const unsigned long long* n_items;
     unsigned int* item_counter;
-    const float* taps;
+    const float* taps;           // zero-padded to taps_bytes
+    uint32_t taps_bytes;
     const float2* grid;          // [C][gnx][gny]
     float2* pred;                // [C][R]
     const float* rec_w;          // RESIDUAL: imaging weight per record
     float2* res;                 // RESIDUAL: w vis - w pred per record
+    int* status;                 // set to CR_TIMEOUT when a bounded wait gives up
 };
 
 // Bins in turn.  The block stages the 38 x 38 model footprint of its home
@@ -864,36 +887,102 @@ struct CubeDegridArgs {
 // (float32), and the 7 lanes' sums are reduced with shuffles.
 // With RESIDUAL each record's w vis - w pred goes to res (record order)
 // instead of pred (sample order).
-template <bool RESIDUAL>
-__global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArgs a) {
+// With TMA the footprints come as tensor-map boxes (float32 view
+// [C][gnx][2 gny], box 76 x 38, zero-filled past the grid edge) into two
+// buffers: while the block works on one item, the next item's footprint is
+// already in flight.  Without TMA (a grid whose rows are not a multiple of
+// 16 bytes, or an unaligned base) the block loads each footprint itself.
+// The tap table arrives by one bulk copy in either case.
+template <bool RESIDUAL, bool TMA>
+__global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
+    const __grid_constant__ CUtensorMap gmap, CubeDegridArgs a) {
     constexpr int kFoot = kTile + 6;
-    __shared__ float2 s_g[kFoot * kRow];   // model footprint, (re, im) pairs
-    __shared__ float s_taps[kMaxTapRows * 7];
-    __shared__ int s_item;
+    constexpr int kPitch = TMA ? kFoot : kRow;   // float2 per footprint row
+    constexpr int kBufs = TMA ? 2 : 1;
+    constexpr uint32_t kBoxBytes = kFoot * kFoot * 8;
+    // each buffer starts on a 128-byte boundary (tensor copy destinations)
+    constexpr int kBufElems = (kFoot * kPitch * 8 + 127) / 128 * 16;
+    __shared__ __align__(128) float2 s_g[kBufs][kBufElems];
+    __shared__ __align__(8) uint64_t s_bar[3];   // footprint buffers 0, 1; taps
+    __shared__ int s_item[2];
+    extern __shared__ __align__(16) float s_taps[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int sub = lane >> 3, ix = lane & 7;   // record slot, tap column (7 = idle)
     const unsigned long long n_items = *a.n_items;
-    for (int k = tid; k < a.tap_rows * 7; k += kCubeThreads) s_taps[k] = a.taps[k];
+    // thread 0: the footprint of `item` into buffer `buf`
+    auto issue = [&](int item, int buf) {
+        const int64_t bin = a.items[item].x;
+        const int64_t c = bin / a.ntiles, T = bin % a.ntiles;
+        const int gx0 = (int)((T / a.nty) * kTile), gy0 = (int)((T % a.nty) * kTile);
+        mbar_expect_tx(&s_bar[buf], kBoxBytes);
+        tensor_load_3d(&s_g[buf][0], &gmap, 2 * gy0, gx0, (int)c, &s_bar[buf]);
+    };
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) mbar_init(&s_bar[k], 1);
+        mbar_fence_init();
+        mbar_expect_tx(&s_bar[2], a.taps_bytes);
+        bulk_load(s_taps, a.taps, a.taps_bytes, &s_bar[2]);
+        const int first = (int)atomicAdd(a.item_counter, 1u);
+        s_item[0] = first;
+        if (TMA) {
+            tensormap_prefetch(&gmap);
+            if ((unsigned long long)first < n_items) issue(first, 0);
+        }
+    }
+    __syncthreads();
+    if (!__syncthreads_and(mbar_wait(&s_bar[2], 0))) {
+        if (tid == 0) {
+            atomicExch(a.status, CR_TIMEOUT);
+            // let this block's copies in flight land before it exits
+            mbar_wait(&s_bar[2], 0);
+            if (TMA && (unsigned long long)s_item[0] < n_items) mbar_wait(&s_bar[0], 0);
+        }
+        return;
+    }
+    uint32_t phase = 0u;   // bit k: parity of buffer k's next phase
+    int b = 0;
     for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
-        __syncthreads();
-        const int64_t item = s_item;
+        const int64_t item = s_item[b];
         if ((unsigned long long)item >= n_items) break;
+        if (TMA) {
+            if (tid == 0) {
+                const int next = (int)atomicAdd(a.item_counter, 1u);
+                s_item[b ^ 1] = next;
+                if ((unsigned long long)next < n_items) issue(next, b ^ 1);
+            }
+        } else if (tid == 0) {
+            s_item[b ^ 1] = (int)atomicAdd(a.item_counter, 1u);
+        }
         const uint2 it = a.items[item];
         const int64_t bin = it.x;
         const uint32_t lo = a.bin_start[bin] + it.y * kDegridChunk;
         const uint32_t hi = min(a.bin_start[bin + 1], lo + kDegridChunk);
-        const int64_t c = bin / a.ntiles, T = bin % a.ntiles;
-        const int64_t gx0 = (T / a.nty) * kTile, gy0 = (T % a.nty) * kTile;
-        const float2* g = a.grid + c * a.gnx * a.gny;
-        for (int k = tid; k < kFoot * kFoot; k += kCubeThreads) {
-            const int fx = k / kFoot, fy = k % kFoot;
-            const int64_t x = gx0 + fx, y = gy0 + fy;
-            float2 v = make_float2(0.0f, 0.0f);
-            if (x < a.gnx && y < a.gny) v = __ldg(&g[x * a.gny + y]);
-            s_g[fx * kRow + fy] = v;
+        const float2* sg = &s_g[TMA ? b : 0][0];
+        if (TMA) {
+            if (!__syncthreads_and(mbar_wait(&s_bar[b], (phase >> b) & 1u))) {
+                if (tid == 0) {
+                    atomicExch(a.status, CR_TIMEOUT);
+                    // let this block's copies in flight land before it exits
+                    mbar_wait(&s_bar[b], (phase >> b) & 1u);
+                    if ((unsigned long long)s_item[b ^ 1] < n_items)
+                        mbar_wait(&s_bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+                }
+                return;
+            }
+            phase ^= 1u << b;
+        } else {
+            const int64_t c = bin / a.ntiles, T = bin % a.ntiles;
+            const int64_t gx0 = (T / a.nty) * kTile, gy0 = (T % a.nty) * kTile;
+            const float2* g = a.grid + c * a.gnx * a.gny;
+            for (int k = tid; k < kFoot * kFoot; k += kCubeThreads) {
+                const int fx = k / kFoot, fy = k % kFoot;
+                const int64_t x = gx0 + fx, y = gy0 + fy;
+                float2 v = make_float2(0.0f, 0.0f);
+                if (x < a.gnx && y < a.gny) v = __ldg(&g[x * a.gny + y]);
+                s_g[0][fx * kPitch + fy] = v;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         for (uint32_t base = lo + warp * 4; base < hi; base += kCubeThreads / 8) {
             const uint32_t k = base + sub;
             float2 acc = make_float2(0.0f, 0.0f);   // (re, im), paired FMAs
@@ -906,12 +995,13 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
                     const uint32_t meta = q.x;
                     const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
                     const float* wy = s_taps + (meta & 2047u) * 7;
-                    const int row = ((int)(meta >> 27) + ix) * kRow + (int)((meta >> 22) & 31);
+                    const int row =
+                        ((int)(meta >> 27) + ix) * kPitch + (int)((meta >> 22) & 31);
                     const float wxi = wx[ix];
 #pragma unroll
                     for (int iy = 0; iy < 7; ++iy) {
                         const float wgt = __fmul_rn(wxi, wy[iy]);
-                        acc = __ffma2_rn(s_g[row + iy], make_float2(wgt, wgt), acc);
+                        acc = __ffma2_rn(sg[row + iy], make_float2(wgt, wgt), acc);
                     }
                 }
             }
@@ -932,6 +1022,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(CubeDegridArg
             }
         }
         __syncthreads();
+        b ^= 1;
     }
 }
 
@@ -1166,9 +1257,10 @@ static void launch_cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, 
     const cr_grid_info& gi = g->info;
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
-    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows, cr.ntx,
-                   cr.nty, gi.grid_nx, gi.grid_ny, cr.grid_items, cr.grid_chunk, cr.grid_chunks,
-                   cr.n_items, counter, psf, dirty, res};
+    CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows,
+                   g->taps_bytes, ctx->status_d, cr.ntx, cr.nty, gi.grid_nx, gi.grid_ny,
+                   cr.grid_items, cr.grid_chunk, cr.grid_chunks, cr.n_items, counter, psf,
+                   dirty, res};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int per_sm = 0;
@@ -1222,11 +1314,23 @@ static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
     CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
-                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d, grid,
-                     pred, cr.rec_w, res};
+                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d,
+                     g->taps_bytes, grid, pred, cr.rec_w, res, ctx->status_d};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    cube_degrid_kernel<RESIDUAL><<<sms * 8, kCubeThreads, 0, ctx->stream>>>(a);
+    // the grids as float32 [C][gnx][2 gny] for footprint boxes of 76 x 38
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof(map));
+    const uint64_t row = (uint64_t)gi.grid_ny * 8;
+    const bool tma = encode_tensor_map_3d(&map, grid, 2 * (uint64_t)gi.grid_ny,
+                                          (uint64_t)gi.grid_nx, (uint64_t)cr.C, row,
+                                          row * (uint64_t)gi.grid_nx, 2 * (kTile + 6), kTile + 6);
+    if (tma)
+        cube_degrid_kernel<RESIDUAL, true>
+            <<<sms * 8, kCubeThreads, g->taps_bytes, ctx->stream>>>(map, a);
+    else
+        cube_degrid_kernel<RESIDUAL, false>
+            <<<sms * 8, kCubeThreads, g->taps_bytes, ctx->stream>>>(map, a);
     note_launch(ctx, RESIDUAL ? "cube_degrid_kernel_residual" : "cube_degrid_kernel");
 }
 

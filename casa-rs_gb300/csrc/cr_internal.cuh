@@ -68,6 +68,10 @@ struct cr_ctx {
     uint64_t ws_epoch = 0;
     // small pinned host buffer for device->host scalars
     void* pinned = nullptr;
+    // mapped host word that kernels set (CR_TIMEOUT) when a bounded wait
+    // gives up; read after the stream synchronises
+    int* status_h = nullptr;
+    int* status_d = nullptr;
 };
 
 // Standard (PSWF) gridder state.
@@ -77,7 +81,8 @@ struct cr_gridder {
     cr_grid_info info = {};
     int32_t tap_rows = 0;
     std::vector<float> taps_h, corr_x_h, corr_y_h;
-    float* taps_d = nullptr;     // [tap_rows][7]
+    float* taps_d = nullptr;     // [tap_rows][7], zero-padded to taps_bytes
+    uint32_t taps_bytes = 0;     // tap_rows * 7 * 4 rounded up to 16 (bulk copies)
     float* corr_x_d = nullptr;   // [grid_nx]
     float* corr_y_d = nullptr;   // [grid_ny]
 };
@@ -112,6 +117,9 @@ void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes);
 void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes);
 void pool_free(cr_ctx* ctx, Pool& pool);
 void note_launch(cr_ctx* ctx, const char* what);
+// After the stream has synchronised: a status that a kernel set (a bounded
+// wait that gave up) becomes an error, and the word is cleared.
+void check_device_status(cr_ctx* ctx);
 // Event pair around one gridding (which = 0) or degridding (which = 1) kernel.
 void kernel_mark(cr_ctx* ctx, int which, bool end);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);

@@ -119,6 +119,31 @@ def test_cube_degrid_matches_oracle(ctx, cube):
         assert np.all(pred[c][~keep] == 0)
 
 
+def test_cube_degrid_footprint_paths_agree(ctx, cube):
+    """Model footprints arrive by tensor-map copies when the model grids are
+    16-byte aligned and by plain loads otherwise (here an 8-byte offset
+    view); both feed the same arithmetic, so predictions agree bit for bit."""
+    torch = pytest.importorskip("torch")
+    obs, flags, vis = cube
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(obs.nx, obs.nx, obs.cell, obs.cell), OS)
+    rng = np.random.default_rng(4)
+    gs = (obs.channels,) + gg.grid_shape()
+    model = (rng.normal(size=gs) + 1j * rng.normal(size=gs)).astype(np.complex64)
+    dev = torch.device("cuda", 0)
+    u, v, vs, fl = (torch.as_tensor(a).to(dev) for a in (obs.u_m, obs.v_m, vis, flags))
+    cb = cc.CubeBatch(u, v, obs.lambda_scale, vs, None, fl)
+    aligned = torch.as_tensor(model).to(dev)
+    assert aligned.data_ptr() % 16 == 0
+    store = torch.zeros(model.size + 1, dtype=torch.complex64, device=dev)
+    offset = store[1:].view(gs)
+    offset.copy_(aligned)
+    assert offset.data_ptr() % 16 == 8
+    a = cc.cube_degrid(gg, cb, aligned)
+    b = cc.cube_degrid(gg, cb, offset)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
 def test_cube_boundary_samples_take_the_oracle_decisions(ctx):
     nx = 256
     cell = 2.0e-5
