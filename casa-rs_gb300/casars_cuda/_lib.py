@@ -163,6 +163,9 @@ SIGNATURES = {
     "cr_hogbom": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64, _i32,
                             _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i32),
                             _err]),
+    "cr_hogbom_plane": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64,
+                                  _i32, _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64),
+                                  _err]),
     "cr_hogbom_noalloc": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _f, _f, _f, _f, _i64, _i32,
                                     _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64),
                                     C.POINTER(_i32), _err]),

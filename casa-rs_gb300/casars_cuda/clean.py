@@ -42,6 +42,51 @@ class CleanConfig:
 
 
 @dataclass
+class HogbomPlaneMinorCycleControl:
+    """HogbomPlaneMinorCycleControl (lib.rs:64555-64580)."""
+    clean: CleanConfig
+    cycle_limit: int
+    cycle_threshold_jy_per_beam: float
+    peak_relative_tolerance: float
+
+
+@dataclass
+class HogbomPlaneComponent:
+    """HogbomPlaneComponent: position (x, y), peak residual, flux added."""
+    position: tuple
+    peak_value_jy_per_beam: float
+    component_jy: float
+
+
+@dataclass
+class HogbomPlaneMinorCycleOutcome:
+    model: object
+    residual: object
+    actual_updates: int
+    reported_updates: int
+    components: list
+
+
+def run_hogbom_plane_minor_cycle(ctx, model, residual, psf, clean_mask,
+                                 control: HogbomPlaneMinorCycleControl
+                                 ) -> HogbomPlaneMinorCycleOutcome:
+    """run_hogbom_plane_minor_cycle (lib.rs:64630-64680) on one image plane:
+    gain, threshold and the CasaInclusive budget from control.clean, peaks
+    with control.peak_relative_tolerance.  Returns updated copies of model
+    and residual."""
+    c = control.clean
+    out = im.hogbom_plane_minor_cycle(ctx, model, residual, psf, c.gain, control.cycle_limit,
+                                      control.cycle_threshold_jy_per_beam,
+                                      control.peak_relative_tolerance,
+                                      threshold=c.threshold_jy_per_beam, mask=clean_mask,
+                                      inclusive=c.inclusive)
+    comps = [HogbomPlaneComponent((int(p[0]), int(p[1])), float(pk), float(fl))
+             for p, pk, fl in zip(out.positions, out.peaks, out.fluxes)]
+    return HogbomPlaneMinorCycleOutcome(out.model, out.residual, out.actual_updates,
+                                        out.reported_updates, comps)
+
+
+@dataclass
 class CleanResult:
     model: object
     residual: object

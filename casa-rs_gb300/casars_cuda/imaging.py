@@ -1222,12 +1222,9 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
     return outs
 
 
-def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycle_niter: int,
-                           threshold: float = 0.0, cycle_threshold: float = 0.0,
-                           nsigma_threshold: float = 0.0, mask=None,
-                           inclusive: bool = True) -> HogbomOutcome:
-    """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) on the
-    device.  model and residual are updated copies (the inputs are kept)."""
+def _hogbom_buffers(ctx: Context, model, residual, psf, mask):
+    """Updated copies of model and residual where the residual lives, and
+    the pointers a Hogbom call takes."""
     arrs = _Arrays()
     if _is_torch(residual) and residual.is_cuda:
         m = model.detach().to(torch.float32).clone().contiguous()
@@ -1245,6 +1242,41 @@ def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycl
     nx, ny = r.shape
     pp = arrs.ptr(psf, np.float32, torch.float32 if torch else None, (nx, ny))
     kp = arrs.ptr(mask, np.uint8, torch.uint8 if torch else None, (nx, ny))
+    return arrs, m, r, mp, rp, pp, kp, nx, ny
+
+
+def hogbom_plane_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycle_limit: int,
+                             cycle_threshold: float, peak_relative_tolerance: float,
+                             threshold: float = 0.0, mask=None,
+                             inclusive: bool = True) -> HogbomOutcome:
+    """run_hogbom_plane_minor_cycle (lib.rs:64630-64680) on the device:
+    finite peaks with the relative tolerance of
+    finite_peak_location_masked_with_relative_tolerance, stop when
+    |peak| <= threshold or <= cycle_threshold.  model and residual are
+    updated copies (the inputs are kept)."""
+    arrs, m, r, mp, rp, pp, kp, nx, ny = _hogbom_buffers(ctx, model, residual, psf, mask)
+    cap = int(cycle_limit) + 1
+    cx = np.zeros(cap, np.int32)
+    cy = np.zeros(cap, np.int32)
+    cpk = np.zeros(cap, np.float32)
+    cfl = np.zeros(cap, np.float32)
+    actual, reported = C.c_int64(), C.c_int64()
+    call("cr_hogbom_plane", ctx.handle, mp, rp, pp, kp, nx, ny, arrs.location, float(gain),
+         float(threshold), float(cycle_threshold), float(peak_relative_tolerance),
+         int(cycle_limit), int(bool(inclusive)), cx.ctypes.data, cy.ctypes.data,
+         cpk.ctypes.data, cfl.ctypes.data, C.byref(actual), C.byref(reported))
+    k = int(actual.value)
+    return HogbomOutcome(m, r, np.stack([cx[:k], cy[:k]], 1), cpk[:k], cfl[:k], k,
+                         int(reported.value), None)
+
+
+def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycle_niter: int,
+                           threshold: float = 0.0, cycle_threshold: float = 0.0,
+                           nsigma_threshold: float = 0.0, mask=None,
+                           inclusive: bool = True) -> HogbomOutcome:
+    """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) on the
+    device.  model and residual are updated copies (the inputs are kept)."""
+    arrs, m, r, mp, rp, pp, kp, nx, ny = _hogbom_buffers(ctx, model, residual, psf, mask)
     cap = int(cycle_niter) + 1
     cx = np.zeros(cap, np.int32)
     cy = np.zeros(cap, np.int32)

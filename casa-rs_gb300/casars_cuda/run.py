@@ -2,8 +2,11 @@
 top-level entry point (run_imaging, lib.rs:3468; ImagingRequest,
 types.rs:2291-2337; ImagingResult) for the standard and W-projection
 gridders, natural / uniform / Briggs weighting and the Hogbom or Clark
-deconvolver.  Mosaic, AW-projection, MT-MFS, multiscale, masks and initial
-models are outside this library."""
+deconvolver, and the standard-MFS plan entry points around it
+(run_standard_mfs_plan, lib.rs:1742; run_standard_mfs_dirty_grid_plan,
+lib.rs:1966; finish_standard_mfs_dirty_grid_result, lib.rs:2000).  Mosaic,
+AW-projection, MT-MFS, multiscale, masks and initial models are outside
+this library."""
 from __future__ import annotations
 
 from dataclasses import dataclass, field
@@ -131,3 +134,76 @@ def _run(ctx: im.Context, request: ImagingRequest, batch: im.VisibilityBatch) ->
                          float(out.psf_state.reported_sumwt), out.beam, out.psf_state,
                          out.major_cycles, out.minor_iterations, out.stop_reason,
                          out.components)
+
+
+def run_standard_mfs_plan(ctx: im.Context, request: ImagingRequest) -> ImagingResult:
+    """run_standard_mfs_plan (lib.rs:1742) over weighted batches: the
+    canonical standard-MFS run, i.e. run_imaging with the standard gridder
+    (no w-term)."""
+    if request.w_term_mode != "none":
+        raise ValueError("the standard-MFS plan takes no w-term")
+    return run_imaging(ctx, request)
+
+
+@dataclass
+class StandardMfsDirtyGridResult:
+    """StandardMfsDirtyGridResult (lib.rs:1861): the raw result of a
+    dirty-only plan -- PSF and dirty grids held on the device by an
+    accumulator -- with the sums of every replayed block."""
+    request: ImagingRequest
+    accumulator: im.DirtyAccumulator
+    block_sums: List[im.GridSums]
+
+    @property
+    def gridded_samples(self) -> int:
+        return sum(s.gridded_samples for s in self.block_sums)
+
+    @property
+    def skipped_samples(self) -> int:
+        return sum(s.skipped_samples for s in self.block_sums)
+
+
+def _split_weights(batches: List[im.VisibilityBatch], weights) -> List[im.VisibilityBatch]:
+    out, at = [], 0
+    for b in batches:
+        n = len(b)
+        w = weights[at:at + n]
+        at += n
+        out.append(im.VisibilityBatch(b.u_lambda, b.v_lambda, b.visibility, w, b.w_lambda,
+                                      b.sumwt_factor, b.gridable))
+    return out
+
+
+def run_standard_mfs_dirty_grid_plan(ctx: im.Context,
+                                     request: ImagingRequest) -> StandardMfsDirtyGridResult:
+    """run_standard_mfs_dirty_grid_plan (lib.rs:1966): the request's batches
+    replayed one block at a time into device-resident grids (grid
+    accumulation only, no FFT).  Non-natural weighting takes its density
+    over all blocks first, as the reference's weighting plan does."""
+    if request.w_term_mode != "none":
+        raise ValueError("the standard-MFS dirty plan takes no w-term")
+    if not request.visibility_batches:
+        raise ValueError("no visibility batches")
+    gg = im.StandardGridder(ctx, request.geometry, request.oversampling, request.padding)
+    blocks = list(request.visibility_batches)
+    if request.weighting != "natural":
+        merged = _merge(blocks)
+        wt, _ = im.apply_weighting(gg, merged, request.weighting, request.robust)
+        blocks = _split_weights(blocks, wt)
+    acc = im.DirtyAccumulator(gg)
+    sums = [acc.add(b) for b in blocks]
+    return StandardMfsDirtyGridResult(request, acc, sums)
+
+
+def finish_standard_mfs_dirty_grid_result(ctx: im.Context,
+                                          result: StandardMfsDirtyGridResult):
+    """finish_standard_mfs_dirty_grid_result (lib.rs:2000): the dirty
+    products of a raw grid result -- (psf, residual, PsfState) -- with the
+    image-stage FFT precision of the result's request."""
+    previous = ctx.image_fft_precision
+    ctx.set_image_fft_precision(result.request.fft_precision)
+    try:
+        psf, residual, state, _ = result.accumulator.finish()
+    finally:
+        ctx.set_image_fft_precision(previous)
+    return psf, residual, state

@@ -1074,6 +1074,40 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, cons
     });
 }
 
+int cr_hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                    const uint8_t* mask, int32_t nx, int32_t ny, int32_t location, float gain,
+                    float threshold, float cycle_threshold, float peak_relative_tolerance,
+                    int64_t cycle_limit, int32_t inclusive, int32_t* comp_x, int32_t* comp_y,
+                    float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
+                    char** err) {
+    return guarded(err, [&] {
+        need(ctx && model && residual && psf, "null argument");
+        need(nx > 0 && ny > 0, "image shape must be positive");
+        need(location == CR_HOST || location == CR_DEVICE, "bad location");
+        need(!comp_x == !comp_y && !comp_x == !comp_peak && !comp_x == !comp_flux,
+             "component arrays must be all given or all null");
+        bind(ctx);
+        size_t nb = (size_t)nx * ny * 4;
+        float* m = location == CR_DEVICE ? model : (float*)workspace(ctx, "hog_model", nb);
+        float* r = location == CR_DEVICE ? residual : (float*)workspace(ctx, "hog_residual", nb);
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(m, model, nb, cudaMemcpyHostToDevice, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(r, residual, nb, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const float* p = (const float*)device_input(ctx, psf, nb, location, "hog_psf");
+        const uint8_t* mk = (const uint8_t*)device_input(ctx, mask, (size_t)nx * ny, location,
+                                                         "hog_mask");
+        cr::hogbom_plane(ctx, m, r, p, mk, nx, ny, gain, threshold, cycle_threshold,
+                         peak_relative_tolerance, cycle_limit, inclusive, comp_x, comp_y,
+                         comp_peak, comp_flux, actual, reported);
+        if (location == CR_HOST) {
+            CR_CUDA_CHECK(cudaMemcpyAsync(model, m, nb, cudaMemcpyDeviceToHost, ctx->stream));
+            CR_CUDA_CHECK(cudaMemcpyAsync(residual, r, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int cr_cube_grid_dirty(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                        int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
                        int32_t out_location, cr_sums* sums, char** err) {

@@ -983,13 +983,25 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
             }
             __syncthreads();
         }
+        // each record is loaded one iteration ahead of its use, so a warp
+        // keeps the next batch's loads in flight while it computes
+        uint4 qn = make_uint4(0u, 0u, 0u, 0u);
+        float wn = 0.0f;
+        if (lo + warp * 4 + sub < hi) {
+            qn = a.rec[lo + warp * 4 + sub];
+            if (RESIDUAL) wn = a.rec_w[lo + warp * 4 + sub];
+        }
         for (uint32_t base = lo + warp * 4; base < hi; base += kCubeThreads / 8) {
             const uint32_t k = base + sub;
+            const uint4 q = qn;
+            const float w = wn;
+            if (k + kCubeThreads / 8 < hi) {
+                qn = a.rec[k + kCubeThreads / 8];
+                if (RESIDUAL) wn = a.rec_w[k + kCubeThreads / 8];
+            }
             float2 acc = make_float2(0.0f, 0.0f);   // (re, im), paired FMAs
             uint32_t sample = 0;
-            uint4 q = make_uint4(0u, 0u, 0u, 0u);
             if (k < hi) {
-                q = a.rec[k];
                 sample = q.y;
                 if (ix < 7) {
                     const uint32_t meta = q.x;
@@ -1013,7 +1025,6 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
             }
             if (ix == 0 && k < hi) {
                 if (RESIDUAL) {
-                    const float w = a.rec_w[k];
                     a.res[k] = make_float2(__fsub_rn(__uint_as_float(q.z), __fmul_rn(w, re)),
                                            __fsub_rn(__uint_as_float(q.w), __fmul_rn(w, im)));
                 } else {

@@ -16,6 +16,7 @@
 // launched cooperatively (all blocks resident); the barrier's wait is bounded
 // and reports CR_TIMEOUT instead of spinning forever.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -53,6 +54,10 @@ struct HogArgs {
     long long* out_actual;
     int* out_stop;
     int* out_status;
+    // run_hogbom_plane_minor_cycle's rules (lib.rs:64630-64680): peaks over
+    // finite values only, stop when |peak| <= threshold or <= the cycle
+    // threshold, no nsigma rule
+    int plane_rules;
 };
 
 __device__ __forceinline__ bool better(float a_abs, int a_key, float b_abs, int b_key) {
@@ -158,6 +163,7 @@ __device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
             if (a.mask && !a.mask[t]) continue;
             int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
             float v = a.residual[t];
+            if (a.plane_rules && !isfinite(v)) continue;
             float av = fabsf(v);
             int key = y * a.nx + x;
             if (better(av, key, ba, bk)) {
@@ -198,6 +204,10 @@ __device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
                 int r = 0;
                 if (c.absval < 0.0f)
                     r = CR_STOP_NO_CLEANABLE_PIXELS;
+                else if (a.plane_rules)
+                    r = c.absval <= a.threshold         ? CR_STOP_GLOBAL_THRESHOLD
+                        : c.absval <= a.cycle_threshold ? CR_STOP_CYCLE_THRESHOLD
+                                                        : 0;
                 else
                     r = stop_reason(c.absval, a.threshold, a.cycle_threshold, a.nsigma_threshold);
                 s_stop = r;
@@ -238,7 +248,7 @@ __device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
                 v = __fsub_rn(v, __fmul_rn(comp, a.psf[kx * a.ny + ky]));
                 a.residual[t] = v;
             }
-            if (!a.mask || a.mask[t]) {
+            if ((!a.mask || a.mask[t]) && (!a.plane_rules || isfinite(v))) {
                 const float av = fabsf(v);
                 const int key = y * a.nx + x;
                 if (better(av, key, ba, bk)) {
@@ -304,13 +314,129 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_planes_kernel(HogPlanesArg
     hogbom_body(a, pa.per_plane, bidx);
 }
 
+// run_hogbom_plane_minor_cycle with a relative peak tolerance > 0
+// (finite_peak_location_masked_with_relative_tolerance, lib.rs:73998-74026):
+// the scan runs y-major (x fastest) and a value replaces the current peak
+// only if |v| > |peak| * (1 + tol) in float32, so the result depends on the
+// scan order and is not a plain argmax.  One block replays it exactly: all
+// threads form each scan row's largest finite unmasked |r|; one warp then
+// walks the rows, skipping a row whose largest value cannot replace the
+// current peak and, inside a row that can, jumping with ballots to the next
+// value that does.  Subtraction and the model update follow as in the fast
+// loop.  No inter-block waits.
+constexpr int kTolThreads = 1024;
+
+struct HogTolArgs {
+    float* model;
+    float* residual;
+    const float* psf;
+    const uint8_t* mask;
+    int nx, ny;
+    float gain, threshold, cycle_threshold, tol;
+    long long budget;
+    float* rowmax;  // [ny]
+    int* comp_x;
+    int* comp_y;
+    float* comp_peak;
+    float* comp_flux;
+    long long* out_actual;
+};
+
+__global__ void __launch_bounds__(kTolThreads) hogbom_tol_kernel(HogTolArgs a) {
+    __shared__ int s_have, s_x, s_y;
+    __shared__ float s_v;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float k1 = __fadd_rn(1.0f, a.tol);
+    const int kcx = a.nx / 2, kcy = a.ny / 2;
+    const int64_t npix = (int64_t)a.nx * a.ny;
+    long long it = 0;
+    for (; it < a.budget; ++it) {
+        for (int y = tid; y < a.ny; y += kTolThreads) {
+            float m = -1.0f;
+            for (int x = 0; x < a.nx; ++x) {
+                const int64_t t = (int64_t)x * a.ny + y;
+                const float v = a.residual[t];
+                if ((!a.mask || a.mask[t]) && isfinite(v)) m = fmaxf(m, fabsf(v));
+            }
+            a.rowmax[y] = m;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            bool have = false;
+            int bx = 0, by = 0;
+            float bv = 0.0f, thr = 0.0f;
+            for (int y0 = 0; y0 < a.ny;) {
+                const int yy = y0 + lane;
+                const float rm = yy < a.ny ? a.rowmax[yy] : -1.0f;
+                const unsigned rows = __ballot_sync(0xffffffffu, have ? rm > thr : rm >= 0.0f);
+                if (!rows) {
+                    y0 += 32;
+                    continue;
+                }
+                const int y = y0 + __ffs(rows) - 1;
+                for (int x0 = 0; x0 < a.nx;) {
+                    const int xx = x0 + lane;
+                    float v = 0.0f;
+                    bool ok = false;
+                    if (xx < a.nx) {
+                        const int64_t t = (int64_t)xx * a.ny + y;
+                        v = a.residual[t];
+                        ok = (!a.mask || a.mask[t]) && isfinite(v) && (!have || fabsf(v) > thr);
+                    }
+                    const unsigned hit = __ballot_sync(0xffffffffu, ok);
+                    if (!hit) {
+                        x0 += 32;
+                        continue;
+                    }
+                    const int src = __ffs(hit) - 1;
+                    bv = __shfl_sync(0xffffffffu, v, src);
+                    bx = x0 + src;
+                    by = y;
+                    have = true;
+                    thr = __fmul_rn(fabsf(bv), k1);
+                    x0 = bx + 1;
+                }
+                y0 = y + 1;
+            }
+            if (lane == 0) {
+                s_have = have;
+                s_x = bx;
+                s_y = by;
+                s_v = bv;
+            }
+        }
+        __syncthreads();
+        if (!s_have) break;
+        const float peak = s_v, pabs = fabsf(peak);
+        if (pabs <= a.threshold || pabs <= a.cycle_threshold) break;
+        const int px = s_x, py = s_y;
+        const float comp = __fmul_rn(a.gain, peak);
+        if (tid == 0) {
+            const int64_t m = (int64_t)px * a.ny + py;
+            a.model[m] = __fadd_rn(a.model[m], comp);
+            a.comp_x[it] = px;
+            a.comp_y[it] = py;
+            a.comp_peak[it] = peak;
+            a.comp_flux[it] = comp;
+        }
+        for (int64_t t = tid; t < npix; t += kTolThreads) {
+            const int x = (int)(t / a.ny), y = (int)(t - (int64_t)x * a.ny);
+            const int kx = x - px + kcx, ky = y - py + kcy;
+            if (kx >= 0 && kx < a.nx && ky >= 0 && ky < a.ny)
+                a.residual[t] = __fsub_rn(a.residual[t], __fmul_rn(comp, a.psf[kx * a.ny + ky]));
+        }
+        __syncthreads();
+    }
+    if (tid == 0) *a.out_actual = it;
+}
+
 }  // namespace
 
 void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const uint8_t* mask,
             int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
             int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
-            int64_t* reported, int32_t* stop_reason_out) {
+            int64_t* reported, int32_t* stop_reason_out, int plane_rules) {
     if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
     if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
     if (cycle_niter < 0) fail(CR_INVALID, "cycle_niter is negative");
@@ -337,7 +463,7 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
     CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, 256, ctx->stream));
     HogArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
               nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual, out_stop,
-              out_status};
+              out_status, plane_rules};
     void* args[] = {&a};
     CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_kernel, dim3(blocks), dim3(kHogThreads),
                                               args, 0, ctx->stream));
@@ -358,6 +484,51 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
     if (actual) *actual = h.actual;
     if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
     if (stop_reason_out) *stop_reason_out = h.stop;
+}
+
+void hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                  const uint8_t* mask, int32_t nx, int32_t ny, float gain, float threshold,
+                  float cycle_threshold, float peak_relative_tolerance, int64_t cycle_limit,
+                  int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                  float* comp_flux, int64_t* actual, int64_t* reported) {
+    if (!(peak_relative_tolerance >= 0.0f) || !std::isfinite(peak_relative_tolerance))
+        fail(CR_INVALID, "peak_relative_tolerance must be finite and non-negative");
+    if (peak_relative_tolerance == 0.0f) {
+        int32_t stop = 0;
+        hogbom(ctx, model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold, 0.0f,
+               cycle_limit, inclusive, comp_x, comp_y, comp_peak, comp_flux, actual, reported,
+               &stop, 1);
+        return;
+    }
+    if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
+    if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
+    if (cycle_limit < 0) fail(CR_INVALID, "cycle_limit is negative");
+    const long long budget = inclusive ? cycle_limit + 1 : cycle_limit;
+    const size_t cap = (size_t)(budget > 0 ? budget : 1);
+    char* wsp = (char*)workspace(ctx, "hogtol_ws", 256 + (size_t)ny * 4 + cap * 16);
+    long long* out_actual = (long long*)wsp;
+    float* rowmax = (float*)(wsp + 256);
+    int* cx = (int*)(rowmax + ny);
+    int* cy = cx + cap;
+    float* cp = (float*)(cy + cap);
+    float* cf = cp + cap;
+    CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, 256, ctx->stream));
+    HogTolArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
+                 peak_relative_tolerance, budget, rowmax, cx, cy, cp, cf, out_actual};
+    hogbom_tol_kernel<<<1, kTolThreads, 0, ctx->stream>>>(a);
+    note_launch(ctx, "hogbom_tol_kernel");
+    long long n = 0;
+    CR_CUDA_CHECK(cudaMemcpyAsync(&n, out_actual, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (comp_x && n > 0) {
+        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    }
+    if (actual) *actual = n;
+    // CasaInclusive reports at most the cycle limit when the budget ran out
+    if (reported) *reported = std::min<int64_t>(n, cycle_limit);
 }
 
 void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,

@@ -327,7 +327,15 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
             int32_t nx, int32_t ny, float gain, float threshold, float cycle_threshold,
             float nsigma_threshold, int64_t cycle_niter, int32_t inclusive, int32_t* comp_x,
             int32_t* comp_y, float* comp_peak, float* comp_flux, int64_t* actual,
-            int64_t* reported, int32_t* stop_reason);
+            int64_t* reported, int32_t* stop_reason, int plane_rules = 0);
+// run_hogbom_plane_minor_cycle (lib.rs:64630-64680) on device images: the
+// fast loop with its rules when the peak tolerance is 0, a single-block
+// replay of the tolerance scan otherwise.
+void hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                  const uint8_t* mask, int32_t nx, int32_t ny, float gain, float threshold,
+                  float cycle_threshold, float peak_relative_tolerance, int64_t cycle_limit,
+                  int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
+                  float* comp_flux, int64_t* actual, int64_t* reported);
 // run_clark_minor_cycle_cpu (lib.rs:62129-62355) on device images; the PSF
 // patch is (3 ncent + 1)^2 about the centre (build_clark_psf_patch).
 void clark_minor_cycle(cr_ctx* ctx, float* model, float* residual, const float* psf,

@@ -491,6 +491,21 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf,
               float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
               int32_t* stop_reason, char** err);
 
+/* run_hogbom_plane_minor_cycle (crates/casa-imaging/src/lib.rs:64630-64680;
+ * HogbomPlaneMinorCycleControl, lib.rs:64555-64580): the finite peak with a
+ * relative tolerance (finite_peak_location_masked_with_relative_tolerance,
+ * lib.rs:73998-74026: y-major scan, a value replaces the peak only if
+ * |v| > |peak| * (1 + tol)), stop when |peak| <= threshold or <= the cycle
+ * threshold, model += gain * peak, subtract_shifted_psf.  Arrays as
+ * cr_hogbom; tolerance 0 runs the same persistent loop as cr_hogbom, a
+ * positive tolerance an exact single-block replay of the scan. */
+int cr_hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
+                    const uint8_t* mask, int32_t nx, int32_t ny, int32_t location, float gain,
+                    float threshold, float cycle_threshold, float peak_relative_tolerance,
+                    int64_t cycle_limit, int32_t inclusive, int32_t* comp_x, int32_t* comp_y,
+                    float* comp_peak, float* comp_flux, int64_t* actual, int64_t* reported,
+                    char** err);
+
 /* The Hogbom minor cycles of several planes in one launch: model, residual,
  * psf (and mask, or NULL) are DEVICE arrays [nplanes][nx][ny]; the n planes
  * listed in `planes` (host) each run run_hogbom_minor_cycle_cpu_with_progress

@@ -1294,6 +1294,65 @@ void oc_subtract_shifted_psf(float* residual, const float* psf, int64_t nx, int6
         }
 }
 
+/* finite_peak_location_masked_with_relative_tolerance (lib.rs:73998-74026):
+ * a y-major scan (x fastest) over finite unmasked values; a value replaces
+ * the current peak only if |v| > |peak| * (1 + tol) in float32. */
+int oc_peak_relative(const float* image, const uint8_t* mask, int64_t nx, int64_t ny,
+                     float tol, int64_t* px, int64_t* py, float* value) {
+    const float k1 = 1.0f + tol;
+    int have = 0;
+    float best = 0.0f;
+    int64_t bx = 0, by = 0;
+    for (int64_t y = 0; y < ny; ++y)
+        for (int64_t x = 0; x < nx; ++x) {
+            if (mask && !mask[x * ny + y]) continue;
+            float v = image[x * ny + y];
+            if (!isfinite(v)) continue;
+            if (!have || fabsf(v) > fabsf(best) * k1) {
+                have = 1;
+                best = v;
+                bx = x;
+                by = y;
+            }
+        }
+    if (!have) return 0;
+    *px = bx;
+    *py = by;
+    *value = best;
+    return 1;
+}
+
+/* run_hogbom_plane_minor_cycle (lib.rs:64630-64680): budget as
+ * hogbom_component_budget, stop when |peak| <= threshold or <= the cycle
+ * threshold; reported = min(actual, cycle_limit) (CasaInclusive). */
+int64_t oc_hogbom_plane(float* model, float* residual, const float* psf, const uint8_t* mask,
+                        int64_t nx, int64_t ny, float gain, float threshold,
+                        float cycle_threshold, float tol, int64_t cycle_limit, int inclusive,
+                        int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                        int64_t* reported) {
+    int64_t budget = inclusive ? cycle_limit + 1 : cycle_limit;
+    int64_t updates = 0;
+    while (updates < budget) {
+        int64_t px, py;
+        float pv;
+        if (!oc_peak_relative(residual, mask, nx, ny, tol, &px, &py, &pv)) break;
+        float pabs = fabsf(pv);
+        if (pabs <= threshold || pabs <= cycle_threshold) break;
+        float comp = gain * pv;
+        model[px * ny + py] = model[px * ny + py] + comp;
+        oc_subtract_shifted_psf(residual, psf, nx, ny, px, py, comp);
+        if (comp_x) {
+            comp_x[updates] = (int32_t)px;
+            comp_y[updates] = (int32_t)py;
+            comp_peak[updates] = pv;
+            comp_flux[updates] = comp;
+        }
+        updates++;
+    }
+    *reported = updates < cycle_limit ? updates : cycle_limit;
+    return updates;
+}
+
 /* run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) with
  * hogbom_component_budget (lib.rs:64541-64552).  Returns the number of
  * components; stop_reason 0 budget exhausted, 1 global, 2 cycle, 3 nsigma

@@ -143,6 +143,13 @@ int64_t oc_hogbom(float* model, float* residual, const float* psf, const uint8_t
                   float nsigma_threshold, int64_t cycle_niter, int inclusive,
                   int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
                   int32_t* stop_reason, int64_t* reported);
+int oc_peak_relative(const float* image, const uint8_t* mask, int64_t nx, int64_t ny,
+                     float tol, int64_t* px, int64_t* py, float* value);
+int64_t oc_hogbom_plane(float* model, float* residual, const float* psf, const uint8_t* mask,
+                        int64_t nx, int64_t ny, float gain, float threshold,
+                        float cycle_threshold, float tol, int64_t cycle_limit, int inclusive,
+                        int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                        int64_t* reported);
 void oc_subtract_shifted_psf(float* residual, const float* psf, int64_t nx, int64_t ny,
                              int64_t px, int64_t py, float component);
 

@@ -105,6 +105,10 @@ def _declare(L):
         "oc_hogbom": (_i64, [_p, _p, _p, _p, _i64, _i64, _f, _f, _f, _f, _i64, C.c_int, _p,
                              _p, _p, _p, C.POINTER(_i32), C.POINTER(_i64)]),
         "oc_subtract_shifted_psf": (None, [_p, _p, _i64, _i64, _i64, _i64, _f]),
+        "oc_peak_relative": (C.c_int, [_p, _p, _i64, _i64, _f, C.POINTER(_i64),
+                                       C.POINTER(_i64), C.POINTER(_f)]),
+        "oc_hogbom_plane": (_i64, [_p, _p, _p, _p, _i64, _i64, _f, _f, _f, _f, _i64, C.c_int,
+                                   _p, _p, _p, _p, C.POINTER(_i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -544,6 +548,37 @@ def hogbom(residual, psf, gain, niter, threshold=0.0, cycle_threshold=0.0,
                         _ptr(cy), _ptr(cp), _ptr(cf), C.byref(stop), C.byref(reported))
     return dict(model=mdl, residual=res, x=cx[:n], y=cy[:n], peak=cp[:n], flux=cf[:n],
                 stop_reason=int(stop.value), actual=int(n), reported=int(reported.value))
+
+
+def peak_relative(image, tol, mask=None):
+    """finite_peak_location_masked_with_relative_tolerance (lib.rs:73998-74026)."""
+    img = _c(image, np.float32)
+    mk = _c(mask, np.uint8)
+    px, py, val = _i64(), _i64(), _f()
+    ok = lib().oc_peak_relative(_ptr(img), _ptr(mk), img.shape[0], img.shape[1], float(tol),
+                                C.byref(px), C.byref(py), C.byref(val))
+    return ((int(px.value), int(py.value)), float(val.value)) if ok else None
+
+
+def hogbom_plane(residual, psf, gain, cycle_limit, cycle_threshold, tol, threshold=0.0,
+                 mask=None, model=None, inclusive=True):
+    """run_hogbom_plane_minor_cycle (lib.rs:64630-64680)."""
+    res = np.array(residual, np.float32, copy=True, order="C")
+    p = _c(psf, np.float32)
+    nx, ny = res.shape
+    mdl = np.zeros_like(res) if model is None else np.array(model, np.float32, copy=True)
+    mk = _c(mask, np.uint8)
+    cap = cycle_limit + 1
+    cx = np.zeros(cap, np.int32)
+    cy = np.zeros(cap, np.int32)
+    cp = np.zeros(cap, np.float32)
+    cf = np.zeros(cap, np.float32)
+    reported = _i64()
+    n = lib().oc_hogbom_plane(_ptr(mdl), _ptr(res), _ptr(p), _ptr(mk), nx, ny, gain, threshold,
+                              cycle_threshold, float(tol), cycle_limit, int(inclusive), _ptr(cx),
+                              _ptr(cy), _ptr(cp), _ptr(cf), C.byref(reported))
+    return dict(model=mdl, residual=res, x=cx[:n], y=cy[:n], peak=cp[:n], flux=cf[:n],
+                actual=int(n), reported=int(reported.value))
 
 
 def radians_from_arcsec(a: float) -> float:

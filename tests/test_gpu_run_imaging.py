@@ -82,3 +82,25 @@ def test_clark_uniform(setup):
     assert r.minor_iterations == ref.minor_iterations > 0
     assert [c[0] for c in r.components] == [c[0] for c in ref.components]
     assert peak_norm_err(r.residual, ref.residual) <= 1e-5
+
+
+def test_dirty_grid_plan_then_finish(setup):
+    """run_standard_mfs_dirty_grid_plan over three blocks with Briggs
+    weighting, then finish_standard_mfs_dirty_grid_result, against
+    run_imaging (niter 0) on the same request."""
+    ctx, obs, wt = setup
+    cuts = [0, obs.rows // 3, 2 * obs.rows // 3, obs.rows]
+    blocks = [cc.VisibilityBatch(obs.u[a:b], obs.v[a:b], obs.vis[a:b], wt[a:b])
+              for a, b in zip(cuts[:-1], cuts[1:])]
+    req = cc.ImagingRequest(_geom(obs), blocks, weighting="briggs", robust=0.5)
+    raw = cc.run_standard_mfs_dirty_grid_plan(ctx, req)
+    assert len(raw.block_sums) == 3
+    psf, res, state = cc.finish_standard_mfs_dirty_grid_result(ctx, raw)
+    ref = cc.run_imaging(ctx, req)
+    assert raw.gridded_samples + raw.skipped_samples == obs.rows
+    assert peak_norm_err(psf, ref.psf) <= 1e-5
+    assert peak_norm_err(res, ref.residual) <= 1e-5
+    assert abs(state.reported_sumwt - ref.sumwt) <= 1e-6 * ref.sumwt
+    with pytest.raises(ValueError):
+        cc.run_standard_mfs_plan(ctx, cc.ImagingRequest(_geom(obs), blocks,
+                                                        w_term_mode="wproject"))
