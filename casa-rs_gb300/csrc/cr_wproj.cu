@@ -372,6 +372,8 @@ __global__ void __launch_bounds__(kGridThreads, 6) wp_grid_kernel(GridArgs a) {
                     ok[k] = av >= 0 && colok;
                     kv[k] = ok[k] ? __ldg(cube + av) : make_float2(0.f, 0.f);
                 }
+                // (paired float32 FMAs here measured 9.40 -> 9.53 ms: the
+                // operand swaps and extra spills cost more than they saved)
 #pragma unroll
                 for (int k = 0; k < kRowsPerWarp; ++k) {
                     if (ok[k]) {
@@ -455,8 +457,7 @@ struct DegridArgs {
 template <int NCH>
 __device__ __forceinline__ void degrid_rows(const float2* g, const float2* cube, int gny, int s,
                                             int w, int ox, int oy, int q, const CubeGeom& cg,
-                                            int half, int hl, float& A, float& B, float& C,
-                                            float& D) {
+                                            int half, int hl, float2& AC, float2& DB) {
     int bcol[NCH];
 #pragma unroll
     for (int c = 0; c < NCH; ++c) {
@@ -475,10 +476,8 @@ __device__ __forceinline__ void degrid_rows(const float2* g, const float2* cube,
         }
 #pragma unroll
         for (int c = 0; c < NCH; ++c) {
-            A = fmaf(kv[c].x, gv[c].x, A);
-            B = fmaf(kv[c].y, gv[c].y, B);
-            C = fmaf(kv[c].x, gv[c].y, C);
-            D = fmaf(kv[c].y, gv[c].x, D);
+            AC = __ffma2_rn(make_float2(kv[c].x, kv[c].x), gv[c], AC);
+            DB = __ffma2_rn(make_float2(kv[c].y, kv[c].y), gv[c], DB);
         }
     }
 }
@@ -486,8 +485,8 @@ __device__ __forceinline__ void degrid_rows(const float2* g, const float2* cube,
 // Any window: lane l takes taps l, l+32, ... of the flattened (2S+1)^2
 // window, tracking its (row, column) incrementally.
 __device__ void degrid_flat(const float2* g, const float2* cube, int gny, int s, int w, int ox,
-                            int oy, int q, const CubeGeom& cg, int lane, float& A, float& B,
-                            float& C, float& D) {
+                            int oy, int q, const CubeGeom& cg, int lane, float2& AC,
+                            float2& DB) {
     const int nt = w * w;
     int i = lane / w, j = lane - (lane / w) * w;
     int goff = i * gny + j;
@@ -495,10 +494,8 @@ __device__ void degrid_flat(const float2* g, const float2* cube, int gny, int s,
     for (int t = lane; t < nt; t += 32) {
         const float2 gv = g[goff];
         const float2 kv = __ldg(cube + arow + cube_b(j - s, oy, q, cg));
-        A = fmaf(kv.x, gv.x, A);
-        B = fmaf(kv.y, gv.y, B);
-        C = fmaf(kv.x, gv.y, C);
-        D = fmaf(kv.y, gv.x, D);
+        AC = __ffma2_rn(make_float2(kv.x, kv.x), gv, AC);
+        DB = __ffma2_rn(make_float2(kv.y, kv.y), gv, DB);
         j += 32;
         goff += 32;
         bool wrapped = false;
@@ -530,11 +527,12 @@ __global__ void __launch_bounds__(256, 4) wp_degrid_kernel(DegridArgs a) {
         const int ox = off / a.axis - a.radius, oy = off % a.axis - a.radius;
         const float2* cube = a.cube + a.cube_off[plane];
         const float2* g = a.grid + (int64_t)(a.rx[r] - s) * a.gny + (a.ry[r] - s);
-        float A = 0.f, B = 0.f, C = 0.f, D = 0.f;
+        // (A, C) = sum kx (gx, gy), (D, B) = sum ky (gx, gy)
+        float2 AC = make_float2(0.f, 0.f), DB = make_float2(0.f, 0.f);
         switch ((w + 15) >> 4) {
 #define CR_DEGRID_CASE(N) \
     case N:               \
-        degrid_rows<N>(g, cube, gny, s, w, ox, oy, q, a.cg, half, hl, A, B, C, D); \
+        degrid_rows<N>(g, cube, gny, s, w, ox, oy, q, a.cg, half, hl, AC, DB); \
         break;
             CR_DEGRID_CASE(1)
             CR_DEGRID_CASE(2)
@@ -547,8 +545,9 @@ __global__ void __launch_bounds__(256, 4) wp_degrid_kernel(DegridArgs a) {
             CR_DEGRID_CASE(9)
 #undef CR_DEGRID_CASE
             default:
-                degrid_flat(g, cube, gny, s, w, ox, oy, q, a.cg, lane, A, B, C, D);
+                degrid_flat(g, cube, gny, s, w, ox, oy, q, a.cg, lane, AC, DB);
         }
+        float A = AC.x, C = AC.y, D = DB.x, B = DB.y;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             A += __shfl_xor_sync(0xffffffffu, A, o);
