@@ -357,6 +357,8 @@ void cr_ctx_destroy(cr_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& kv : ctx->fft_plans) cufftDestroy(kv.second);
     for (auto& kv : ctx->fft_plans_c2c) cufftDestroy(kv.second);
+    for (auto& m : ctx->fft_plans_real)
+        for (auto& kv : m.second) cufftDestroy(kv.second);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->kev)

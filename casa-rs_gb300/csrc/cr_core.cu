@@ -91,6 +91,10 @@ cufftHandle fft_plan_c2c(cr_ctx* ctx, int64_t nx, int64_t ny) {
     return cached_plan(ctx, ctx->fft_plans_c2c, nx, ny, CUFFT_C2C);
 }
 
+cufftHandle fft_plan_type(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type) {
+    return cached_plan(ctx, ctx->fft_plans_real[(int)type], nx, ny, type);
+}
+
 // ---- host tables --------------------------------------------------------------
 // casa_composite_padded_len (gridder.rs:4152-4173).
 int64_t casa_composite_padded_len(int64_t image_len, double padding) {

@@ -4,9 +4,15 @@
 // fftshift; fft.rs:600-630, 969-1070) equal a checkerboard-modulated plain
 // DFT: centred(g)[m] = (-1)^(mx+my+hx+hy) DFT((-1)^(kx+ky) g)[m], hx = Nx/2.
 // The input modulation is fused with the widening of the FP32 grid to FP64,
-// cuFFT does the bare transform (double precision, in place), and the output
-// modulation is folded into the crop and correction kernel (gridder.rs:
-// 1646-1657, 1685-1715) or into the narrowing of the model grid to FP32.
+// cuFFT does the bare transform, and the output modulation is folded into
+// the crop and correction kernel (gridder.rs:1646-1657, 1685-1715) or into
+// the narrowing of the model grid to FP32.
+// Only real parts leave the stage: the image is Re(IDFT(g)), which equals the
+// real inverse transform (C2R) of g's Hermitian part h(k) = (g(k) +
+// conj(g(-k))) / 2, and the model grid is the DFT of a real image, whose
+// upper half follows from the lower by the same symmetry.  So the bare
+// transforms are C2R and R2C over half spectra: half the arithmetic of the
+// complex transforms, which matters for FP64 on this part.
 // The transform runs in FP64 like the reference's standard-gridder FFT
 // (fft.rs:600-630 on Complex64 grids): the grid correction amplifies FFT
 // rounding near the image edge by up to 1/grdsf, which an FP32 transform
@@ -26,29 +32,32 @@ __device__ __forceinline__ float2 make_work(float re, float im, float2*) {
     return make_float2(re, im);
 }
 
+// h[kx][ky] = (-1)^(kx+ky) (g[k] + conj(g[-k])) / 2 for ky in [0, gny/2]
+// (indices mod the grid size; both points of a pair carry the same sign on
+// even grids): the input of the real inverse transform.  real_g: a PSF grid
+// kept as its float32 real part.
 template <typename W>
-__global__ void widen_checker_kernel(const float2* g, int64_t gnx, int64_t gny, W* out) {
-    using S = decltype(out->x);
-    const int64_t n = gnx * gny;
+__global__ void hermitian_half_kernel(const float2* g, const float* real_g, int64_t gnx,
+                                      int64_t gny, W* h) {
+    using S = decltype(h->x);
+    const int64_t hy = gny / 2 + 1, n = gnx * hy;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t x = t / gny, y = t - x * gny;
-        float2 v = g[t];
-        S s = ((x + y) & 1) ? S(-1) : S(1);
-        out[t] = make_work(s * (S)v.x, s * (S)v.y, out);
-    }
-}
-
-// The real part alone (a PSF grid kept as float32).
-template <typename W>
-__global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t gny, W* out) {
-    using S = decltype(out->x);
-    const int64_t n = gnx * gny;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t x = t / gny, y = t - x * gny;
-        S s = ((x + y) & 1) ? S(-1) : S(1);
-        out[t] = make_work(s * (S)g[t], S(0), out);
+        const int64_t kx = t / hy, ky = t - kx * hy;
+        const int64_t mx = kx == 0 ? 0 : gnx - kx, my = ky == 0 ? 0 : gny - ky;
+        S re, im = S(0);
+        if (real_g) {
+            re = ((S)real_g[kx * gny + ky] + (S)real_g[mx * gny + my]) * S(0.5);
+        } else {
+            const float2 a = g[kx * gny + ky], b = g[mx * gny + my];
+            re = ((S)a.x + (S)b.x) * S(0.5);
+            im = ((S)a.y - (S)b.y) * S(0.5);
+        }
+        if ((kx + ky) & 1) {
+            re = -re;
+            im = -im;
+        }
+        h[t] = make_work(re, im, h);
     }
 }
 
@@ -56,8 +65,8 @@ __global__ void widen_checker_real_kernel(const float* g, int64_t gnx, int64_t g
 // sinc_mode 1 (W-projection image correction) further divides by
 // sinc_x * sinc_y with the reference's 1e-6 guard; sinc_mode 2 multiplies by
 // it, which is the transpose of the W-projection model apodisation.
-template <typename W>
-__global__ void crop_correct_kernel(const W* raw, int64_t gny, int32_t nx, int32_t ny,
+template <typename S>
+__global__ void crop_correct_kernel(const S* raw, int64_t gny, int32_t nx, int32_t ny,
                                     int64_t blc_x, int64_t blc_y, int parity, double scale,
                                     const float* corr_x, const float* corr_y, const float* sx,
                                     const float* sy, int sinc_mode, float* image) {
@@ -66,7 +75,7 @@ __global__ void crop_correct_kernel(const W* raw, int64_t gny, int32_t nx, int32
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / ny, y = t - x * ny;
         int64_t gx = blc_x + x, gy = blc_y + y;
-        double r = (double)raw[gx * gny + gy].x;
+        double r = (double)raw[gx * gny + gy];
         if ((gx + gy + parity) & 1) r = -r;
         float v = (float)(r * scale);
         float factor = __fmul_rn(corr_x[gx], corr_y[gy]);
@@ -84,12 +93,11 @@ __global__ void crop_correct_kernel(const W* raw, int64_t gny, int32_t nx, int32
 
 // apodize_model / apodize_w_project_model (gridder.rs:1554-1592) into a
 // zeroed grid, with the input checkerboard of the centred forward FFT.
-template <typename W>
+template <typename S>
 __global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64_t gny,
                                int64_t blc_x, int64_t blc_y, const float* corr_x,
                                const float* corr_y, const float* sinc_x, const float* sinc_y,
-                               W* grid) {
-    using S = decltype(grid->x);
+                               S* grid) {
     const int64_t n = (int64_t)nx * ny;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
@@ -99,19 +107,30 @@ __global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64
         if (sinc_x) f = __fmul_rn(__fmul_rn(f, sinc_x[gx]), sinc_y[gy]);
         float v = model[t] * f;
         if ((gx + gy) & 1) v = -v;
-        grid[gx * gny + gy] = make_work((S)v, S(0), grid);
+        grid[gx * gny + gy] = (S)v;
     }
 }
 
+// The full model grid from the half spectrum of the real forward transform:
+// G[x][y] = half[x][y] for y <= gny/2, conj(half[-x][-y]) above; then the
+// output checkerboard and the narrowing to float32.
 template <typename W>
-__global__ void narrow_sign_kernel(const W* g, int64_t gnx, int64_t gny, int parity,
+__global__ void narrow_sign_kernel(const W* half, int64_t gnx, int64_t gny, int parity,
                                    float2* out) {
-    const int64_t n = gnx * gny;
+    const int64_t n = gnx * gny, hy = gny / 2 + 1;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x = t / gny, y = t - x * gny;
-        W v = g[t];
-        float re = (float)v.x, im = (float)v.y;
+        float re, im;
+        if (y < hy) {
+            const W v = half[x * hy + y];
+            re = (float)v.x;
+            im = (float)v.y;
+        } else {
+            const W v = half[(x == 0 ? 0 : gnx - x) * hy + (gny - y)];
+            re = (float)v.x;
+            im = -(float)v.y;
+        }
         if ((x + y + parity) & 1) {
             re = -re;
             im = -im;
@@ -144,35 +163,44 @@ __global__ void scale_image_kernel(float* img, int64_t n, float scale, const uns
 
 }  // namespace
 
-// The bare transform in place: cuFFT Z2Z (FP64) or C2C (float32).
-static void exec_fft(cr_ctx* ctx, int64_t gnx, int64_t gny, double2* work, int dir) {
-    check_cufft(cufftExecZ2Z(fft_plan(ctx, gnx, gny), (cufftDoubleComplex*)work,
-                             (cufftDoubleComplex*)work, dir),
-                "cufftExecZ2Z");
+// The bare transforms, out of place: C2R for images (Z2D in FP64, C2R in
+// float32), R2C for model grids.  A C2R transform may overwrite its input,
+// which is scratch here.
+static void exec_c2r(cr_ctx* ctx, int64_t gnx, int64_t gny, double2* in, double* out) {
+    check_cufft(cufftExecZ2D(fft_plan_type(ctx, gnx, gny, CUFFT_Z2D), (cufftDoubleComplex*)in,
+                             (cufftDoubleReal*)out),
+                "cufftExecZ2D");
 }
-static void exec_fft(cr_ctx* ctx, int64_t gnx, int64_t gny, float2* work, int dir) {
-    check_cufft(cufftExecC2C(fft_plan_c2c(ctx, gnx, gny), (cufftComplex*)work,
-                             (cufftComplex*)work, dir),
-                "cufftExecC2C");
+static void exec_c2r(cr_ctx* ctx, int64_t gnx, int64_t gny, float2* in, float* out) {
+    check_cufft(cufftExecC2R(fft_plan_type(ctx, gnx, gny, CUFFT_C2R), (cufftComplex*)in,
+                             (cufftReal*)out),
+                "cufftExecC2R");
+}
+static void exec_r2c(cr_ctx* ctx, int64_t gnx, int64_t gny, double* in, double2* out) {
+    check_cufft(cufftExecD2Z(fft_plan_type(ctx, gnx, gny, CUFFT_D2Z), (cufftDoubleReal*)in,
+                             (cufftDoubleComplex*)out),
+                "cufftExecD2Z");
+}
+static void exec_r2c(cr_ctx* ctx, int64_t gnx, int64_t gny, float* in, float2* out) {
+    check_cufft(cufftExecR2C(fft_plan_type(ctx, gnx, gny, CUFFT_R2C), (cufftReal*)in,
+                             (cufftComplex*)out),
+                "cufftExecR2C");
 }
 
 template <typename W>
 static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float2* grid,
                                float scale, float* image, bool adjoint, const float* real_grid) {
+    using S = decltype(W::x);
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
-    W* work = (W*)workspace(ctx, sizeof(W) == 16 ? "fft_z" : "fft_c",
-                            (size_t)gnx * gny * sizeof(W));
-    if (real_grid) {
-        widen_checker_real_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
-            real_grid, gnx, gny, work);
-        note_launch(ctx, "widen_checker_real_kernel");
-    } else {
-        widen_checker_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(
-            grid, gnx, gny, work);
-        note_launch(ctx, "widen_checker_kernel");
-    }
-    exec_fft(ctx, gnx, gny, work, CUFFT_INVERSE);
+    const bool f64 = sizeof(S) == 8;
+    const int64_t nh = gnx * (gny / 2 + 1);
+    W* half = (W*)workspace(ctx, f64 ? "fft_h64" : "fft_h32", (size_t)nh * sizeof(W));
+    S* raw = (S*)workspace(ctx, f64 ? "fft_r64" : "fft_r32", (size_t)gnx * gny * sizeof(S));
+    hermitian_half_kernel<W><<<grid_blocks(nh, 256), 256, 0, ctx->stream>>>(
+        grid, real_grid, gnx, gny, half);
+    note_launch(ctx, "hermitian_half_kernel");
+    exec_c2r(ctx, gnx, gny, half, raw);
     int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
     double inv = 1.0 / ((double)gnx * (double)gny);
     const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
@@ -184,8 +212,8 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
         sx = adjoint ? wp->sinc_gx_d : wp->sinc_x_d;
         sy = adjoint ? wp->sinc_gy_d : wp->sinc_x_d;
     }
-    crop_correct_kernel<W><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
-        work, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity,
+    crop_correct_kernel<S><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
+        raw, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity,
         inv * (double)scale, g->corr_x_d, g->corr_y_d, sx, sy, mode, image);
     note_launch(ctx, "crop_correct_kernel");
 }
@@ -193,19 +221,22 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
 template <typename W>
 static void image_to_grid_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
                                float2* grid) {
+    using S = decltype(W::x);
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
-    W* work = (W*)workspace(ctx, sizeof(W) == 16 ? "fft_z" : "fft_c",
-                            (size_t)gnx * gny * sizeof(W));
-    CR_CUDA_CHECK(cudaMemsetAsync(work, 0, (size_t)gnx * gny * sizeof(W), ctx->stream));
+    const bool f64 = sizeof(S) == 8;
+    const int64_t nh = gnx * (gny / 2 + 1);
+    W* half = (W*)workspace(ctx, f64 ? "fft_h64" : "fft_h32", (size_t)nh * sizeof(W));
+    S* raw = (S*)workspace(ctx, f64 ? "fft_r64" : "fft_r32", (size_t)gnx * gny * sizeof(S));
+    CR_CUDA_CHECK(cudaMemsetAsync(raw, 0, (size_t)gnx * gny * sizeof(S), ctx->stream));
     const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
-    apodize_kernel<W><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
+    apodize_kernel<S><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
         model, g->geom.nx, g->geom.ny, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d,
-        g->corr_y_d, wp ? wp->sinc_gx_d : nullptr, wp ? wp->sinc_gy_d : nullptr, work);
+        g->corr_y_d, wp ? wp->sinc_gx_d : nullptr, wp ? wp->sinc_gy_d : nullptr, raw);
     note_launch(ctx, "apodize_kernel");
-    exec_fft(ctx, gnx, gny, work, CUFFT_FORWARD);
+    exec_r2c(ctx, gnx, gny, raw, half);
     int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
-    narrow_sign_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(work, gnx, gny,
+    narrow_sign_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(half, gnx, gny,
                                                                                parity, grid);
     note_launch(ctx, "narrow_sign_kernel");
 }

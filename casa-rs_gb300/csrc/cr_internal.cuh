@@ -49,6 +49,8 @@ struct cr_ctx {
     cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans_c2c;
+    // real-to-complex and complex-to-real plans, by cufftType
+    std::map<int, std::map<std::pair<int64_t, int64_t>, cufftHandle>> fft_plans_real;
     cudaEvent_t ev[8] = {};
     // [0,1] bracket the last gridding kernel, [2,3] the last degridding kernel
     cudaEvent_t kev[4] = {};
@@ -124,6 +126,7 @@ void check_device_status(cr_ctx* ctx);
 void kernel_mark(cr_ctx* ctx, int which, bool end);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
 cufftHandle fft_plan_c2c(cr_ctx* ctx, int64_t nx, int64_t ny);
+cufftHandle fft_plan_type(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type);
 
 // ---- host-side tables (restated from gridder.rs) ----------------------------
 int64_t casa_composite_padded_len(int64_t image_len, double padding);
