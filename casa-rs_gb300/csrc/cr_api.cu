@@ -425,6 +425,12 @@ int cr_gridder_create(cr_ctx* ctx, const cr_geometry* geom, double padding, int3
             g->taps_bytes = (uint32_t)((g->taps_h.size() * 4 + 15) & ~size_t(15));
             CR_CUDA_CHECK(cudaMalloc(&g->taps_d, g->taps_bytes));
             CR_CUDA_CHECK(cudaMemset(g->taps_d, 0, g->taps_bytes));
+            std::vector<float> taps8((size_t)g->tap_rows * 8, 0.0f);
+            for (int32_t r = 0; r < g->tap_rows; ++r)
+                for (int k = 0; k < 7; ++k) taps8[(size_t)r * 8 + k] = g->taps_h[(size_t)r * 7 + k];
+            CR_CUDA_CHECK(cudaMalloc(&g->taps8_d, taps8.size() * 4));
+            CR_CUDA_CHECK(cudaMemcpy(g->taps8_d, taps8.data(), taps8.size() * 4,
+                                     cudaMemcpyHostToDevice));
             CR_CUDA_CHECK(cudaMalloc(&g->corr_x_d, (size_t)gnx * 4));
             CR_CUDA_CHECK(cudaMalloc(&g->corr_y_d, (size_t)gny * 4));
             CR_CUDA_CHECK(cudaMemcpy(g->taps_d, g->taps_h.data(), g->taps_h.size() * 4, cudaMemcpyHostToDevice));
@@ -445,6 +451,7 @@ void cr_gridder_destroy(cr_gridder* g) {
     cudaStreamSynchronize(g->ctx->stream);
     g->ctx->cube_graphs.clear();   // captured pipelines may read this gridder's tables
     cudaFree(g->taps_d);
+    cudaFree(g->taps8_d);
     cudaFree(g->corr_x_d);
     cudaFree(g->corr_y_d);
     delete g;

@@ -872,8 +872,8 @@ struct CubeDegridArgs {
     const uint2* items;          // (bin, chunk)
     const unsigned long long* n_items;
     unsigned int* item_counter;
-    const float* taps;           // zero-padded to taps_bytes
-    uint32_t taps_bytes;
+    const float* taps8;          // [tap_rows][8], rows padded to 32 bytes
+    uint32_t taps8_bytes;
     const float2* grid;          // [C][gnx][gny]
     float2* pred;                // [C][R]
     const float* rec_w;          // RESIDUAL: imaging weight per record
@@ -892,7 +892,9 @@ struct CubeDegridArgs {
 // buffers: while the block works on one item, the next item's footprint is
 // already in flight.  Without TMA (a grid whose rows are not a multiple of
 // 16 bytes, or an unaligned base) the block loads each footprint itself.
-// The tap table arrives by one bulk copy in either case.
+// The tap table arrives by one bulk copy in either case, its rows padded to
+// 8 floats so that a record's 7 y taps come in two 16-byte loads (the
+// kernel is bound by shared-memory instructions).
 template <bool RESIDUAL, bool TMA>
 __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
     const __grid_constant__ CUtensorMap gmap, CubeDegridArgs a) {
@@ -920,8 +922,8 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
     if (tid == 0) {
         for (int k = 0; k < 3; ++k) mbar_init(&s_bar[k], 1);
         mbar_fence_init();
-        mbar_expect_tx(&s_bar[2], a.taps_bytes);
-        bulk_load(s_taps, a.taps, a.taps_bytes, &s_bar[2]);
+        mbar_expect_tx(&s_bar[2], a.taps8_bytes);
+        bulk_load(s_taps, a.taps8, a.taps8_bytes, &s_bar[2]);
         const int first = (int)atomicAdd(a.item_counter, 1u);
         s_item[0] = first;
         if (TMA) {
@@ -1005,11 +1007,13 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
                 sample = q.y;
                 if (ix < 7) {
                     const uint32_t meta = q.x;
-                    const float* wx = s_taps + ((meta >> 11) & 2047u) * 7;
-                    const float* wy = s_taps + (meta & 2047u) * 7;
+                    const float wxi = s_taps[((meta >> 11) & 2047u) * 8 + ix];
+                    const float4* wy4 = reinterpret_cast<const float4*>(s_taps) +
+                                        (meta & 2047u) * 2;
+                    const float4 ya = wy4[0], yb = wy4[1];
+                    const float wy[7] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z};
                     const int row =
                         ((int)(meta >> 27) + ix) * kPitch + (int)((meta >> 22) & 31);
-                    const float wxi = wx[ix];
 #pragma unroll
                     for (int iy = 0; iy < 7; ++iy) {
                         const float wgt = __fmul_rn(wxi, wy[iy]);
@@ -1324,9 +1328,10 @@ static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr
     const cr_grid_info& gi = g->info;
     unsigned int* counter = (unsigned int*)workspace(ctx, "cube_counter", 8);
     CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 8, ctx->stream));
+    const uint32_t taps8_bytes = (uint32_t)g->tap_rows * 32u;
     CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
-                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps_d,
-                     g->taps_bytes, grid, pred, cr.rec_w, res, ctx->status_d};
+                     gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps8_d,
+                     taps8_bytes, grid, pred, cr.rec_w, res, ctx->status_d};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     // the grids as float32 [C][gnx][2 gny] for footprint boxes of 76 x 38
@@ -1338,10 +1343,10 @@ static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr
                                           row * (uint64_t)gi.grid_nx, 2 * (kTile + 6), kTile + 6);
     if (tma)
         cube_degrid_kernel<RESIDUAL, true>
-            <<<sms * 8, kCubeThreads, g->taps_bytes, ctx->stream>>>(map, a);
+            <<<sms * 8, kCubeThreads, taps8_bytes, ctx->stream>>>(map, a);
     else
         cube_degrid_kernel<RESIDUAL, false>
-            <<<sms * 8, kCubeThreads, g->taps_bytes, ctx->stream>>>(map, a);
+            <<<sms * 8, kCubeThreads, taps8_bytes, ctx->stream>>>(map, a);
     note_launch(ctx, RESIDUAL ? "cube_degrid_kernel_residual" : "cube_degrid_kernel");
 }
 

@@ -85,6 +85,7 @@ struct cr_gridder {
     std::vector<float> taps_h, corr_x_h, corr_y_h;
     float* taps_d = nullptr;     // [tap_rows][7], zero-padded to taps_bytes
     uint32_t taps_bytes = 0;     // tap_rows * 7 * 4 rounded up to 16 (bulk copies)
+    float* taps8_d = nullptr;    // [tap_rows][8]: rows padded with a zero to 32 bytes
     float* corr_x_d = nullptr;   // [grid_nx]
     float* corr_y_d = nullptr;   // [grid_ny]
 };
