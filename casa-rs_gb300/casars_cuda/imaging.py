@@ -43,6 +43,7 @@ class _Arrays:
     def __init__(self):
         self.keep = []
         self.location = None
+        self.pinned = False   # a host input was a page-locked torch tensor
 
     def _loc(self, loc):
         if self.location is None:
@@ -55,6 +56,7 @@ class _Arrays:
             return None
         if _is_torch(a):
             if not a.is_cuda:
+                self.pinned = self.pinned or a.is_pinned()
                 a = a.detach().cpu().numpy()
             else:
                 self._loc(CR_DEVICE)
@@ -78,6 +80,11 @@ class _Arrays:
         if loc == CR_DEVICE:
             t = torch.empty(shape, dtype=torch_dtype, device=device or "cuda")
             return t, t.data_ptr(), CR_DEVICE
+        if self.pinned and torch is not None:
+            # page-locked inputs get page-locked outputs: the device-to-host
+            # copies then run at full link speed
+            t = torch.empty(shape, dtype=torch_dtype, pin_memory=True)
+            return t, t.data_ptr(), CR_HOST
         arr = np.empty(shape, np_dtype)
         return arr, arr.ctypes.data, CR_HOST
 

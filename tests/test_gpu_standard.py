@@ -181,3 +181,20 @@ def test_dirty_accumulator_matches_one_batch(device):
     assert peak_norm_err(get(res), res_o) <= 1e-5
     acc.close()
     ctx.close()
+
+
+def test_pinned_host_inputs_give_pinned_outputs(ctx):
+    """Page-locked torch host inputs: the call copies them like numpy
+    arrays and returns its images in page-locked torch tensors."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(29)
+    geom, og, gg = make(ctx, 64, 1e-4, 100)
+    u, v, w, wt, vis = random_batch(rng, 6000, og.gnx, og.du, margin=2)
+    psf, res, state, _ = cc.dirty_image(gg, cc.VisibilityBatch(u, v, vis, wt))
+    pin = lambda a: torch.as_tensor(a).pin_memory()
+    psf_p, res_p, state_p, _ = cc.dirty_image(
+        gg, cc.VisibilityBatch(pin(u), pin(v), pin(vis), pin(wt)))
+    assert isinstance(res_p, torch.Tensor) and res_p.is_pinned() and not res_p.is_cuda
+    assert peak_norm_err(psf_p.numpy(), psf) <= TOL
+    assert peak_norm_err(res_p.numpy(), res) <= TOL
+    assert state_p.psf_peak == pytest.approx(state.psf_peak, rel=1e-6)
