@@ -294,3 +294,33 @@ def test_cube_density_boundary_samples_take_the_oracle_cells(ctx):
         ox, _, _, _ = og.plan_many(u, v)
         np.testing.assert_array_equal(wt[c], np.where((ox >= 0) & (wo > 0), wo, 0.0)
                                       .astype(np.float32))
+
+
+def test_cube_edge_cases(ctx, cube):
+    """No rows at all: empty grids and zero sums.  A channel whose samples
+    are all flagged: empty grids for it, and the other channels as in the
+    run without that flag (PerPlane density keeps channels apart)."""
+    obs, flags, vis = cube
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(obs.nx, obs.nx, obs.cell, obs.cell), OS)
+    C = obs.channels
+    empty = cc.CubeBatch(np.zeros(0), np.zeros(0), obs.lambda_scale,
+                         np.zeros((C, 0), np.complex64), None, np.zeros((C, 0), np.uint8))
+    psf, dirty, sums = cc.cube_grid_dirty(gg, empty, "briggs", 0.5)
+    assert not np.any(psf) and not np.any(dirty)
+    assert all(s.gridded_samples == 0 and s.normalization_sumwt == 0.0 for s in sums)
+
+    ref_psf, ref_dirty, ref_sums = cc.cube_grid_dirty(
+        gg, cc.CubeBatch(obs.u_m, obs.v_m, obs.lambda_scale, vis, None, flags), "briggs", 0.5)
+    f2 = flags.copy()
+    f2[3] = 1
+    psf, dirty, sums = cc.cube_grid_dirty(
+        gg, cc.CubeBatch(obs.u_m, obs.v_m, obs.lambda_scale, vis, None, f2), "briggs", 0.5)
+    assert not np.any(psf[3]) and not np.any(dirty[3]) and sums[3].gridded_samples == 0
+    for c in range(C):
+        if c == 3:
+            continue
+        assert sums[c].gridded_samples == ref_sums[c].gridded_samples
+        assert sums[c].normalization_sumwt == ref_sums[c].normalization_sumwt
+        # tiles shared by several work items add with atomics in any order
+        assert peak_norm_err(psf[c], ref_psf[c]) <= 1e-6
+        assert peak_norm_err(dirty[c], ref_dirty[c]) <= 1e-6

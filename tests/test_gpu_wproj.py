@@ -84,8 +84,9 @@ def test_grid_and_degrid_match_oracle(ctx, case):
 
 def test_plane_choice_and_conjugation(ctx):
     og, ow, gg, gw = build(ctx, *CASES[0][:5], CASES[0][5])
-    # a single sample with w > 0 uses the conjugated kernel (lib.rs:95167)
-    for wv in (-1200.0, 1200.0, 0.0, 1e-9):
+    # a single sample with w > 0 uses the conjugated kernel (lib.rs:95167);
+    # |w| past the largest planned |w| clamps to the last plane
+    for wv in (-1200.0, 1200.0, 0.0, 1e-9, 4500.0, -9000.0):
         u = np.array([3.3 * og.du]); v = np.array([-5.7 * og.du]); w = np.array([wv])
         psf_o, dirty_o, acc = ow.grid_dirty(u, v, w, np.ones(1, np.float32), np.ones(1, np.complex64))
         psf_g, dirty_g, sums = cc.grid_dirty(gg, cc.VisibilityBatch(u, v, np.ones(1, np.complex64),
@@ -119,3 +120,23 @@ def test_residual_refresh_matches_oracle(ctx):
     res_o, acc = ow.residual(mg_o, u, v, w, wt, vis)
     res_g, sums = cc.grid_residual(gg, cc.VisibilityBatch(u, v, vis, wt, w), mg_g, gw)
     assert peak_norm_err(res_g, res_o) <= TOL
+
+
+def test_footprints_at_the_grid_edge(ctx):
+    """Samples whose W-kernel footprint would leave the grid are rejected
+    (counted as skipped) exactly as the oracle rejects them; those just
+    inside are gridded."""
+    og, ow, gg, gw = build(ctx, *CASES[0][:5], CASES[0][5])
+    s_max = int(ow.support.max())
+    half = og.gnx // 2
+    xs = np.arange(half - s_max - 4, half + 1, dtype=np.float64)   # cells from the centre
+    u = np.concatenate([xs, -xs]) * og.du + 0.3 * og.du
+    v = np.full(len(u), 2.2 * og.du)
+    w = np.linspace(-1500.0, 1500.0, len(u))
+    wt = np.ones(len(u), np.float32)
+    vis = np.ones(len(u), np.complex64)
+    psf_o, dirty_o, acc = ow.grid_dirty(u, v, w, wt, vis)
+    psf_g, dirty_g, sums = cc.grid_dirty(gg, cc.VisibilityBatch(u, v, vis, wt, w), gw)
+    assert acc.skipped > 0 and acc.gridded > 0
+    assert sums.gridded_samples == acc.gridded and sums.skipped_samples == acc.skipped
+    assert peak_norm_err(dirty_g, dirty_o) <= TOL
