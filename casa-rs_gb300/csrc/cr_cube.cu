@@ -482,7 +482,9 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_hist_kernel(CubeArgs a) 
 }
 
 // Pass 2: scatter records into (channel, home tile) bins from pass 1's
-// per-sample results.
+// per-sample results, kScatterVec samples per thread and iteration so that
+// more cursor atomics are in flight.
+constexpr int kScatterVec = 8;
 __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs a) {
     const int c = blockIdx.y;
     const int64_t ntiles = a.ntx * a.nty;
@@ -490,17 +492,18 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
     const int wp = threadIdx.x >> 5;
-    for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
-        // loads first, then every cursor atomic, then the stores: the kVec
+    for (int64_t base = r0 + wp * 32 * kScatterVec; base < r1;
+         base += kCubeThreads * kScatterVec) {
+        // loads first, then every cursor atomic, then the stores: the kScatterVec
         // atomics of a thread are in flight together.  (The samples of a
         // warp -- consecutive rows of one channel, different baselines --
         // almost never share a cell bin, so the atomics are not aggregated:
         // a warp match cost more than it saved.)
-        uint32_t tile[kVec], meta[kVec], pos[kVec];
-        float w[kVec];
-        float2 vv[kVec];
+        uint32_t tile[kScatterVec], meta[kScatterVec], pos[kScatterVec];
+        float w[kScatterVec];
+        float2 vv[kScatterVec];
 #pragma unroll
-        for (int j = 0; j < kVec; ++j) {
+        for (int j = 0; j < kScatterVec; ++j) {
             const int64_t r = base + lane + 32 * j;
             const int64_t i = (int64_t)c * a.R + (r < r1 ? r : r0);
             tile[j] = r < r1 ? a.ev_tile[i] : ~0u;
@@ -509,13 +512,13 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
             vv[j] = a.vis[i];
         }
 #pragma unroll
-        for (int j = 0; j < kVec; ++j) {
+        for (int j = 0; j < kScatterVec; ++j) {
             pos[j] = 0u;
             if (tile[j] != ~0u)
                 pos[j] = atomicAdd(&a.cursor[cell_bin(c, ntiles, tile[j], meta[j])], 1u);
         }
 #pragma unroll
-        for (int j = 0; j < kVec; ++j) {
+        for (int j = 0; j < kScatterVec; ++j) {
             if (tile[j] == ~0u) continue;
             const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
             float vr = 0.0f, vi = 0.0f;
