@@ -359,6 +359,8 @@ void cr_ctx_destroy(cr_ctx* ctx) {
     for (auto& kv : ctx->fft_plans_c2c) cufftDestroy(kv.second);
     for (auto& m : ctx->fft_plans_real)
         for (auto& kv : m.second) cufftDestroy(kv.second);
+    for (auto& m : ctx->fft_plans_many)
+        for (auto& kv : m.second) cufftDestroy(kv.second);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->kev)
@@ -1420,22 +1422,26 @@ int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
         const bool single = p->fft_bits == 32;
         CR_CUDA_CHECK(cudaMemsetAsync(peaks, 0, C * 4, ctx->stream));
         std::vector<float> sumwt(C);
+        std::vector<int> live;
+        std::vector<float> scales;
         for (size_t c = 0; c < C; ++c) {
             sumwt[c] = (float)p->sums[c].normalization_sumwt;
-            float* pc = pi + c * np;
-            float* rc = ri + c * np;
             if (!(p->sums[c].normalization_sumwt > 0.0 && p->sums[c].reported_sumwt > 0.0)) {
-                CR_CUDA_CHECK(cudaMemsetAsync(pc, 0, np * 4, ctx->stream));
-                CR_CUDA_CHECK(cudaMemsetAsync(rc, 0, np * 4, ctx->stream));
+                CR_CUDA_CHECK(cudaMemsetAsync(pi + c * np, 0, np * 4, ctx->stream));
+                CR_CUDA_CHECK(cudaMemsetAsync(ri + c * np, 0, np * 4, ctx->stream));
                 continue;
             }
-            // the normalisation of dirty_grids_to_psf_and_residual_owned,
-            // as the single-plane cr_dirty_image
-            grid_to_image_real(ctx, g, psf + c * cells, 1.0f / sumwt[c], pc, single);
-            abs_peak(ctx, pc, (int64_t)np, peaks + c);
-            scale_image(ctx, pc, (int64_t)np, 1.0f, peaks + c);
-            grid_to_image(ctx, g, nullptr, dirty + c * cells, 1.0f / sumwt[c], rc, single);
-            scale_image(ctx, rc, (int64_t)np, 1.0f, peaks + c);
+            live.push_back((int)c);
+            scales.push_back(1.0f / sumwt[c]);
+        }
+        // the normalisation of dirty_grids_to_psf_and_residual_owned, as the
+        // single-plane cr_dirty_image, with the transforms batched over planes
+        grid_to_image_planes(ctx, g, nullptr, psf, live, scales, pi, single);
+        grid_to_image_planes(ctx, g, dirty, nullptr, live, scales, ri, single);
+        for (int c : live) {
+            abs_peak(ctx, pi + c * np, (int64_t)np, peaks + c);
+            scale_image(ctx, pi + c * np, (int64_t)np, 1.0f, peaks + c);
+            scale_image(ctx, ri + c * np, (int64_t)np, 1.0f, peaks + c);
         }
         tm.mark();
         std::vector<unsigned int> pk(C);
@@ -1490,16 +1496,16 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
                                                     "cube_models");
         float2* mg = (float2*)workspace(ctx, "cpr_model_grids", C * cells * 8);
         const bool single = p->fft_bits == 32;
-        for (int c : chosen)
-            image_to_grid(ctx, g, nullptr, m + (size_t)c * np, mg + c * cells, single);
+        image_to_grid_planes(ctx, g, m, chosen, mg, single);
         tm.mark();
         float2* res = (float2*)workspace(ctx, "cpr_residual_grids", C * cells * 8);
         cube_grid_residual(ctx, g, p->rec, mg, res, mask);
         tm.mark();
         float* img = out_ptr<float>(ctx, residual_images, out_location, C * np * 4, "cpr_image");
+        std::vector<float> scales;
+        for (int c : chosen) scales.push_back(1.0f / states[c].normalization_sumwt);
+        grid_to_image_planes(ctx, g, res, nullptr, chosen, scales, img, single);
         for (int c : chosen) {
-            grid_to_image(ctx, g, nullptr, res + (size_t)c * cells,
-                          1.0f / states[c].normalization_sumwt, img + (size_t)c * np, single);
             scale_image(ctx, img + (size_t)c * np, (int64_t)np, 1.0f / states[c].psf_peak,
                         nullptr);
             if (out_location == CR_HOST)

@@ -95,6 +95,21 @@ cufftHandle fft_plan_type(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type) {
     return cached_plan(ctx, ctx->fft_plans_real[(int)type], nx, ny, type);
 }
 
+cufftHandle fft_plan_many(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type, int batch) {
+    auto& plans = ctx->fft_plans_many[std::make_pair((int)type, batch)];
+    auto key = std::make_pair(nx, ny);
+    auto it = plans.find(key);
+    if (it == plans.end()) {
+        cufftHandle h;
+        int n[2] = {(int)nx, (int)ny};
+        check_cufft(cufftPlanMany(&h, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, batch),
+                    "cufftPlanMany");
+        it = plans.emplace(key, h).first;
+    }
+    check_cufft(cufftSetStream(it->second, ctx->stream), "cufftSetStream");
+    return it->second;
+}
+
 // ---- host tables --------------------------------------------------------------
 // casa_composite_padded_len (gridder.rs:4152-4173).
 int64_t casa_composite_padded_len(int64_t image_len, double padding) {

@@ -17,6 +17,8 @@
 // (fft.rs:600-630 on Complex64 grids): the grid correction amplifies FFT
 // rounding near the image edge by up to 1/grdsf, which an FP32 transform
 // would carry into the image at the 1e-6 level.
+#include <algorithm>
+
 #include "cr_internal.cuh"
 
 namespace cr {
@@ -37,7 +39,8 @@ __device__ __forceinline__ float2 make_work(float re, float im, float2*) {
 // even grids): the input of the real inverse transform.  real_g: a PSF grid
 // kept as its float32 real part.
 template <typename W>
-__global__ void hermitian_half_kernel(const float2* g, const float* real_g, int64_t gnx,
+__device__ __forceinline__ void hermitian_half_body(const float2* g, const float* real_g,
+                                                    int64_t gnx,
                                       int64_t gny, W* h) {
     using S = decltype(h->x);
     const int64_t hy = gny / 2 + 1, n = gnx * hy;
@@ -61,12 +64,18 @@ __global__ void hermitian_half_kernel(const float2* g, const float* real_g, int6
     }
 }
 
+template <typename W>
+__global__ void hermitian_half_kernel(const float2* g, const float* real_g, int64_t gnx,
+                                      int64_t gny, W* h) {
+    hermitian_half_body(g, real_g, gnx, gny, h);
+}
+
 // image(x, y) = Re(raw[blc + (x, y)]) * sign * scale * corr_x * corr_y.
 // sinc_mode 1 (W-projection image correction) further divides by
 // sinc_x * sinc_y with the reference's 1e-6 guard; sinc_mode 2 multiplies by
 // it, which is the transpose of the W-projection model apodisation.
 template <typename S>
-__global__ void crop_correct_kernel(const S* raw, int64_t gny, int32_t nx, int32_t ny,
+__device__ __forceinline__ void crop_correct_body(const S* raw, int64_t gny, int32_t nx, int32_t ny,
                                     int64_t blc_x, int64_t blc_y, int parity, double scale,
                                     const float* corr_x, const float* corr_y, const float* sx,
                                     const float* sy, int sinc_mode, float* image) {
@@ -91,10 +100,20 @@ __global__ void crop_correct_kernel(const S* raw, int64_t gny, int32_t nx, int32
     }
 }
 
+template <typename S>
+__global__ void crop_correct_kernel(const S* raw, int64_t gny, int32_t nx, int32_t ny,
+                                    int64_t blc_x, int64_t blc_y, int parity, double scale,
+                                    const float* corr_x, const float* corr_y, const float* sx,
+                                    const float* sy, int sinc_mode, float* image) {
+    crop_correct_body(raw, gny, nx, ny, blc_x, blc_y, parity, scale, corr_x, corr_y, sx, sy,
+                      sinc_mode, image);
+}
+
 // apodize_model / apodize_w_project_model (gridder.rs:1554-1592) into a
 // zeroed grid, with the input checkerboard of the centred forward FFT.
 template <typename S>
-__global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64_t gny,
+__device__ __forceinline__ void apodize_body(const float* model, int32_t nx, int32_t ny,
+                                             int64_t gny,
                                int64_t blc_x, int64_t blc_y, const float* corr_x,
                                const float* corr_y, const float* sinc_x, const float* sinc_y,
                                S* grid) {
@@ -111,11 +130,20 @@ __global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64
     }
 }
 
+template <typename S>
+__global__ void apodize_kernel(const float* model, int32_t nx, int32_t ny, int64_t gny,
+                               int64_t blc_x, int64_t blc_y, const float* corr_x,
+                               const float* corr_y, const float* sinc_x, const float* sinc_y,
+                               S* grid) {
+    apodize_body(model, nx, ny, gny, blc_x, blc_y, corr_x, corr_y, sinc_x, sinc_y, grid);
+}
+
 // The full model grid from the half spectrum of the real forward transform:
 // G[x][y] = half[x][y] for y <= gny/2, conj(half[-x][-y]) above; then the
 // output checkerboard and the narrowing to float32.
 template <typename W>
-__global__ void narrow_sign_kernel(const W* half, int64_t gnx, int64_t gny, int parity,
+__device__ __forceinline__ void narrow_sign_body(const W* half, int64_t gnx, int64_t gny,
+                                                 int parity,
                                    float2* out) {
     const int64_t n = gnx * gny, hy = gny / 2 + 1;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -137,6 +165,12 @@ __global__ void narrow_sign_kernel(const W* half, int64_t gnx, int64_t gny, int 
         }
         out[t] = make_float2(re, im);
     }
+}
+
+template <typename W>
+__global__ void narrow_sign_kernel(const W* half, int64_t gnx, int64_t gny, int parity,
+                                   float2* out) {
+    narrow_sign_body(half, gnx, gny, parity, out);
 }
 
 __global__ void abs_peak_kernel(const float* img, int64_t n, unsigned int* peak) {
@@ -239,6 +273,158 @@ static void image_to_grid_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
     narrow_sign_kernel<W><<<grid_blocks(gnx * gny, 256), 256, 0, ctx->stream>>>(half, gnx, gny,
                                                                                parity, grid);
     note_launch(ctx, "narrow_sign_kernel");
+}
+
+// ---- the same stage over planes of a cube, kPlaneBatch planes per cuFFT call ----
+namespace {
+
+constexpr int kPlaneBatch = 16;
+
+struct PlaneChunk {
+    int plane[kPlaneBatch];   // cube plane of batch entry b
+    float scale[kPlaneBatch]; // its image scale (grid_to_image's `scale`)
+};
+
+template <typename W>
+__global__ void hermitian_half_planes(const float2* grids, const float* real_grids,
+                                      int64_t gnx, int64_t gny, PlaneChunk pc, W* half) {
+    const int64_t cells = gnx * gny, nh = gnx * (gny / 2 + 1);
+    const int b = blockIdx.y;
+    const int64_t p = pc.plane[b];
+    hermitian_half_body(grids ? grids + p * cells : nullptr,
+                        real_grids ? real_grids + p * cells : nullptr, gnx, gny, half + b * nh);
+}
+
+template <typename S>
+__global__ void crop_correct_planes(const S* raw, int64_t gnx, int64_t gny, int32_t nx,
+                                    int32_t ny, int64_t blc_x, int64_t blc_y, int parity,
+                                    double inv, PlaneChunk pc, const float* corr_x,
+                                    const float* corr_y, float* images) {
+    const int b = blockIdx.y;
+    crop_correct_body(raw + b * gnx * gny, gny, nx, ny, blc_x, blc_y, parity,
+                      inv * (double)pc.scale[b], corr_x, corr_y, nullptr, nullptr, 0,
+                      images + (int64_t)pc.plane[b] * nx * ny);
+}
+
+template <typename S>
+__global__ void apodize_planes(const float* models, int32_t nx, int32_t ny, int64_t gnx,
+                               int64_t gny, int64_t blc_x, int64_t blc_y, const float* corr_x,
+                               const float* corr_y, PlaneChunk pc, S* raw) {
+    const int b = blockIdx.y;
+    apodize_body(models + (int64_t)pc.plane[b] * nx * ny, nx, ny, gny, blc_x, blc_y, corr_x,
+                 corr_y, nullptr, nullptr, raw + b * gnx * gny);
+}
+
+template <typename W>
+__global__ void narrow_sign_planes(const W* half, int64_t gnx, int64_t gny, int parity,
+                                   PlaneChunk pc, float2* grids) {
+    const int b = blockIdx.y;
+    narrow_sign_body(half + b * gnx * (gny / 2 + 1), gnx, gny, parity,
+                     grids + (int64_t)pc.plane[b] * gnx * gny);
+}
+
+void exec_c2r_many(cr_ctx* ctx, int64_t gnx, int64_t gny, int n, double2* in, double* out) {
+    check_cufft(cufftExecZ2D(fft_plan_many(ctx, gnx, gny, CUFFT_Z2D, n),
+                             (cufftDoubleComplex*)in, (cufftDoubleReal*)out),
+                "cufftExecZ2D");
+}
+void exec_c2r_many(cr_ctx* ctx, int64_t gnx, int64_t gny, int n, float2* in, float* out) {
+    check_cufft(cufftExecC2R(fft_plan_many(ctx, gnx, gny, CUFFT_C2R, n), (cufftComplex*)in,
+                             (cufftReal*)out),
+                "cufftExecC2R");
+}
+void exec_r2c_many(cr_ctx* ctx, int64_t gnx, int64_t gny, int n, double* in, double2* out) {
+    check_cufft(cufftExecD2Z(fft_plan_many(ctx, gnx, gny, CUFFT_D2Z, n), (cufftDoubleReal*)in,
+                             (cufftDoubleComplex*)out),
+                "cufftExecD2Z");
+}
+void exec_r2c_many(cr_ctx* ctx, int64_t gnx, int64_t gny, int n, float* in, float2* out) {
+    check_cufft(cufftExecR2C(fft_plan_many(ctx, gnx, gny, CUFFT_R2C, n), (cufftReal*)in,
+                             (cufftComplex*)out),
+                "cufftExecR2C");
+}
+
+template <typename W>
+void grid_to_image_planes_impl(cr_ctx* ctx, cr_gridder* g, const float2* grids,
+                               const float* real_grids, const std::vector<int>& planes,
+                               const std::vector<float>& scales, float* images) {
+    using S = decltype(W::x);
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
+    const bool f64 = sizeof(S) == 8;
+    const int64_t nh = gnx * (gny / 2 + 1);
+    W* half = (W*)workspace(ctx, f64 ? "fftp_h64" : "fftp_h32",
+                            (size_t)nh * kPlaneBatch * sizeof(W));
+    S* raw = (S*)workspace(ctx, f64 ? "fftp_r64" : "fftp_r32",
+                           (size_t)gnx * gny * kPlaneBatch * sizeof(S));
+    const int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
+    const double inv = 1.0 / ((double)gnx * (double)gny);
+    const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
+    for (size_t k0 = 0; k0 < planes.size(); k0 += kPlaneBatch) {
+        const int nb = (int)std::min<size_t>(kPlaneBatch, planes.size() - k0);
+        PlaneChunk pc{};
+        for (int b = 0; b < nb; ++b) {
+            pc.plane[b] = planes[k0 + b];
+            pc.scale[b] = scales[k0 + b];
+        }
+        hermitian_half_planes<W><<<dim3(grid_blocks(nh, 256, 152 * 4), nb), 256, 0,
+                                   ctx->stream>>>(grids, real_grids, gnx, gny, pc, half);
+        note_launch(ctx, "hermitian_half_planes");
+        exec_c2r_many(ctx, gnx, gny, nb, half, raw);
+        crop_correct_planes<S><<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+            raw, gnx, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity, inv,
+            pc, g->corr_x_d, g->corr_y_d, images);
+        note_launch(ctx, "crop_correct_planes");
+    }
+}
+
+template <typename W>
+void image_to_grid_planes_impl(cr_ctx* ctx, cr_gridder* g, const float* models,
+                               const std::vector<int>& planes, float2* grids) {
+    using S = decltype(W::x);
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
+    const bool f64 = sizeof(S) == 8;
+    const int64_t nh = gnx * (gny / 2 + 1);
+    W* half = (W*)workspace(ctx, f64 ? "fftp_h64" : "fftp_h32",
+                            (size_t)nh * kPlaneBatch * sizeof(W));
+    S* raw = (S*)workspace(ctx, f64 ? "fftp_r64" : "fftp_r32",
+                           (size_t)gnx * gny * kPlaneBatch * sizeof(S));
+    const int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
+    const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
+    for (size_t k0 = 0; k0 < planes.size(); k0 += kPlaneBatch) {
+        const int nb = (int)std::min<size_t>(kPlaneBatch, planes.size() - k0);
+        PlaneChunk pc{};
+        for (int b = 0; b < nb; ++b) pc.plane[b] = planes[k0 + b];
+        CR_CUDA_CHECK(cudaMemsetAsync(raw, 0, (size_t)gnx * gny * nb * sizeof(S), ctx->stream));
+        apodize_planes<S><<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+            models, g->geom.nx, g->geom.ny, gnx, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d,
+            g->corr_y_d, pc, raw);
+        note_launch(ctx, "apodize_planes");
+        exec_r2c_many(ctx, gnx, gny, nb, raw, half);
+        narrow_sign_planes<W><<<dim3(grid_blocks(gnx * gny, 256, 152 * 4), nb), 256, 0,
+                                ctx->stream>>>(half, gnx, gny, parity, pc, grids);
+        note_launch(ctx, "narrow_sign_planes");
+    }
+}
+
+}  // namespace
+
+void grid_to_image_planes(cr_ctx* ctx, cr_gridder* g, const float2* grids,
+                          const float* real_grids, const std::vector<int>& planes,
+                          const std::vector<float>& scales, float* images, bool single) {
+    if (single)
+        grid_to_image_planes_impl<float2>(ctx, g, grids, real_grids, planes, scales, images);
+    else
+        grid_to_image_planes_impl<double2>(ctx, g, grids, real_grids, planes, scales, images);
+}
+
+void image_to_grid_planes(cr_ctx* ctx, cr_gridder* g, const float* models,
+                          const std::vector<int>& planes, float2* grids, bool single) {
+    if (single)
+        image_to_grid_planes_impl<float2>(ctx, g, models, planes, grids);
+    else
+        image_to_grid_planes_impl<double2>(ctx, g, models, planes, grids);
 }
 
 void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,

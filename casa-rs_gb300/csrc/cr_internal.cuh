@@ -51,6 +51,9 @@ struct cr_ctx {
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans_c2c;
     // real-to-complex and complex-to-real plans, by cufftType
     std::map<int, std::map<std::pair<int64_t, int64_t>, cufftHandle>> fft_plans_real;
+    // batched real transforms over cube planes, by (type, batch)
+    std::map<std::pair<int, int>, std::map<std::pair<int64_t, int64_t>, cufftHandle>>
+        fft_plans_many;
     cudaEvent_t ev[8] = {};
     // [0,1] bracket the last gridding kernel, [2,3] the last degridding kernel
     cudaEvent_t kev[4] = {};
@@ -128,6 +131,7 @@ void kernel_mark(cr_ctx* ctx, int which, bool end);
 cufftHandle fft_plan(cr_ctx* ctx, int64_t nx, int64_t ny);
 cufftHandle fft_plan_c2c(cr_ctx* ctx, int64_t nx, int64_t ny);
 cufftHandle fft_plan_type(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type);
+cufftHandle fft_plan_many(cr_ctx* ctx, int64_t nx, int64_t ny, cufftType type, int batch);
 
 // ---- host-side tables (restated from gridder.rs) ----------------------------
 int64_t casa_composite_padded_len(int64_t image_len, double padding);
@@ -226,6 +230,15 @@ void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
 void grid_to_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                    float* image, bool single = false);
 // the exact adjoint of image_to_grid's image-side factor (no sinc division)
+// The image stage over planes of a cube, batched: grids (complex, or the
+// PSF's real parts) [C][gnx][gny] -> images [C][nx][ny] for the listed
+// planes, plane k scaled by scales[k] as grid_to_image scales; and models
+// [C][nx][ny] -> model grids for the listed planes.
+void grid_to_image_planes(cr_ctx* ctx, cr_gridder* g, const float2* grids,
+                          const float* real_grids, const std::vector<int>& planes,
+                          const std::vector<float>& scales, float* images, bool single);
+void image_to_grid_planes(cr_ctx* ctx, cr_gridder* g, const float* models,
+                          const std::vector<int>& planes, float2* grids, bool single);
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                            float* image, bool single = false);
 // model image (device) -> centred model grid (device)
