@@ -1438,11 +1438,10 @@ int cr_cube_plan_dirty_images(cr_ctx* ctx, cr_cube_plan* p, float* psf_images,
         // single-plane cr_dirty_image, with the transforms batched over planes
         grid_to_image_planes(ctx, g, nullptr, psf, live, scales, pi, single);
         grid_to_image_planes(ctx, g, dirty, nullptr, live, scales, ri, single);
-        for (int c : live) {
-            abs_peak(ctx, pi + c * np, (int64_t)np, peaks + c);
-            scale_image(ctx, pi + c * np, (int64_t)np, 1.0f, peaks + c);
-            scale_image(ctx, ri + c * np, (int64_t)np, 1.0f, peaks + c);
-        }
+        const std::vector<float> ones(live.size(), 1.0f);
+        abs_peak_planes(ctx, pi, (int64_t)np, live, peaks);
+        scale_image_planes(ctx, pi, (int64_t)np, live, ones, peaks);
+        scale_image_planes(ctx, ri, (int64_t)np, live, ones, peaks);
         tm.mark();
         std::vector<unsigned int> pk(C);
         CR_CUDA_CHECK(cudaMemcpyAsync(pk.data(), peaks, C * 4, cudaMemcpyDeviceToHost,
@@ -1505,9 +1504,10 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
         std::vector<float> scales;
         for (int c : chosen) scales.push_back(1.0f / states[c].normalization_sumwt);
         grid_to_image_planes(ctx, g, res, nullptr, chosen, scales, img, single);
+        std::vector<float> inv_peaks;
+        for (int c : chosen) inv_peaks.push_back(1.0f / states[c].psf_peak);
+        scale_image_planes(ctx, img, (int64_t)np, chosen, inv_peaks, nullptr);
         for (int c : chosen) {
-            scale_image(ctx, img + (size_t)c * np, (int64_t)np, 1.0f / states[c].psf_peak,
-                        nullptr);
             if (out_location == CR_HOST)
                 copy_out(ctx, residual_images + (size_t)c * np, img + (size_t)c * np, np * 4,
                          CR_HOST);

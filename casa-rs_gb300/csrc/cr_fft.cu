@@ -323,6 +323,35 @@ __global__ void narrow_sign_planes(const W* half, int64_t gnx, int64_t gny, int 
                      grids + (int64_t)pc.plane[b] * gnx * gny);
 }
 
+// abs_peak_kernel / scale_image_kernel over the planes of a chunk
+__global__ void abs_peak_planes_kernel(const float* images, int64_t n, PlaneChunk pc,
+                                       unsigned int* peaks) {
+    const int64_t p = pc.plane[blockIdx.y];
+    const float* img = images + p * n;
+    float m = 0.0f;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        float v = fabsf(img[t]);
+        if (v > m) m = v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(peaks + p, __float_as_uint(m));
+}
+
+__global__ void scale_planes(float* images, int64_t n, PlaneChunk pc, const unsigned int* peaks) {
+    const int64_t p = pc.plane[blockIdx.y];
+    float* img = images + p * n;
+    const float scale = pc.scale[blockIdx.y];
+    const float pk = peaks ? __uint_as_float(peaks[p]) : 1.0f;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        float v = img[t] * scale;
+        if (peaks) v = v / pk;
+        img[t] = v;
+    }
+}
+
 void exec_c2r_many(cr_ctx* ctx, int64_t gnx, int64_t gny, int n, double2* in, double* out) {
     check_cufft(cufftExecZ2D(fft_plan_many(ctx, gnx, gny, CUFFT_Z2D, n),
                              (cufftDoubleComplex*)in, (cufftDoubleReal*)out),
@@ -409,6 +438,33 @@ void image_to_grid_planes_impl(cr_ctx* ctx, cr_gridder* g, const float* models,
 }
 
 }  // namespace
+
+void abs_peak_planes(cr_ctx* ctx, const float* images, int64_t n,
+                     const std::vector<int>& planes, unsigned int* peaks) {
+    for (size_t k0 = 0; k0 < planes.size(); k0 += kPlaneBatch) {
+        const int nb = (int)std::min<size_t>(kPlaneBatch, planes.size() - k0);
+        PlaneChunk pc{};
+        for (int b = 0; b < nb; ++b) pc.plane[b] = planes[k0 + b];
+        abs_peak_planes_kernel<<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0,
+                                 ctx->stream>>>(images, n, pc, peaks);
+        note_launch(ctx, "abs_peak_planes_kernel");
+    }
+}
+
+void scale_image_planes(cr_ctx* ctx, float* images, int64_t n, const std::vector<int>& planes,
+                        const std::vector<float>& scales, const unsigned int* peaks) {
+    for (size_t k0 = 0; k0 < planes.size(); k0 += kPlaneBatch) {
+        const int nb = (int)std::min<size_t>(kPlaneBatch, planes.size() - k0);
+        PlaneChunk pc{};
+        for (int b = 0; b < nb; ++b) {
+            pc.plane[b] = planes[k0 + b];
+            pc.scale[b] = scales[k0 + b];
+        }
+        scale_planes<<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+            images, n, pc, peaks);
+        note_launch(ctx, "scale_planes");
+    }
+}
 
 void grid_to_image_planes(cr_ctx* ctx, cr_gridder* g, const float2* grids,
                           const float* real_grids, const std::vector<int>& planes,

@@ -239,6 +239,13 @@ void grid_to_image_planes(cr_ctx* ctx, cr_gridder* g, const float2* grids,
                           const std::vector<float>& scales, float* images, bool single);
 void image_to_grid_planes(cr_ctx* ctx, cr_gridder* g, const float* models,
                           const std::vector<int>& planes, float2* grids, bool single);
+// abs_peak and scale_image over the listed planes of images [C][n]: peaks
+// indexed by plane; plane k scaled by scales[k] (then divided by its peak
+// when peaks is given).
+void abs_peak_planes(cr_ctx* ctx, const float* images, int64_t n,
+                     const std::vector<int>& planes, unsigned int* peaks);
+void scale_image_planes(cr_ctx* ctx, float* images, int64_t n, const std::vector<int>& planes,
+                        const std::vector<float>& scales, const unsigned int* peaks);
 void grid_to_image_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* grid, float scale,
                            float* image, bool single = false);
 // model image (device) -> centred model grid (device)
