@@ -87,7 +87,9 @@ SIGNATURES = {
     "cr_ctx_synchronize": (C.c_int, [_p, _err]),
     "cr_ctx_last_timings": (C.c_int, [_p, C.POINTER(Timings)]),
     "cr_ctx_launch_count": (_i64, [_p]),
+    "cr_ctx_workspace_bytes": (_i64, [_p]),
     "cr_ctx_set_cube_graphs": (C.c_int, [_p, _i32]),
+    "cr_ctx_set_wait_limits": (C.c_int, [_p, _i64, _i64]),
     "cr_ctx_set_image_fft_precision": (C.c_int, [_p, _i32]),
     "cr_accumulator_create": (C.c_int, [_p, _p, C.POINTER(_p), _err]),
     "cr_accumulator_destroy": (None, [_p]),
@@ -166,6 +168,8 @@ SIGNATURES = {
     "cr_hogbom_plane": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64,
                                   _i32, _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64),
                                   _err]),
+    "cr_robust_rms": (C.c_int, [_p, _p, _p, _i32, _i32, _i32, _i32, _p, _i32, _p, _p, _p,
+                                _err]),
     "cr_hogbom_noalloc": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _f, _f, _f, _f, _i64, _i32,
                                     _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64),
                                     C.POINTER(_i32), _err]),

@@ -8,8 +8,11 @@ than 10 % over its minimum (update_divergence_state, lib.rs:74690-74712),
 and the residual is refreshed from the model through one materialised plan:
 apodise + forward FFT, degrid, residual gridding, inverse FFT, correction
 and the PSF normalisation (the residual refresh of compute_residual,
-lib.rs:68560-68620 / 70592-70644).  The robust-RMS n-sigma threshold of the
-reference is not restated; thresholds are absolute (Jy/beam).
+lib.rs:68560-68620 / 70592-70644).  With CleanConfig.nsigma > 0 the n-sigma
+threshold (nsigma times the robust RMS of the residual, computed on the
+device by cr_robust_rms) joins the stop rules at each cycle start and after
+each refresh, and the minor cycle stops at it, as in the reference
+(lib.rs:59395-59396, 59563-59564).
 """
 from __future__ import annotations
 
@@ -32,6 +35,7 @@ class CleanConfig:
     niter: int
     gain: float = 0.1
     threshold_jy_per_beam: float = 0.0
+    nsigma: float = 0.0
     minor_cycle_length: int = 2000
     cyclefactor: float = 1.0
     min_psf_fraction: float = 0.05
@@ -101,6 +105,7 @@ class CleanResult:
     beam: Optional[im.BeamFit] = None
     restored: object = None
     max_psf_sidelobe: float = 0.0
+    nsigma_thresholds: list = field(default_factory=list)
 
 
 def clean_cycle_threshold(peak: float, max_psf_sidelobe: float, cfg: CleanConfig) -> float:
@@ -174,14 +179,16 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
     stop = None
     min_peak = np.float32(_absmax(residual))
     needs_refresh = False
-    comps, thresholds = [], []
+    comps, thresholds, nsigs = [], [], []
     try:
         while reported < cfg.niter:
             if cfg.major_cycle_limit is not None and major >= cfg.major_cycle_limit:
                 stop = "MajorCycleLimitReached"
                 break
             peak = _absmax(residual)
-            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam)
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma)
+            nsigs.append(nsig)
+            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam, nsig)
             if s is not None:
                 stop = s
                 break
@@ -190,7 +197,8 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
             thresholds.append(thr)
             out = im.run_hogbom_minor_cycle(ctx, model, residual, psf, cfg.gain, cycle_niter,
                                             threshold=cfg.threshold_jy_per_beam,
-                                            cycle_threshold=thr, inclusive=cfg.inclusive)
+                                            cycle_threshold=thr, nsigma_threshold=nsig,
+                                            inclusive=cfg.inclusive)
             model, residual = out.model, out.residual
             comps.extend(zip(map(tuple, out.positions.tolist()), out.fluxes.tolist()))
             actual += out.actual_updates
@@ -219,9 +227,10 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
             residual = plan.residual_image(model, state)
             major += 1
             needs_refresh = False
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma)
             if stop_after is not None:
                 break
-            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam)
+            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam, nsig)
             if s is not None:
                 stop = s
                 break
@@ -233,7 +242,7 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
         plan.close()
     restored = im.restore(gridder.ctx, model, residual, cell, beam) if beam is not None else None
     return CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
-                       thresholds, beam, restored, sidelobe)
+                       thresholds, beam, restored, sidelobe, nsigs)
 
 
 # ----------------------------------------------------------------------------
@@ -507,14 +516,16 @@ def run_clark_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
     actual = reported = major = 0
     stop = None
     min_peak = np.float32(_absmax(residual))
-    comps, thresholds = [], []
+    comps, thresholds, nsigs = [], [], []
     try:
         while reported < cfg.niter:
             if cfg.major_cycle_limit is not None and major >= cfg.major_cycle_limit:
                 stop = "MajorCycleLimitReached"
                 break
             peak = _absmax(residual)
-            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam)
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma)
+            nsigs.append(nsig)
+            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam, nsig)
             if s is not None:
                 stop = s
                 break
@@ -523,7 +534,7 @@ def run_clark_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
             thresholds.append(thr)
             out = im.run_clark_minor_cycle(ctx, model, residual, psf, ncent, cfg.gain, step,
                                            threshold=cfg.threshold_jy_per_beam,
-                                           cycle_threshold=thr)
+                                           cycle_threshold=thr, nsigma_threshold=nsig)
             model, residual = out.model, out.residual
             comps.extend(zip(map(tuple, out.positions.tolist()), out.fluxes.tolist()))
             updated = out.actual_updates > 0
@@ -554,7 +565,8 @@ def run_clark_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
             if stop is None and reported >= cfg.niter:
                 stop = "IterationLimitReached"
                 break
-            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam)
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma)
+            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam, nsig)
             if s is not None:
                 stop = s
                 break
@@ -564,5 +576,5 @@ def run_clark_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
         plan.close()
     restored = im.restore(gridder.ctx, model, residual, cell, beam) if beam is not None else None
     return CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
-                       thresholds, beam, restored, sidelobe)
+                       thresholds, beam, restored, sidelobe, nsigs)
 

@@ -141,6 +141,13 @@ class Context:
         if self._lib.cr_ctx_set_cube_graphs(self._h, 1 if enable else 0) != 0:
             raise ValueError("null context")
 
+    def set_wait_limits(self, barrier_polls: int = -1, mbar_polls: int = -1):
+        """Bounds of the device-side waits (Hogbom grid barrier, cube bulk-copy
+        waits), for tests of the timeout paths; -1 restores a default, 0 gives
+        up at once (the call then raises CasarsCudaError with code CR_TIMEOUT)."""
+        if self._lib.cr_ctx_set_wait_limits(self._h, int(barrier_polls), int(mbar_polls)) != 0:
+            raise ValueError("null context")
+
     def set_image_fft_precision(self, precision):
         """Image-stage FFT precision of the single-plane calls, mirroring
         DirtyProductFftPolicy.precision (casa-imaging/src/lib.rs:1280-1312):
@@ -157,6 +164,11 @@ class Context:
     @property
     def launch_count(self) -> int:
         return int(self._lib.cr_ctx_launch_count(self._h))
+
+    @property
+    def workspace_bytes(self) -> int:
+        """Device workspace bytes the context holds."""
+        return int(self._lib.cr_ctx_workspace_bytes(self._h))
 
     def last_timings(self) -> dict:
         t = _lib.Timings()
@@ -1227,6 +1239,47 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
                                   cpk[o:o + k].copy(), cfl[o:o + k].copy(), k,
                                   int(reported[s]), STOP_REASONS[int(stop[s])]))
     return outs
+
+
+def robust_rms(ctx: Context, images, masks=None, planes=None):
+    """robust_rms_jy_per_beam (lib.rs:74130-74183) on the device (cr_robust_rms).
+
+    images: one image [nx][ny] or a stack [P][nx][ny] (numpy, or torch CUDA);
+    masks: clean masks of the same shape (nonzero = cleanable) or None;
+    planes: the stack's planes to evaluate (all when None).  Returns
+    (rms float32 array, madfm float64 array, counts int64 array), one entry
+    per listed plane (scalars for a single image)."""
+    single = len(images.shape) == 2
+    shape = tuple(images.shape)
+    P = 1 if single else shape[0]
+    nx, ny = shape[-2:]
+    pl = np.arange(P, dtype=np.int32) if planes is None else \
+        np.ascontiguousarray(np.asarray(planes, np.int32))
+    arrs = _Arrays()
+    ip = arrs.ptr(images, np.float32, torch.float32 if torch else None, shape)
+    mp = arrs.ptr(masks, np.uint8, torch.uint8 if torch else None, shape)
+    if arrs.location == CR_DEVICE:
+        ctx.use_torch_stream()
+    else:
+        ctx.use_own_stream()
+    n = len(pl)
+    rms = np.zeros(max(n, 1), np.float32)
+    mad = np.zeros(max(n, 1), np.float64)
+    cnt = np.zeros(max(n, 1), np.int64)
+    call("cr_robust_rms", ctx.handle, ip, mp, P, nx, ny, arrs.location, pl.ctypes.data, n,
+         rms.ctypes.data, mad.ctypes.data, cnt.ctypes.data)
+    if single:
+        return float(rms[0]), float(mad[0]), int(cnt[0])
+    return rms[:n], mad[:n], cnt[:n]
+
+
+def nsigma_threshold(ctx: Context, residual, nsigma: float, mask=None) -> float:
+    """nsigma_threshold_jy_per_beam (lib.rs:74474-74484): nsigma times the
+    robust RMS (float32), 0 when nsigma is not positive."""
+    if not nsigma > 0.0:
+        return 0.0
+    rms = robust_rms(ctx, residual, mask)[0]
+    return float(np.float32(nsigma) * np.float32(rms))
 
 
 def _hogbom_buffers(ctx: Context, model, residual, psf, mask):

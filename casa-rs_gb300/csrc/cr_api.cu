@@ -336,6 +336,10 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
         CR_CUDA_CHECK(cudaSetDevice(device));
         cr_ctx* c = new cr_ctx();
         c->device = device;
+        CR_CUDA_CHECK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+        // commit the allocation-free Hogbom's static scratch on this device
+        // now, so that its calls never load a module (and allocate) later
+        cr::noalloc_prepare(device);
         CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
         c->stream = c->own_stream;
         for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
@@ -394,6 +398,13 @@ int cr_ctx_last_timings(cr_ctx* ctx, cr_timings* out) {
 }
 
 int64_t cr_ctx_launch_count(cr_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int64_t cr_ctx_workspace_bytes(cr_ctx* ctx) {
+    if (!ctx) return -1;
+    int64_t total = 0;
+    for (const auto& kv : ctx->ws) total += (int64_t)kv.second.bytes;
+    return total;
+}
 
 int cr_gridder_create(cr_ctx* ctx, const cr_geometry* geom, double padding, int32_t oversampling,
                       cr_gridder** out, cr_grid_info* info, char** err) {
@@ -1085,6 +1096,28 @@ int cr_hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, cons
     });
 }
 
+int cr_robust_rms(cr_ctx* ctx, const float* images, const uint8_t* masks, int32_t nimages,
+                  int32_t nx, int32_t ny, int32_t location, const int32_t* planes,
+                  int32_t nplanes, float* rms, double* madfm, int64_t* counts, char** err) {
+    return guarded(err, [&] {
+        need(ctx && images, "null argument");
+        need(nx > 0 && ny > 0 && nimages > 0, "image shape must be positive");
+        need(nplanes >= 0 && (nplanes == 0 || planes), "planes must be given");
+        need(location == CR_HOST || location == CR_DEVICE, "bad location");
+        for (int32_t k = 0; k < nplanes; ++k)
+            need(planes[k] >= 0 && planes[k] < nimages, "plane index out of range");
+        bind(ctx);
+        const int64_t npix = (int64_t)nx * ny;
+        need(npix < (1ll << 31), "image larger than 2^31 pixels");
+        const float* im = (const float*)device_input(ctx, images, (size_t)nimages * npix * 4,
+                                                     location, "rms_images");
+        const uint8_t* mk = (const uint8_t*)device_input(ctx, masks, (size_t)nimages * npix,
+                                                         location, "rms_masks");
+        std::vector<int> pl(planes, planes + nplanes);
+        cr::robust_rms(ctx, im, mk, npix, pl, rms, madfm, counts);
+    });
+}
+
 int cr_hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
                     const uint8_t* mask, int32_t nx, int32_t ny, int32_t location, float gain,
                     float threshold, float cycle_threshold, float peak_relative_tolerance,
@@ -1238,6 +1271,15 @@ int cr_psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32
         const float* p = (const float*)device_input(ctx, psf, n * 4, location, "sl_psf");
         *level = psf_sidelobe(ctx, p, nx, ny, cell_x_rad, cell_y_rad, *beam);
     });
+}
+
+int cr_ctx_set_wait_limits(cr_ctx* ctx, int64_t barrier_polls, int64_t mbar_polls) {
+    if (!ctx) return CR_INVALID;
+    ctx->barrier_polls = barrier_polls < 0 ? cr::kBarrierPollsDefault : barrier_polls;
+    ctx->mbar_polls = mbar_polls < 0 ? cr::kMbarPollsDefault : mbar_polls;
+    // captured pipelines hold the kernels' arguments, limits included
+    ctx->cube_graphs.clear();
+    return CR_OK;
 }
 
 int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable) {

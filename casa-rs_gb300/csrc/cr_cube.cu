@@ -640,6 +640,7 @@ struct CubeGridArgs {
     float* psf;                  // [C][gnx][gny] real part of the PSF grid
     float2* dirty;               // [C][gnx][gny] (the residual grid with RESIDUAL)
     const float2* res;           // RESIDUAL: w (vis - pred) per record
+    long long wait_polls;        // bound of the tap-table wait (the drain keeps the default)
 };
 
 // A block per work item: the chunk's records (from the four source bins)
@@ -677,7 +678,7 @@ __global__ void __launch_bounds__(kGridThreads, 6) cube_grid_kernel(CubeGridArgs
         bulk_load(s_taps, a.taps, a.taps_bytes, &s_bar);
     }
     __syncthreads();
-    if (!__syncthreads_and(mbar_wait(&s_bar, 0))) {
+    if (!__syncthreads_and(mbar_wait(&s_bar, 0, a.wait_polls))) {
         if (tid == 0) {
             atomicExch(a.status, CR_TIMEOUT);
             mbar_wait(&s_bar, 0);   // let the copy land before the block exits
@@ -882,6 +883,7 @@ struct CubeDegridArgs {
     const float* rec_w;          // RESIDUAL: imaging weight per record
     float2* res;                 // RESIDUAL: w vis - w pred per record
     int* status;                 // set to CR_TIMEOUT when a bounded wait gives up
+    long long wait_polls;        // bound of the first waits (the drains keep the default)
 };
 
 // Bins in turn.  The block stages the 38 x 38 model footprint of its home
@@ -935,7 +937,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
         }
     }
     __syncthreads();
-    if (!__syncthreads_and(mbar_wait(&s_bar[2], 0))) {
+    if (!__syncthreads_and(mbar_wait(&s_bar[2], 0, a.wait_polls))) {
         if (tid == 0) {
             atomicExch(a.status, CR_TIMEOUT);
             // let this block's copies in flight land before it exits
@@ -964,7 +966,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
         const uint32_t hi = min(a.bin_start[bin + 1], lo + kDegridChunk);
         const float2* sg = &s_g[TMA ? b : 0][0];
         if (TMA) {
-            if (!__syncthreads_and(mbar_wait(&s_bar[b], (phase >> b) & 1u))) {
+            if (!__syncthreads_and(mbar_wait(&s_bar[b], (phase >> b) & 1u, a.wait_polls))) {
                 if (tid == 0) {
                     atomicExch(a.status, CR_TIMEOUT);
                     // let this block's copies in flight land before it exits
@@ -1278,7 +1280,7 @@ static void launch_cube_grid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr, 
     CubeGridArgs a{cr.rec, cr.rec_w, cr.bin_start, cr.cell_end, g->taps_d, g->tap_rows,
                    g->taps_bytes, ctx->status_d, cr.ntx, cr.nty, gi.grid_nx, gi.grid_ny,
                    cr.grid_items, cr.grid_chunk, cr.grid_chunks, cr.n_items, counter, psf,
-                   dirty, res};
+                   dirty, res, ctx->mbar_polls};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int per_sm = 0;
@@ -1334,7 +1336,7 @@ static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr
     const uint32_t taps8_bytes = (uint32_t)g->tap_rows * 32u;
     CubeDegridArgs a{cr.rec, cr.bin_start, g->tap_rows, cr.ntiles, cr.nty, gi.grid_nx,
                      gi.grid_ny, cr.R, cr.degrid_items, cr.n_items + 1, counter, g->taps8_d,
-                     taps8_bytes, grid, pred, cr.rec_w, res, ctx->status_d};
+                     taps8_bytes, grid, pred, cr.rec_w, res, ctx->status_d, ctx->mbar_polls};
     int sms = 0;
     CR_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     // the grids as float32 [C][gnx][2 gny] for footprint boxes of 76 x 38

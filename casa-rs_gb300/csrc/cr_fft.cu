@@ -396,11 +396,11 @@ void grid_to_image_planes_impl(cr_ctx* ctx, cr_gridder* g, const float2* grids,
             pc.plane[b] = planes[k0 + b];
             pc.scale[b] = scales[k0 + b];
         }
-        hermitian_half_planes<W><<<dim3(grid_blocks(nh, 256, 152 * 4), nb), 256, 0,
+        hermitian_half_planes<W><<<dim3(grid_blocks(nh, 256, ctx->sms * 4), nb), 256, 0,
                                    ctx->stream>>>(grids, real_grids, gnx, gny, pc, half);
         note_launch(ctx, "hermitian_half_planes");
         exec_c2r_many(ctx, gnx, gny, nb, half, raw);
-        crop_correct_planes<S><<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+        crop_correct_planes<S><<<dim3(grid_blocks(n, 256, ctx->sms * 4), nb), 256, 0, ctx->stream>>>(
             raw, gnx, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity, inv,
             pc, g->corr_x_d, g->corr_y_d, images);
         note_launch(ctx, "crop_correct_planes");
@@ -426,12 +426,12 @@ void image_to_grid_planes_impl(cr_ctx* ctx, cr_gridder* g, const float* models,
         PlaneChunk pc{};
         for (int b = 0; b < nb; ++b) pc.plane[b] = planes[k0 + b];
         CR_CUDA_CHECK(cudaMemsetAsync(raw, 0, (size_t)gnx * gny * nb * sizeof(S), ctx->stream));
-        apodize_planes<S><<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+        apodize_planes<S><<<dim3(grid_blocks(n, 256, ctx->sms * 4), nb), 256, 0, ctx->stream>>>(
             models, g->geom.nx, g->geom.ny, gnx, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d,
             g->corr_y_d, pc, raw);
         note_launch(ctx, "apodize_planes");
         exec_r2c_many(ctx, gnx, gny, nb, raw, half);
-        narrow_sign_planes<W><<<dim3(grid_blocks(gnx * gny, 256, 152 * 4), nb), 256, 0,
+        narrow_sign_planes<W><<<dim3(grid_blocks(gnx * gny, 256, ctx->sms * 4), nb), 256, 0,
                                 ctx->stream>>>(half, gnx, gny, parity, pc, grids);
         note_launch(ctx, "narrow_sign_planes");
     }
@@ -445,7 +445,7 @@ void abs_peak_planes(cr_ctx* ctx, const float* images, int64_t n,
         const int nb = (int)std::min<size_t>(kPlaneBatch, planes.size() - k0);
         PlaneChunk pc{};
         for (int b = 0; b < nb; ++b) pc.plane[b] = planes[k0 + b];
-        abs_peak_planes_kernel<<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0,
+        abs_peak_planes_kernel<<<dim3(grid_blocks(n, 256, ctx->sms * 4), nb), 256, 0,
                                  ctx->stream>>>(images, n, pc, peaks);
         note_launch(ctx, "abs_peak_planes_kernel");
     }
@@ -460,7 +460,7 @@ void scale_image_planes(cr_ctx* ctx, float* images, int64_t n, const std::vector
             pc.plane[b] = planes[k0 + b];
             pc.scale[b] = scales[k0 + b];
         }
-        scale_planes<<<dim3(grid_blocks(n, 256, 152 * 4), nb), 256, 0, ctx->stream>>>(
+        scale_planes<<<dim3(grid_blocks(n, 256, ctx->sms * 4), nb), 256, 0, ctx->stream>>>(
             images, n, pc, peaks);
         note_launch(ctx, "scale_planes");
     }

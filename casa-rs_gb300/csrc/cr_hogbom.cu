@@ -28,7 +28,6 @@ namespace cr {
 namespace {
 
 constexpr int kHogThreads = 512;
-constexpr long long kBarrierSpinLimit = 1ll << 24;  // x ~64 ns sleeps: about a second
 
 struct Cand {
     float absval;  // -1 when the block has no cleanable pixel
@@ -58,6 +57,9 @@ struct HogArgs {
     // finite values only, stop when |peak| <= threshold or <= the cycle
     // threshold, no nsigma rule
     int plane_rules;
+    // polls of a grid-barrier wait before it gives up (each poll sleeps
+    // ~64 ns); set from the context by every launch
+    long long barrier_polls;
 };
 
 __device__ __forceinline__ bool better(float a_abs, int a_key, float b_abs, int b_key) {
@@ -99,8 +101,10 @@ __device__ Cand block_argmax(float a, int k, float v) {
 }
 
 // Bounded grid barrier (all blocks are co-resident under the cooperative
-// launch).  Returns false on every thread of a block whose wait timed out.
-__device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks) {
+// launch).  A waiting block polls the generation word at most `polls` times
+// after its first look.  Returns false on every thread of a block whose
+// wait timed out.
+__device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks, long long polls) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -116,7 +120,7 @@ __device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks) {
         } else {
             long long spins = 0;
             while (*gen == g) {
-                if (++spins > kBarrierSpinLimit) {
+                if (++spins > polls) {
                     ok = 0;
                     break;
                 }
@@ -175,7 +179,7 @@ __device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
         Cand c = block_argmax(ba, bk, bv);
         if (threadIdx.x == 0) a.cands[bidx] = c;
     }
-    if (!grid_barrier(a.bar, (unsigned)nblocks)) {
+    if (!grid_barrier(a.bar, (unsigned)nblocks, a.barrier_polls)) {
         if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
         return;
     }
@@ -266,7 +270,7 @@ __device__ void hogbom_body(const HogArgs& a, int nblocks, int bidx) {
         }
         Cand c = block_argmax(ba, bk, bv);
         if (threadIdx.x == 0) nxt[bidx] = c;
-        if (!grid_barrier(a.bar, (unsigned)nblocks)) {
+        if (!grid_barrier(a.bar, (unsigned)nblocks, a.barrier_polls)) {
             if (threadIdx.x == 0) atomicExch(a.out_status, CR_TIMEOUT);
             return;
         }
@@ -463,7 +467,7 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
     CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, 256, ctx->stream));
     HogArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
               nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual, out_stop,
-              out_status, plane_rules};
+              out_status, plane_rules, ctx->barrier_polls};
     void* args[] = {&a};
     CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_kernel, dim3(blocks), dim3(kHogThreads),
                                               args, 0, ctx->stream));
@@ -476,10 +480,12 @@ void hogbom(cr_ctx* ctx, float* model, float* residual, const float* psf, const 
     CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     if (h.status) fail(CR_TIMEOUT, "Hogbom grid barrier timed out");
     if (comp_x && h.actual > 0) {
-        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        const size_t nb = (size_t)h.actual * 4;
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_x, cx, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_y, cy, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_peak, cp, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_flux, cf, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     }
     if (actual) *actual = h.actual;
     if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
@@ -581,7 +587,7 @@ void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
         HogPlanesArgs pa;
         pa.base = HogArgs{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
                           nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual,
-                          out_stop, out_status};
+                          out_stop, out_status, 0, ctx->barrier_polls};
         pa.planes = plist;
         pa.per_plane = per_plane;
         pa.comp_cap = cap;
@@ -658,7 +664,9 @@ std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array for the current device, looked up once
-// per device (the caller has made `device` current).
+// per device (the caller has made `device` current).  cr_ctx_create does the
+// lookup, so the module holding the array (and the array's memory) is
+// loaded when a context is created, not during a later call.
 void* scratch_address(int device) {
     if (device < 0 || device >= kMaxDevices) fail(CR_INVALID, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -708,7 +716,7 @@ void hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf
     CR_CUDA_CHECK(cudaMemsetAsync(base, 0, kNoAllocHeader, ctx->stream));
     HogArgs a{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
               nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual, out_stop,
-              out_status};
+              out_status, 0, ctx->barrier_polls};
     void* args[] = {&a};
     CR_CUDA_CHECK(cudaLaunchCooperativeKernel((void*)hogbom_kernel, dim3(blocks), dim3(kHogThreads),
                                               args, 0, ctx->stream));
@@ -721,10 +729,12 @@ void hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf
     CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     if (h.status) fail(CR_TIMEOUT, "Hogbom grid barrier timed out");
     if (comp_x && h.actual > 0) {
-        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)h.actual * 4, cudaMemcpyDeviceToHost));
+        const size_t nb = (size_t)h.actual * 4;
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_x, cx, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_y, cy, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_peak, cp, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_flux, cf, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     }
     if (actual) *actual = h.actual;
     if (reported) *reported = std::min<int64_t>(h.actual, cycle_niter);
@@ -732,6 +742,9 @@ void hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf
 }
 
 }  // namespace
+
+void noalloc_prepare(int device) { scratch_address(device); }
+
 }  // namespace cr
 
 extern "C" int cr_hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf,

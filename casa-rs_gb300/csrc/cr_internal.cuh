@@ -38,12 +38,19 @@ using Pool = std::map<std::string, DevBuf>;
 
 struct CubeGraph;   // a captured cube pipeline (cr_cube.cu)
 
+// Default bounds of the device-side waits: polls of a grid barrier (each
+// followed by a 64 ns sleep: about a second) and of an mbarrier (try_wait
+// polls: milliseconds).  cr_ctx_set_wait_limits lowers them for tests.
+constexpr long long kBarrierPollsDefault = 1ll << 24;
+constexpr long long kMbarPollsDefault = 1ll << 22;
+
 }  // namespace cr
 
 // A context: one device, one stream, grow-only device workspaces, cached
 // cuFFT plans and a launch counter.
 struct cr_ctx {
     int device = 0;
+    int sms = 0;           // multiprocessors of the device (grid sizing)
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     cr::Pool ws;
@@ -77,6 +84,11 @@ struct cr_ctx {
     // gives up; read after the stream synchronises
     int* status_h = nullptr;
     int* status_d = nullptr;
+    // bounds of the first wait of a grid barrier (Hogbom) and of a
+    // bulk-copy mbarrier (cube kernels); the drain waits after a timeout
+    // keep the defaults
+    long long barrier_polls = cr::kBarrierPollsDefault;
+    long long mbar_polls = cr::kMbarPollsDefault;
 };
 
 // Standard (PSWF) gridder state.
@@ -119,6 +131,9 @@ namespace cr {
 
 // ---- context helpers -------------------------------------------------------
 void* workspace(cr_ctx* ctx, const std::string& name, size_t bytes);
+// Looks up the allocation-free Hogbom's static scratch on `device` (which the
+// caller has made current), loading the module that holds it.
+void noalloc_prepare(int device);
 // the same from another pool (stream-ordered on ctx's stream)
 void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes);
 void pool_free(cr_ctx* ctx, Pool& pool);
@@ -223,6 +238,13 @@ void std_grid(cr_ctx* ctx, cr_gridder* g, const Records& r, float2* psf, float2*
               int mode);
 void std_degrid(cr_ctx* ctx, cr_gridder* g, const Records& r, const float2* grid);
 void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
+
+// ---- robust RMS (n-sigma threshold) ----------------------------------------------
+// robust_rms_jy_per_beam of the listed planes of device images [P][npix]
+// (masks [P][npix] or null); rms / madfm / counts per listed plane (host).
+void robust_rms(cr_ctx* ctx, const float* images, const uint8_t* masks, int64_t npix,
+                const std::vector<int>& planes, float* rms, double* madfm, int64_t* counts);
+double chauvenet_max_zscore(uint64_t npts);
 
 // ---- FFT stage -------------------------------------------------------------------
 // grid (device, modified in place) -> image * scale (device)

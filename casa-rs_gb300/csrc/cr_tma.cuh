@@ -15,7 +15,7 @@
 
 namespace cr {
 
-constexpr long long kMbarSpinLimit = 1ll << 22;
+constexpr long long kMbarSpinLimit = 1ll << 22;   // equals kMbarPollsDefault
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -51,11 +51,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// true once the phase with this parity has completed; false after the limit
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (long long i = 0; i < kMbarSpinLimit; ++i)
+// true once the phase with this parity has completed; false after `limit`
+// unsuccessful polls (0: give up without polling)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    return mbar_wait(bar, parity, kMbarSpinLimit);
 }
 
 // bytes from global src to shared dst (both 16-byte aligned, bytes % 16 == 0)

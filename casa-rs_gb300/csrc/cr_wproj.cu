@@ -663,7 +663,7 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
     for (int32_t p0 = 0; p0 < planes; p0 += batch) {
         int nb = std::min<int32_t>(batch, planes - p0);
         CR_CUDA_CHECK(cudaMemsetAsync(buf, 0, plane_bytes * nb, ctx->stream));
-        screen_kernel<<<grid_blocks(inner * inner * nb, 256, 152 * 64), 256, 0, ctx->stream>>>(
+        screen_kernel<<<grid_blocks(inner * inner * nb, 256, (int64_t)ctx->sms * 64), 256, 0, ctx->stream>>>(
             buf, conv, inner, nb, p0, planes, w_scale, s0, s1, corr_d);
         note_launch(ctx, "screen_kernel");
         // cufftExecC2C on a plan of `batch` transforms; a short final batch

@@ -171,6 +171,19 @@ int cr_ctx_synchronize(cr_ctx* ctx, char** err);
 int cr_ctx_last_timings(cr_ctx* ctx, cr_timings* out);
 /* Number of this library's kernel launches since the context was created. */
 int64_t cr_ctx_launch_count(cr_ctx* ctx);
+/* Bytes of device workspace the context holds (its grow-only buffers). */
+int64_t cr_ctx_workspace_bytes(cr_ctx* ctx);
+/* Bounds of the device-side waits, for tests of the timeout paths.  The
+ * reference has no device waits; its counterpart is the error taxonomy of
+ * ImagingError (crates/casa-imaging/src/error.rs:7-24).  barrier_polls bounds
+ * each wait of the Hogbom grid barrier (polls ~64 ns apart; default 2^24,
+ * about a second), mbar_polls the first wait on each bulk copy of the cube
+ * kernels (default 2^22 polls).  0 gives up at once: a call whose wait gives
+ * up returns CR_TIMEOUT and leaves its outputs undefined; the context stays
+ * usable.  A negative value restores the default.  Waits that let a block's
+ * copies in flight land after a timeout always keep the default bound.
+ * Changing a limit retires the context's captured cube pipelines. */
+int cr_ctx_set_wait_limits(cr_ctx* ctx, int64_t barrier_polls, int64_t mbar_polls);
 /* Precision of the image-stage FFTs (grid correction, fftshift, 2-D FFT) of
  * the single-plane calls: 0 (Auto) or 64 = FP64, the default; 32 = FP32.
  * Replaces the precision field of DirtyProductFftPolicy
@@ -538,6 +551,25 @@ int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const
              int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
              int64_t* actual, int32_t* stop_reason, float* max_exterior_abs, char** err);
 
+/* Robust RMS of residual images for the n-sigma threshold:
+ * robust_rms_jy_per_beam (crates/casa-imaging/src/lib.rs:74130-74183), the
+ * threshold being nsigma * rms (nsigma_threshold_jy_per_beam,
+ * lib.rs:74474-74484).  images [nimages][nx][ny] float32 and optional clean
+ * masks [nimages][nx][ny] (nonzero = cleanable) at `location`; for each of
+ * the nplanes listed planes (host array of image indices):
+ *   values = the finite pixels (only those outside the clean mask when the
+ *            plane's mask is not all true), Chauvenet-clipped (automatic z,
+ *            at most 5 iterations, lib.rs:74512-74622) when not restricted
+ *            by a mask;
+ *   rms[k] = f32(MADFM(values)) * 1.4826f, 0 when no value remains.
+ * Optional host outputs: madfm[k] (FP64) and counts[k] (values the MADFM was
+ * taken over).  The MADFM is an exact selection (bit-identical to sorting);
+ * the clipping windows come from FP64 sums in another order than the
+ * reference's sequential sums. */
+int cr_robust_rms(cr_ctx* ctx, const float* images, const uint8_t* masks, int32_t nimages,
+                  int32_t nx, int32_t ny, int32_t location, const int32_t* planes,
+                  int32_t nplanes, float* rms, double* madfm, int64_t* counts, char** err);
+
 /* ---- allocation-free Hogbom minor cycle ----------------------------------
  * No counterpart in the reference.  The same minor cycle as cr_hogbom for
  * callers that may not allocate device memory once they run: for example a
@@ -553,11 +585,15 @@ int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const
  * list) is one fixed 295,168-byte array in the library's device memory, which
  * every GPU that loads the library holds until the process exits.  Limit:
  * at most 16384 components per call (cycle_niter, plus one when inclusive);
- * a larger budget is rejected with CR_INVALID.  The first call on a device
- * looks up the array's device address (once per device, with that device
- * current); make that first call before any stream capture.  Every call on
- * a device shares the one array: calls that overlap on the GPU (other
- * streams, contexts or threads) race and must be serialised by the caller. */
+ * a larger budget is rejected with CR_INVALID.  The array's memory is
+ * committed when a context is created on the device: cr_ctx_create looks up
+ * its device address (once per device, with that device current), which
+ * loads the module that holds it, so this call does no set-up of its own;
+ * create the context before any stream capture.  Every call on a device
+ * shares the one array: calls that overlap on the GPU (other streams,
+ * contexts or threads) race and must be serialised by the caller.  Like the
+ * library's other calls, it makes the context's device current
+ * (cudaSetDevice) and leaves it current. */
 int cr_hogbom_noalloc(cr_ctx* ctx, float* model, float* residual, const float* psf,
                       const uint8_t* mask, int32_t nx, int32_t ny, float gain, float threshold,
                       float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,

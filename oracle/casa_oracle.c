@@ -1393,3 +1393,156 @@ int64_t oc_hogbom(float* model, float* residual, const float* psf, const uint8_t
     *reported = updates < cycle_niter ? updates : cycle_niter;
     return updates;
 }
+
+/* ------------------------------------------------------------------------ */
+/* robust RMS for the n-sigma threshold                                      */
+/* ------------------------------------------------------------------------ */
+/* mean_stddev (lib.rs:74560-74576): sequential FP64 sums, sample variance. */
+void oc_mean_stddev(const float* v, int64_t n, double* mean_out, double* std_out) {
+    double nn = (double)n;
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += (double)v[i];
+    double mean = s / nn;
+    double sq = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        double d = (double)v[i] - mean;
+        sq += d * d;
+    }
+    double var = n > 1 ? sq / (nn - 1.0) : 0.0;
+    *mean_out = mean;
+    *std_out = sqrt(var);
+}
+
+/* `(0.5 / erfc(z / sqrt 2)) as u64` (lib.rs:74624-74626) with Rust's
+ * saturating float-to-integer cast. */
+static uint64_t oc_chauvenet_npts(double z) {
+    double x = 0.5 / erfc(z / 1.4142135623730951);
+    if (!(x >= 0.0)) return 0;               /* NaN or negative */
+    if (x >= 18446744073709551615.0) return UINT64_MAX;
+    return (uint64_t)x;
+}
+
+/* chauvenet_max_zscore (lib.rs:74578-74622). */
+double oc_chauvenet_max_zscore(uint64_t npts) {
+    static const uint64_t cnt[14] = {0, 1, 3, 10, 40, 185, 1074, 7893, 73579, 872138,
+                                     13165126ull, 253398672ull, 6225098696ull,
+                                     195341107722ull};
+    static const double zs[14] = {0.5, 1.0, 1.5, 2.0, 2.5, 3.0, 3.5,
+                                  4.0, 4.5, 5.0, 5.5, 6.0, 6.5, 7.0};
+    const int L = 14;
+    for (int i = 0; i < L; ++i)
+        if (cnt[i] == npts) return zs[i];
+    int lo = 0, hi = 1;
+    if (npts > cnt[L - 1]) {
+        double z = zs[L - 1] + 0.5;
+        for (;;) {
+            if (oc_chauvenet_npts(z) >= npts) {
+                lo = L - 2;
+                hi = L - 1;
+                break;
+            }
+            z += 0.5;
+        }
+    } else {
+        while (hi < L && cnt[hi] < npts) {
+            ++lo;
+            ++hi;
+        }
+    }
+    double low_z = zs[lo], high_z = zs[hi];
+    double z = (low_z + high_z) / 2.0;
+    for (;;) {
+        uint64_t m = oc_chauvenet_npts(z);
+        if (m == npts || fabs(high_z - low_z) <= 1e-12) return z;
+        if (m > npts)
+            high_z = z;
+        else
+            low_z = z;
+        z = (low_z + high_z) / 2.0;
+    }
+}
+
+/* apply_chauvenet_clipping (lib.rs:74512-74558): values are compacted in
+ * place keeping their order; returns the new count. */
+int64_t oc_chauvenet_clip(float* v, int64_t n, double zscore, int32_t max_iterations) {
+    if (n == 0) return 0;
+    uint64_t max_i = max_iterations >= 0 ? (uint64_t)max_iterations : 1000u;
+    int64_t prev = 0;
+    uint64_t it = 0;
+    while (it <= max_i && n > 0) {
+        int64_t cur = n;
+        if (it > 0 && cur == prev) break;
+        double mean, sd;
+        oc_mean_stddev(v, n, &mean, &sd);
+        if (!isfinite(mean) || !isfinite(sd) || sd <= 0.0) break;
+        double z = zscore >= 0.0 ? zscore : oc_chauvenet_max_zscore((uint64_t)cur);
+        double low = mean - z * sd, high = mean + z * sd;
+        int64_t k = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            double x = (double)v[i];
+            if (x >= low && x <= high) v[k++] = v[i];
+        }
+        n = k;
+        prev = cur;
+        ++it;
+    }
+    return n;
+}
+
+static int oc_cmp_f64(const void* a, const void* b) {
+    double x = *(const double*)a, y = *(const double*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* casacore_median / casacore_madfm (casa-lattices statistics.rs:1346-1379)
+ * over FP64 copies of the values; sorts `w` (n doubles) in place. */
+static double oc_sorted_median(double* w, int64_t n) {
+    qsort(w, (size_t)n, sizeof(double), oc_cmp_f64);
+    int64_t n2 = (n - 1) / 2;
+    return (n % 2 == 0) ? (w[n2] + w[n2 + 1]) / 2.0 : w[n2];
+}
+
+double oc_madfm(const float* v, int64_t n, double* median_out) {
+    if (n <= 0) {
+        if (median_out) *median_out = 0.0;
+        return 0.0;
+    }
+    double* w = (double*)malloc((size_t)n * sizeof(double));
+    for (int64_t i = 0; i < n; ++i) w[i] = (double)v[i];
+    double med = oc_sorted_median(w, n);
+    for (int64_t i = 0; i < n; ++i) w[i] = fabs((double)v[i] - med);
+    double mad = oc_sorted_median(w, n);
+    free(w);
+    if (median_out) *median_out = med;
+    return mad;
+}
+
+/* robust_rms_jy_per_beam (lib.rs:74130-74183), the default (sorted MADFM)
+ * path: the finite values (all of them when the mask is absent or all true;
+ * else those outside the clean mask), Chauvenet clipping (automatic z, at
+ * most 5 iterations) for the full mask only, then f32(madfm) * 1.4826f. */
+float oc_robust_rms(const float* residual, const uint8_t* mask, int64_t n, double* madfm_out,
+                    int64_t* count_out) {
+    int full = 1;
+    if (mask)
+        for (int64_t i = 0; i < n; ++i)
+            if (!mask[i]) {
+                full = 0;
+                break;
+            }
+    float* vals = (float*)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
+    int64_t m = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        float x = residual[i];
+        if (!isfinite(x)) continue;
+        if (!full && mask[i]) continue;
+        vals[m++] = x;
+    }
+    if (m > 0 && full) m = oc_chauvenet_clip(vals, m, -1.0, 5);
+    double mad = m > 0 ? oc_madfm(vals, m, NULL) : 0.0;
+    free(vals);
+    if (madfm_out) *madfm_out = mad;
+    if (count_out) *count_out = m;
+    if (m == 0) return 0.0f;
+    return (float)mad * 1.4826f;
+}

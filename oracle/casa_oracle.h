@@ -153,6 +153,14 @@ int64_t oc_hogbom_plane(float* model, float* residual, const float* psf, const u
 void oc_subtract_shifted_psf(float* residual, const float* psf, int64_t nx, int64_t ny,
                              int64_t px, int64_t py, float component);
 
+/* robust RMS of the n-sigma threshold (lib.rs:74130-74626) */
+void oc_mean_stddev(const float* v, int64_t n, double* mean_out, double* std_out);
+double oc_chauvenet_max_zscore(uint64_t npts);
+int64_t oc_chauvenet_clip(float* v, int64_t n, double zscore, int32_t max_iterations);
+double oc_madfm(const float* v, int64_t n, double* median_out);
+float oc_robust_rms(const float* residual, const uint8_t* mask, int64_t n, double* madfm_out,
+                    int64_t* count_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,6 +109,11 @@ def _declare(L):
                                        C.POINTER(_i64), C.POINTER(_f)]),
         "oc_hogbom_plane": (_i64, [_p, _p, _p, _p, _i64, _i64, _f, _f, _f, _f, _i64, C.c_int,
                                    _p, _p, _p, _p, C.POINTER(_i64)]),
+        "oc_mean_stddev": (None, [_p, _i64, C.POINTER(_d), C.POINTER(_d)]),
+        "oc_chauvenet_max_zscore": (_d, [C.c_uint64]),
+        "oc_chauvenet_clip": (_i64, [_p, _i64, _d, _i32]),
+        "oc_madfm": (_d, [_p, _i64, C.POINTER(_d)]),
+        "oc_robust_rms": (_f, [_p, _p, _i64, C.POINTER(_d), C.POINTER(_i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -581,6 +586,54 @@ def hogbom_plane(residual, psf, gain, cycle_limit, cycle_threshold, tol, thresho
                 actual=int(n), reported=int(reported.value))
 
 
+# --------------------------------------------------------------------------
+# robust RMS and the n-sigma threshold
+# --------------------------------------------------------------------------
+def mean_stddev(values):
+    """mean_stddev (lib.rs:74560-74576): sequential FP64 sums, sample variance."""
+    v = _c(values, np.float32)
+    m, s = _d(), _d()
+    lib().oc_mean_stddev(_ptr(v), len(v), C.byref(m), C.byref(s))
+    return float(m.value), float(s.value)
+
+
+def chauvenet_max_zscore(npts: int) -> float:
+    """chauvenet_max_zscore (lib.rs:74578-74622)."""
+    return float(lib().oc_chauvenet_max_zscore(int(npts)))
+
+
+def chauvenet_clip(values, zscore: float, max_iterations: int) -> np.ndarray:
+    """apply_chauvenet_clipping (lib.rs:74512-74558): the kept values, in order."""
+    v = np.array(values, np.float32, copy=True)
+    n = lib().oc_chauvenet_clip(_ptr(v), len(v), float(zscore), int(max_iterations))
+    return v[:n]
+
+
+def madfm(values):
+    """casacore madfm (casa-lattices statistics.rs:1367-1379): (median, madfm)."""
+    v = _c(values, np.float32)
+    med = _d()
+    mad = lib().oc_madfm(_ptr(v), len(v), C.byref(med))
+    return float(med.value), float(mad)
+
+
+def robust_rms(residual, mask=None):
+    """robust_rms_jy_per_beam (lib.rs:74130-74183): returns (rms float32,
+    madfm FP64, number of values it was taken over)."""
+    r = _c(residual, np.float32).reshape(-1)
+    mk = None if mask is None else _c(np.asarray(mask, np.uint8), np.uint8).reshape(-1)
+    mad, cnt = _d(), _i64()
+    rms = lib().oc_robust_rms(_ptr(r), _ptr(mk), len(r), C.byref(mad), C.byref(cnt))
+    return float(np.float32(rms)), float(mad.value), int(cnt.value)
+
+
+def nsigma_threshold(residual, nsigma: float, mask=None) -> float:
+    """nsigma_threshold_jy_per_beam (lib.rs:74474-74484), float32."""
+    if not nsigma > 0.0:
+        return 0.0
+    return float(np.float32(nsigma) * np.float32(robust_rms(residual, mask)[0]))
+
+
 def radians_from_arcsec(a: float) -> float:
     return a / 3600.0 * math.pi / 180.0
 
@@ -622,9 +675,11 @@ _STOP_NAMES = {0: None, 1: "GlobalThresholdReached", 2: "CycleThresholdReached",
 def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000,
                   cyclefactor=1.0, min_psf_fraction=0.05, max_psf_fraction=0.8,
                   major_cycle_limit=None, sidelobe=0.0, inclusive=True, model=None,
-                  cycle_threshold_override=None):
-    """run_hogbom_cotton_schwab (lib.rs:59354-59636) without mask and n-sigma
-    threshold.  `refresh(model) -> residual` is the measured major cycle.
+                  cycle_threshold_override=None, nsigma=0.0):
+    """run_hogbom_cotton_schwab (lib.rs:59354-59636) without mask; `nsigma`
+    > 0 adds the robust-RMS threshold nsigma_threshold_jy_per_beam at each
+    cycle start and after each refresh (lib.rs:59395-59396, 59563-59564).
+    `refresh(model) -> residual` is the measured major cycle.
     `model` continues from an earlier model; `cycle_threshold_override`
     replaces the per-cycle threshold (the cube-wide threshold of
     run_standard_mfs_cube_clean).  Returns a dict with model, residual,
@@ -637,7 +692,7 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
     stop = None
     min_peak = f32(np.max(np.abs(res)))
     needs_refresh = False
-    comps, thresholds = [], []
+    comps, thresholds, nsig_thresholds = [], [], []
     while reported < niter:
         if major_cycle_limit is not None and major >= major_cycle_limit:
             stop = "MajorCycleLimitReached"
@@ -647,7 +702,9 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
             stop = "NoCleanablePixels"
             break
         peak = abs(pk[1])
-        s = tolerant_clean_stop_reason(peak, threshold, 0.0)
+        nsig = nsigma_threshold(res, nsigma)
+        nsig_thresholds.append(nsig)
+        s = tolerant_clean_stop_reason(peak, threshold, nsig)
         if s is not None:
             stop = s
             break
@@ -658,7 +715,7 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
             thr = float(cycle_threshold_override)
         thresholds.append(thr)
         out = hogbom(res, psf, gain, cyc_niter, threshold=threshold, cycle_threshold=thr,
-                     model=model, inclusive=inclusive)
+                     nsigma_threshold=nsig, model=model, inclusive=inclusive)
         model, res = out["model"], out["residual"]
         comps.extend(zip(zip(out["x"].tolist(), out["y"].tolist()), out["flux"].tolist()))
         actual += out["actual"]
@@ -689,9 +746,10 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
         res = np.asarray(refresh(model), np.float32)
         major += 1
         needs_refresh = False
+        nsig = nsigma_threshold(res, nsigma)
         if stop_after is not None:
             break
-        s = tolerant_clean_stop_reason(f32(np.max(np.abs(res))), threshold, 0.0)
+        s = tolerant_clean_stop_reason(f32(np.max(np.abs(res))), threshold, nsig)
         if s is not None:
             stop = s
             break
@@ -700,7 +758,8 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
     if needs_refresh:
         res = np.asarray(refresh(model), np.float32)
     return dict(model=model, residual=res, major_cycles=major, actual=actual, reported=reported,
-                stop_reason=stop, thresholds=thresholds, components=comps)
+                stop_reason=stop, thresholds=thresholds, components=comps,
+                nsigma_thresholds=nsig_thresholds)
 
 
 def cube_clean(planes, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000, cyclefactor=1.0,

@@ -1,10 +1,11 @@
 """Confirm that every known-answer value in reference_kats.json is literally
 present in the reference test lines it cites.
 
-Run in a container that has the casa-rs sources at /root/reference:
-    python tests/golden/check_reference_citations.py [/root/reference]
+Run where a casa-rs checkout is available, giving its root as the argument
+or in the CASA_RS_ROOT environment variable:
+    python tests/golden/check_reference_citations.py <casa-rs root>
 It prints one line per KAT and exits non-zero if a literal is missing.  The
-GPU machines do not carry the reference; the unit tests only load the JSON.
+unit tests only load the JSON and need no checkout.
 """
 from __future__ import annotations
 
@@ -32,4 +33,7 @@ def main(root: str) -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CASA_RS_ROOT")
+    if not root:
+        sys.exit("usage: check_reference_citations.py <casa-rs root> (or set CASA_RS_ROOT)")
+    sys.exit(main(root))

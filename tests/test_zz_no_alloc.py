@@ -7,7 +7,9 @@ array in the library's device memory, shared by every call on the device.
 This test runs it twice in a row on different inputs and checks each call
 against the ordinary entry point, cr_hogbom, bit for bit (the Hogbom path's
 tolerance): a second call must not see the first call's barrier, candidates
-or components.  It also checks that a budget beyond the fixed scratch is
+or components.  It also checks that a call leaves both the context's
+workspaces and the device's free memory unchanged, that a budget of exactly
+16384 components (the scratch's limit) runs, and that a budget beyond it is
 rejected.  The file sorts last so that a run stopping at the first failure
 has already run every other test.
 """
@@ -88,5 +90,61 @@ def test_noalloc_rejects_budget_beyond_its_scratch():
         with pytest.raises(cc.CasarsCudaError) as e:
             _run(ctx, "cr_hogbom_noalloc", res, psf, mask, 16384)
         assert e.value.kind == "InvalidRequest" and "16384" in str(e.value)
+    finally:
+        ctx.close()
+
+
+def test_noalloc_allocates_nothing():
+    """A fresh context holds no workspace; a call through the C ABI with all
+    buffers already in place leaves the context's workspaces empty and the
+    device's free memory (cudaMemGetInfo) unchanged."""
+    ctx = cc.Context(0)
+    try:
+        res, psf, mask = _inputs(8, (128, 128))
+        nx, ny = res.shape
+        dev = torch.device("cuda", 0)
+        model_t = torch.zeros((nx, ny), dtype=torch.float32, device=dev)
+        res_t = torch.as_tensor(res, device=dev).clone()
+        psf_t = torch.as_tensor(psf, device=dev)
+        mask_t = torch.as_tensor(mask, device=dev)
+        cap = 301
+        cx, cy = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+        cp, cf = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+        actual, reported, stop = C.c_int64(), C.c_int64(), C.c_int32()
+        ctx.use_own_stream()
+        torch.cuda.synchronize()
+
+        def call():
+            _lib.call("cr_hogbom_noalloc", ctx.handle, model_t.data_ptr(), res_t.data_ptr(),
+                      psf_t.data_ptr(), mask_t.data_ptr(), nx, ny, 0.1, 0.0, 0.0, 0.0, 300, 1,
+                      cx.ctypes.data, cy.ctypes.data, cp.ctypes.data, cf.ctypes.data,
+                      C.byref(actual), C.byref(reported), C.byref(stop))
+            ctx.synchronize()
+
+        assert ctx.workspace_bytes == 0
+        free0, _ = torch.cuda.mem_get_info(0)
+        call()
+        free1, _ = torch.cuda.mem_get_info(0)
+        call()
+        free2, _ = torch.cuda.mem_get_info(0)
+        assert actual.value == 301
+        assert ctx.workspace_bytes == 0
+        assert free0 == free1 == free2
+    finally:
+        ctx.close()
+
+
+def test_noalloc_runs_a_budget_of_exactly_its_limit():
+    """cycle_niter 16383 with the inclusive budget: 16384 components, the
+    scratch's capacity, bit-identical to cr_hogbom."""
+    ctx = cc.Context(0)
+    try:
+        res, psf, mask = _inputs(9, (48, 40))
+        ref = _run(ctx, "cr_hogbom", res, psf, mask, 16383, threshold=0.0)
+        got = _run(ctx, "cr_hogbom_noalloc", res, psf, mask, 16383, threshold=0.0)
+        assert got["actual"] == ref["actual"] == 16384
+        assert got["reported"] == ref["reported"] == 16383
+        for key in ("x", "y", "peak", "flux", "model", "residual"):
+            np.testing.assert_array_equal(got[key], ref[key])
     finally:
         ctx.close()
