@@ -90,6 +90,7 @@ SIGNATURES = {
     "cr_ctx_workspace_bytes": (_i64, [_p]),
     "cr_ctx_set_cube_graphs": (C.c_int, [_p, _i32]),
     "cr_ctx_set_wait_limits": (C.c_int, [_p, _i64, _i64]),
+    "cr_ctx_set_cube_grid_chunk": (C.c_int, [_p, _i32]),
     "cr_ctx_set_image_fft_precision": (C.c_int, [_p, _i32]),
     "cr_accumulator_create": (C.c_int, [_p, _p, C.POINTER(_p), _err]),
     "cr_accumulator_destroy": (None, [_p]),
@@ -99,7 +100,7 @@ SIGNATURES = {
     "cr_clark": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _i32, _f, _f, _f, _f, _i64, _p,
                            _p, _p, _p, C.POINTER(_i64), C.POINTER(_i32), C.POINTER(_f), _err]),
     "cr_hogbom_planes": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _p, _i32, _f, _f, _f,
-                                   _f, _i64, _i32, _p, _p, _p, _p, _p, _p, _p, _err]),
+                                   _f, _p, _i64, _i32, _p, _p, _p, _p, _p, _p, _p, _err]),
     "cr_gridder_create": (C.c_int, [_p, C.POINTER(Geometry), _d, _i32, C.POINTER(_p),
                                     C.POINTER(GridInfo), _err]),
     "cr_gridder_destroy": (None, [_p]),

@@ -282,7 +282,7 @@ def _f32max(values) -> np.float32:
 
 
 def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom, refresh,
-                    hogbom_many=None):
+                    hogbom_many=None, nsigma_fn=None):
     """The control of run_standard_mfs_cube_clean (lib.rs:3026-3210).
 
     Planes advance in ascending order; per synchronized pass every plane whose
@@ -296,15 +296,28 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
     minor cycles gives the same residuals as refreshing each in turn.
 
     residuals / models / psfs are indexable by plane (arrays [C][nx][ny]);
-    hogbom(model, residual, psf, niter, threshold, cycle_threshold) returns a
-    HogbomOutcome-like object; refresh(planes) recomputes residuals[c] for
-    the listed planes from models[c] in place.  hogbom_many(planes, niter,
-    threshold, cycle_threshold), when given, runs the listed planes' minor
-    cycles together (in place; outcomes in list order) -- the planes are
-    independent, so this equals running them in turn.  Returns a dict of the
-    loop's results."""
+    hogbom(model, residual, psf, niter, threshold, cycle_threshold,
+    nsigma_threshold) returns a HogbomOutcome-like object; refresh(planes)
+    recomputes residuals[c] for the listed planes from models[c] in place.
+    hogbom_many(planes, niter, threshold, cycle_threshold, nsigma_thresholds),
+    when given, runs the listed planes' minor cycles together (in place;
+    outcomes in list order) -- the planes are independent, so this equals
+    running them in turn.  With cfg.nsigma > 0, nsigma_fn(planes) gives the
+    listed planes' n-sigma thresholds from their current residuals; each
+    plane's controller applies its own at its cycle start, in its minor
+    cycle, after its refresh (lib.rs:59395-59396, 59563-59564) and in its
+    final stop reason (lib.rs:46395-46409).  Returns a dict of the loop's
+    results."""
     f32 = np.float32
     n = len(sidelobes)
+
+    def nsigmas(planes):
+        planes = list(planes)
+        if not cfg.nsigma > 0.0 or not planes:
+            return {c: 0.0 for c in planes}
+        if nsigma_fn is None:
+            raise ValueError("CleanConfig.nsigma > 0 needs nsigma_fn")
+        return dict(zip(planes, (float(x) for x in nsigma_fn(planes))))
 
     def plane_peaks():
         # every plane's |residual| peak at once (one reduction, one copy)
@@ -344,9 +357,10 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
         # the planes' controllers (run_hogbom_cotton_schwab, niter =
         # cycle_niter, major_cycle_limit = 1) up to their residual refresh
         todo, start_peak = [], {}
+        nstart = nsigmas(active)
         for c in active:
             p = absmax(c)
-            s = tolerant_clean_stop_reason(p, cfg.threshold_jy_per_beam)
+            s = tolerant_clean_stop_reason(p, cfg.threshold_jy_per_beam, nstart[c])
             if s is not None:
                 plane_stop[c] = s
                 continue
@@ -354,10 +368,11 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
             start_peak[c] = p
         budget = min(cycle_niter, cfg.minor_cycle_length)
         if hogbom_many is not None:
-            outs = hogbom_many(todo, budget, cfg.threshold_jy_per_beam, thr)
+            outs = hogbom_many(todo, budget, cfg.threshold_jy_per_beam, thr,
+                               [nstart[c] for c in todo])
         else:
             outs = [hogbom(models[c], residuals[c], psfs[c], budget, cfg.threshold_jy_per_beam,
-                           thr) for c in todo]
+                           thr, nstart[c]) for c in todo]
         for c, out in zip(todo, outs):
             if out.model is not None:
                 models[c], residuals[c] = out.model, out.residual
@@ -389,12 +404,14 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
                 pending[c] = ("IterationLimitReached", None, False)
             else:
                 pending[c] = (stop, stop_after, True)
+        nafter = {}
         if pending:
             refresh(sorted(pending))
             pk = plane_peaks()
+            nafter = nsigmas(c for c in sorted(pending) if pending[c][2] and pending[c][1] is None)
         for c, (stop, stop_after, in_loop) in pending.items():
             if in_loop and stop_after is None:
-                s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam)
+                s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam, nafter[c])
                 # otherwise the next turn of the plane's loop meets its
                 # one-major-cycle limit
                 stop = s if s is not None else "MajorCycleLimitReached"
@@ -405,12 +422,13 @@ def cube_clean_loop(residuals, psfs, models, sidelobes, cfg: CleanConfig, hogbom
         if pass_iters == 0:
             break
     final_thr = cyc(_f32max(absmax(c) for c in range(n)), max_sidelobe)
+    nfinal = nsigmas(c for c in range(n) if plane_iters[c] < cfg.niter)
     stops = []
     for c in range(n):
         if plane_iters[c] >= cfg.niter:
             stops.append("IterationLimitReached")
             continue
-        s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam)
+        s = tolerant_clean_stop_reason(absmax(c), cfg.threshold_jy_per_beam, nfinal[c])
         if s is None:
             s = plane_stop[c]
             if s in (None, "MajorCycleLimitReached"):
@@ -451,11 +469,17 @@ def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
             sidelobes.append(sl if max_psf_sidelobe is None else max_psf_sidelobe)
         models = _zeros_like(residuals)
 
-        def hogbom(model, residual, psf, niter, threshold, cycle_threshold):
+        def hogbom(model, residual, psf, niter, threshold, cycle_threshold, nsigma_threshold):
             return im.run_hogbom_minor_cycle(ctx, model, residual, psf, cfg.gain, niter,
                                              threshold=threshold,
                                              cycle_threshold=cycle_threshold,
+                                             nsigma_threshold=nsigma_threshold,
                                              inclusive=cfg.inclusive)
+
+        def nsigma_fn(planes):
+            # the listed planes' robust RMS in one batched call
+            rms, _, _ = im.robust_rms(ctx, residuals, None, planes)
+            return [float(np.float32(cfg.nsigma) * np.float32(r)) for r in rms]
 
         def refresh(planes):
             mask = np.zeros(n, np.uint8)
@@ -464,14 +488,15 @@ def run_cube_clean(gridder, cube, cfg: CleanConfig, weighting: str = "natural",
 
         hogbom_many = None
         if torch is not None and isinstance(residuals, torch.Tensor) and residuals.is_cuda:
-            def hogbom_many(planes, niter, threshold, cycle_threshold):
+            def hogbom_many(planes, niter, threshold, cycle_threshold, nsigma_thresholds):
                 return im.run_hogbom_planes(ctx, models, residuals, psfs, planes, cfg.gain,
                                             niter, threshold=threshold,
                                             cycle_threshold=cycle_threshold,
+                                            nsigma_threshold=nsigma_thresholds,
                                             inclusive=cfg.inclusive)
 
         out = cube_clean_loop(residuals, psfs, models, sidelobes, cfg, hogbom, refresh,
-                              hogbom_many)
+                              hogbom_many, nsigma_fn)
     finally:
         plan.close()
     restored = None

@@ -141,6 +141,12 @@ class Context:
         if self._lib.cr_ctx_set_cube_graphs(self._h, 1 if enable else 0) != 0:
             raise ValueError("null context")
 
+    def set_cube_grid_chunk(self, chunk: int = 0):
+        """Records per work item of the cube gridding pass: 0 lets the tuner
+        choose (the default); 1024, 2048 or 4096 forces that size."""
+        if self._lib.cr_ctx_set_cube_grid_chunk(self._h, int(chunk)) != 0:
+            raise ValueError(f"unsupported cube grid chunk {chunk}")
+
     def set_wait_limits(self, barrier_polls: int = -1, mbar_polls: int = -1):
         """Bounds of the device-side waits (Hogbom grid barrier, cube bulk-copy
         waits), for tests of the timeout paths; -1 restores a default, 0 gives
@@ -1203,8 +1209,10 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
                       nsigma_threshold: float = 0.0, masks=None, inclusive: bool = True):
     """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) on the
     listed planes of [P][nx][ny] device images in one launch
-    (cr_hogbom_planes); models and residuals are updated in place.  Returns
-    one HogbomOutcome per listed plane (model / residual None: in place)."""
+    (cr_hogbom_planes); models and residuals are updated in place.
+    nsigma_threshold is one value for all planes or one per listed plane.
+    Returns one HogbomOutcome per listed plane (model / residual None: in
+    place)."""
     if not (_is_torch(models) and models.is_cuda):
         raise ValueError("run_hogbom_planes takes torch CUDA images")
     for t in (models, residuals, psfs):
@@ -1224,11 +1232,19 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
     mk = None
     if masks is not None:
         mk = masks.to(torch.uint8).contiguous()
+    ns_arr = None
+    if np.ndim(nsigma_threshold) > 0:
+        # one n-sigma threshold per listed plane
+        ns_arr = np.ascontiguousarray(np.asarray(nsigma_threshold, np.float32))
+        if len(ns_arr) != n:
+            raise ValueError("one n-sigma threshold per listed plane")
+        nsigma_threshold = 0.0
     ctx.use_torch_stream()
     call("cr_hogbom_planes", ctx.handle, models.data_ptr(), residuals.data_ptr(),
          psfs.data_ptr(), mk.data_ptr() if mk is not None else None, P, nx, ny,
          pl.ctypes.data, n, float(gain), float(threshold), float(cycle_threshold),
-         float(nsigma_threshold), int(cycle_niter), int(bool(inclusive)), cx.ctypes.data,
+         float(nsigma_threshold), ns_arr.ctypes.data if ns_arr is not None else None,
+         int(cycle_niter), int(bool(inclusive)), cx.ctypes.data,
          cy.ctypes.data, cpk.ctypes.data, cfl.ctypes.data, actual.ctypes.data,
          reported.ctypes.data, stop.ctypes.data)
     outs = []

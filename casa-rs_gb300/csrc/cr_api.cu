@@ -1273,6 +1273,14 @@ int cr_psf_sidelobe(cr_ctx* ctx, const float* psf, int32_t nx, int32_t ny, int32
     });
 }
 
+int cr_ctx_set_cube_grid_chunk(cr_ctx* ctx, int32_t chunk) {
+    if (!ctx) return CR_INVALID;
+    if (chunk != 0 && !cr::cube_grid_chunk_valid((uint32_t)chunk)) return CR_INVALID;
+    ctx->cube_chunk_forced = (uint32_t)chunk;
+    ctx->cube_graphs.clear();
+    return CR_OK;
+}
+
 int cr_ctx_set_wait_limits(cr_ctx* ctx, int64_t barrier_polls, int64_t mbar_polls) {
     if (!ctx) return CR_INVALID;
     ctx->barrier_polls = barrier_polls < 0 ? cr::kBarrierPollsDefault : barrier_polls;
@@ -1565,10 +1573,10 @@ int cr_cube_plan_residual_images(cr_ctx* ctx, cr_cube_plan* p, const float* mode
 int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
                      const uint8_t* mask, int32_t nplanes, int32_t nx, int32_t ny,
                      const int32_t* planes, int32_t n, float gain, float threshold,
-                     float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
-                     int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
-                     float* comp_flux, int64_t* actual, int64_t* reported,
-                     int32_t* stop_reason, char** err) {
+                     float cycle_threshold, float nsigma_threshold,
+                     const float* nsigma_thresholds, int64_t cycle_niter, int32_t inclusive,
+                     int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                     int64_t* actual, int64_t* reported, int32_t* stop_reason, char** err) {
     return guarded(err, [&] {
         need(ctx != nullptr && model != nullptr && residual != nullptr && psf != nullptr,
              "null argument");
@@ -1577,8 +1585,9 @@ int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* ps
         StageTimer tm(ctx);
         tm.mark();
         hogbom_planes(ctx, model, residual, psf, mask, nx, ny, nplanes, planes, n, gain,
-                      threshold, cycle_threshold, nsigma_threshold, cycle_niter, inclusive,
-                      comp_x, comp_y, comp_peak, comp_flux, actual, reported, stop_reason);
+                      threshold, cycle_threshold, nsigma_threshold, nsigma_thresholds,
+                      cycle_niter, inclusive, comp_x, comp_y, comp_peak, comp_flux, actual,
+                      reported, stop_reason);
         tm.mark();
         set_timings(ctx, cr_timings{0.f, 0.f, 0.f, 0.f, tm.between(0, 1)});
     });

@@ -1295,10 +1295,16 @@ static std::string cube_shape_key(const cr_gridder* g, const CubeRecords& cr) {
            "/" + std::to_string(g->info.oversampling);
 }
 
+bool cube_grid_chunk_valid(uint32_t chunk) {
+    for (uint32_t c : kGridChunkCandidates)
+        if (c == chunk) return true;
+    return false;
+}
+
 void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* dirty) {
     const std::string key = cube_shape_key(g, cr);
     auto tuned = ctx->cube_chunk.find(key);
-    if (tuned == ctx->cube_chunk.end() && !ctx->capturing) {
+    if (tuned == ctx->cube_chunk.end() && !ctx->capturing && !ctx->cube_chunk_forced) {
         // first use of this cube shape: time the gridding pass (work lists
         // and kernel) for every candidate chunk size and keep the fastest
         cudaEvent_t e0 = ctx->kev[0], e1 = ctx->kev[1];
@@ -1320,7 +1326,8 @@ void cube_grid(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, float* psf, float2* 
         ctx->cube_chunk[key] = best;
         tuned = ctx->cube_chunk.find(key);
     }
-    const uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    if (ctx->cube_chunk_forced) chunk = ctx->cube_chunk_forced;
     make_work_lists(ctx, g, cr, chunk, psf, dirty);
     kernel_mark(ctx, 0, false);
     launch_cube_grid<false>(ctx, g, cr, psf, dirty);
@@ -1358,7 +1365,8 @@ static void launch_cube_degrid(cr_ctx* ctx, cr_gridder* g, const CubeRecords& cr
 void cube_grid_residual(cr_ctx* ctx, cr_gridder* g, CubeRecords& cr, const float2* model,
                         float2* residual, const uint8_t* plane_mask) {
     auto tuned = ctx->cube_chunk.find(cube_shape_key(g, cr));
-    const uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    uint32_t chunk = tuned != ctx->cube_chunk.end() ? tuned->second : kGridChunkDefault;
+    if (ctx->cube_chunk_forced) chunk = ctx->cube_chunk_forced;
     // the lists skip masked planes and zero the heavy tiles of the others
     make_work_lists(ctx, g, cr, chunk, nullptr, residual, plane_mask);
     const size_t nrec = cr.n_records >= 0 ? (size_t)std::max<int64_t>(cr.n_records, 1)

@@ -291,6 +291,7 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_kernel(HogArgs a) {
 struct HogPlanesArgs {
     HogArgs base;           // pointers to plane 0; cands / bar / comp / out of slot 0
     const int* planes;      // [n] plane indices
+    const float* nsigma;    // [n] n-sigma threshold of each slot, or null (base's)
     int per_plane;
     int64_t comp_cap;       // components per slot
 };
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(kHogThreads) hogbom_planes_kernel(HogPlanesArg
     }
     a.out_actual += slot;
     a.out_stop += slot;
+    if (pa.nsigma) a.nsigma_threshold = pa.nsigma[slot];
     hogbom_body(a, pa.per_plane, bidx);
 }
 
@@ -540,10 +542,10 @@ void hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
 void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
                    const uint8_t* mask, int32_t nx, int32_t ny, int32_t nplanes,
                    const int32_t* planes, int32_t n, float gain, float threshold,
-                   float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
-                   int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
-                   float* comp_flux, int64_t* actual, int64_t* reported,
-                   int32_t* stop_reason_out) {
+                   float cycle_threshold, float nsigma_threshold,
+                   const float* nsigma_per_plane, int64_t cycle_niter, int32_t inclusive,
+                   int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                   int64_t* actual, int64_t* reported, int32_t* stop_reason_out) {
     if (nx <= 0 || ny <= 0) fail(CR_INVALID, "image shape must be positive");
     if ((int64_t)nx * ny >= (1ll << 31)) fail(CR_INVALID, "image larger than 2^31 pixels");
     if (cycle_niter < 0) fail(CR_INVALID, "cycle_niter is negative");
@@ -577,6 +579,9 @@ void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
     float* cp = (float*)(cy + (size_t)batch * cap);
     float* cf = cp + (size_t)batch * cap;
     int* plist = (int*)workspace(ctx, "hogp_planes", (size_t)batch * 4);
+    float* nslist = nsigma_per_plane
+                        ? (float*)workspace(ctx, "hogp_nsigma", (size_t)batch * 4)
+                        : nullptr;
     std::vector<long long> h_actual((size_t)batch);
     std::vector<int> h_stop((size_t)batch);
     for (int32_t s0 = 0; s0 < n; s0 += batch) {
@@ -584,11 +589,15 @@ void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
         CR_CUDA_CHECK(cudaMemsetAsync(wsp, 0, head_al, ctx->stream));
         CR_CUDA_CHECK(cudaMemcpyAsync(plist, planes + s0, (size_t)m * 4, cudaMemcpyHostToDevice,
                                       ctx->stream));
+        if (nslist)
+            CR_CUDA_CHECK(cudaMemcpyAsync(nslist, nsigma_per_plane + s0, (size_t)m * 4,
+                                          cudaMemcpyHostToDevice, ctx->stream));
         HogPlanesArgs pa;
         pa.base = HogArgs{model, residual, psf, mask, nx, ny, gain, threshold, cycle_threshold,
                           nsigma_threshold, budget, cands, bar, cx, cy, cp, cf, out_actual,
                           out_stop, out_status, 0, ctx->barrier_polls};
         pa.planes = plist;
+        pa.nsigma = nslist;
         pa.per_plane = per_plane;
         pa.comp_cap = cap;
         void* args[] = {&pa};

@@ -71,6 +71,7 @@ struct cr_ctx {
     // call signature; ws_epoch changes whenever a workspace is (re)allocated,
     // which retires the captured graphs (they hold workspace addresses)
     std::map<std::string, uint32_t> cube_chunk;
+    uint32_t cube_chunk_forced = 0;   // nonzero: this chunk instead of the tuner's
     std::map<std::string, std::shared_ptr<cr::CubeGraph>> cube_graphs;
     bool cube_graphs_enabled = true;
     // Precision of the image-stage FFTs of single-plane calls: 64 (default)
@@ -239,6 +240,9 @@ void std_grid(cr_ctx* ctx, cr_gridder* g, const Records& r, float2* psf, float2*
 void std_degrid(cr_ctx* ctx, cr_gridder* g, const Records& r, const float2* grid);
 void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
 
+// the cube gridding chunk sizes the tuner chooses from
+bool cube_grid_chunk_valid(uint32_t chunk);
+
 // ---- robust RMS (n-sigma threshold) ----------------------------------------------
 // robust_rms_jy_per_beam of the listed planes of device images [P][npix]
 // (masks [P][npix] or null); rms / madfm / counts per listed plane (host).
@@ -396,10 +400,10 @@ void clark_minor_cycle(cr_ctx* ctx, float* model, float* residual, const float* 
 void hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
                    const uint8_t* mask, int32_t nx, int32_t ny, int32_t nplanes,
                    const int32_t* planes, int32_t n, float gain, float threshold,
-                   float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
-                   int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
-                   float* comp_flux, int64_t* actual, int64_t* reported,
-                   int32_t* stop_reason_out);
+                   float cycle_threshold, float nsigma_threshold,
+                   const float* nsigma_per_plane, int64_t cycle_niter, int32_t inclusive,
+                   int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                   int64_t* actual, int64_t* reported, int32_t* stop_reason_out);
 
 inline unsigned int grid_blocks(int64_t n, int threads, int64_t cap = 152 * 32) {
     int64_t b = (n + threads - 1) / threads;

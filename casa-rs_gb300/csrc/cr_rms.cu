@@ -343,6 +343,7 @@ void robust_rms(cr_ctx* ctx, const float* images, const uint8_t* masks, int64_t 
     const int np = (int)planes.size();
     if (np == 0) return;
     if (npix <= 0) fail(CR_INVALID, "image shape must be positive");
+    if (np > 65535) fail(CR_INVALID, "at most 65535 planes per call");
     // blocks per plane: about four waves of the device over all planes
     const int bx = (int)std::max<int64_t>(
         1, std::min<int64_t>((npix + kRmsThreads - 1) / kRmsThreads,

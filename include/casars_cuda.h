@@ -350,6 +350,12 @@ typedef struct {
  * replayed afterwards (cr_timings.grid_ms then times the whole pipeline);
  * this switches that off (0) or on (nonzero, the default). */
 int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable);
+/* Records per work item of the cube gridding pass.  0 (the default): the
+ * first call of each cube shape times 1024, 2048 and 4096 and keeps the
+ * fastest for the context; one of those values: that size, no timing.
+ * Returns CR_INVALID for any other value.  New; no counterpart in the
+ * reference (its CPU cube path has no work items). */
+int cr_ctx_set_cube_grid_chunk(cr_ctx* ctx, int32_t chunk);
 int cr_cube_grid_dirty(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,
                        int32_t weighting, float robust, float* psf_grids, float* dirty_grids,
                        int32_t out_location, cr_sums* sums, char** err);
@@ -523,16 +529,19 @@ int cr_hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf
  * psf (and mask, or NULL) are DEVICE arrays [nplanes][nx][ny]; the n planes
  * listed in `planes` (host) each run run_hogbom_minor_cycle_cpu_with_progress
  * with the same gain, thresholds and budget, as cr_hogbom would one by one
- * (each plane's blocks only touch that plane).  actual, reported and
- * stop_reason are host [n]; the component arrays (host, or NULL) hold
- * [n][cycle_niter + 1] entries, plane s's first actual[s] of them valid. */
+ * (each plane's blocks only touch that plane).  nsigma_thresholds (host [n],
+ * or NULL for nsigma_threshold on every plane) gives each listed plane its
+ * own n-sigma threshold, as the cube's per-plane controllers compute them
+ * (lib.rs:46395-46396).  actual, reported and stop_reason are host [n]; the
+ * component arrays (host, or NULL) hold [n][cycle_niter + 1] entries, plane
+ * s's first actual[s] of them valid. */
 int cr_hogbom_planes(cr_ctx* ctx, float* model, float* residual, const float* psf,
                      const uint8_t* mask, int32_t nplanes, int32_t nx, int32_t ny,
                      const int32_t* planes, int32_t n, float gain, float threshold,
-                     float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
-                     int32_t inclusive, int32_t* comp_x, int32_t* comp_y, float* comp_peak,
-                     float* comp_flux, int64_t* actual, int64_t* reported,
-                     int32_t* stop_reason, char** err);
+                     float cycle_threshold, float nsigma_threshold,
+                     const float* nsigma_thresholds, int64_t cycle_niter, int32_t inclusive,
+                     int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
+                     int64_t* actual, int64_t* reported, int32_t* stop_reason, char** err);
 
 /* ---- Clark minor cycle ------------------------------------------------------
  * run_clark_minor_cycle_cpu (lib.rs:62129-62355): subcycles over the active

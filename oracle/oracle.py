@@ -764,7 +764,7 @@ def cotton_schwab(residual, psf, refresh, niter, gain=0.1, threshold=0.0, minor_
 
 def cube_clean(planes, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000, cyclefactor=1.0,
                min_psf_fraction=0.05, max_psf_fraction=0.8, major_cycle_limit=None,
-               inclusive=True):
+               inclusive=True, nsigma=0.0):
     """run_standard_mfs_cube_clean (casa-imaging lib.rs:3026-3210) over
     planes in ascending order.  Each plane is a dict with residual, psf,
     refresh(model) -> residual and sidelobe (its PSF sidelobe level).  Per
@@ -815,7 +815,7 @@ def cube_clean(planes, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000, 
                                 min_psf_fraction=min_psf_fraction,
                                 max_psf_fraction=max_psf_fraction, major_cycle_limit=1,
                                 sidelobe=max_sidelobe, inclusive=inclusive, model=model[i],
-                                cycle_threshold_override=thr)
+                                cycle_threshold_override=thr, nsigma=nsigma)
             model[i], res[i] = out["model"], out["residual"]
             comps[i].extend(out["components"])
             plane_iters[i] += out["reported"]
@@ -830,7 +830,8 @@ def cube_clean(planes, niter, gain=0.1, threshold=0.0, minor_cycle_length=2000, 
         if plane_iters[i] >= niter:
             stops.append("IterationLimitReached")
             continue
-        s = tolerant_clean_stop_reason(absmax(res[i]), threshold, 0.0)
+        s = tolerant_clean_stop_reason(absmax(res[i]), threshold,
+                                       nsigma_threshold(res[i], nsigma))
         if s is None:
             s = plane_stop[i]
             if s in (None, "MajorCycleLimitReached"):

@@ -45,40 +45,47 @@ def _planes(obs, flags, vis, os_=64):
     return planes
 
 
-# (niter, minor cycle length, major-cycle limit, threshold, weak plane scale):
-# several passes on every plane, a budget that one pass exceeds, a pass
-# limit, and a global threshold with a faint plane that joins late.
-@pytest.mark.parametrize("niter,mcl,limit,thr,weak", [
-    (120, 25, None, 0.0, 1.0), (40, 1000, None, 0.0, 1.0), (200, 30, 2, 0.0, 1.0),
-    (600, 40, None, 0.02, 0.15)])
-def test_cube_clean_loop_matches_oracle(niter, mcl, limit, thr, weak):
+# (niter, minor cycle length, major-cycle limit, threshold, weak plane scale,
+# nsigma): several passes on every plane, a budget that one pass exceeds, a
+# pass limit, a global threshold with a faint plane that joins late, and the
+# n-sigma threshold of each plane's robust RMS.
+@pytest.mark.parametrize("niter,mcl,limit,thr,weak,nsigma", [
+    (120, 25, None, 0.0, 1.0, 0.0), (40, 1000, None, 0.0, 1.0, 0.0), (200, 30, 2, 0.0, 1.0, 0.0),
+    (600, 40, None, 0.02, 0.15, 0.0), (2000, 30, None, 0.0, 0.3, 6.0)])
+def test_cube_clean_loop_matches_oracle(niter, mcl, limit, thr, weak, nsigma):
     obs = S.cube_observation(channels=4, nx=64, hours=1.0, dump_s=120.0, n_sources=3, seed=5)
     flags = S.cube_flags(obs)
     vis = S.cube_visibilities(obs)
     vis[2] *= np.float32(weak)
     planes = _planes(obs, flags, vis)
     kw = dict(gain=0.1, threshold=thr, minor_cycle_length=mcl, major_cycle_limit=limit)
-    ref = O.cube_clean(planes, niter, **kw)
-    if weak < 1.0:
+    ref = O.cube_clean(planes, niter, nsigma=nsigma, **kw)
+    if weak < 1.0 and nsigma == 0.0:
         assert 2 not in ref["active"][0] and any(2 in a for a in ref["active"])
         assert "GlobalThresholdReached" in ref["plane_stops"]
+    if nsigma > 0.0:
+        assert "NsigmaThresholdReached" in ref["plane_stops"]
 
     cfg = CL.CleanConfig(niter=niter, gain=0.1, threshold_jy_per_beam=thr,
-                         minor_cycle_length=mcl, major_cycle_limit=limit)
+                         minor_cycle_length=mcl, major_cycle_limit=limit, nsigma=nsigma)
     res = np.stack([p["residual"] for p in planes])
     psfs = np.stack([p["psf"] for p in planes])
     models = np.zeros_like(res)
 
-    def hogbom(model, residual, psf, n, threshold, cycle_threshold):
+    def hogbom(model, residual, psf, n, threshold, cycle_threshold, nsigma_threshold):
         return _Out(O.hogbom(residual, psf, 0.1, n, threshold=threshold,
-                             cycle_threshold=cycle_threshold, model=model, inclusive=True))
+                             cycle_threshold=cycle_threshold,
+                             nsigma_threshold=nsigma_threshold, model=model, inclusive=True))
 
     def refresh(cs):
         for c in cs:
             res[c] = planes[c]["refresh"](models[c])
 
+    def nsigma_fn(cs):
+        return [O.nsigma_threshold(res[c], nsigma) for c in cs]
+
     out = CL.cube_clean_loop(res, psfs, models, [p["sidelobe"] for p in planes], cfg, hogbom,
-                             refresh)
+                             refresh, nsigma_fn=nsigma_fn)
     assert out["major_cycles"] == ref["major_cycles"] and out["major_cycles"] > 0
     assert out["minor_iterations"] == ref["minor_iterations"]
     assert out["active"] == ref["active"]

@@ -226,3 +226,62 @@ def test_hogbom_planes_equals_single_plane_calls(ctx, cube):
     for c in set(range(P)) - set(planes):
         np.testing.assert_array_equal(res_d[c].cpu().numpy(), res[c])
         assert float(mod_d[c].abs().max()) == 0.0
+
+
+def test_cube_clean_nsigma_matches_oracle(ctx, cube):
+    """The per-plane n-sigma threshold (nsigma * the plane's robust RMS, all
+    active planes in one batched cr_robust_rms call) in the cube loop: the
+    same passes, budgets and stop reasons as the oracle's loop, most planes
+    stopping at their n-sigma threshold."""
+    import torch
+    obs, flags, vis = cube
+    vis = vis.copy()
+    vis[3] *= np.float32(0.2)
+    gg = _gridder(ctx, obs)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    cb = cc.CubeBatch(t(obs.u_m), t(obs.v_m), obs.lambda_scale, t(vis), None,
+                      t(flags.astype(np.uint8)))
+    ref_planes = _oracle_planes(obs, flags, vis)
+    for p in ref_planes:
+        p["sidelobe"] = 0.2
+    kw = dict(gain=0.1, threshold=0.0, minor_cycle_length=40, nsigma=10.0)
+    ref = O.cube_clean(ref_planes, 1000, **kw)
+    assert ref["plane_stops"].count("NsigmaThresholdReached") >= 4
+    cfg = cc.CleanConfig(niter=1000, gain=0.1, minor_cycle_length=40, nsigma=10.0)
+    out = cc.run_cube_clean(gg, cb, cfg, max_psf_sidelobe=0.2, restore=False)
+    assert out.major_cycles == ref["major_cycles"]
+    assert out.active_planes == ref["active"]
+    assert out.plane_iterations == ref["plane_iterations"]
+    assert out.plane_stop_reasons == ref["plane_stops"]
+    for c in range(obs.channels):
+        assert [tuple(p) for p, _ in out.components[c]] == \
+            [tuple(p) for p, _ in ref["components"][c]]
+        assert peak_norm_err(out.residuals[c].cpu().numpy(), ref["residuals"][c]) <= 1e-5
+
+
+def test_hogbom_planes_per_plane_nsigma(ctx, cube):
+    """cr_hogbom_planes with one n-sigma threshold per listed plane equals
+    cr_hogbom on each plane with its own threshold."""
+    import torch
+    obs, flags, vis = cube
+    gg = _gridder(ctx, obs)
+    cb = cc.CubeBatch(obs.u_m, obs.v_m, obs.lambda_scale, vis, None, flags)
+    plan = cc.CubePlan(gg, cb)
+    psf, res, states = plan.dirty_images()
+    plan.close()
+    psf_d = torch.as_tensor(psf).cuda().contiguous()
+    res_d = torch.as_tensor(res).cuda().contiguous()
+    mod_d = torch.zeros_like(res_d)
+    planes = [1, 3, 4]
+    peaks = [float(np.max(np.abs(res[c]))) for c in planes]
+    nsig = [0.5 * peaks[0], 0.05 * peaks[1], 0.3 * peaks[2]]
+    outs = cc.run_hogbom_planes(ctx, mod_d, res_d, psf_d, planes, 0.1, 200,
+                                nsigma_threshold=nsig)
+    for s, c in enumerate(planes):
+        one = cc.run_hogbom_minor_cycle(ctx, np.zeros_like(res[c]), res[c], psf[c], 0.1, 200,
+                                        nsigma_threshold=nsig[s])
+        assert outs[s].actual_updates == one.actual_updates > 0
+        assert outs[s].stop_reason == one.stop_reason
+        np.testing.assert_array_equal(outs[s].positions, one.positions)
+        np.testing.assert_array_equal(res_d[c].cpu().numpy(), one.residual)
+    assert outs[0].stop_reason == "NsigmaThresholdReached"
