@@ -516,6 +516,7 @@ void cr_wproj_destroy(cr_wproj* wp) {
     cudaFree(wp->sinc_x_d);
     cudaFree(wp->sinc_gx_d);
     cudaFree(wp->sinc_gy_d);
+    cudaFree(wp->first_plane_d);
     delete wp;
 }
 

@@ -126,6 +126,8 @@ struct cr_wproj {
     float* sinc_x_d = nullptr;        // sinc axis for the image correction (max(g) long)
     float* sinc_gx_d = nullptr;       // sinc axes for the model apodisation
     float* sinc_gy_d = nullptr;
+    int32_t* first_plane_d = nullptr;  // [max support + 1] first plane with support >= S
+    bool support_monotone = false;     // supports non-decreasing in the plane index
 };
 
 namespace cr {

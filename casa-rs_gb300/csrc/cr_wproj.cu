@@ -16,11 +16,10 @@
 // planes with supports up to 64 at oversampling 8), small enough to stay in
 // L2, where per-offset copies of the taps would not.
 //
-// Gridding is output-stationary: a block owns a 32 x 32 tile of the grid in
-// registers (each of 8 warps owns a band of 4 rows, each lane one column),
-// streams the
+// Gridding is output-stationary: a warp owns an 8-row band of a 32 x 32
+// tile of the grid in registers (each lane one column), streams the
 // deduplicated records whose windows can reach the tile, and adds
-// value * kernel for every owned cell inside a record's window.  The tile is
+// value * kernel for every owned cell inside a record's window.  The band is
 // flushed once per work item with FP32 atomics.  Degridding is a gather: a
 // warp per record takes the window's rows in pairs, 16 lanes per row, with
 // the cube column addresses held in registers, and reduces with warp
@@ -35,11 +34,7 @@ namespace cr {
 
 namespace {
 
-constexpr int kGridThreads = 256;
-constexpr int kRowsPerWarp = kTile / (kGridThreads / 32);  // 4
-constexpr int kMaxSegRadius = 4;
-constexpr int kMaxSeg = (2 * kMaxSegRadius + 1) * (2 * kMaxSegRadius + 1);
-constexpr int kChunk = 512;  // candidate records per work item
+constexpr int kMaxSegRadius = 4;   // neighbourhood radius in tiles (supports up to 127)
 
 // ---- construction ----------------------------------------------------------------
 __global__ void screen_kernel(float2* buf, int64_t conv, int64_t inner, int planes_in_batch,
@@ -191,23 +186,84 @@ __device__ __forceinline__ int cube_b(int t, int off, int q, const CubeGeom& c) 
     return (k - qk * c.s) * q * q + qk;
 }
 
-// ---- gridding ----------------------------------------------------------------------
-struct GridArgs {
-    const int32_t *rx, *ry, *rplane, *roff, *rconj;
-    const double2* vsum;
-    const double* wsum;
-    const float2* pred;
-    const uint32_t* tile_start;
-    int64_t ntx, nty;
-    const int32_t* support;
+// ---- gridding ---------------------------------------------------------------------
+// One warp per work item (output tile, band of kBandRows rows, chunk of
+// candidate records); no block-level barriers.  Lane l owns column l of the
+// tile and keeps per band row three float2 accumulators,
+//   X = sum k (.) (vr, -t vi),  Y = sum k (.) (vi, t vr),  P = sum k (.) (w, t w)
+// (k = (kr, ki) the kernel value, t = -1 for a conjugated record, (.) the
+// element-wise product), one paired FMA each per tap; the flush forms
+// dirty = (X.x + X.y, Y.x + Y.y) and psf = P.  The warp examines its
+// candidates 32 at a time, one per lane, from records packed once per pass
+// (16 bytes each, prefetched a batch ahead with cp.async), and compacts those
+// whose window reaches its band into warp-private shared memory with their
+// row addresses.
+constexpr int kBandRows = 8;
+constexpr int kBands = kTile / kBandRows;   // 4 bands per tile
+constexpr int kBandWarps = 8;               // warps per block
+constexpr int kBandChunk = 256;             // candidate records per work item
+constexpr int kNbr = (2 * kMaxSegRadius + 1) * (2 * kMaxSegRadius + 1);
+
+struct __align__(16) BandEntry {
+    float4 vx;        // (vr, -t vi, vi, t vr)
+    float2 pw;        // (w, t w)
+    int cb, w;        // window column of tile column 0; window width 2S+1
+    long long base;   // element offset of the plane's residue cube
+    int s, oy, q, pad;
+};
+
+// Each record packed once per pass: x = (lx << 16) | ly, y = plane |
+// (ox + radius) << 12 | (oy + radius) << 18 | conj << 24 | support << 25,
+// z, w = the float32 value (vr, vi) (w vis - w pred with RESIDUAL); the
+// weight separately.
+inline bool band_pack_fits(int64_t gn, int planes, int radius, int smax) {
+    return gn <= 65536 && planes <= 4096 && 2 * radius + 1 <= 64 && smax <= 127;
+}
+
+template <bool RESIDUAL>
+__global__ void band_pack_kernel(const int32_t* rx, const int32_t* ry, const int32_t* rplane,
+                                 const int32_t* roff, const int32_t* rconj, const double2* vsum,
+                                 const double* wsum, const float2* pred, const int32_t* support,
+                                 int32_t axis, const unsigned long long* counts, uint4* packed,
+                                 float* weight) {
+    const int64_t n = (int64_t)counts[2];
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int plane = rplane[r];
+        const int off = roff[r];
+        const unsigned meta = (unsigned)plane | (unsigned)(off / axis) << 12 |
+                              (unsigned)(off % axis) << 18 | (unsigned)(rconj[r] ? 1 : 0) << 24 |
+                              (unsigned)support[plane] << 25;
+        const double2 vs = vsum[r];
+        const double ws = wsum[r];
+        float vr, vi;
+        if (RESIDUAL) {
+            const float2 p = pred[r];
+            vr = (float)(vs.x - (double)p.x * ws);
+            vi = (float)(vs.y - (double)p.y * ws);
+        } else {
+            vr = (float)vs.x;
+            vi = (float)vs.y;
+        }
+        packed[r] = make_uint4((unsigned)rx[r] << 16 | (unsigned)ry[r], meta, __float_as_uint(vr),
+                               __float_as_uint(vi));
+        weight[r] = (float)ws;
+    }
+}
+
+struct BandArgs {
+    const uint4* packed;
+    const float* weight;
     const int64_t* cube_off;
     const int32_t* cube_q;
     const float2* cube;
     CubeGeom cg;
-    int32_t radius, axis;
-    int32_t seg_radius;
-    const uint32_t* item_tile;
-    const uint32_t* item_begin;
+    int32_t radius;
+    int64_t nty;
+    const uint32_t* seg_lo;    // [ntiles][kNbr] first candidate record of each segment
+    const uint32_t* seg_pre;   // [ntiles][kNbr + 1] exclusive prefix of segment lengths
+    const uint8_t* nseg;       // [ntiles]
+    const uint2* items;        // (tile * kBands + band, first candidate)
     const unsigned long long* n_items;
     unsigned int* item_counter;
     float2* psf;
@@ -215,224 +271,240 @@ struct GridArgs {
     int64_t gnx, gny;
 };
 
-struct __align__(16) Entry {
-    int64_t base;    // element offset of the record's plane cube
-    int32_t cb;      // window column of tile column 0
-    int32_t ra;      // window row of tile row 0
-    int32_t w;       // window width 2S+1
-    int32_t s;       // support S
-    int32_t ox, oy;  // oversampling offsets
-    int32_t q;       // cube extent Q of the plane
-    int32_t pad;
-    float vr, vi, tvi, tvr, pw, tpw, pad2, pad3;
-};
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
 
-constexpr int kCand = 128;  // candidate records examined per batch
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kGridThreads, 6) wp_grid_kernel(GridArgs a) {
-    __shared__ int s_item;
-    __shared__ uint32_t s_seg_start[kMaxSeg];
-    __shared__ uint32_t s_seg_pref[kMaxSeg + 1];
-    __shared__ int s_nseg;
-    __shared__ Entry s_list[kCand];
-    // x-side cube address of each tile row per entry, -1 outside the window
-    __shared__ int s_rowa[kCand][kTile + 1];
-    __shared__ int s_nlist;
-    __shared__ int s_warp_cnt[kCand / 32];
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+__global__ void __launch_bounds__(kBandWarps * 32, 3) wp_grid_kernel(BandArgs a) {
+    __shared__ BandEntry s_ent[kBandWarps][32];
+    __shared__ __align__(16) int s_rows[kBandWarps][32][kBandRows];
+    __shared__ uint32_t s_lo[kBandWarps][kNbr];
+    __shared__ uint32_t s_pre[kBandWarps][kNbr + 1];
+    // the packed candidates of the current and the next batch
+    __shared__ uint4 s_pk[kBandWarps][2][32];
+    __shared__ float s_wt[kBandWarps][2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned long long n_items = *a.n_items;
-    const int R = a.seg_radius;
-
+    BandEntry* ent = s_ent[warp];
+    uint32_t* lo_s = s_lo[warp];
+    uint32_t* pre_s = s_pre[warp];
     for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(a.item_counter, 1u);
-        __syncthreads();
-        const int item = s_item;
+        unsigned int item = 0;
+        if (lane == 0) item = atomicAdd(a.item_counter, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
         if ((unsigned long long)item >= n_items) break;
-        const uint32_t T = a.item_tile[item];
-        const uint32_t begin = a.item_begin[item];
-        const int64_t tx = T / a.nty, ty = T % a.nty;
-        const int x0 = (int)(tx * kTile), y0 = (int)(ty * kTile);
-        if (tid == 0) {
-            int ns = 0;
-            uint32_t run = 0;
-            for (int dx = -R; dx <= R; ++dx) {
-                int64_t hx = tx + dx;
-                if (hx < 0 || hx >= a.ntx) continue;
-                int64_t h0 = hx * a.nty + (ty - R < 0 ? 0 : ty - R);
-                int64_t h1 = hx * a.nty + (ty + R >= a.nty ? a.nty - 1 : ty + R);
-                // the home tiles of one column dx are consecutive: one segment
-                uint32_t st = a.tile_start[h0], en = a.tile_start[h1 + 1];
-                s_seg_start[ns] = st;
-                s_seg_pref[ns] = run;
-                run += en - st;
-                ns++;
-            }
-            s_seg_pref[ns] = run;
-            s_nseg = ns;
-        }
-        __syncthreads();
-        const int nseg = s_nseg;
-        const uint32_t total = s_seg_pref[nseg];
-        const uint32_t end = min(total, begin + (uint32_t)kChunk);
-
-        float pr[kRowsPerWarp], pi[kRowsPerWarp], dr[kRowsPerWarp], di[kRowsPerWarp];
-#pragma unroll
-        for (int k = 0; k < kRowsPerWarp; ++k) pr[k] = pi[k] = dr[k] = di[k] = 0.0f;
-
-        for (uint32_t base = begin; base < end; base += kCand) {
-            // 1. candidates -> overlapping entries (the first kCand threads)
-            uint32_t vidx = base + tid;
-            bool take = false;
-            Entry e;
-            if (tid < kCand && vidx < end) {
-                int k = 0;
-                while (k + 1 < nseg && s_seg_pref[k + 1] <= vidx) ++k;
-                uint32_t r = s_seg_start[k] + (vidx - s_seg_pref[k]);
-                int lx = a.rx[r], ly = a.ry[r];
-                int plane = a.rplane[r];
-                int sup = a.support[plane];
-                if (lx - sup <= x0 + kTile - 1 && lx + sup >= x0 && ly - sup <= y0 + kTile - 1 &&
-                    ly + sup >= y0) {
-                    take = true;
-                    int off = a.roff[r];
-                    e.ox = off / a.axis - a.radius;
-                    e.oy = off % a.axis - a.radius;
-                    e.s = sup;
-                    e.w = 2 * sup + 1;
-                    e.q = a.cube_q[plane];
-                    e.base = a.cube_off[plane];
-                    e.ra = x0 - lx + sup;
-                    e.cb = y0 - ly + sup;
-                    double2 vs = a.vsum[r];
-                    double ws = a.wsum[r];
-                    float vr, vi;
-                    if (RESIDUAL) {
-                        float2 p = a.pred[r];
-                        vr = (float)(vs.x - (double)p.x * ws);
-                        vi = (float)(vs.y - (double)p.y * ws);
-                    } else {
-                        vr = (float)vs.x;
-                        vi = (float)vs.y;
-                    }
-                    float t = a.rconj[r] ? -1.0f : 1.0f;
-                    e.vr = vr;
-                    e.vi = vi;
-                    e.tvi = t * vi;
-                    e.tvr = t * vr;
-                    e.pw = (float)ws;
-                    e.tpw = t * (float)ws;
-                    e.pad = 0;
-                    e.pad2 = e.pad3 = 0.0f;
+        const uint2 it = a.items[item];
+        const int64_t T = it.x / kBands;
+        const int band = (int)(it.x % kBands);
+        const int x0 = (int)((T / a.nty) * kTile) + band * kBandRows;
+        const int y0 = (int)((T % a.nty) * kTile);
+        const int ns = a.nseg[T];
+        for (int k = lane; k < ns; k += 32) lo_s[k] = a.seg_lo[T * kNbr + k];
+        for (int k = lane; k <= ns; k += 32) pre_s[k] = a.seg_pre[T * (kNbr + 1) + k];
+        __syncwarp();
+        const uint32_t cbeg = it.y, cend = min(pre_s[ns], cbeg + (uint32_t)kBandChunk);
+        // lane l's candidate c (segment k with pre[k] <= c < pre[k+1]) into
+        // candidate buffer b
+        auto fetch = [&](uint32_t c, int b) {
+            if (c < cend) {
+                int lo = 0, hi = ns - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (pre_s[mid] <= c) lo = mid; else hi = mid - 1;
                 }
+                const uint32_t r = lo_s[lo] + (c - pre_s[lo]);
+                cp_async16(&s_pk[warp][b][lane], a.packed + r);
+                cp_async4(&s_wt[warp][b][lane], a.weight + r);
             }
-            unsigned bal = 0;
-            if (tid < kCand) {  // whole warps: kCand is a multiple of 32
-                bal = __ballot_sync(0xffffffffu, take);
-                if (lane == 0) s_warp_cnt[warp] = __popc(bal);
+            cp_async_commit();
+        };
+        fetch(cbeg + lane, 0);
+        int buf = 0;
+
+        float2 X[kBandRows], Y[kBandRows], P[kBandRows];
+#pragma unroll
+        for (int k = 0; k < kBandRows; ++k) X[k] = Y[k] = P[k] = make_float2(0.f, 0.f);
+
+        for (uint32_t c0 = cbeg; c0 < cend; c0 += 32) {
+            // 1. one candidate per lane: does its window reach the band?  The
+            // taken ones write their entry and row addresses straight into
+            // their compacted slot.  The next batch's candidates are copied
+            // in while this batch is worked on.
+            if (c0 + 32 < cend) {
+                fetch(c0 + 32 + lane, buf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
-            __syncthreads();
+            const bool valid = c0 + lane < cend;
+            const uint4 pk = valid ? s_pk[warp][buf][lane] : make_uint4(0u, 0u, 0u, 0u);
+            const float wt = valid ? s_wt[warp][buf][lane] : 0.0f;
+            buf ^= 1;
+            const int lx = (int)(pk.x >> 16), ly = (int)(pk.x & 0xffffu);
+            const int sup = (int)(pk.y >> 25);
+            const bool take = valid && lx - sup <= x0 + kBandRows - 1 && lx + sup >= x0 &&
+                              ly - sup <= y0 + kTile - 1 && ly + sup >= y0;
+            const unsigned bal = __ballot_sync(0xffffffffu, take);
             if (take) {
-                int slot = 0;
-                for (int w2 = 0; w2 < warp; ++w2) slot += s_warp_cnt[w2];
-                slot += __popc(bal & ((1u << lane) - 1u));
-                s_list[slot] = e;
-            }
-            if (tid == 0) {
-                int t = 0;
-                for (int w2 = 0; w2 < kCand / 32; ++w2) t += s_warp_cnt[w2];
-                s_nlist = t;
-            }
-            __syncthreads();
-            // x-side cube address of every (entry, tile row), all threads
-            const int nlist = s_nlist;
-            for (int idx = tid; idx < nlist * kTile; idx += kGridThreads) {
-                const int qn = idx / kTile, rr = idx - (idx / kTile) * kTile;
-                const Entry& en = s_list[qn];
-                const int i = en.ra + rr;  // window row index
-                s_rowa[qn][rr] = (i >= 0 && i < en.w) ? cube_a(i - en.s, en.ox, en.q, a.cg) : -1;
-            }
-            __syncthreads();
-            // 2. accumulate the entries into the register tile; warp w owns
-            // rows 4w .. 4w+3 and skips entries whose window misses them
-            const int band0 = warp * kRowsPerWarp;
-            for (int qn = 0; qn < nlist; ++qn) {
-                const Entry& en = s_list[qn];
-                if (band0 > en.w - 1 - en.ra || band0 + kRowsPerWarp - 1 < -en.ra) continue;
-                const int col = en.cb + lane;
-                const bool colok = (unsigned)col < (unsigned)en.w;
-                const int bcol = colok ? cube_b(col - en.s, en.oy, en.q, a.cg) : 0;
-                const float2* cube = a.cube + en.base + bcol;
-                float2 kv[kRowsPerWarp];
-                bool ok[kRowsPerWarp];
+                const int slot = __popc(bal & ((1u << lane) - 1u));
+                BandEntry& e = ent[slot];
+                const int plane = (int)(pk.y & 0xfffu);
+                const int ox = (int)((pk.y >> 12) & 63u) - a.radius;
+                const int q = a.cube_q[plane];
+                const int w = 2 * sup + 1;
+                e.oy = (int)((pk.y >> 18) & 63u) - a.radius;
+                e.s = sup;
+                e.w = w;
+                e.q = q;
+                e.base = a.cube_off[plane];
+                e.cb = y0 - ly + sup;
+                const float vr = __uint_as_float(pk.z), vi = __uint_as_float(pk.w);
+                const float t = ((pk.y >> 24) & 1u) ? -1.0f : 1.0f;
+                e.vx = make_float4(vr, -t * vi, vi, t * vr);
+                e.pw = make_float2(wt, t * wt);
+                int* rows = s_rows[warp][slot];
 #pragma unroll
-                for (int k = 0; k < kRowsPerWarp; ++k) {
-                    const int av = s_rowa[qn][band0 + k];
-                    ok[k] = av >= 0 && colok;
-                    kv[k] = ok[k] ? __ldg(cube + av) : make_float2(0.f, 0.f);
-                }
-                // (paired float32 FMAs here measured 9.40 -> 9.53 ms: the
-                // operand swaps and extra spills cost more than they saved)
-#pragma unroll
-                for (int k = 0; k < kRowsPerWarp; ++k) {
-                    if (ok[k]) {
-                        if (!RESIDUAL) {
-                            pr[k] = fmaf(en.pw, kv[k].x, pr[k]);
-                            pi[k] = fmaf(en.tpw, kv[k].y, pi[k]);
-                        }
-                        dr[k] = fmaf(-en.tvi, kv[k].y, fmaf(en.vr, kv[k].x, dr[k]));
-                        di[k] = fmaf(en.vi, kv[k].x, fmaf(en.tvr, kv[k].y, di[k]));
-                    }
+                for (int k = 0; k < kBandRows; ++k) {
+                    const int i = x0 + k - lx + sup;   // window row
+                    rows[k] = (i >= 0 && i < w) ? cube_a(i - sup, ox, q, a.cg) : -1;
                 }
             }
-            __syncthreads();
+            __syncwarp();
+            // 2. accumulate the taken entries into the band: all the rows'
+            // kernel values are loaded (zero outside the window) before the
+            // paired FMAs
+            const int nt = __popc(bal);
+            for (int q = 0; q < nt; ++q) {
+                const BandEntry& E = ent[q];
+                const int col = E.cb + lane;
+                const bool colok = (unsigned)col < (unsigned)E.w;
+                const int bcol = colok ? cube_b(col - E.s, E.oy, E.q, a.cg) : 0;
+                const float2* kp = a.cube + E.base + bcol;
+                const int4 ra = *reinterpret_cast<const int4*>(&s_rows[warp][q][0]);
+                const int4 rb = *reinterpret_cast<const int4*>(&s_rows[warp][q][4]);
+                const int av[kBandRows] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+                float2 kv[kBandRows];
+#pragma unroll
+                for (int k = 0; k < kBandRows; ++k)
+                    kv[k] = (colok && av[k] >= 0) ? __ldg(kp + av[k]) : make_float2(0.f, 0.f);
+                const float4 vx = E.vx;
+                const float2 v1 = make_float2(vx.x, vx.y), v2 = make_float2(vx.z, vx.w);
+                const float2 pw = E.pw;
+#pragma unroll
+                for (int k = 0; k < kBandRows; ++k) {
+                    X[k] = __ffma2_rn(kv[k], v1, X[k]);
+                    Y[k] = __ffma2_rn(kv[k], v2, Y[k]);
+                    if (!RESIDUAL) P[k] = __ffma2_rn(kv[k], pw, P[k]);
+                }
+            }
+            __syncwarp();
         }
-        // 3. flush the tile
+        // 3. flush the band
 #pragma unroll
-        for (int k = 0; k < kRowsPerWarp; ++k) {
-            int64_t x = x0 + warp * kRowsPerWarp + k;
-            int64_t y = y0 + lane;
+        for (int k = 0; k < kBandRows; ++k) {
+            const int64_t x = x0 + k, y = y0 + lane;
             if (x < a.gnx && y < a.gny) {
-                int64_t cell = x * a.gny + y;
-                if (!RESIDUAL && (pr[k] != 0.0f || pi[k] != 0.0f))
-                    atomicAdd(&a.psf[cell], make_float2(pr[k], pi[k]));
-                if (dr[k] != 0.0f || di[k] != 0.0f)
-                    atomicAdd(&a.dirty[cell], make_float2(dr[k], di[k]));
+                const int64_t cell = x * a.gny + y;
+                const float2 d = make_float2(X[k].x + X[k].y, Y[k].x + Y[k].y);
+                if (!RESIDUAL && (P[k].x != 0.0f || P[k].y != 0.0f)) atomicAdd(&a.psf[cell], P[k]);
+                if (d.x != 0.0f || d.y != 0.0f) atomicAdd(&a.dirty[cell], d);
             }
         }
+        __syncwarp();
     }
 }
 
-// Work items: per output tile, the candidate records of its neighbourhood,
-// cut into chunks of kChunk.
-__global__ void tile_work_count(const uint32_t* tile_start, int64_t ntx, int64_t nty, int R,
-                                uint32_t* nchunks) {
-    int64_t ntiles = ntx * nty;
+// Per output tile: the segments of candidate records of its neighbourhood
+// (home tiles within R tiles), each trimmed to the records whose support can
+// reach the tile when supports grow with the plane index (records of a home
+// tile are sorted by plane); the work items are the tile's bands times the
+// chunks of kBandChunk candidates.
+__global__ void band_work_count(const uint32_t* tile_start, const int32_t* rplane,
+                                const int32_t* first_plane, int32_t max_support, int monotone,
+                                int64_t ntx, int64_t nty, int R, int64_t gnx,
+                                uint32_t* seg_lo, uint32_t* seg_pre, uint8_t* nseg,
+                                uint32_t* nitems) {
+    const int64_t ntiles = ntx * nty;
     for (int64_t T = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; T < ntiles;
          T += (int64_t)gridDim.x * blockDim.x) {
-        int64_t tx = T / nty, ty = T % nty;
-        uint64_t total = 0;
+        const int64_t tx = T / nty, ty = T % nty;
+        uint32_t total = 0;
+        int n = 0;
         for (int dx = -R; dx <= R; ++dx) {
-            int64_t hx = tx + dx;
+            const int64_t hx = tx + dx;
             if (hx < 0 || hx >= ntx) continue;
-            int64_t h0 = hx * nty + (ty - R < 0 ? 0 : ty - R);
-            int64_t h1 = hx * nty + (ty + R >= nty ? nty - 1 : ty + R);
-            total += tile_start[h1 + 1] - tile_start[h0];
+            for (int dy = -R; dy <= R; ++dy) {
+                const int64_t hy = ty + dy;
+                if (hy < 0 || hy >= nty) continue;
+                const int64_t h = hx * nty + hy;
+                uint32_t lo = tile_start[h];
+                const uint32_t hi = tile_start[h + 1];
+                if (lo >= hi) continue;
+                if (monotone) {
+                    const int ax = dx == 0 ? 0 : kTile * (abs(dx) - 1) + 1;
+                    const int ay = dy == 0 ? 0 : kTile * (abs(dy) - 1) + 1;
+                    const int need = max(ax, ay);
+                    if (need > max_support) continue;
+                    const int p = first_plane[need];
+                    uint32_t l = lo, u = hi;   // first record with plane >= p
+                    while (l < u) {
+                        const uint32_t m = l + ((u - l) >> 1);
+                        if (rplane[m] < p) l = m + 1; else u = m;
+                    }
+                    lo = l;
+                    if (lo >= hi) continue;
+                }
+                seg_lo[T * kNbr + n] = lo;
+                seg_pre[T * (kNbr + 1) + n] = total;
+                total += hi - lo;
+                ++n;
+            }
         }
-        nchunks[T] = (uint32_t)((total + kChunk - 1) / kChunk);
+        seg_pre[T * (kNbr + 1) + n] = total;
+        nseg[T] = (uint8_t)n;
+        const int64_t rows_left = gnx - tx * kTile;
+        const int64_t nb = (rows_left + kBandRows - 1) / kBandRows;
+        const int bands = (int)(nb < kBands ? nb : kBands);
+        nitems[T] = total ? (uint32_t)bands * ((total + kBandChunk - 1) / kBandChunk) : 0u;
     }
 }
 
-__global__ void tile_work_fill(const uint32_t* nchunks, const uint32_t* first, int64_t ntiles,
-                               uint32_t* item_tile, uint32_t* item_begin) {
+__global__ void band_work_fill(const uint32_t* nitems, const uint32_t* first, int64_t ntx,
+                               int64_t nty, int64_t gnx, uint2* items) {
+    const int64_t ntiles = ntx * nty;
     for (int64_t T = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; T < ntiles;
          T += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t c = nchunks[T], f = first[T];
-        for (uint32_t k = 0; k < c; ++k) {
-            item_tile[f + k] = (uint32_t)T;
-            item_begin[f + k] = k * kChunk;
-        }
+        const uint32_t n = nitems[T];
+        if (!n) continue;
+        const int64_t rows_left = gnx - (T / nty) * kTile;
+        const int64_t nb = (rows_left + kBandRows - 1) / kBandRows;
+        const uint32_t bands = (uint32_t)(nb < kBands ? nb : kBands);
+        const uint32_t chunks = n / bands, f = first[T];
+        // chunk-major, band-minor: the bands of one chunk are consecutive items
+        for (uint32_t ch = 0; ch < chunks; ++ch)
+            for (uint32_t b = 0; b < bands; ++b)
+                items[f + ch * bands + b] =
+                    make_uint2((uint32_t)T * kBands + b, ch * (uint32_t)kBandChunk);
     }
 }
 
@@ -806,47 +878,90 @@ void build_wproj(cr_ctx* ctx, cr_wproj* wp, double max_abs_w, int32_t planes,
     wp->info.sampling = sampling;
     wp->info.w_scale = w_scale;
     wp->info.max_support = *std::max_element(support.begin(), support.end());
+    // first plane whose support reaches S, for S = 0 .. max support (the
+    // gridder trims candidates that cannot reach a tile when supports grow
+    // with the plane index)
+    {
+        wp->support_monotone = std::is_sorted(support.begin(), support.end());
+        const int32_t ms = wp->info.max_support;
+        std::vector<int32_t> fp((size_t)ms + 1, planes);
+        for (int32_t S = 0; S <= ms; ++S)
+            for (int32_t p = 0; p < planes; ++p)
+                if (support[p] >= S) {
+                    fp[S] = p;
+                    break;
+                }
+        CR_CUDA_CHECK(cudaMalloc(&wp->first_plane_d, fp.size() * 4));
+        CR_CUDA_CHECK(cudaMemcpy(wp->first_plane_d, fp.data(), fp.size() * 4,
+                                 cudaMemcpyHostToDevice));
+    }
     wp->info.kernel_width = width;
     wp->info.cube_elements = total;
 }
 
 // ---- gridding / degridding drivers ------------------------------------------------------
+static void wproj_grid_band(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf,
+                            float2* dirty, int mode) {
+    const int64_t ntiles = r.ntx * r.nty;
+    const int R = (31 + wp->info.max_support) / kTile;
+    if (R > kMaxSegRadius) fail(CR_INVALID, "W-projection support above 127 is not supported");
+    const int64_t gnx = wp->g->info.grid_nx;
+    uint32_t* seg_lo = (uint32_t*)workspace(ctx, "wb_seg_lo", (size_t)ntiles * kNbr * 4);
+    uint32_t* seg_pre = (uint32_t*)workspace(ctx, "wb_seg_pre", (size_t)ntiles * (kNbr + 1) * 4);
+    uint8_t* nseg = (uint8_t*)workspace(ctx, "wb_nseg", (size_t)ntiles);
+    uint32_t* nitems = (uint32_t*)workspace(ctx, "wb_nitems", (size_t)ntiles * 4);
+    uint32_t* first = (uint32_t*)workspace(ctx, "wb_first", (size_t)ntiles * 4);
+    unsigned long long* total = (unsigned long long*)workspace(ctx, "wb_total", 16);
+    band_work_count<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(
+        r.tile_start, r.rec_a, wp->first_plane_d, wp->info.max_support,
+        wp->support_monotone ? 1 : 0, r.ntx, r.nty, R, gnx, seg_lo, seg_pre, nseg, nitems);
+    note_launch(ctx, "band_work_count");
+    exclusive_scan_u32(ctx, nitems, first, ntiles, total);
+    // every record is a candidate of at most (2R+1)^2 tiles; each tile has
+    // at most kBands items per started chunk
+    const size_t max_items = (size_t)kBands * ((size_t)ntiles +
+                             (size_t)((2 * R + 1) * (2 * R + 1)) *
+                                 (size_t)(r.n_samples / kBandChunk + 1));
+    uint2* items = (uint2*)workspace(ctx, "wb_items", max_items * 8);
+    band_work_fill<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(nitems, first, r.ntx,
+                                                                       r.nty, gnx, items);
+    note_launch(ctx, "band_work_fill");
+    unsigned int* counter = (unsigned int*)(total + 1);
+    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 4, ctx->stream));
+    const size_t nrec = (size_t)std::max<int64_t>(r.n_samples, 1);
+    uint4* packed = (uint4*)workspace(ctx, "wb_packed", nrec * 16);
+    float* weight = (float*)workspace(ctx, "wb_weight", nrec * 4);
+    if (mode == 0)
+        band_pack_kernel<false><<<grid_blocks(r.n_samples, 256), 256, 0, ctx->stream>>>(
+            r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum, r.rec_pred,
+            wp->support_d, wp->axis, r.counts, packed, weight);
+    else
+        band_pack_kernel<true><<<grid_blocks(r.n_samples, 256), 256, 0, ctx->stream>>>(
+            r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum, r.rec_pred,
+            wp->support_d, wp->axis, r.counts, packed, weight);
+    note_launch(ctx, "band_pack_kernel");
+    BandArgs a{packed, weight, wp->cube_off_d, wp->cube_q_d, wp->cube_d, cube_geom(wp),
+               wp->radius, r.nty, seg_lo, seg_pre, nseg, items, total, counter, psf, dirty, gnx,
+               wp->g->info.grid_ny};
+    auto kern = mode == 0 ? wp_grid_kernel<false> : wp_grid_kernel<true>;
+    CR_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
+    int per_sm = 0;
+    CR_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBandWarps * 32, 0));
+    const int blocks = sm_count(ctx) * std::max(per_sm, 1);
+    kernel_mark(ctx, 0, false);
+    kern<<<blocks, kBandWarps * 32, 0, ctx->stream>>>(a);
+    note_launch(ctx, mode == 0 ? "wp_grid_kernel" : "wp_grid_kernel_residual");
+    kernel_mark(ctx, 0, true);
+}
+
 void wproj_grid(cr_ctx* ctx, cr_wproj* wp, const Records& r, float2* psf, float2* dirty,
                 int mode) {
-    const int64_t ntiles = r.ntx * r.nty;
-    int R = (31 + wp->info.max_support) / kTile;
-    if (R > kMaxSegRadius) fail(CR_INVALID, "W-projection support above 127 is not supported");
-    uint32_t* nchunks = (uint32_t*)workspace(ctx, "wg_nchunks", (size_t)ntiles * 4);
-    uint32_t* first = (uint32_t*)workspace(ctx, "wg_first", (size_t)ntiles * 4);
-    unsigned long long* nitems = (unsigned long long*)workspace(ctx, "wg_nitems", 16);
-    tile_work_count<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(r.tile_start, r.ntx, r.nty,
-                                                                        R, nchunks);
-    note_launch(ctx, "tile_work_count");
-    exclusive_scan_u32(ctx, nchunks, first, ntiles, nitems);
-    // upper bound on the items: every candidate list chunked
-    size_t max_items = (size_t)ntiles + (size_t)((2 * R + 1) * (2 * R + 1)) *
-                                            (size_t)(r.n_samples / kChunk + 1);
-    uint32_t* item_tile = (uint32_t*)workspace(ctx, "wg_item_tile", max_items * 4);
-    uint32_t* item_begin = (uint32_t*)workspace(ctx, "wg_item_begin", max_items * 4);
-    tile_work_fill<<<grid_blocks(ntiles, 256), 256, 0, ctx->stream>>>(nchunks, first, ntiles,
-                                                                       item_tile, item_begin);
-    note_launch(ctx, "tile_work_fill");
-    unsigned int* counter = (unsigned int*)(nitems + 1);
-    CR_CUDA_CHECK(cudaMemsetAsync(counter, 0, 4, ctx->stream));
-    GridArgs a{r.rec_x, r.rec_y, r.rec_a, r.rec_b, r.rec_conj, r.rec_vsum, r.rec_wsum,
-               r.rec_pred, r.tile_start, r.ntx, r.nty, wp->support_d, wp->cube_off_d,
-               wp->cube_q_d, wp->cube_d, cube_geom(wp), wp->radius, wp->axis, R, item_tile,
-               item_begin, nitems, counter, psf, dirty, wp->g->info.grid_nx, wp->g->info.grid_ny};
-    int blocks = sm_count(ctx) * 8;
-    kernel_mark(ctx, 0, false);
-    if (mode == 0) {
-        wp_grid_kernel<false><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
-        note_launch(ctx, "wp_grid_kernel");
-    } else {
-        wp_grid_kernel<true><<<blocks, kGridThreads, 0, ctx->stream>>>(a);
-        note_launch(ctx, "wp_grid_kernel_residual");
-    }
-    kernel_mark(ctx, 0, true);
+    if (!band_pack_fits(std::max(wp->g->info.grid_nx, wp->g->info.grid_ny), wp->info.planes,
+                        wp->radius, wp->info.max_support))
+        fail(CR_INVALID, "W-projection gridding needs grid sides of at most 65536 cells, at "
+                         "most 4096 planes, oversampling below 63 and supports up to 127");
+    wproj_grid_band(ctx, wp, r, psf, dirty, mode);
 }
 
 void wproj_degrid(cr_ctx* ctx, cr_wproj* wp, const Records& r, const float2* grid) {
