@@ -167,16 +167,17 @@ def measured_peaks():
 
 
 def cpu_rate(obs, kernels, norm, support, w_scale, model_grid, budget_s=12.0):
-    """Oracle (the C restatement of the reference CPU path, multi-threaded like
-    the reference) timed on host cores: grid + degrid of a bounded, evenly
-    strided sample of the same rows, with the same kernels."""
+    """The reference CPU path restated in C (multi-threaded like the reference,
+    in its Complex32 grid precision, gridder.rs:3680-3747) timed on host
+    cores: grid + degrid of a bounded, evenly strided sample of the same rows,
+    with the same kernels."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     geom = O.Geometry(obs.nx, obs.ny, obs.cell, obs.cell)
     og = O.StdGridder(geom, 100)
     wp = O.WProjector.from_arrays(geom, og, w_scale, support, kernels.astype(np.complex128),
                                   norm.astype(np.float64), SAMPLING)
-    mg = np.asarray(model_grid, np.complex128)
+    mg = np.asarray(model_grid, np.complex64)
     rng = np.random.default_rng(SEED)
     vis = (rng.normal(size=len(obs.u)) + 1j * rng.normal(size=len(obs.u))).astype(np.complex64)
     wt = np.ones(len(obs.u), np.float32)
@@ -185,8 +186,8 @@ def cpu_rate(obs, kernels, norm, support, w_scale, model_grid, budget_s=12.0):
         sl = slice(0, None, stride)
         u, v, w = obs.u[sl], obs.v[sl], obs.w[sl]
         t0 = time.perf_counter()
-        _, _, acc = wp.grid_dirty(u, v, w, wt[sl], vis[sl], threads=threads)
-        wp.degrid(mg, u, v, w, threads=threads)
+        _, _, acc = wp.grid_dirty_f32(u, v, w, wt[sl], vis[sl], threads=threads)
+        wp.degrid_f32(mg, u, v, w, threads=threads)
         return acc.gridded, time.perf_counter() - t0
 
     # The reference scheme allocates, zeroes and merges one full grid pair per
@@ -479,9 +480,11 @@ def run_major_minor(args, ctx, dev):
 
 
 def run_reference(args):
-    """Reference arm: the reference's CPU path (restated in C, the oracle; the
-    Rust original cannot be built here) on the host cores, with its own FP64
-    W-kernels, timed per step on a bounded sample of the same workload."""
+    """Reference arm: the reference's CPU path (restated in C; the Rust
+    original cannot be built here) on the host cores, with W-kernels built by
+    the FP64 oracle and gridded / degridded in the reference's Complex32
+    precision, timed per step on a bounded sample of the same workload and
+    extrapolated to all rows by t = a + b rows (the sample line says how)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -496,15 +499,16 @@ def run_reference(args):
     n_all = len(obs.u)
     vis = (rng.normal(size=n_all) + 1j * rng.normal(size=n_all)).astype(np.complex64)
     wt = np.ones(n_all, np.float32)
-    mg = np.zeros((og.gnx, og.gny), np.complex128)
+    mg = np.zeros((og.gnx, og.gny), np.complex64)
     mg[og.gnx // 2, og.gny // 2] = 1.0
     stride = 400  # ~12.6k rows per step
 
     def step(stride):
         sl = slice(0, None, stride)
         t0 = time.perf_counter()
-        _, _, acc = wp.grid_dirty(obs.u[sl], obs.v[sl], obs.w[sl], wt[sl], vis[sl], threads=threads)
-        wp.degrid(mg, obs.u[sl], obs.v[sl], obs.w[sl], threads=threads)
+        _, _, acc = wp.grid_dirty_f32(obs.u[sl], obs.v[sl], obs.w[sl], wt[sl], vis[sl],
+                                      threads=threads)
+        wp.degrid_f32(mg, obs.u[sl], obs.v[sl], obs.w[sl], threads=threads)
         return acc.gridded, time.perf_counter() - t0
 
     # The reference scheme's per-call cost has a fixed part (one full grid
@@ -529,7 +533,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot_t / max(args.steps, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 (the reference's Complex32 grids)",
+            "data": "synthetic",
             "config": {"workload": "W-proj dirty 4096^2, 5,054,400 rows, 128 planes, "
                                    "support 8-64, oversampling 8", "rows": n_all,
                        "sample_rows_per_step": tot_n // max(args.steps, 1)},
@@ -658,6 +663,16 @@ def main():
                  "degrid_per_s": sums.taps / (dk * 1e-3)},
         "clocks": clk.summary(),
     }
+    # the tap-rate ceiling: one L2-resident kernel value and three paired
+    # FMAs per tap, nothing else (cr_probe_tap_rate), on a buffer the size of
+    # this W-projector's kernel cube
+    floor_rate, _ = cc.probe_tap_rate(ctx, int(gw.info.cube_elements) * 8, 256)
+    result["roofline"]["tap_bound"] = {
+        "unit": "taps/s", "ceiling": floor_rate,
+        "grid_achieved": sums.taps / (gk * 1e-3), "grid_frac": sums.taps / (gk * 1e-3) / floor_rate,
+        "degrid_achieved": sums.taps / (dk * 1e-3),
+        "degrid_frac": sums.taps / (dk * 1e-3) / floor_rate,
+        "ceiling_kernel": "tap_probe_kernel: per tap one float2 L2 load + 3 paired FP32 FMAs"}
 
     if not args.no_e2e:
         # the reference-facing calls with host (pinned) buffers

@@ -1257,6 +1257,16 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
     return outs
 
 
+def probe_tap_rate(ctx: Context, buffer_bytes: int = 110 << 20, iters: int = 256):
+    """Taps per second of the W-projection tap work alone (cr_probe_tap_rate):
+    the ceiling that the gridding and degridding kernels are measured
+    against."""
+    rate, taps = C.c_double(), C.c_double()
+    call("cr_probe_tap_rate", ctx.handle, int(buffer_bytes), int(iters), C.byref(rate),
+         C.byref(taps))
+    return float(rate.value), float(taps.value)
+
+
 def robust_rms(ctx: Context, images, masks=None, planes=None):
     """robust_rms_jy_per_beam (lib.rs:74130-74183) on the device (cr_robust_rms).
 

@@ -579,6 +579,16 @@ int cr_robust_rms(cr_ctx* ctx, const float* images, const uint8_t* masks, int32_
                   int32_t nx, int32_t ny, int32_t location, const int32_t* planes,
                   int32_t nplanes, float* rms, double* madfm, int64_t* counts, char** err);
 
+/* Measurement, not imaging (no counterpart in the reference): the tap-rate
+ * ceiling of the W-projection gridding loop.  Runs only the irreducible work
+ * of a tap -- one float2 read from an L2-resident buffer of buffer_bytes
+ * (rows of 32 consecutive values at scattered addresses, as the kernel cube
+ * is read) and three paired FP32 FMAs into register accumulators -- for
+ * `iters` iterations of 8 rows per thread on every resident thread, and
+ * returns the taps per second of one timed launch and the taps it made. */
+int cr_probe_tap_rate(cr_ctx* ctx, int64_t buffer_bytes, int32_t iters,
+                      double* taps_per_second, double* taps, char** err);
+
 /* ---- allocation-free Hogbom minor cycle ----------------------------------
  * No counterpart in the reference.  The same minor cycle as cr_hogbom for
  * callers that may not allocate device memory once they run: for example a

@@ -1546,3 +1546,150 @@ float oc_robust_rms(const float* residual, const uint8_t* mask, int64_t n, doubl
     if (m == 0) return 0.0f;
     return (float)mad * 1.4826f;
 }
+
+/* ------------------------------------------------------------------------ */
+/* W-projection in the reference's own precision (timed CPU baseline)        */
+/* ------------------------------------------------------------------------ */
+/* grid_sample_planned_pair / degrid_sample_planned (gridder.rs:3680-3747)
+ * as the reference runs them: Complex32 kernels and grids, float32 complex
+ * products, iy outer and ix inner.  Per-thread private grids merged in order
+ * (lib.rs:71428-71540).  The FP64 functions above stay the checker; these
+ * are what the CPU baseline times. */
+typedef struct {
+    const oc_wproj* p;
+    const float* k32;
+    const double *u, *v, *w;
+    const float *weight, *sumwt_factor, *vis;
+    const uint8_t* gridable;
+    float** psf;
+    float** dirty;
+    oc_accum* acc;
+    const float* model;
+    float* pred;
+} oc_wp32_job;
+
+static void oc_wp32_grid_chunk(void* vctx, int64_t b, int64_t e, int32_t worker) {
+    oc_wp32_job* j = (oc_wp32_job*)vctx;
+    const oc_wproj* p = j->p;
+    float* psf = j->psf[worker];
+    float* dirty = j->dirty[worker];
+    oc_accum* acc = &j->acc[worker];
+    for (int64_t i = b; i < e; ++i) {
+        float wt = j->weight[i];
+        float f = j->sumwt_factor ? j->sumwt_factor[i] : 1.0f;
+        float vr = j->vis[2 * i], vi = j->vis[2 * i + 1];
+        if (!oc_wproj_sample_valid(j->gridable, i, wt, f, vr, vi, j->u[i], j->v[i], j->w[i])) {
+            acc->skipped++;
+            continue;
+        }
+        int64_t lx, ly, ox, oy;
+        int32_t pl, cj;
+        double nrm;
+        if (!oc_wproj_plan(p, j->u[i], j->v[i], j->w[i], &lx, &ly, &ox, &oy, &pl, &cj, &nrm)) {
+            acc->skipped++;
+            continue;
+        }
+        acc->normalization_sumwt += 2.0 * (double)wt * nrm;
+        acc->reported_sumwt += (double)wt * (double)f;
+        acc->gridded++;
+        const float dr = vr * wt, di = vi * wt;
+        const float* k = j->k32 + (size_t)pl * p->width * p->width * 2;
+        const int32_t s = p->support[pl];
+        const float sg = cj ? -1.0f : 1.0f;
+        for (int32_t iy = -s; iy <= s; ++iy) {
+            const int64_t ky = llabs((int64_t)iy * p->sampling + oy);
+            for (int32_t ix = -s; ix <= s; ++ix) {
+                const int64_t kx = llabs((int64_t)ix * p->sampling + ox);
+                const float kr = k[2 * (kx * p->width + ky)];
+                const float ki = sg * k[2 * (kx * p->width + ky) + 1];
+                const int64_t cell = (lx + ix) * p->gny + (ly + iy);
+                psf[2 * cell] += wt * kr;
+                psf[2 * cell + 1] += wt * ki;
+                dirty[2 * cell] += dr * kr - di * ki;
+                dirty[2 * cell + 1] += dr * ki + di * kr;
+            }
+        }
+    }
+}
+
+void oc_wproj_grid_dirty_f32(const oc_wproj* p, const float* kernels32, int64_t n,
+                             const double* u, const double* v, const double* w,
+                             const float* weight, const float* sumwt_factor,
+                             const uint8_t* gridable, const float* vis, float* psf_grid,
+                             float* dirty_grid, oc_accum* acc, int32_t nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if ((int64_t)nthreads > n) nthreads = (int32_t)(n > 0 ? n : 1);
+    const int64_t len = 2 * p->gnx * p->gny;
+    oc_wp32_job j = {p, kernels32, u, v, w, weight, sumwt_factor, vis, gridable,
+                     NULL, NULL, NULL, NULL, NULL};
+    j.psf = (float**)calloc((size_t)nthreads, sizeof(float*));
+    j.dirty = (float**)calloc((size_t)nthreads, sizeof(float*));
+    j.acc = (oc_accum*)calloc((size_t)nthreads, sizeof(oc_accum));
+    for (int32_t t = 0; t < nthreads; ++t) {
+        j.psf[t] = nthreads == 1 ? psf_grid : (float*)calloc((size_t)len, sizeof(float));
+        j.dirty[t] = nthreads == 1 ? dirty_grid : (float*)calloc((size_t)len, sizeof(float));
+    }
+    const int32_t used = oc_parallel_chunks(n, nthreads, oc_wp32_grid_chunk, &j);
+    memset(acc, 0, sizeof(*acc));
+    for (int32_t t = 0; t < used; ++t) {
+        acc->normalization_sumwt += j.acc[t].normalization_sumwt;
+        acc->reported_sumwt += j.acc[t].reported_sumwt;
+        acc->gridded += j.acc[t].gridded;
+        acc->skipped += j.acc[t].skipped;
+    }
+    if (nthreads > 1) {
+        for (int32_t t = 0; t < used; ++t)
+            for (int64_t c = 0; c < len; ++c) {
+                psf_grid[c] += j.psf[t][c];
+                dirty_grid[c] += j.dirty[t][c];
+            }
+        for (int32_t t = 0; t < nthreads; ++t) {
+            free(j.psf[t]);
+            free(j.dirty[t]);
+        }
+    }
+    free(j.psf);
+    free(j.dirty);
+    free(j.acc);
+}
+
+static void oc_wp32_degrid_chunk(void* vctx, int64_t b, int64_t e, int32_t worker) {
+    (void)worker;
+    oc_wp32_job* j = (oc_wp32_job*)vctx;
+    const oc_wproj* p = j->p;
+    for (int64_t i = b; i < e; ++i) {
+        int64_t lx, ly, ox, oy;
+        int32_t pl, cj;
+        double nrm;
+        j->pred[2 * i] = 0.0f;
+        j->pred[2 * i + 1] = 0.0f;
+        if (!oc_wproj_plan(p, j->u[i], j->v[i], j->w[i], &lx, &ly, &ox, &oy, &pl, &cj, &nrm))
+            continue;
+        const float* k = j->k32 + (size_t)pl * p->width * p->width * 2;
+        const int32_t s = p->support[pl];
+        const float sg = cj ? -1.0f : 1.0f;
+        float re = 0.0f, im = 0.0f;
+        for (int32_t iy = -s; iy <= s; ++iy) {
+            const int64_t ky = llabs((int64_t)iy * p->sampling + oy);
+            for (int32_t ix = -s; ix <= s; ++ix) {
+                const int64_t kx = llabs((int64_t)ix * p->sampling + ox);
+                const float kr = k[2 * (kx * p->width + ky)];
+                const float ki = -sg * k[2 * (kx * p->width + ky) + 1];
+                const int64_t cell = (lx + ix) * p->gny + (ly + iy);
+                const float gr = j->model[2 * cell], gi = j->model[2 * cell + 1];
+                re += kr * gr - ki * gi;
+                im += kr * gi + ki * gr;
+            }
+        }
+        j->pred[2 * i] = re;
+        j->pred[2 * i + 1] = im;
+    }
+}
+
+void oc_wproj_degrid_f32(const oc_wproj* p, const float* kernels32, const float* model_grid,
+                         int64_t n, const double* u, const double* v, const double* w,
+                         float* pred, int32_t nthreads) {
+    oc_wp32_job j = {p, kernels32, u, v, w, NULL, NULL, NULL, NULL, NULL, NULL, NULL,
+                     model_grid, pred};
+    oc_parallel_chunks(n, nthreads, oc_wp32_degrid_chunk, &j);
+}

@@ -153,6 +153,18 @@ int64_t oc_hogbom_plane(float* model, float* residual, const float* psf, const u
 void oc_subtract_shifted_psf(float* residual, const float* psf, int64_t nx, int64_t ny,
                              int64_t px, int64_t py, float component);
 
+/* W-projection grid / degrid in the reference's Complex32 precision (the
+ * timed CPU baseline; gridder.rs:3680-3747); kernels32 is the FP64 kernel
+ * array of `p` rounded to float32, grids are float32 complex */
+void oc_wproj_grid_dirty_f32(const oc_wproj* p, const float* kernels32, int64_t n,
+                             const double* u, const double* v, const double* w,
+                             const float* weight, const float* sumwt_factor,
+                             const uint8_t* gridable, const float* vis, float* psf_grid,
+                             float* dirty_grid, oc_accum* acc, int32_t nthreads);
+void oc_wproj_degrid_f32(const oc_wproj* p, const float* kernels32, const float* model_grid,
+                         int64_t n, const double* u, const double* v, const double* w,
+                         float* pred, int32_t nthreads);
+
 /* robust RMS of the n-sigma threshold (lib.rs:74130-74626) */
 void oc_mean_stddev(const float* v, int64_t n, double* mean_out, double* std_out);
 double oc_chauvenet_max_zscore(uint64_t npts);

@@ -109,6 +109,9 @@ def _declare(L):
                                        C.POINTER(_i64), C.POINTER(_f)]),
         "oc_hogbom_plane": (_i64, [_p, _p, _p, _p, _i64, _i64, _f, _f, _f, _f, _i64, C.c_int,
                                    _p, _p, _p, _p, C.POINTER(_i64)]),
+        "oc_wproj_grid_dirty_f32": (None, [C.POINTER(WpParams), _p, _i64, _p, _p, _p, _p, _p, _p,
+                                           _p, _p, _p, C.POINTER(Accum), _i32]),
+        "oc_wproj_degrid_f32": (None, [C.POINTER(WpParams), _p, _p, _i64, _p, _p, _p, _p, _i32]),
         "oc_mean_stddev": (None, [_p, _i64, C.POINTER(_d), C.POINTER(_d)]),
         "oc_chauvenet_max_zscore": (_d, [C.c_uint64]),
         "oc_chauvenet_clip": (_i64, [_p, _i64, _d, _i32]),
@@ -422,6 +425,35 @@ class WProjector:
                                 _ptr(weight), _ptr(sumwt_factor), _ptr(gridable), _ptr(vis),
                                 _ptr(res), C.byref(acc), threads)
         return res, acc
+
+    # the reference's Complex32 precision (timed CPU baseline) -------------
+    def _k32(self):
+        if getattr(self, "_kernels32", None) is None:
+            self._kernels32 = np.ascontiguousarray(self.kernels.astype(np.complex64))
+        return self._kernels32
+
+    def grid_dirty_f32(self, u, v, w, weight, vis, threads=1):
+        """grid_sample_planned_pair (gridder.rs:3702-3724) on Complex32 grids."""
+        n = len(u)
+        u, v, w = _c(u, np.float64), _c(v, np.float64), _c(w, np.float64)
+        weight, vis = _c(weight, np.float32), _c(vis, np.complex64)
+        g = self.gridder
+        psf = np.zeros((g.gnx, g.gny), np.complex64)
+        dirty = np.zeros((g.gnx, g.gny), np.complex64)
+        acc = Accum()
+        lib().oc_wproj_grid_dirty_f32(C.byref(self._p), _ptr(self._k32()), n, _ptr(u), _ptr(v),
+                                      _ptr(w), _ptr(weight), None, None, _ptr(vis), _ptr(psf),
+                                      _ptr(dirty), C.byref(acc), threads)
+        return psf, dirty, acc
+
+    def degrid_f32(self, model_grid, u, v, w, threads=1):
+        """degrid_sample_planned (gridder.rs:3726-3747) in Complex32."""
+        g = _c(model_grid, np.complex64)
+        u, v, w = _c(u, np.float64), _c(v, np.float64), _c(w, np.float64)
+        pred = np.zeros(len(u), np.complex64)
+        lib().oc_wproj_degrid_f32(C.byref(self._p), _ptr(self._k32()), _ptr(g), len(u), _ptr(u),
+                                  _ptr(v), _ptr(w), _ptr(pred), threads)
+        return pred
 
     # image-domain stages --------------------------------------------------
     def _sinc(self):
