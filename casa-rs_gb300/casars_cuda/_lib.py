@@ -169,6 +169,15 @@ SIGNATURES = {
     "cr_hogbom_plane": (C.c_int, [_p, _p, _p, _p, _p, _i32, _i32, _i32, _f, _f, _f, _f, _i64,
                                   _i32, _p, _p, _p, _p, C.POINTER(_i64), C.POINTER(_i64),
                                   _err]),
+    "cr_multiscale_create": (C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _i32, _f,
+                                       C.POINTER(_p), _err]),
+    "cr_multiscale_destroy": (None, [_p]),
+    "cr_multiscale_set_residual": (C.c_int, [_p, _p, _i32, _err]),
+    "cr_multiscale_residual": (C.c_int, [_p, _p, _i32, _err]),
+    "cr_multiscale_peak": (C.c_int, [_p, C.POINTER(_i32), C.POINTER(_f), _err]),
+    "cr_multiscale_minor_cycle": (C.c_int, [_p, _p, _i32, _f, _f, _f, _f, _i64, _p, _p, _p, _p,
+                                            _p, C.POINTER(_i64), C.POINTER(_i64),
+                                            C.POINTER(_i32), _err]),
     "cr_probe_tap_rate": (C.c_int, [_p, _i64, _i32, C.POINTER(_d), C.POINTER(_d), _err]),
     "cr_robust_rms": (C.c_int, [_p, _p, _p, _i32, _i32, _i32, _i32, _p, _i32, _p, _p, _p,
                                 _err]),

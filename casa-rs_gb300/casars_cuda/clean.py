@@ -245,6 +245,95 @@ def run_cotton_schwab(gridder, batch, cfg: CleanConfig, wproj=None,
                        thresholds, beam, restored, sidelobe, nsigs)
 
 
+def run_multiscale_cotton_schwab(gridder, batch, cfg: CleanConfig, scales,
+                                 small_scale_bias: float = 0.0, wproj=None,
+                                 max_psf_sidelobe: Optional[float] = None,
+                                 mask=None) -> CleanResult:
+    """run_multiscale_cotton_schwab (lib.rs:63543-63963): the deconvolver
+    state on the device (im.Multiscale: scale images, PSF cross terms,
+    residual convolved with every scale), one multiscale minor cycle per
+    major cycle on the device, the residual refreshed through one
+    materialised plan and the convolved residuals rebuilt from it, with the
+    reference's stop, n-sigma and divergence rules.  Components are
+    ((x, y), flux) as for Hogbom, with result.component_scales the scale index
+    of each."""
+    psf, residual, state, _ = im.dirty_image(gridder, batch, wproj)
+    plan = im.Plan(gridder, batch, wproj)
+    geom = gridder.geometry
+    cell = (geom.cell_x_rad, geom.cell_y_rad)
+    beam, fitted_sidelobe = psf_beam_and_sidelobe(gridder.ctx, psf, cell, cfg.psf_cutoff)
+    sidelobe = fitted_sidelobe if max_psf_sidelobe is None else max_psf_sidelobe
+    ctx = gridder.ctx
+    ms = im.Multiscale(ctx, psf, scales, small_scale_bias, mask)
+    ms.set_residual(residual)
+    model = _zeros_like(residual)
+    actual = reported = major = 0
+    stop = None
+    min_peak = np.float32(_absmax(residual))
+    needs_refresh = False
+    comps, comp_scales, thresholds, nsigs = [], [], [], []
+    try:
+        while reported < cfg.niter:
+            if cfg.major_cycle_limit is not None and major >= cfg.major_cycle_limit:
+                stop = "MajorCycleLimitReached"
+                break
+            has, peak = ms.peak()
+            if not has:
+                stop = "NoCleanablePixels"
+                break
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma, mask)
+            nsigs.append(nsig)
+            s = tolerant_clean_stop_reason(peak, cfg.threshold_jy_per_beam, nsig)
+            if s is not None:
+                stop = s
+                break
+            cycle_niter = min(cfg.niter - reported, cfg.minor_cycle_length)
+            thr = clean_cycle_threshold(peak, sidelobe, cfg)
+            thresholds.append(thr)
+            out = ms.minor_cycle(model, cfg.gain, cycle_niter, cfg.threshold_jy_per_beam, thr,
+                                 nsig)
+            comps.extend(zip(map(tuple, out.positions.tolist()), out.fluxes.tolist()))
+            comp_scales.extend(out.scales.tolist())
+            actual += out.actual_updates
+            reported += out.reported_updates
+            if out.actual_updates == 0:
+                stop = out.stop_reason
+                break
+            residual = ms.residual()
+            needs_refresh = True
+            minor_peak = np.float32(_absmax(residual))
+            if minor_peak < min_peak:
+                min_peak = minor_peak
+            elif min_peak > 0 and (minor_peak - min_peak) / min_peak > np.float32(0.1):
+                stop = "DivergenceDetected"
+                break
+            if stop is None and reported >= cfg.niter:
+                stop = "IterationLimitReached"
+                break
+            residual = plan.residual_image(model, state)
+            ms.set_residual(residual)
+            major += 1
+            needs_refresh = False
+            nsig = im.nsigma_threshold(ctx, residual, cfg.nsigma, mask)
+            s = tolerant_clean_stop_reason(_absmax(residual), cfg.threshold_jy_per_beam, nsig)
+            if s is not None:
+                stop = s
+                break
+        if cfg.niter > 0 and stop is None:
+            stop = "IterationLimitReached"
+        if needs_refresh:
+            residual = plan.residual_image(model, state)
+            major += 1
+    finally:
+        plan.close()
+        ms.close()
+    restored = im.restore(ctx, model, residual, cell, beam) if beam is not None else None
+    res = CleanResult(model, residual, psf, state, major, actual, reported, stop, comps,
+                      thresholds, beam, restored, sidelobe, nsigs)
+    res.component_scales = comp_scales
+    return res
+
+
 # ----------------------------------------------------------------------------
 # cube CLEAN
 # ----------------------------------------------------------------------------

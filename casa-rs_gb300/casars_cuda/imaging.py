@@ -1257,6 +1257,95 @@ def run_hogbom_planes(ctx: Context, models, residuals, psfs, planes, gain: float
     return outs
 
 
+@dataclass
+class MultiscaleOutcome:
+    """One multiscale minor cycle: components (x, y), their scale indices,
+    strengths and fluxes, the updates made and reported, the stop reason."""
+    positions: np.ndarray
+    scales: np.ndarray
+    strengths: np.ndarray
+    fluxes: np.ndarray
+    actual_updates: int
+    reported_updates: int
+    stop_reason: Optional[str]
+
+
+class Multiscale:
+    """run_multiscale_cotton_schwab's deconvolver state on the device
+    (cr_multiscale_*, lib.rs:64172-64230): the scale images, the PSF
+    convolved with scale k then scale l, and the residual convolved with
+    every scale.  Images are numpy arrays or torch CUDA tensors."""
+
+    def __init__(self, ctx: Context, psf, scales, small_scale_bias: float = 0.0, mask=None):
+        self.ctx = ctx
+        self.shape = tuple(psf.shape)
+        arrs = _Arrays()
+        pp = arrs.ptr(psf, np.float32, torch.float32 if torch else None, self.shape)
+        mp = arrs.ptr(mask, np.uint8, torch.uint8 if torch else None, self.shape)
+        self._device = arrs.location == CR_DEVICE
+        sc = np.ascontiguousarray(np.asarray(list(scales), np.float32))
+        h = C.c_void_p()
+        call("cr_multiscale_create", ctx.handle, pp, mp, self.shape[0], self.shape[1],
+             arrs.location, sc.ctypes.data if len(sc) else None, len(sc),
+             float(small_scale_bias), C.byref(h))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().cr_multiscale_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_residual(self, residual):
+        arrs = _Arrays()
+        rp = arrs.ptr(residual, np.float32, torch.float32 if torch else None, self.shape)
+        call("cr_multiscale_set_residual", self._h, rp, arrs.location)
+
+    def residual(self):
+        """The residual convolved with scale 0 (the deconvolver's residual)."""
+        if self._device:
+            out = torch.empty(self.shape, dtype=torch.float32, device="cuda")
+            call("cr_multiscale_residual", self._h, C.c_void_p(out.data_ptr()), CR_DEVICE)
+        else:
+            out = np.empty(self.shape, np.float32)
+            call("cr_multiscale_residual", self._h, out.ctypes.data, CR_HOST)
+        return out
+
+    def peak(self):
+        """(any scale has a candidate, masked peak |residual|)."""
+        has, pk = C.c_int32(), C.c_float()
+        call("cr_multiscale_peak", self._h, C.byref(has), C.byref(pk))
+        return bool(has.value), float(pk.value)
+
+    def minor_cycle(self, model, gain: float, cycle_niter: int, threshold: float = 0.0,
+                    cycle_threshold: float = 0.0, nsigma_threshold: float = 0.0):
+        """One minor cycle; `model` (same kind as the PSF) is updated in place."""
+        arrs = _Arrays()
+        mp = arrs.ptr(model, np.float32, torch.float32 if torch else None, self.shape)
+        if arrs.location == CR_HOST and not (isinstance(model, np.ndarray) and
+                                              model.dtype == np.float32 and
+                                              model.flags["C_CONTIGUOUS"]):
+            raise ValueError("model must be a contiguous float32 array (updated in place)")
+        cap = max(int(cycle_niter), 1)
+        cx, cy, cs = (np.zeros(cap, np.int32) for _ in range(3))
+        cst, cfl = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+        actual, reported, stop = C.c_int64(), C.c_int64(), C.c_int32()
+        call("cr_multiscale_minor_cycle", self._h, mp, arrs.location, float(gain),
+             float(threshold), float(cycle_threshold), float(nsigma_threshold),
+             int(cycle_niter), cx.ctypes.data, cy.ctypes.data, cs.ctypes.data, cst.ctypes.data,
+             cfl.ctypes.data, C.byref(actual), C.byref(reported), C.byref(stop))
+        k = int(actual.value)
+        code = int(stop.value)
+        reason = "DivergenceDetected" if code == -1 else STOP_REASONS[code]
+        return MultiscaleOutcome(np.stack([cx[:k], cy[:k]], 1), cs[:k], cst[:k], cfl[:k], k,
+                                 int(reported.value), reason)
+
+
 def probe_tap_rate(ctx: Context, buffer_bytes: int = 110 << 20, iters: int = 256):
     """Taps per second of the W-projection tap work alone (cr_probe_tap_rate):
     the ceiling that the gridding and degridding kernels are measured

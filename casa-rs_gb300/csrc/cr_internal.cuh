@@ -245,6 +245,11 @@ void broadcast_pred(cr_ctx* ctx, const Records& r, float2* pred);
 // the cube gridding chunk sizes the tuner chooses from
 bool cube_grid_chunk_valid(uint32_t chunk);
 
+// ---- multiscale CLEAN (cr_msclean.cu) ----------------------------------------------
+void multiscale_create(cr_multiscale* ms, const float* psf, const uint8_t* mask,
+                       float small_scale_bias);
+void multiscale_set_residual(cr_multiscale* ms, const float* residual);
+
 // ---- robust RMS (n-sigma threshold) ----------------------------------------------
 // robust_rms_jy_per_beam of the listed planes of device images [P][npix]
 // (masks [P][npix] or null); rms / madfm / counts per listed plane (host).

@@ -61,6 +61,7 @@ typedef struct cr_wproj cr_wproj;
 typedef struct cr_plan cr_plan;
 typedef struct cr_cube_plan cr_cube_plan;
 typedef struct cr_accumulator cr_accumulator;
+typedef struct cr_multiscale cr_multiscale;
 
 /* ImageGeometry (types.rs:885-930). */
 typedef struct {
@@ -559,6 +560,44 @@ int cr_clark(cr_ctx* ctx, float* model, float* residual, const float* psf, const
              float threshold, float cycle_threshold, float nsigma_threshold, int64_t cycle_niter,
              int32_t* comp_x, int32_t* comp_y, float* comp_peak, float* comp_flux,
              int64_t* actual, int32_t* stop_reason, float* max_exterior_abs, char** err);
+
+/* ---- multiscale CLEAN ------------------------------------------------------
+ * run_multiscale_cotton_schwab's deconvolver state and minor cycle
+ * (crates/casa-imaging/src/lib.rs:63543-64405).  cr_multiscale_create builds
+ * the state of build_multiscale_state (lib.rs:64172-64230) from the PSF
+ * (nx x ny float32 at `location`), an optional clean mask (nonzero =
+ * cleanable; it then gives each scale its mask, lib.rs:64232-64261), the
+ * scale sizes in pixels (host array; none = the single scale 0,
+ * lib.rs:64164-64170; at most 16) and the small-scale bias.  The state
+ * lives on the device: the scale images, the PSF convolved with scale k
+ * then scale l, and the residual convolved with every scale.
+ * cr_multiscale_set_residual refreshes the convolved residuals after a major
+ * cycle (refresh_multiscale_dirty_conv_scales, lib.rs:63261-63267);
+ * cr_multiscale_residual copies out the residual convolved with scale 0 (the
+ * deconvolver's residual); cr_multiscale_peak reports whether any scale has
+ * a candidate and the masked peak |value| of that residual.
+ * cr_multiscale_minor_cycle runs one minor cycle (lib.rs:63700-63800) on the
+ * device: at most cycle_niter components, each gain * strength of the
+ * scale-biased best candidate, added to `model` (nx x ny float32 at
+ * `location`, updated in place) over the scale image's support and
+ * subtracted from every convolved residual inside the component's window.
+ * Component arrays (host, capacity cycle_niter, or all NULL) receive
+ * position, scale index, strength and flux; *stop_reason is a CR_STOP_*
+ * code, or -1 for the divergence rule (DivergenceDetected, lib.rs:64011-64023). */
+int cr_multiscale_create(cr_ctx* ctx, const float* psf, const uint8_t* mask, int32_t nx,
+                         int32_t ny, int32_t location, const float* scales, int32_t nscales,
+                         float small_scale_bias, cr_multiscale** out, char** err);
+void cr_multiscale_destroy(cr_multiscale* ms);
+int cr_multiscale_set_residual(cr_multiscale* ms, const float* residual, int32_t location,
+                               char** err);
+int cr_multiscale_residual(cr_multiscale* ms, float* out, int32_t location, char** err);
+int cr_multiscale_peak(cr_multiscale* ms, int32_t* has_candidate, float* peak0, char** err);
+int cr_multiscale_minor_cycle(cr_multiscale* ms, float* model, int32_t location, float gain,
+                              float threshold, float cycle_threshold, float nsigma_threshold,
+                              int64_t cycle_niter, int32_t* comp_x, int32_t* comp_y,
+                              int32_t* comp_scale, float* comp_strength, float* comp_flux,
+                              int64_t* actual, int64_t* reported, int32_t* stop_reason,
+                              char** err);
 
 /* Robust RMS of residual images for the n-sigma threshold:
  * robust_rms_jy_per_beam (crates/casa-imaging/src/lib.rs:74130-74183), the
