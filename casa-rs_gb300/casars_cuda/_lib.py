@@ -58,6 +58,24 @@ class Polarization(C.Structure):
                 ("sumwt_factor", _f)]
 
 
+class RowFeedConfig(C.Structure):
+    _fields_ = [("max_live_row_blocks", _i32), ("row_block_rows", _i64), ("channels", _i32),
+                ("correlations", _i32), ("lambda_scale", _p), ("polarization", Polarization),
+                ("has_flag", _i32), ("has_weight_spectrum", _i32), ("has_gridable", _i32)]
+
+
+class RowBlock(C.Structure):
+    _fields_ = [("slot", _i32), ("max_rows", _i64), ("uvw_m", _p), ("data", _p), ("flag", _p),
+                ("weight", _p), ("weight_spectrum", _p), ("gridable", _p)]
+
+
+class RowFeedSummary(C.Structure):
+    _fields_ = [("row_blocks", _i64), ("streamed_samples", _i64), ("source_bytes", _i64),
+                ("live_row_block_high_water", _i32), ("producer_send_blocked_s", _d),
+                ("consumer_recv_blocked_s", _d), ("consumer_elapsed_s", _d),
+                ("producer_consumer_overlap_s", _d)]
+
+
 class Beam(C.Structure):
     _fields_ = [("major_fwhm_rad", _d), ("minor_fwhm_rad", _d), ("position_angle_rad", _d)]
 
@@ -158,6 +176,12 @@ SIGNATURES = {
                                      C.POINTER(_f), _err]),
     "cr_row_runs_prepare": (C.c_int, [_p, C.POINTER(RowRuns), C.POINTER(Polarization), _p, _p, _p,
                                        _p, _p, _p, _p, _p, _p, _i32, C.POINTER(_i64), _err]),
+    "cr_row_feed_create": (C.c_int, [_p, _p, C.POINTER(RowFeedConfig), C.POINTER(_p), _err]),
+    "cr_row_feed_destroy": (None, [_p]),
+    "cr_row_feed_acquire": (C.c_int, [_p, C.POINTER(RowBlock), _err]),
+    "cr_row_feed_submit": (C.c_int, [_p, _i32, _i64, _err]),
+    "cr_row_feed_finish": (C.c_int, [_p, _p, _p, _i32, C.POINTER(PsfState), C.POINTER(Sums),
+                                     C.POINTER(RowFeedSummary), _err]),
     "cr_polarization_for_plane": (C.c_int, [_i32, _p, _i32, C.POINTER(Polarization), _err]),
     "cr_apply_weighting_rows": (C.c_int, [_p, _p, C.POINTER(VisBatch), _p, _p, _i32, _f, _p, _i32,
                                           _p, _err]),

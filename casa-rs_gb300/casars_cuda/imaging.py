@@ -949,6 +949,133 @@ class DirtyAccumulator:
             GridSums.from_c(s)
 
 
+@dataclass
+class ReadAheadSummary:
+    """ImagingSourceReadAheadSummary (casars-imager/src/lib.rs:36324-36335)."""
+    row_blocks: int
+    streamed_samples: int
+    source_bytes: int
+    live_row_block_high_water: int
+    producer_send_blocked_s: float
+    consumer_recv_blocked_s: float
+    consumer_elapsed_s: float
+    producer_consumer_overlap_s: float
+
+    @staticmethod
+    def from_c(s: _lib.RowFeedSummary) -> "ReadAheadSummary":
+        return ReadAheadSummary(int(s.row_blocks), int(s.streamed_samples), int(s.source_bytes),
+                                int(s.live_row_block_high_water), s.producer_send_blocked_s,
+                                s.consumer_recv_blocked_s, s.consumer_elapsed_s,
+                                s.producer_consumer_overlap_s)
+
+
+class RowBlockSlot:
+    """One page-locked staging slot of a RowFeed, as numpy views the reader
+    fills in place: uvw_m [max_rows][3], data [max_rows][channels][corr]
+    complex64, flag / weight_spectrum [max_rows][channels][corr], weight
+    [max_rows][corr], gridable [max_rows] (absent columns are None)."""
+
+    def __init__(self, blk: _lib.RowBlock, channels: int, correlations: int):
+        self.slot, self.max_rows = int(blk.slot), int(blk.max_rows)
+        r, c, k = self.max_rows, channels, correlations
+
+        def view(ptr, ctype, shape):
+            if not ptr:
+                return None
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape)
+
+        self.uvw_m = view(blk.uvw_m, C.c_double, (r, 3))
+        d = view(blk.data, C.c_float, (r, c, 2 * k))
+        self.data = d.view(np.complex64)
+        self.flag = view(blk.flag, C.c_uint8, (r, c, k))
+        self.weight = view(blk.weight, C.c_float, (r, k))
+        self.weight_spectrum = view(blk.weight_spectrum, C.c_float, (r, c, k))
+        self.gridable = view(blk.gridable, C.c_uint8, (r,))
+
+
+class RowFeed:
+    """The device side of stream_imaging_source_read_ahead_blocks
+    (casars-imager/src/lib.rs:36608-36760): MeasurementSet row blocks of one
+    spectral window pass through max_live_row_blocks page-locked slots; each
+    submitted block is uploaded on the feed's copy stream while the previous
+    one is prepared (cr_row_runs_prepare) and gridded into the streaming
+    accumulator (StandardMfsDirtyAccumulator) by the feed's worker thread.
+    Weights are used as given (natural weighting).  While the feed is open
+    its context belongs to the feed: make no other call on that context
+    before finish() returns."""
+
+    def __init__(self, gridder, lambda_scale, polarization: Polarization, correlations: int,
+                 row_block_rows: int, max_live_row_blocks: int = 2, has_flag: bool = True,
+                 has_weight_spectrum: bool = False, has_gridable: bool = False):
+        self.gridder = gridder
+        ls = np.ascontiguousarray(np.asarray(lambda_scale, np.float64))
+        self.channels, self.correlations = int(ls.shape[0]), int(correlations)
+        cfg = _lib.RowFeedConfig()
+        cfg.max_live_row_blocks = int(max_live_row_blocks)
+        cfg.row_block_rows = int(row_block_rows)
+        cfg.channels = self.channels
+        cfg.correlations = self.correlations
+        cfg.lambda_scale = ls.ctypes.data
+        cfg.polarization = polarization.to_c()
+        cfg.has_flag = 1 if has_flag else 0
+        cfg.has_weight_spectrum = 1 if has_weight_spectrum else 0
+        cfg.has_gridable = 1 if has_gridable else 0
+        gridder.ctx.use_own_stream()
+        h = C.c_void_p()
+        call("cr_row_feed_create", gridder.ctx.handle, gridder.handle, C.byref(cfg), C.byref(h))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().cr_row_feed_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def acquire(self) -> RowBlockSlot:
+        """The next free slot (waits while every slot is live)."""
+        blk = _lib.RowBlock()
+        call("cr_row_feed_acquire", self._h, C.byref(blk))
+        return RowBlockSlot(blk, self.channels, self.correlations)
+
+    def submit(self, slot: RowBlockSlot, rows: int):
+        """Queue the slot's first `rows` rows; 0 hands the slot back unused."""
+        call("cr_row_feed_submit", self._h, int(slot.slot), int(rows))
+
+    def finish(self):
+        """(psf, residual, PsfState, GridSums, ReadAheadSummary) of every
+        block submitted so far; the images are host arrays."""
+        g = self.gridder.geometry
+        psf = np.empty((g.nx, g.ny), np.float32)
+        res = np.empty((g.nx, g.ny), np.float32)
+        st, s, sm = _lib.PsfState(), _lib.Sums(), _lib.RowFeedSummary()
+        call("cr_row_feed_finish", self._h, psf.ctypes.data, res.ctypes.data, CR_HOST,
+             C.byref(st), C.byref(s), C.byref(sm))
+        return psf, res, PsfState(st.psf_peak, st.normalization_sumwt, st.reported_sumwt), \
+            GridSums.from_c(s), ReadAheadSummary.from_c(sm)
+
+
+def stream_row_blocks(feed: RowFeed, produce_next) -> int:
+    """The producer loop of stream_imaging_source_read_ahead_blocks
+    (casars-imager/src/lib.rs:36608-36760) over a RowFeed: produce_next(slot)
+    fills the slot's views with the next row block and returns its row count,
+    or None when the source is exhausted.  Returns the number of blocks
+    submitted; feed.finish() gives the images and the summary."""
+    blocks = 0
+    while True:
+        slot = feed.acquire()
+        rows = produce_next(slot)
+        if rows is None:
+            feed.submit(slot, 0)
+            return blocks
+        feed.submit(slot, rows)
+        blocks += 1
+
+
 class CubePlan:
     """A persistent cube plan (cr_cube_plan): the cube's weighting and records
     made once and replayed by gridding, degridding and residual calls -- the

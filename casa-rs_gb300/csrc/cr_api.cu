@@ -15,35 +15,6 @@ using namespace cr;
 
 namespace {
 
-void set_err(char** err, const std::string& msg) {
-    if (!err) return;
-    char* s = (char*)std::malloc(msg.size() + 1);
-    if (s) std::memcpy(s, msg.c_str(), msg.size() + 1);
-    *err = s;
-}
-
-template <class F>
-int guarded(char** err, F&& f) {
-    if (err) *err = nullptr;
-    try {
-        f();
-        return CR_OK;
-    } catch (const Error& e) {
-        set_err(err, e.what());
-        return e.code;
-    } catch (const std::exception& e) {
-        set_err(err, e.what());
-        return CR_INVALID;
-    } catch (...) {
-        set_err(err, "unknown error");
-        return CR_INVALID;
-    }
-}
-
-void need(bool c, const char* what) {
-    if (!c) fail(CR_INVALID, what);
-}
-
 struct StageTimer {
     cr_ctx* ctx;
     int n = 0;

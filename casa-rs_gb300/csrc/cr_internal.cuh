@@ -5,6 +5,8 @@
 #include <cufft.h>
 
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -27,6 +29,37 @@ void check_cuda(cudaError_t e, const char* what);
 void check_cufft(cufftResult r, const char* what);
 
 #define CR_CUDA_CHECK(call) ::cr::check_cuda((call), #call)
+
+// The C-ABI convention: *err receives a heap copy of the message (freed by
+// cr_free_error), the call returns the error's status code.
+inline void set_err(char** err, const std::string& msg) {
+    if (!err) return;
+    char* s = (char*)std::malloc(msg.size() + 1);
+    if (s) std::memcpy(s, msg.c_str(), msg.size() + 1);
+    *err = s;
+}
+
+template <class F>
+int guarded(char** err, F&& f) {
+    if (err) *err = nullptr;
+    try {
+        f();
+        return CR_OK;
+    } catch (const Error& e) {
+        set_err(err, e.what());
+        return e.code;
+    } catch (const std::exception& e) {
+        set_err(err, e.what());
+        return CR_INVALID;
+    } catch (...) {
+        set_err(err, "unknown error");
+        return CR_INVALID;
+    }
+}
+
+inline void need(bool c, const char* what) {
+    if (!c) fail(CR_INVALID, what);
+}
 
 struct DevBuf {
     void* ptr = nullptr;

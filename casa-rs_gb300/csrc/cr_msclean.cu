@@ -592,28 +592,11 @@ void multiscale_minor_cycle(cr_multiscale* ms, float* model, float gain, float t
 }  // namespace cr
 
 // ---- C ABI -------------------------------------------------------------------------
-namespace {
-template <typename F>
-int ms_guarded(char** err, F&& f) {
-    if (err) *err = nullptr;
-    try {
-        f();
-        return CR_OK;
-    } catch (const cr::Error& e) {
-        if (err) *err = strdup(e.what());
-        return e.code;
-    } catch (const std::exception& e) {
-        if (err) *err = strdup(e.what());
-        return CR_INVALID;
-    }
-}
-}  // namespace
-
 extern "C" int cr_multiscale_create(cr_ctx* ctx, const float* psf, const uint8_t* mask,
                                     int32_t nx, int32_t ny, int32_t location,
                                     const float* scales, int32_t nscales,
                                     float small_scale_bias, cr_multiscale** out, char** err) {
-    return ms_guarded(err, [&] {
+    return cr::guarded(err, [&] {
         if (!ctx || !psf || !out) cr::fail(CR_INVALID, "null argument");
         *out = nullptr;
         if (nx <= 1 || ny <= 1) cr::fail(CR_INVALID, "image shape must be at least 2 x 2");
@@ -659,7 +642,7 @@ extern "C" void cr_multiscale_destroy(cr_multiscale* ms) {
 
 extern "C" int cr_multiscale_set_residual(cr_multiscale* ms, const float* residual,
                                           int32_t location, char** err) {
-    return ms_guarded(err, [&] {
+    return cr::guarded(err, [&] {
         if (!ms || !residual) cr::fail(CR_INVALID, "null argument");
         CR_CUDA_CHECK(cudaSetDevice(ms->ctx->device));
         const float* r = (const float*)cr::device_input(
@@ -671,7 +654,7 @@ extern "C" int cr_multiscale_set_residual(cr_multiscale* ms, const float* residu
 
 extern "C" int cr_multiscale_residual(cr_multiscale* ms, float* out, int32_t location,
                                       char** err) {
-    return ms_guarded(err, [&] {
+    return cr::guarded(err, [&] {
         if (!ms || !out) cr::fail(CR_INVALID, "null argument");
         CR_CUDA_CHECK(cudaSetDevice(ms->ctx->device));
         cr::copy_out(ms->ctx, out, ms->dirty, (size_t)ms->nx * ms->ny * 4, location);
@@ -681,7 +664,7 @@ extern "C" int cr_multiscale_residual(cr_multiscale* ms, float* out, int32_t loc
 
 extern "C" int cr_multiscale_peak(cr_multiscale* ms, int32_t* has_candidate, float* peak0,
                                   char** err) {
-    return ms_guarded(err, [&] {
+    return cr::guarded(err, [&] {
         if (!ms) cr::fail(CR_INVALID, "null argument");
         CR_CUDA_CHECK(cudaSetDevice(ms->ctx->device));
         cr::multiscale_peak(ms, has_candidate, peak0);
@@ -695,7 +678,7 @@ extern "C" int cr_multiscale_minor_cycle(cr_multiscale* ms, float* model, int32_
                                          float* comp_strength, float* comp_flux,
                                          int64_t* actual, int64_t* reported,
                                          int32_t* stop_reason, char** err) {
-    return ms_guarded(err, [&] {
+    return cr::guarded(err, [&] {
         if (!ms || !model) cr::fail(CR_INVALID, "null argument");
         if (!comp_x != !comp_y || !comp_x != !comp_scale || !comp_x != !comp_strength ||
             !comp_x != !comp_flux)

@@ -57,6 +57,11 @@ pub struct cr_multiscale {
 }
 
 #[repr(C)]
+pub struct cr_row_feed {
+    _private: [u8; 0],
+}
+
+#[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
 pub struct cr_geometry {
     pub nx: i32,
@@ -174,6 +179,46 @@ pub struct cr_cube_batch {
 }
 
 #[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct cr_row_feed_config {
+    pub max_live_row_blocks: i32,
+    pub row_block_rows: i64,
+    pub channels: i32,
+    pub correlations: i32,
+    pub lambda_scale: *const f64,
+    pub polarization: cr_polarization,
+    pub has_flag: i32,
+    pub has_weight_spectrum: i32,
+    pub has_gridable: i32,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct cr_row_block {
+    pub slot: i32,
+    pub max_rows: i64,
+    pub uvw_m: *mut f64,
+    pub data: *mut f32,
+    pub flag: *mut u8,
+    pub weight: *mut f32,
+    pub weight_spectrum: *mut f32,
+    pub gridable: *mut u8,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct cr_row_feed_summary {
+    pub row_blocks: i64,
+    pub streamed_samples: i64,
+    pub source_bytes: i64,
+    pub live_row_block_high_water: i32,
+    pub producer_send_blocked_s: f64,
+    pub consumer_recv_blocked_s: f64,
+    pub consumer_elapsed_s: f64,
+    pub producer_consumer_overlap_s: f64,
+}
+
+#[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
 pub struct cr_beam {
     pub major_fwhm_rad: f64,
@@ -238,6 +283,11 @@ extern "C" {
     pub fn cr_row_runs_prepare(ctx: *mut cr_ctx, runs: *const cr_row_runs, pol: *const cr_polarization, u: *mut f64, v: *mut f64, w: *mut f64, weight: *mut f32, sumwt_factor: *mut f32, gridable: *mut u8, vis: *mut f32, density_u: *mut f64, density_v: *mut f64, out_location: i32, n_out: *mut i64, err: *mut *mut c_char) -> c_int;
     pub fn cr_polarization_for_plane(plane: i32, corr_types: *const i32, correlations: i32, out: *mut cr_polarization, err: *mut *mut c_char) -> c_int;
     pub fn cr_apply_weighting_rows(ctx: *mut cr_ctx, g: *mut cr_gridder, batch: *const cr_vis_batch, density_u: *const f64, density_v: *const f64, mode: i32, robust: f32, out_weight: *mut f32, out_location: i32, f2: *mut f32, err: *mut *mut c_char) -> c_int;
+    pub fn cr_row_feed_create(ctx: *mut cr_ctx, g: *mut cr_gridder, config: *const cr_row_feed_config, out: *mut *mut cr_row_feed, err: *mut *mut c_char) -> c_int;
+    pub fn cr_row_feed_destroy(feed: *mut cr_row_feed);
+    pub fn cr_row_feed_acquire(feed: *mut cr_row_feed, block: *mut cr_row_block, err: *mut *mut c_char) -> c_int;
+    pub fn cr_row_feed_submit(feed: *mut cr_row_feed, slot: i32, rows: i64, err: *mut *mut c_char) -> c_int;
+    pub fn cr_row_feed_finish(feed: *mut cr_row_feed, psf: *mut f32, residual: *mut f32, out_location: i32, state: *mut cr_psf_state, total: *mut cr_sums, summary: *mut cr_row_feed_summary, err: *mut *mut c_char) -> c_int;
     pub fn cr_fit_beam(ctx: *mut cr_ctx, psf: *const f32, nx: i32, ny: i32, location: i32, cell_x_rad: f64, cell_y_rad: f64, cutoff: f32, beam: *mut cr_beam, fitted: *mut i32, attempts: *mut i32, cutoff_used: *mut f32, err: *mut *mut c_char) -> c_int;
     pub fn cr_restore(ctx: *mut cr_ctx, model: *const f32, residual: *const f32, nx: i32, ny: i32, location: i32, cell_x_rad: f64, cell_y_rad: f64, beam: *const cr_beam, restored: *mut f32, out_location: i32, err: *mut *mut c_char) -> c_int;
     pub fn cr_psf_sidelobe(ctx: *mut cr_ctx, psf: *const f32, nx: i32, ny: i32, location: i32, cell_x_rad: f64, cell_y_rad: f64, beam: *const cr_beam, level: *mut f32, err: *mut *mut c_char) -> c_int;

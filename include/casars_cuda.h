@@ -457,6 +457,82 @@ int cr_apply_weighting_rows(cr_ctx* ctx, cr_gridder* g, const cr_vis_batch* batc
                             float robust, float* out_weight, int32_t out_location, float* f2,
                             char** err);
 
+/* ---- row-block read-ahead feed ---------------------------------------------
+ * The device side of stream_imaging_source_read_ahead_blocks
+ * (casars-imager/src/lib.rs:36608-36760): a bounded read-ahead pipeline of
+ * MeasurementSet row blocks.  The caller's reader (the producer) fills one
+ * page-locked staging slot at a time with a row block's UVW, DATA, FLAG,
+ * WEIGHT or WEIGHT_SPECTRUM and FLAG_ROW columns in the layout of
+ * cr_row_runs and submits it; the slot is uploaded on the feed's own copy
+ * stream while the previous block is prepared and gridded, and a worker
+ * thread of the feed (the consumer) runs cr_row_runs_prepare and
+ * cr_accumulator_add on the context's stream for each block in submission
+ * order.  At most max_live_row_blocks blocks are live (acquired and not yet
+ * consumed; the reference's default read-ahead depth is 2,
+ * imaging_source_read_ahead_max_live_row_blocks, lib.rs:36542-36544);
+ * acquire waits for a slot when all are live, which is the reference's
+ * producer back-pressure.  Weights are used as given (natural weighting, as
+ * for cr_accumulator_*).  While a feed is between create and finish its
+ * context belongs to the feed's worker: the caller makes no other call on
+ * that context until finish returns. */
+typedef struct cr_row_feed cr_row_feed;
+typedef struct {
+    int32_t max_live_row_blocks;    /* staging slots, >= 1 */
+    int64_t row_block_rows;         /* rows per slot, >= 1 */
+    int32_t channels;               /* of the one spectral window fed */
+    int32_t correlations;
+    const double* lambda_scale;     /* host [channels]: CHAN_FREQ / c, copied */
+    cr_polarization polarization;   /* the plane's collapse (cr_polarization_for_plane) */
+    int32_t has_flag;               /* FLAG present */
+    int32_t has_weight_spectrum;    /* WEIGHT_SPECTRUM instead of WEIGHT */
+    int32_t has_gridable;           /* per-row gridable (not FLAG_ROW) present */
+} cr_row_feed_config;
+/* A staging slot: page-locked host arrays of max_rows rows in the layout of
+ * cr_row_runs; the absent columns are NULL. */
+typedef struct {
+    int32_t slot;
+    int64_t max_rows;
+    double* uvw_m;                  /* [rows][3] */
+    float* data;                    /* complex64 [rows][channels][correlations] */
+    uint8_t* flag;                  /* [rows][channels][correlations] */
+    float* weight;                  /* [rows][correlations] */
+    float* weight_spectrum;         /* [rows][channels][correlations] */
+    uint8_t* gridable;              /* [rows] */
+} cr_row_block;
+/* ImagingSourceReadAheadSummary (casars-imager/src/lib.rs:36324-36335):
+ * blocks consumed, samples prepared (kept), host bytes uploaded, the most
+ * blocks live at once, and wall times: acquire waiting for a free slot
+ * (producer_send_blocked), the worker waiting for a block
+ * (consumer_recv_blocked), the worker busy (consumer_elapsed), and the time
+ * a block was being filled while the worker was busy
+ * (producer_consumer_overlap). */
+typedef struct {
+    int64_t row_blocks;
+    int64_t streamed_samples;
+    int64_t source_bytes;
+    int32_t live_row_block_high_water;
+    double producer_send_blocked_s;
+    double consumer_recv_blocked_s;
+    double consumer_elapsed_s;
+    double producer_consumer_overlap_s;
+} cr_row_feed_summary;
+int cr_row_feed_create(cr_ctx* ctx, cr_gridder* g, const cr_row_feed_config* config,
+                       cr_row_feed** out, char** err);
+/* Stops the worker (blocks still queued are dropped) and frees the slots. */
+void cr_row_feed_destroy(cr_row_feed* feed);
+/* The next free slot (waits while max_live_row_blocks blocks are live).  A
+ * failure of an earlier block is reported here, by submit and by finish. */
+int cr_row_feed_acquire(cr_row_feed* feed, cr_row_block* block, char** err);
+/* Queues the acquired slot's first `rows` rows (0 <= rows <= max_rows);
+ * rows = 0 hands the slot back unused (not counted as a row block). */
+int cr_row_feed_submit(cr_row_feed* feed, int32_t slot, int64_t rows, char** err);
+/* Waits for every submitted block, then forms the normalised PSF and residual
+ * images from the accumulated grids (cr_accumulator_finish); CR_NO_SAMPLES
+ * when nothing usable was fed.  The feed can take more blocks afterwards. */
+int cr_row_feed_finish(cr_row_feed* feed, float* psf, float* residual, int32_t out_location,
+                       cr_psf_state* state, cr_sums* total, cr_row_feed_summary* summary,
+                       char** err);
+
 /* ---- restoring beam ---------------------------------------------------------
  * fit_beam_from_psf (beam.rs:27-103): the main lobe above `cutoff` (clamped
  * to [0.01, 0.99], lowered by 1.5x per failed attempt, at most 50 attempts),
