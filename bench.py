@@ -55,6 +55,10 @@ def parse():
                     help="skip the batched-cube versus per-channel-loop comparison")
     ap.add_argument("--cube-channels", type=int, default=256)
     ap.add_argument("--no-rows", action="store_true", help="skip the row-runs measurement")
+    ap.add_argument("--no-feed", action="store_true",
+                    help="skip the row-block read-ahead feed measurement")
+    ap.add_argument("--feed-only", action="store_true",
+                    help="run only the row-block feed measurement (profiling runs)")
     ap.add_argument("--no-major-minor", action="store_true",
                     help="skip the device-resident major/minor CLEAN loop")
     ap.add_argument("--cube-only", action="store_true",
@@ -431,6 +435,115 @@ def run_rows(args, ctx, dev, peak):
             "frac_of_measured_hbm": algo / (ms * 1e-3) / 1e9 / peak}
 
 
+def run_feed(args, ctx, dev):
+    """The row-block read-ahead feed (cr_row_feed_*): the cube's rows
+    (1,263,600, 27 antennas to 1 km, 10 h of 10 s dumps) with 16 channels
+    over 1.0-2.0 GHz and 4 correlations, 10 % flags, a weight spectrum,
+    Stokes I into a 1024^2 image, natural weights.  A producer copies each
+    block of 65,536 rows from host arrays (the reader's output) into the
+    feed's page-locked slot; the feed uploads it and prepares and grids it
+    on the device while the next block is filled.  Timed on the host clock
+    from the first acquire to the images of finish(), against the same work
+    with the whole input already on the device (one prepare, one
+    accumulation, finish) and against a read-ahead depth of 1."""
+    import time
+
+    import torch
+    import casars_cuda as cc
+    from casars_cuda import synthetic as S
+    obs = S.cube_observation(channels=16)
+    R, C, K = obs.rows, obs.channels, 4
+    rng = np.random.default_rng(31)
+    data = rng.standard_normal((R, C, 2 * K), dtype=np.float32).view(np.complex64)
+    flag = (rng.random((R, C, K), dtype=np.float32) < 0.1).astype(np.uint8)
+    spec = rng.random((R, C, K), dtype=np.float32) + np.float32(0.5)
+    uvw = np.stack([obs.u_m, obs.v_m, np.zeros_like(obs.u_m)], 1)
+    weight = np.ones((R, K), np.float32)
+    pol = cc.Polarization.for_plane("I", [9, 10, 11, 12])
+    geom = cc.ImageGeometry(obs.nx, obs.nx, obs.cell, obs.cell)
+    block = 65536
+    fill_s = [0.0]
+
+    def producer():
+        pos = [0]
+
+        def produce(slot):
+            r0 = pos[0]
+            if r0 >= R:
+                return None
+            t0 = time.perf_counter()
+            n = min(block, R - r0)
+            sl = slice(r0, r0 + n)
+            np.copyto(slot.uvw_m[:n], uvw[sl])
+            np.copyto(slot.data[:n], data[sl])
+            np.copyto(slot.flag[:n], flag[sl])
+            np.copyto(slot.weight[:n], weight[sl])
+            np.copyto(slot.weight_spectrum[:n], spec[sl])
+            pos[0] = r0 + n
+            fill_s[0] += time.perf_counter() - t0
+            return n
+
+        return produce
+
+    def fed(live):
+        gg = cc.StandardGridder(ctx, geom, 128)
+        feed = cc.RowFeed(gg, obs.lambda_scale, pol, K, block, live, has_flag=True,
+                          has_weight_spectrum=True)
+        try:
+            fill_s[0] = 0.0
+            t0 = time.perf_counter()
+            cc.stream_row_blocks(feed, producer())
+            psf, res, _, sums, summary = feed.finish()
+            return time.perf_counter() - t0, fill_s[0], sums, summary, res
+        finally:
+            feed.close()
+
+    fed(2)                                   # warm-up: plans, workspaces
+    runs = [fed(2) for _ in range(2)]
+    wall, fill, sums, summary, res = min(runs, key=lambda r: r[0])
+    wall1 = min(fed(1)[0] for _ in range(2))
+    # the same work with the whole input resident in HBM
+    tt = lambda a: torch.from_numpy(a).to(dev)
+    rr = cc.RowRuns(tt(uvw), obs.lambda_scale, tt(data), tt(flag), tt(weight), tt(spec), None)
+    gg = cc.StandardGridder(ctx, geom, 128)
+
+    def resident():
+        ctx.use_torch_stream()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b, _, _ = cc.prepare_row_runs(ctx, rr, pol)
+        acc = cc.DirtyAccumulator(gg)
+        acc.add(b)
+        _, r_img, _, s = acc.finish()
+        torch.cuda.synchronize()
+        out = time.perf_counter() - t0
+        acc.close()
+        return out, r_img, s
+
+    resident()
+    res_runs = [resident() for _ in range(2)]
+    t_res, r_img, s_res = min(res_runs, key=lambda r: r[0])
+    ctx.use_own_stream()
+    err = float(np.max(np.abs(res - r_img.cpu().numpy())) / max(np.max(np.abs(res)), 1e-30))
+    del rr
+    torch.cuda.empty_cache()
+    return {"workload": f"{R} rows x {C} channels x {K} correlations in blocks of {block} rows, "
+                        "Stokes I from XX+YY, 10 % flags, weight spectrum, 1024^2 image, "
+                        "natural weights, host arrays copied into the feed's slots",
+            "rows": R, "samples": R * C, "kept": summary.streamed_samples,
+            "gridded": sums.gridded_samples, "source_bytes": summary.source_bytes,
+            "wall_s": wall, "rows_per_s": R / wall, "source_gbs": summary.source_bytes / wall / 1e9,
+            "read_ahead": 2, "wall_s_read_ahead_1": wall1,
+            "producer_fill_s": fill, "consumer_elapsed_s": summary.consumer_elapsed_s,
+            "producer_send_blocked_s": summary.producer_send_blocked_s,
+            "consumer_recv_blocked_s": summary.consumer_recv_blocked_s,
+            "producer_consumer_overlap_s": summary.producer_consumer_overlap_s,
+            "live_row_block_high_water": summary.live_row_block_high_water,
+            "row_blocks": summary.row_blocks,
+            "device_resident_s": t_res, "residual_vs_device_resident": err,
+            "gridded_equal": int(s_res.gridded_samples) == int(sums.gridded_samples)}
+
+
 def run_major_minor(args, ctx, dev):
     """The device-resident major/minor loop: 2048^2 Stokes I, 10,108,800
     visibilities (21 km layout, 4 channels 1.3-1.5 GHz gridded together), 64
@@ -561,6 +674,9 @@ def main():
     dev = torch.device("cuda", local)
 
     ctx = cc.Context(local)
+    if args.feed_only:
+        print(json.dumps({"row_feed": run_feed(args, ctx, dev)}), flush=True)
+        return
     if args.cube_only:
         print(json.dumps({"cube": run_cube(args, ctx, dev, measured_peaks()[0])}), flush=True)
         return
@@ -716,6 +832,8 @@ def main():
         result["cube"] = run_cube(args, ctx, dev, peak)
     if not args.no_rows:
         result["row_runs"] = run_rows(args, ctx, dev, peak)
+    if not args.no_feed:
+        result["row_feed"] = run_feed(args, ctx, dev)
     if not args.no_major_minor:
         result["major_minor"] = run_major_minor(args, ctx, dev)
 
