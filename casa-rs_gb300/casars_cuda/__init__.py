@@ -11,7 +11,7 @@ from .imaging import (Context, GridSums, HogbomOutcome, ImageGeometry, Plan, Psf
                       run_hogbom_planes, run_clark_minor_cycle, clark_ncent,
                       DirtyAccumulator, hogbom_plane_minor_cycle, robust_rms, nsigma_threshold,
                       probe_tap_rate, Multiscale, MultiscaleOutcome, RowFeed, RowBlockSlot,
-                      ReadAheadSummary, stream_row_blocks)
+                      ReadAheadSummary, stream_row_blocks, append_hogbom_trace)
 from .clean import (CleanConfig, CleanResult, clean_cycle_threshold, run_cotton_schwab,  # noqa: F401
                     CubeCleanResult, cube_clean_loop, run_cube_clean, run_clark_cotton_schwab,
                     run_multiscale_cotton_schwab,

@@ -1572,12 +1572,43 @@ def hogbom_plane_minor_cycle(ctx: Context, model, residual, psf, gain: float, cy
                          int(reported.value), None)
 
 
+def append_hogbom_trace(components, peaks, fluxes, reffreq_hz: float = 0.0,
+                        first_update: int = 0, backend: str = "cuda") -> int:
+    """append_hogbom_trace (lib.rs:54046-54066): when CASA_RS_HOGBOM_TRACE
+    names a file, one JSON line per component is appended to it with the
+    reference's fields (event, backend, reffreq_hz, cycle_update, x, y, peak,
+    component; lib.rs:59795-59798, 60272-60275).  Returns the lines written."""
+    import json
+    import os
+    path = os.environ.get("CASA_RS_HOGBOM_TRACE")
+    if not path or len(peaks) == 0:
+        return 0
+    lines = []
+    for k in range(len(peaks)):
+        lines.append(json.dumps({"event": "component", "backend": backend,
+                                 "reffreq_hz": float(reffreq_hz),
+                                 "cycle_update": int(first_update + k),
+                                 "x": int(components[k][0]), "y": int(components[k][1]),
+                                 "peak": float(peaks[k]), "component": float(fluxes[k])},
+                                separators=(",", ":")))
+    try:
+        with open(path, "a") as f:
+            f.write("\n".join(lines) + "\n")
+    except OSError as e:
+        import sys
+        print(f"failed to append CASA_RS_HOGBOM_TRACE: {e}", file=sys.stderr)
+        return 0
+    return len(lines)
+
+
 def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycle_niter: int,
                            threshold: float = 0.0, cycle_threshold: float = 0.0,
                            nsigma_threshold: float = 0.0, mask=None,
-                           inclusive: bool = True) -> HogbomOutcome:
+                           inclusive: bool = True, reffreq_hz: float = 0.0) -> HogbomOutcome:
     """run_hogbom_minor_cycle_cpu_with_progress (lib.rs:59748-59883) on the
-    device.  model and residual are updated copies (the inputs are kept)."""
+    device.  model and residual are updated copies (the inputs are kept).
+    With CASA_RS_HOGBOM_TRACE set, the cycle's components are appended to
+    that file as the reference's trace lines (append_hogbom_trace)."""
     arrs, m, r, mp, rp, pp, kp, nx, ny = _hogbom_buffers(ctx, model, residual, psf, mask)
     cap = int(cycle_niter) + 1
     cx = np.zeros(cap, np.int32)
@@ -1590,5 +1621,7 @@ def run_hogbom_minor_cycle(ctx: Context, model, residual, psf, gain: float, cycl
          int(bool(inclusive)), cx.ctypes.data, cy.ctypes.data, cpk.ctypes.data, cfl.ctypes.data,
          C.byref(actual), C.byref(reported), C.byref(stop))
     k = int(actual.value)
-    return HogbomOutcome(m, r, np.stack([cx[:k], cy[:k]], 1), cpk[:k], cfl[:k], k,
+    comps = np.stack([cx[:k], cy[:k]], 1)
+    append_hogbom_trace(comps, cpk[:k], cfl[:k], reffreq_hz)
+    return HogbomOutcome(m, r, comps, cpk[:k], cfl[:k], k,
                          int(reported.value), STOP_REASONS[int(stop.value)])

@@ -42,6 +42,28 @@ def test_hogbom_kats(ctx):
     assert abs(out.model[3, 3] - 0.9) < 1e-6
 
 
+def test_hogbom_trace_lists_the_cycle_components(ctx, tmp_path, monkeypatch):
+    """CASA_RS_HOGBOM_TRACE: one line per component of the device cycle, in
+    order, with the returned positions, peaks and fluxes."""
+    path = tmp_path / "trace.jsonl"
+    monkeypatch.setenv("CASA_RS_HOGBOM_TRACE", str(path))
+    rng = np.random.default_rng(5)
+    res = (0.01 * rng.normal(size=(64, 64))).astype(np.float32)
+    res[20, 30] = 1.0
+    res[40, 12] = -0.7
+    psf = np.zeros((64, 64), np.float32)
+    psf[32, 32] = 1.0
+    out = cc.run_hogbom_minor_cycle(ctx, np.zeros_like(res), res, psf, 0.2, 25,
+                                    reffreq_hz=1.25e9)
+    lines = [json.loads(x) for x in path.read_text().splitlines()]
+    assert len(lines) == out.actual_updates > 0
+    for k, rec in enumerate(lines):
+        assert rec["event"] == "component" and rec["backend"] == "cuda"
+        assert rec["cycle_update"] == k and rec["reffreq_hz"] == 1.25e9
+        assert (rec["x"], rec["y"]) == tuple(int(v) for v in out.positions[k])
+        assert rec["peak"] == float(out.peaks[k]) and rec["component"] == float(out.fluxes[k])
+
+
 @pytest.mark.parametrize("shape,masked", [((64, 64), False), ((200, 150), True), ((512, 512), False)])
 def test_hogbom_bit_exact_against_oracle(ctx, shape, masked):
     rng = np.random.default_rng(3)
