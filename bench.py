@@ -824,7 +824,7 @@ def main():
                          "h2d_bytes_per_step": 2 * n * row_bytes + obs.nx * obs.ny * 4,
                          "d2h_bytes_per_step": 2 * obs.nx * obs.ny * 4 + n * 8,
                          "ms_per_step": e_ms, "calls": "cr_dirty_image + cr_predict",
-                         "image_fft": "f64",
+                         "image_fft": "f64-grade (float-pair transform kernels)",
                          "f32_image_fft": {"value": world * accepted / (e32_ms * 1e-3) / 1e6,
                                            "ms_per_step": e32_ms}}
 

@@ -163,6 +163,14 @@ class Context:
             raise ValueError(f"unsupported FFT precision {precision!r}")
         self._image_fft_bits = 32 if int(bits) == 32 else 64
 
+    def set_image_fft_engine(self, engine: str = "auto"):
+        """How the FP64-grade image transforms run: "auto" (float-pair
+        kernels where the grid allows, else cuFFT FP64) or "cufft" (always
+        cuFFT FP64)."""
+        code = {"auto": 0, "cufft": 1}[engine]
+        if self._lib.cr_ctx_set_image_fft_engine(self._h, code) != 0:
+            raise ValueError(f"unsupported FFT engine {engine!r}")
+
     @property
     def image_fft_precision(self) -> str:
         return "f32" if getattr(self, "_image_fft_bits", 64) == 32 else "f64"

@@ -1277,6 +1277,12 @@ int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits) {
     return CR_OK;
 }
 
+int cr_ctx_set_image_fft_engine(cr_ctx* ctx, int32_t engine) {
+    if (!ctx || (engine != 0 && engine != 1)) return CR_INVALID;
+    ctx->image_fft_engine = engine;
+    return CR_OK;
+}
+
 // ---- persistent cube plans --------------------------------------------------
 
 int cr_cube_plan_create(cr_ctx* ctx, cr_gridder* g, const cr_cube_batch* batch,

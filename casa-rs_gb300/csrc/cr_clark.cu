@@ -434,10 +434,12 @@ void clark_minor_cycle(cr_ctx* ctx, float* model, float* residual, const float* 
     CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     if (comp_x && updates > 0) {
         const size_t m = (size_t)updates * 4;
-        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, m, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, m, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, m, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, m, cudaMemcpyDeviceToHost));
+        // one synchronisation for the four lists, on the context's stream
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_x, cx, m, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_y, cy, m, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_peak, cp, m, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_flux, cf, m, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     }
     if (actual) *actual = updates;
     if (stop_out) *stop_out = stop;

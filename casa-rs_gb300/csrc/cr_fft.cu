@@ -228,13 +228,6 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
     const bool f64 = sizeof(S) == 8;
-    const int64_t nh = gnx * (gny / 2 + 1);
-    W* half = (W*)workspace(ctx, f64 ? "fft_h64" : "fft_h32", (size_t)nh * sizeof(W));
-    S* raw = (S*)workspace(ctx, f64 ? "fft_r64" : "fft_r32", (size_t)gnx * gny * sizeof(S));
-    hermitian_half_kernel<W><<<grid_blocks(nh, 256), 256, 0, ctx->stream>>>(
-        grid, real_grid, gnx, gny, half);
-    note_launch(ctx, "hermitian_half_kernel");
-    exec_c2r(ctx, gnx, gny, half, raw);
     int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
     double inv = 1.0 / ((double)gnx * (double)gny);
     const int64_t n = (int64_t)g->geom.nx * g->geom.ny;
@@ -246,6 +239,17 @@ static void grid_to_image_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
         sx = adjoint ? wp->sinc_gx_d : wp->sinc_x_d;
         sy = adjoint ? wp->sinc_gy_d : wp->sinc_x_d;
     }
+    if (f64 && ctx->image_fft_engine == 0 && dfft_supported(gnx, gny)) {
+        dfft_grid_to_image(ctx, g, grid, real_grid, inv * (double)scale, sx, sy, mode, image);
+        return;
+    }
+    const int64_t nh = gnx * (gny / 2 + 1);
+    W* half = (W*)workspace(ctx, f64 ? "fft_h64" : "fft_h32", (size_t)nh * sizeof(W));
+    S* raw = (S*)workspace(ctx, f64 ? "fft_r64" : "fft_r32", (size_t)gnx * gny * sizeof(S));
+    hermitian_half_kernel<W><<<grid_blocks(nh, 256), 256, 0, ctx->stream>>>(
+        grid, real_grid, gnx, gny, half);
+    note_launch(ctx, "hermitian_half_kernel");
+    exec_c2r(ctx, gnx, gny, half, raw);
     crop_correct_kernel<S><<<grid_blocks(n, 256), 256, 0, ctx->stream>>>(
         raw, gny, g->geom.nx, g->geom.ny, g->info.blc_x, g->info.blc_y, parity,
         inv * (double)scale, g->corr_x_d, g->corr_y_d, sx, sy, mode, image);
@@ -259,6 +263,11 @@ static void image_to_grid_impl(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const f
     const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
     if ((gnx & 1) || (gny & 1)) fail(CR_INVALID, "grid sizes must be even");
     const bool f64 = sizeof(S) == 8;
+    if (f64 && ctx->image_fft_engine == 0 && dfft_supported(gnx, gny)) {
+        dfft_image_to_grid(ctx, g, model, wp ? wp->sinc_gx_d : nullptr,
+                           wp ? wp->sinc_gy_d : nullptr, grid);
+        return;
+    }
     const int64_t nh = gnx * (gny / 2 + 1);
     W* half = (W*)workspace(ctx, f64 ? "fft_h64" : "fft_h32", (size_t)nh * sizeof(W));
     S* raw = (S*)workspace(ctx, f64 ? "fft_r64" : "fft_r32", (size_t)gnx * gny * sizeof(S));

@@ -437,10 +437,13 @@ void hogbom_plane(cr_ctx* ctx, float* model, float* residual, const float* psf,
     CR_CUDA_CHECK(cudaMemcpyAsync(&n, out_actual, 8, cudaMemcpyDeviceToHost, ctx->stream));
     CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     if (comp_x && n > 0) {
-        CR_CUDA_CHECK(cudaMemcpy(comp_x, cx, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_y, cy, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_peak, cp, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        CR_CUDA_CHECK(cudaMemcpy(comp_flux, cf, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        // one synchronisation for the four lists, on the context's stream
+        const size_t b = (size_t)n * 4;
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_x, cx, b, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_y, cy, b, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_peak, cp, b, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaMemcpyAsync(comp_flux, cf, b, cudaMemcpyDeviceToHost, ctx->stream));
+        CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
     }
     if (actual) *actual = n;
     // CasaInclusive reports at most the cycle limit when the budget ran out

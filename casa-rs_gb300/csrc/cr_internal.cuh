@@ -70,6 +70,7 @@ struct DevBuf {
 using Pool = std::map<std::string, DevBuf>;
 
 struct CubeGraph;   // a captured cube pipeline (cr_cube.cu)
+struct DfPlan;      // a float-pair transform plan for one line length (cr_dfft.cu)
 
 // Default bounds of the device-side waits: polls of a grid barrier (each
 // followed by a 64 ns sleep: about a second) and of an mbarrier (try_wait
@@ -110,6 +111,10 @@ struct cr_ctx {
     // Precision of the image-stage FFTs of single-plane calls: 64 (default)
     // or 32.
     int image_fft_bits = 64;
+    // How the FP64-grade image transforms run: 0 float-pair kernels where
+    // the grid allows (cr_dfft.cu), else cuFFT FP64; 1 always cuFFT FP64.
+    int image_fft_engine = 0;
+    std::map<int64_t, std::shared_ptr<cr::DfPlan>> df_plans;
     bool capturing = false;
     uint64_t ws_epoch = 0;
     // small pinned host buffer for device->host scalars
@@ -320,6 +325,16 @@ void image_to_grid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const float* model,
 // grid_to_image of a real grid (the real part of a PSF grid), standard gridder
 void grid_to_image_real(cr_ctx* ctx, cr_gridder* g, const float* grid, float scale,
                         float* image, bool single = false);
+// The FP64-grade image transforms in float-pair arithmetic (cr_dfft.cu):
+// whether both grid sizes are served; grid (or the PSF's real parts) ->
+// image, with crop_correct_body's scale, sinc factors and mode; image ->
+// model grid (apodize_body's factors, then the float32 grid).
+bool dfft_supported(int64_t gnx, int64_t gny);
+void dfft_grid_to_image(cr_ctx* ctx, cr_gridder* g, const float2* grid, const float* real_grid,
+                        double scale, const float* sx, const float* sy, int sinc_mode,
+                        float* image);
+void dfft_image_to_grid(cr_ctx* ctx, cr_gridder* g, const float* model, const float* sinc_x,
+                        const float* sinc_y, float2* grid);
 // max |image| into *peak_dev (float bits as uint32)
 void abs_peak(cr_ctx* ctx, const float* image, int64_t n, unsigned int* peak_dev);
 // image *= scale, then / *peak_dev when peak_dev != null

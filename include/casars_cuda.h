@@ -192,6 +192,13 @@ int cr_ctx_set_wait_limits(cr_ctx* ctx, int64_t barrier_polls, int64_t mbar_poll
  * crates/casa-imaging/src/fft_backend.rs:61-68). Cube plans carry their own
  * setting (cr_cube_plan_set_fft_precision). */
 int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits);
+/* How the FP64-grade image transforms of the single-plane calls run:
+ * 0 (the default) = float-pair kernels (values as a sum of two floats, about
+ * 48 significant bits, on the float32 pipes) for grids whose sides are even,
+ * 5-smooth and at most 13824, cuFFT FP64 otherwise; 1 = always cuFFT FP64.
+ * New; no counterpart in the reference (whose host FFT has no such
+ * choice).  Returns CR_INVALID for other values. */
+int cr_ctx_set_image_fft_engine(cr_ctx* ctx, int32_t engine);
 const char* cr_version(void);
 
 /* ---- gridders ------------------------------------------------------------
