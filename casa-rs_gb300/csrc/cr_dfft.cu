@@ -45,7 +45,7 @@ struct DfPlan {
 
 namespace {
 
-constexpr int kDfThreads = 256;
+constexpr int kDfThreads = 512;
 constexpr int kDfMaxStages = 16;
 // lines up to this length fit one block's shared memory (16 bytes a point)
 constexpr int64_t kDfMaxN = 13824;
@@ -96,8 +96,22 @@ __device__ __forceinline__ dd dmul(dd a, dd b) {
 
 __device__ __forceinline__ cdd cadd(cdd a, cdd b) { return {dadd(a.re, b.re), dadd(a.im, b.im)}; }
 __device__ __forceinline__ cdd csub(cdd a, cdd b) { return {dsub(a.re, b.re), dsub(a.im, b.im)}; }
+// a b + sgn c d as one float pair: the two products' high parts are summed
+// exactly, their rounding errors and cross terms gathered by fused
+// multiply-adds into one correction
+__device__ __forceinline__ dd dot2(dd a, dd b, dd c, dd d, float sgn) {
+    const float p = __fmul_rn(a.h, b.h), q = sgn * __fmul_rn(c.h, d.h);
+    float t = __fmaf_rn(a.h, b.h, -p);
+    t = __fmaf_rn(a.h, b.l, t);
+    t = __fmaf_rn(a.l, b.h, t);
+    t = __fmaf_rn(sgn, __fmaf_rn(c.h, d.h, -sgn * q), t);
+    t = __fmaf_rn(sgn * c.h, d.l, t);
+    t = __fmaf_rn(sgn * c.l, d.h, t);
+    const dd s = two_sum(p, q);
+    return quick_two_sum(s.h, __fadd_rn(s.l, t));
+}
 __device__ __forceinline__ cdd cmul(cdd a, cdd b) {
-    return {dsub(dmul(a.re, b.re), dmul(a.im, b.im)), dadd(dmul(a.re, b.im), dmul(a.im, b.re))};
+    return {dot2(a.re, b.re, a.im, b.im, -1.0f), dot2(a.re, b.im, a.im, b.re, 1.0f)};
 }
 __device__ __forceinline__ cdd cscale(cdd a, dd c) { return {dmul(a.re, c), dmul(a.im, c)}; }
 // times +i for the inverse transform, -i for the forward one
@@ -216,7 +230,7 @@ __device__ void line_transform(float4* sm, const DfStages& s, const float4* tw,
 
 // grid -> image, pass 1: column y of the modulated grid transformed along x;
 // the image's rows [bx0, bx0 + nx) kept in t[(x - bx0) gny + y].
-__global__ void __launch_bounds__(kDfThreads) dfft_inv_cols(
+__global__ void __launch_bounds__(kDfThreads, 2) dfft_inv_cols(
     const float2* grid, const float* real_grid, int64_t gny, int64_t bx0, int32_t nx,
     const int32_t* src, const float4* tw, DfStages s, DfConsts c, float4* t) {
     extern __shared__ float4 sm[];
@@ -244,7 +258,7 @@ __global__ void __launch_bounds__(kDfThreads) dfft_inv_cols(
 
 // grid -> image, pass 2: image row xr transformed along y, then the crop and
 // correction of crop_correct_body (the same operations on the FP64 value).
-__global__ void __launch_bounds__(kDfThreads) dfft_inv_rows(
+__global__ void __launch_bounds__(kDfThreads, 2) dfft_inv_rows(
     const float4* t, int64_t gny, int32_t ny, int64_t bx0, int64_t by0, int parity,
     double scale, const float* corr_x, const float* corr_y, const float* sx, const float* sy,
     int sinc_mode, const int32_t* src, const float4* tw, DfStages s, DfConsts c,
@@ -255,12 +269,15 @@ __global__ void __launch_bounds__(kDfThreads) dfft_inv_rows(
     for (int i = threadIdx.x; i < s.n; i += blockDim.x) sm[i] = row[src[i]];
     __syncthreads();
     line_transform<true>(sm, s, tw, c);
+    // the scale as a float pair: the product's high part is the float32
+    // value (float)(r * scale) of the FP64 path, but for ties at half an ulp
+    const float sh = (float)scale;
+    const dd sc{sh, (float)(scale - (double)sh)};
     for (int yr = threadIdx.x; yr < ny; yr += blockDim.x) {
         const int64_t gy = by0 + yr;
         const float4 w = sm[gy];
-        double r = (double)w.x + (double)w.y;
-        if ((gx + gy + parity) & 1) r = -r;
-        float v = (float)(r * scale);
+        const dd r = ((gx + gy + parity) & 1) ? dd{-w.x, -w.y} : dd{w.x, w.y};
+        float v = dmul(r, sc).h;
         const float factor = __fmul_rn(corr_x[gx], corr_y[gy]);
         if (sinc_mode == 1) {
             const float sf = __fmul_rn(sx[gx], sy[gy]);
@@ -276,7 +293,7 @@ __global__ void __launch_bounds__(kDfThreads) dfft_inv_rows(
 
 // image -> grid, pass 1: row xr of the apodised, modulated model (zero
 // outside the image's columns) transformed along y into t[xr gny + y].
-__global__ void __launch_bounds__(kDfThreads) dfft_fwd_rows(
+__global__ void __launch_bounds__(kDfThreads, 2) dfft_fwd_rows(
     const float* model, int32_t ny, int64_t gny, int64_t bx0, int64_t by0, const float* corr_x,
     const float* corr_y, const float* sinc_x, const float* sinc_y, const int32_t* src,
     const float4* tw, DfStages s, DfConsts c, float4* t) {
@@ -302,7 +319,7 @@ __global__ void __launch_bounds__(kDfThreads) dfft_fwd_rows(
 
 // image -> grid, pass 2: column y transformed along x (rows outside
 // [bx0, bx0 + nx) are zero), the output checkerboard, float32 grid.
-__global__ void __launch_bounds__(kDfThreads) dfft_fwd_cols(
+__global__ void __launch_bounds__(kDfThreads, 2) dfft_fwd_cols(
     const float4* t, int64_t gny, int32_t nx, int64_t bx0, int parity, const int32_t* src,
     const float4* tw, DfStages s, DfConsts c, float2* grid) {
     extern __shared__ float4 sm[];
@@ -316,8 +333,8 @@ __global__ void __launch_bounds__(kDfThreads) dfft_fwd_cols(
     line_transform<false>(sm, s, tw, c);
     for (int x = threadIdx.x; x < s.n; x += blockDim.x) {
         const float4 w = sm[x];
-        float re = (float)((double)w.x + (double)w.y);
-        float im = (float)((double)w.z + (double)w.w);
+        // the pairs are normalised: the high part is the float32 value
+        float re = w.x, im = w.z;
         if ((x + y + parity) & 1) {
             re = -re;
             im = -im;
