@@ -59,6 +59,8 @@ def parse():
                     help="skip the row-block read-ahead feed measurement")
     ap.add_argument("--feed-only", action="store_true",
                     help="run only the row-block feed measurement (profiling runs)")
+    ap.add_argument("--fft-only", action="store_true",
+                    help="run only the image-stage transform measurement (profiling runs)")
     ap.add_argument("--no-major-minor", action="store_true",
                     help="skip the device-resident major/minor CLEAN loop")
     ap.add_argument("--cube-only", action="store_true",
@@ -544,6 +546,47 @@ def run_feed(args, ctx, dev):
             "gridded_equal": int(s_res.gridded_samples) == int(sums.gridded_samples)}
 
 
+def run_image_stage(args, ctx, dev):
+    """The FP64-grade image-stage transforms at the headline size: a random
+    complex 5000^2 grid to the 4096^2 image (inverse transform, crop,
+    correction) and a random 4096^2 model image to its grid (apodisation,
+    forward transform), each timed with CUDA events on the context's
+    stream, with the float-pair kernels (the default engine) and with cuFFT
+    FP64."""
+    import torch
+    import casars_cuda as cc
+    nx = 4096
+    gg = cc.StandardGridder(ctx, cc.ImageGeometry(nx, nx, 1.5e-6, 1.5e-6), 100)
+    gs = gg.grid_shape()
+    g = torch.Generator(device=dev).manual_seed(5)
+    grid = torch.complex(torch.randn(gs, device=dev, generator=g),
+                         torch.randn(gs, device=dev, generator=g))
+    model = torch.randn((nx, nx), device=dev, generator=g)
+    reps = max(1, min(args.steps, 10))
+    out = {"workload": f"{nx}^2 image, {gs[0]}^2 grid, random complex grid and model image"}
+    for engine in ("auto", "cufft"):
+        ctx.set_image_fft_engine(engine)
+        for name, fn in (("grid_to_image_ms", lambda: cc.grid_to_image(gg, grid, 1.0)),
+                         ("image_to_grid_ms", lambda: cc.image_to_grid(gg, model))):
+            for _ in range(max(args.warmup, 1)):
+                fn()
+            ts = []
+            for _ in range(reps):
+                stream = torch.cuda.current_stream(dev)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(a.elapsed_time(b))
+            key = "float_pair" if engine == "auto" else "cufft_fp64"
+            out.setdefault(key, {})[name] = float(np.median(ts))
+    ctx.set_image_fft_engine("auto")
+    del grid, model
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_major_minor(args, ctx, dev):
     """The device-resident major/minor loop: 2048^2 Stokes I, 10,108,800
     visibilities (21 km layout, 4 channels 1.3-1.5 GHz gridded together), 64
@@ -676,6 +719,9 @@ def main():
     ctx = cc.Context(local)
     if args.feed_only:
         print(json.dumps({"row_feed": run_feed(args, ctx, dev)}), flush=True)
+        return
+    if args.fft_only:
+        print(json.dumps({"image_stage": run_image_stage(args, ctx, dev)}), flush=True)
         return
     if args.cube_only:
         print(json.dumps({"cube": run_cube(args, ctx, dev, measured_peaks()[0])}), flush=True)
@@ -834,6 +880,7 @@ def main():
         result["row_runs"] = run_rows(args, ctx, dev, peak)
     if not args.no_feed:
         result["row_feed"] = run_feed(args, ctx, dev)
+    result["image_stage"] = run_image_stage(args, ctx, dev)
     if not args.no_major_minor:
         result["major_minor"] = run_major_minor(args, ctx, dev)
 
