@@ -138,6 +138,12 @@ impl Context {
         check(unsafe { sys::cr_ctx_set_image_fft_precision(self.raw, bits) }, null_mut())
     }
 
+    /// How the FP64-grade image transforms run: 0 the library's float-pair
+    /// kernels where the grid allows, 1 cuFFT FP64.
+    pub fn set_image_fft_engine(&self, engine: i32) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_image_fft_engine(self.raw, engine) }, null_mut())
+    }
+
     pub fn synchronize(&self) -> Result<()> {
         call(|e| unsafe { sys::cr_ctx_synchronize(self.raw, e) })
     }
@@ -557,4 +563,111 @@ pub fn restore(ctx: &Context, model: &[f32], residual: Option<&[f32]>, nx: usize
                         out.as_mut_ptr(), sys::CR_HOST, e)
     })?;
     Ok(out)
+}
+
+/// The device side of `stream_imaging_source_read_ahead_blocks`
+/// (casars-imager/src/lib.rs:36608-36760): MeasurementSet row blocks of one
+/// spectral window pass through `max_live_row_blocks` page-locked slots;
+/// each submitted block is uploaded while the previous one is prepared and
+/// gridded by the feed's worker thread.  The reader (casa-ms) writes a
+/// block's columns straight into the slot `acquire` hands out.  The context
+/// belongs to the feed until `finish` returns.
+pub struct RowFeed<'g> {
+    g: &'g Gridder<'g>,
+    raw: *mut sys::cr_row_feed,
+    channels: usize,
+    correlations: usize,
+}
+
+/// One acquired staging slot: page-locked arrays of `max_rows` rows in the
+/// row-run layout (`[row][channel][correlation]`, DATA as `f32` pairs).
+pub struct RowBlockSlot<'f> {
+    raw: sys::cr_row_block,
+    channels: usize,
+    correlations: usize,
+    _feed: PhantomData<&'f ()>,
+}
+
+impl RowBlockSlot<'_> {
+    pub fn max_rows(&self) -> usize {
+        self.raw.max_rows as usize
+    }
+
+    fn slice<'a, T>(p: *mut T, n: usize) -> Option<&'a mut [T]> {
+        // SAFETY: the slot's arrays hold max_rows rows, stay allocated while
+        // the feed lives, and belong to this slot until it is submitted.
+        if p.is_null() { None } else { Some(unsafe { std::slice::from_raw_parts_mut(p, n) }) }
+    }
+
+    pub fn uvw_m(&mut self) -> &mut [f64] {
+        Self::slice(self.raw.uvw_m, self.max_rows() * 3).unwrap()
+    }
+    pub fn data(&mut self) -> &mut [f32] {
+        Self::slice(self.raw.data, self.max_rows() * self.channels * self.correlations * 2).unwrap()
+    }
+    pub fn weight(&mut self) -> &mut [f32] {
+        Self::slice(self.raw.weight, self.max_rows() * self.correlations).unwrap()
+    }
+    pub fn flag(&mut self) -> Option<&mut [u8]> {
+        Self::slice(self.raw.flag, self.max_rows() * self.channels * self.correlations)
+    }
+    pub fn weight_spectrum(&mut self) -> Option<&mut [f32]> {
+        Self::slice(self.raw.weight_spectrum, self.max_rows() * self.channels * self.correlations)
+    }
+    pub fn gridable(&mut self) -> Option<&mut [u8]> {
+        Self::slice(self.raw.gridable, self.max_rows())
+    }
+}
+
+impl<'g> RowFeed<'g> {
+    #[allow(clippy::too_many_arguments)]
+    pub fn new(g: &'g Gridder<'g>, lambda_scale: &[f64], polarization: sys::cr_polarization,
+               correlations: usize, row_block_rows: usize, max_live_row_blocks: i32,
+               has_flag: bool, has_weight_spectrum: bool, has_gridable: bool)
+               -> Result<RowFeed<'g>> {
+        let cfg = sys::cr_row_feed_config {
+            max_live_row_blocks, row_block_rows: row_block_rows as i64,
+            channels: lambda_scale.len() as i32, correlations: correlations as i32,
+            lambda_scale: lambda_scale.as_ptr(), polarization,
+            has_flag: has_flag as i32, has_weight_spectrum: has_weight_spectrum as i32,
+            has_gridable: has_gridable as i32,
+        };
+        let mut raw = null_mut();
+        call(|e| unsafe { sys::cr_row_feed_create(g.ctx.raw, g.raw, &cfg, &mut raw, e) })?;
+        Ok(RowFeed { g, raw, channels: lambda_scale.len(), correlations })
+    }
+
+    /// The next free slot; waits while every slot is live.
+    pub fn acquire(&self) -> Result<RowBlockSlot<'_>> {
+        // SAFETY: plain-old-data out parameter, filled by the call.
+        let mut blk: sys::cr_row_block = unsafe { std::mem::zeroed() };
+        call(|e| unsafe { sys::cr_row_feed_acquire(self.raw, &mut blk, e) })?;
+        Ok(RowBlockSlot { raw: blk, channels: self.channels, correlations: self.correlations,
+                          _feed: PhantomData })
+    }
+
+    /// Queue the slot's first `rows` rows (0 hands the slot back unused).
+    pub fn submit(&self, slot: RowBlockSlot<'_>, rows: usize) -> Result<()> {
+        call(|e| unsafe { sys::cr_row_feed_submit(self.raw, slot.raw.slot, rows as i64, e) })
+    }
+
+    /// Images of every block submitted so far, and the read-ahead summary
+    /// (`ImagingSourceReadAheadSummary`, lib.rs:36324-36335).
+    pub fn finish(&self) -> Result<(DirtyProducts, sys::cr_row_feed_summary)> {
+        let n = self.g.nx * self.g.ny;
+        let mut out = DirtyProducts { psf: vec![0.0; n], residual: vec![0.0; n],
+                                      state: cr_psf_state::default(), sums: cr_sums::default() };
+        let mut summary = sys::cr_row_feed_summary::default();
+        call(|e| unsafe {
+            sys::cr_row_feed_finish(self.raw, out.psf.as_mut_ptr(), out.residual.as_mut_ptr(),
+                                    sys::CR_HOST, &mut out.state, &mut out.sums, &mut summary, e)
+        })?;
+        Ok((out, summary))
+    }
+}
+
+impl Drop for RowFeed<'_> {
+    fn drop(&mut self) {
+        unsafe { sys::cr_row_feed_destroy(self.raw) };
+    }
 }

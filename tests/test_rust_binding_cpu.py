@@ -70,12 +70,17 @@ def test_structs_match_the_ctypes_layout():
              "cr_wproj_info": _lib.WProjInfo, "cr_vis_batch": _lib.VisBatch,
              "cr_cube_batch": _lib.CubeBatch, "cr_row_runs": _lib.RowRuns,
              "cr_polarization": _lib.Polarization, "cr_beam": _lib.Beam,
-             "cr_sums": _lib.Sums, "cr_psf_state": _lib.PsfState, "cr_timings": _lib.Timings}
+             "cr_sums": _lib.Sums, "cr_psf_state": _lib.PsfState, "cr_timings": _lib.Timings,
+             "cr_row_feed_config": _lib.RowFeedConfig, "cr_row_block": _lib.RowBlock,
+             "cr_row_feed_summary": _lib.RowFeedSummary}
     sizes = {"i32": 4, "i64": 8, "f32": 4, "f64": 8, "u8": 1}
     for name, cls in pairs.items():
         fields = re.findall(r"pub (\w+): ([^,]+),", structs[name])
         assert [f for f, _ in fields] == [f for f, _ in cls._fields_], name
         for (f, t), (_, ct) in zip(fields, cls._fields_):
+            if t in pairs:   # a nested struct
+                assert C.sizeof(ct) == C.sizeof(pairs[t]), (name, f, t)
+                continue
             want = 8 if t.startswith("*") else sizes[t]
             assert C.sizeof(ct) == want, (name, f, t)
 
