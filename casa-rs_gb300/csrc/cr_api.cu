@@ -15,6 +15,43 @@ using namespace cr;
 
 namespace {
 
+// Work issued between to_aux() and to_main() goes to the context's auxiliary
+// stream, which first waits for everything already on the main stream;
+// join() makes the main stream wait for that work.  The destructor restores
+// the main stream and joins, also when an exception leaves the call early,
+// so no auxiliary work outlives the call unordered.
+struct AuxFork {
+    cr_ctx* ctx;
+    cudaStream_t main;
+    bool on_aux = false, joined = true;
+    explicit AuxFork(cr_ctx* c) : ctx(c), main(c->stream) {}
+    void to_aux() {
+        CR_CUDA_CHECK(cudaEventRecord(ctx->fork_ev, main));
+        CR_CUDA_CHECK(cudaStreamWaitEvent(ctx->aux_stream, ctx->fork_ev, 0));
+        ctx->stream = ctx->aux_stream;
+        on_aux = true;
+        joined = false;
+    }
+    void to_main() {
+        if (!on_aux) return;
+        ctx->stream = main;
+        on_aux = false;
+        CR_CUDA_CHECK(cudaEventRecord(ctx->join_ev, ctx->aux_stream));
+    }
+    void join() {
+        to_main();
+        if (!joined) CR_CUDA_CHECK(cudaStreamWaitEvent(main, ctx->join_ev, 0));
+        joined = true;
+    }
+    ~AuxFork() {
+        if (on_aux) {
+            ctx->stream = main;
+            cudaEventRecord(ctx->join_ev, ctx->aux_stream);
+        }
+        if (!joined) cudaStreamWaitEvent(main, ctx->join_ev, 0);
+    }
+};
+
 struct StageTimer {
     cr_ctx* ctx;
     int n = 0;
@@ -313,6 +350,9 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
         cr::noalloc_prepare(device);
         CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
         c->stream = c->own_stream;
+        CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
+        CR_CUDA_CHECK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+        CR_CUDA_CHECK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
         for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
         for (auto& e : c->kev) CR_CUDA_CHECK(cudaEventCreate(&e));
         CR_CUDA_CHECK(cudaMallocHost(&c->pinned, 4096));
@@ -342,6 +382,12 @@ void cr_ctx_destroy(cr_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->status_h) cudaFreeHost(ctx->status_h);
+    if (ctx->aux_stream) {
+        cudaStreamSynchronize(ctx->aux_stream);
+        cudaStreamDestroy(ctx->aux_stream);
+    }
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -730,11 +776,16 @@ int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         bind(ctx);
         DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
+        // the model's upload and transform run beside the plan
+        AuxFork fork(ctx);
+        fork.to_aux();
         const float* m = (const float*)device_input(ctx, model, image_pixels(g) * 4,
                                                     model_location, "model");
         float2* mgrid = (float2*)workspace(ctx, "pr_model_grid", gb);
         image_to_grid(ctx, g, wp, m, mgrid, image_single(ctx));
+        fork.to_main();
         Records r = plan(ctx, g, wp, b);
+        fork.join();
         degrid_records(ctx, g, wp, r, mgrid);
         float2* out = out_ptr<float2>(ctx, pred, out_location, (size_t)b.n * 8 + 8, "pred");
         broadcast_pred(ctx, r, out);

@@ -87,6 +87,10 @@ struct cr_ctx {
     int sms = 0;           // multiprocessors of the device (grid sizing)
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    // a second stream for work that runs beside the main stream's inside one
+    // call, forked from and joined back to `stream` by these events
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans_c2c;
