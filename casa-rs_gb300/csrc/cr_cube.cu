@@ -20,10 +20,11 @@
 //   * degridding (degrid_sample_taps_planned_normalized, gridder.rs:1278-1312).
 //
 // Layout: rows' u, v (f64 metres) are shared by all channels; vis, weight
-// and flags are channel-major [C][R].  Planning makes one pass to histogram
-// the samples by (channel, 32 x 32 home tile), a scan, and a second pass that
-// scatters 16-byte records {cell | tap rows, sample, w vis} plus the weight into
-// bin order.  The index selection runs on the integer fixed-point path of
+// and flags are channel-major [C][R].  Planning makes one pass that builds
+// the weight density and histograms the samples by (channel, 32 x 32 home
+// tile, start cell), a scan, and a second pass that forms each imaging weight
+// and scatters 16-byte records {cell | tap rows, sample, w vis} plus the
+// weight into bin order.  The index selection runs on the integer fixed-point path of
 // cr_fixed.cuh with the FP64 operations as the fallback.  Gridding gives
 // every (channel, output tile) to one block, which gathers the records of
 // the four home tiles whose 7 x 7 footprints reach it, accumulates the tile
@@ -91,9 +92,8 @@ struct CubeArgs {
     float* rec_w;
     // per-sample results kept between the passes ([C][R])
     uint32_t* dcell;           // density cell x ny + y of (u, v), ~0 when none
-    uint32_t* ev_tile;         // home tile, ~0 when the sample is not gridded
+    uint32_t* ev_tile;         // home tile, or kFlaggedSample / kUngriddedSample
     uint32_t* ev_meta;         // cell in tile | tap rows
-    float* ev_w;               // imaging weight
 };
 
 // Rows' u, v as float32 pairs for the fast path.  Rows whose coordinates are
@@ -203,6 +203,44 @@ struct Eval {
     float w;
 };
 
+// sample_tap_span of row r at channel ch: the home tile and meta = start cell
+// in the tile | tap rows; float32 pairs first, then the integer path, then
+// the reference's FP64 operations.  False when the sample does not grid.
+__device__ __forceinline__ bool plan_sample(const CubeArgs& a, const CubeChan& ch, float4 uv,
+                                            int64_t r, uint32_t* tile, uint32_t* meta) {
+    int64_t x0 = 0, y0 = 0;
+    int32_t rx = 0, ry = 0;
+    // x = u K_x + G/2, y = -v K_y + G/2
+    float px, ex, py, ey;
+    df_product(uv.x, uv.y, ch.fx, &px, &ex);
+    df_product(-uv.z, -uv.w, ch.fy, &py, &ey);
+    int sx = df_tap_span(px, ex, a.gnx, a.os, a.tap_rows, &x0, &rx);
+    int sy = sx == 0 ? 0 : df_tap_span(py, ey, a.gny, a.os, a.tap_rows, &y0, &ry);
+    if (sx == 0 || sy == 0) return false;
+    long long tx, ty;
+    if ((sx < 0 || sy < 0) && fix_mul(a.u[r], ch.kx, &tx) && fix_mul(a.v[r], ch.ky, &ty)) {
+        sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
+        if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
+        if (sx == 0 || sy == 0) return false;
+    }
+    if (sx < 0 || sy < 0) {
+        const double u = __dmul_rn(a.u[r], ch.lscale), v = __dmul_rn(a.v[r], ch.lscale);
+        const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+        const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+        if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
+            !f64_tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry))
+            return false;
+    }
+    *tile = (uint32_t)((x0 >> 5) * a.nty + (y0 >> 5));
+    *meta = ((uint32_t)(x0 & 31) << 27) | ((uint32_t)(y0 & 31) << 22) | ((uint32_t)rx << 11) |
+            (uint32_t)ry;
+    return true;
+}
+
+// ev_tile values of samples without a home tile
+constexpr uint32_t kFlaggedSample = ~0u;        // flagged: left out of the channel batch
+constexpr uint32_t kUngriddedSample = ~0u - 1;  // unflagged, but no grid plan or weight
+
 // Samples are evaluated kVec at a time per thread (rows row0 + 32 j): their
 // loads are issued together, so each thread keeps kVec gathers in flight.
 constexpr int kVec = 4;
@@ -258,45 +296,37 @@ __device__ __forceinline__ void eval_samples(const CubeArgs& a, const CubeChan& 
 #pragma unroll
     for (int j = 0; j < kVec; ++j) {
         if (!live[j] || !(finite_f(w[j]) && w[j] > 0.0f)) continue;
-        int64_t x0 = 0, y0 = 0;
-        int32_t rx = 0, ry = 0;
-        // float32 pairs first: x = u K_x + G/2, y = -v K_y + G/2
-        float px, ex, py, ey;
-        df_product(uv[j].x, uv[j].y, ch.fx, &px, &ex);
-        df_product(-uv[j].z, -uv[j].w, ch.fy, &py, &ey);
-        int sx = df_tap_span(px, ex, a.gnx, a.os, a.tap_rows, &x0, &rx);
-        int sy = sx == 0 ? 0 : df_tap_span(py, ey, a.gny, a.os, a.tap_rows, &y0, &ry);
-        if (sx == 0 || sy == 0) continue;
-        const int64_t r = row0 + 32 * j;
-        long long tx, ty;
-        if ((sx < 0 || sy < 0) && fix_mul(a.u[r], ch.kx, &tx) && fix_mul(a.v[r], ch.ky, &ty)) {
-            sx = fix_tap_span(tx + a.cx_fix, a.gnx, a.os, a.tap_rows, &x0, &rx);
-            if (sx != 0) sy = fix_tap_span(a.cy_fix - ty, a.gny, a.os, a.tap_rows, &y0, &ry);
-            if (sx == 0 || sy == 0) continue;
-        }
-        if (sx < 0 || sy < 0) {
-            const double u = __dmul_rn(a.u[r], ch.lscale), v = __dmul_rn(a.v[r], ch.lscale);
-            const double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
-            const double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
-            if (!f64_tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) ||
-                !f64_tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry))
-                continue;
-        }
+        if (!plan_sample(a, ch, uv[j], row0 + 32 * j, &e[j].tile, &e[j].meta)) continue;
         e[j].ok = true;
-        e[j].tile = (uint32_t)((x0 >> 5) * a.nty + (y0 >> 5));
-        e[j].meta = ((uint32_t)(x0 & 31) << 27) | ((uint32_t)(y0 & 31) << 22) |
-                    ((uint32_t)rx << 11) | (uint32_t)ry;
         e[j].w = w[j];
     }
 }
 
+// Records are binned by (channel, home tile, start cell in the tile), so that
+// within a home tile they follow the cell order and records with one start
+// cell are adjacent.
+__device__ __forceinline__ int64_t cell_bin(int c, int64_t ntiles, uint32_t tile,
+                                            uint32_t meta) {
+    return (((int64_t)c * ntiles + tile) << 10) | (int64_t)(meta >> 22);
+}
+
+// Pass 1 over every sample: with DENSITY the weight density of both cells
+// (u, v) and (-u, -v) and the sample's own density cell; then its grid plan
+// and the histogram of (channel, home tile, cell) over the samples that can
+// grid -- unflagged, a positive natural weight, an own density cell
+// (DENSITY) and a plan.  This counts a superset of the gridded samples: the
+// imaging weight w / d or w / (d f2 + 1), known only once every density is
+// complete, must also come out positive; the scatter gives a sample for
+// which it does not a null record, so the counts stay exact.
+template <bool DENSITY>
 __global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs a) {
     const int c = blockIdx.y;
     const CubeChan ch = a.ch[c];
+    const int64_t ntiles = a.ntx * a.nty;
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* dens = a.density + (int64_t)c * a.nx * a.ny;
+    float* dens = DENSITY ? a.density + (int64_t)c * a.nx * a.ny : nullptr;
     for (int64_t base = r0 + warp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
         float w[kVec];
         float4 uv[kVec];
@@ -313,26 +343,42 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_density_kernel(CubeArgs 
 #pragma unroll
         for (int j = 0; j < kVec; ++j) {
             const int64_t r = base + lane + 32 * j;
-            uint32_t cell = ~0u;
-            if (live[j]) {
-                int x = 0, y = 0, xm = 0, ym = 0;
-                bool ok = false, okm = false;
-                // float32 pairs first: (u, v) -> x = u s_x + nx/2, y = -v s_y + ny/2;
-                // the mirror negates both products
-                float px, ex, py, ey;
-                df_product(uv[j].x, uv[j].y, ch.fdx, &px, &ex);
-                df_product(-uv[j].z, -uv[j].w, ch.fdy, &py, &ey);
-                if (!df_density_cell(px, ex, py, ey, a.nx, a.ny, &x, &y, &ok) ||
-                    !df_density_cell(-px, -ex, -py, -ey, a.nx, a.ny, &xm, &ym, &okm))
-                    density_cells(a, ch, a.u[r], a.v[r], &x, &y, &ok, &xm, &ym, &okm);
-                const bool pos = finite_f(w[j]) && w[j] > 0.0f;
-                if (ok) {
-                    cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
-                    if (pos) atomicAdd(&dens[cell], w[j]);
+            if (r >= r1) continue;
+            const int64_t i = (int64_t)c * a.R + r;
+            const bool pos = finite_f(w[j]) && w[j] > 0.0f;
+            bool own = true;
+            if (DENSITY) {
+                uint32_t cell = ~0u;
+                if (live[j]) {
+                    int x = 0, y = 0, xm = 0, ym = 0;
+                    bool ok = false, okm = false;
+                    // float32 pairs first: (u, v) -> x = u s_x + nx/2,
+                    // y = -v s_y + ny/2; the mirror negates both products
+                    float px, ex, py, ey;
+                    df_product(uv[j].x, uv[j].y, ch.fdx, &px, &ex);
+                    df_product(-uv[j].z, -uv[j].w, ch.fdy, &py, &ey);
+                    if (!df_density_cell(px, ex, py, ey, a.nx, a.ny, &x, &y, &ok) ||
+                        !df_density_cell(-px, -ex, -py, -ey, a.nx, a.ny, &xm, &ym, &okm))
+                        density_cells(a, ch, a.u[r], a.v[r], &x, &y, &ok, &xm, &ym, &okm);
+                    if (ok) {
+                        cell = (uint32_t)x * (uint32_t)a.ny + (uint32_t)y;
+                        if (pos) atomicAdd(&dens[cell], w[j]);
+                    }
+                    if (okm && pos) atomicAdd(&dens[(int64_t)xm * a.ny + ym], w[j]);
                 }
-                if (okm && pos) atomicAdd(&dens[(int64_t)xm * a.ny + ym], w[j]);
+                a.dcell[i] = cell;
+                own = cell != ~0u;
             }
-            if (r < r1) a.dcell[(int64_t)c * a.R + r] = cell;
+            uint32_t tile = kUngriddedSample, meta = 0u;
+            if (!live[j]) {
+                tile = kFlaggedSample;
+            } else if (pos && own && plan_sample(a, ch, uv[j], r, &tile, &meta)) {
+                atomicAdd(&a.hist[cell_bin(c, ntiles, tile, meta)], 1u);
+            } else {
+                tile = kUngriddedSample;
+            }
+            a.ev_tile[i] = tile;
+            a.ev_meta[i] = meta;
         }
     }
 }
@@ -407,14 +453,6 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     return v;
 }
 
-// Records are binned by (channel, home tile, start cell in the tile), so that
-// within a home tile they follow the cell order and records with one start
-// cell are adjacent.
-__device__ __forceinline__ int64_t cell_bin(int c, int64_t ntiles, uint32_t tile,
-                                            uint32_t meta) {
-    return (((int64_t)c * ntiles + tile) << 10) | (int64_t)(meta >> 22);
-}
-
 // Tile-level starts from the cell-level exclusive scan.
 __global__ void tile_starts_from_cells(const uint32_t* cell_start, int64_t nbins,
                                        uint32_t* bin_start) {
@@ -423,75 +461,31 @@ __global__ void tile_starts_from_cells(const uint32_t* cell_start, int64_t nbins
         bin_start[b] = cell_start[b << 10];
 }
 
-// Pass 1: histogram of (channel, home tile, cell), per-channel sumwt and counts.
-__global__ void __launch_bounds__(kCubeThreads, 4) cube_hist_kernel(CubeArgs a) {
+// Pass 2: records scattered into (channel, home tile, cell) bins from pass
+// 1's plans, kScatterVec samples per thread and iteration so that more
+// cursor atomics are in flight.  The imaging weight is formed here, from the
+// complete density: w itself, w / d (uniform) or w / (d f2 + 1) (Briggs,
+// casa_briggs_denominator, weighting.rs:2440-2443).  A counted sample whose
+// weight does not come out positive and finite gets a null record (zero
+// weight and value, no sample index), which grids and degrids nothing.  The
+// channel's sum of weights and its gridded and unflagged-but-not-gridded
+// counts are summed here.
+constexpr int kScatterVec = 6;
+constexpr uint32_t kNullSample = ~0u;   // sample index of a null record
+__global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs a) {
     __shared__ double s_sum[kCubeThreads / 32];
     __shared__ unsigned long long s_ok[kCubeThreads / 32], s_skip[kCubeThreads / 32];
-    const int c = blockIdx.y;
-    const CubeChan ch = a.ch[c];
-    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
-    const int64_t ntiles = a.ntx * a.nty;
-    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
-    const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
-    double sw = 0.0;
-    unsigned long long n_ok = 0, n_skip = 0;
-    const int wl = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    for (int64_t base = r0 + wp * kWarpRows; base < r1; base += kCubeThreads * kVec) {
-        Eval e[kVec];
-        eval_samples(a, ch, f2, c, base + wl, r1, e);
-#pragma unroll
-        for (int j = 0; j < kVec; ++j) {
-            const int64_t r = base + wl + 32 * j;
-            if (r >= r1) continue;
-            const int64_t i = (int64_t)c * a.R + r;
-            a.ev_tile[i] = e[j].ok ? e[j].tile : ~0u;
-            a.ev_meta[i] = e[j].meta;
-            a.ev_w[i] = e[j].w;
-            if (a.flags && a.flags[i]) continue;
-            if (e[j].ok) {
-                ++n_ok;
-                sw += (double)e[j].w;
-                atomicAdd(&a.hist[cell_bin(c, ntiles, e[j].tile, e[j].meta)], 1u);
-            } else {
-                ++n_skip;
-            }
-        }
-    }
-    sw = warp_sum(sw);
-    n_ok = warp_sum(n_ok);
-    n_skip = warp_sum(n_skip);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        s_sum[warp] = sw;
-        s_ok[warp] = n_ok;
-        s_skip[warp] = n_skip;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        unsigned long long o = 0, s = 0;
-        for (int k = 0; k < kCubeThreads / 32; ++k) {
-            t += s_sum[k];
-            o += s_ok[k];
-            s += s_skip[k];
-        }
-        if (t != 0.0) atomicAdd(&a.sumwt[c], t);
-        if (o) atomicAdd(&a.counts[2 * c], o);
-        if (s) atomicAdd(&a.counts[2 * c + 1], s);
-    }
-}
-
-// Pass 2: scatter records into (channel, home tile) bins from pass 1's
-// per-sample results, kScatterVec samples per thread and iteration so that
-// more cursor atomics are in flight.
-constexpr int kScatterVec = 8;
-__global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs a) {
     const int c = blockIdx.y;
     const int64_t ntiles = a.ntx * a.nty;
     const int lane = threadIdx.x & 31;
     const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
     const int64_t r1 = min(a.R, r0 + kRowsPerBlock);
     const int wp = threadIdx.x >> 5;
+    const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
+    const float* dens = a.mode != CR_WEIGHT_NATURAL ? a.density + (int64_t)c * a.nx * a.ny
+                                                    : nullptr;
+    double sw = 0.0;
+    unsigned long long n_ok = 0, n_skip = 0;
     for (int64_t base = r0 + wp * 32 * kScatterVec; base < r1;
          base += kCubeThreads * kScatterVec) {
         // loads first, then every cursor atomic, then the stores: the kScatterVec
@@ -506,30 +500,79 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
         for (int j = 0; j < kScatterVec; ++j) {
             const int64_t r = base + lane + 32 * j;
             const int64_t i = (int64_t)c * a.R + (r < r1 ? r : r0);
-            tile[j] = r < r1 ? a.ev_tile[i] : ~0u;
+            tile[j] = r < r1 ? a.ev_tile[i] : kFlaggedSample;
             meta[j] = a.ev_meta[i];
-            w[j] = a.ev_w[i];
+            w[j] = a.weight ? a.weight[i] : 1.0f;
             vv[j] = a.vis[i];
+        }
+        if (dens) {
+            float d[kScatterVec];
+#pragma unroll
+            for (int j = 0; j < kScatterVec; ++j) {
+                const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
+                d[j] = tile[j] < kUngriddedSample ? dens[a.dcell[i]] : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kScatterVec; ++j) {
+                float nw = 0.0f;
+                if (finite_f(w[j]) && w[j] > 0.0f && finite_f(d[j]) && d[j] > 0.0f)
+                    nw = a.mode == CR_WEIGHT_UNIFORM
+                             ? __fdiv_rn(w[j], d[j])
+                             : __fdiv_rn(w[j], __fadd_rn(__fmul_rn(d[j], f2), 1.0f));
+                w[j] = nw;
+            }
         }
 #pragma unroll
         for (int j = 0; j < kScatterVec; ++j) {
             pos[j] = 0u;
-            if (tile[j] != ~0u)
+            if (tile[j] < kUngriddedSample)
                 pos[j] = atomicAdd(&a.cursor[cell_bin(c, ntiles, tile[j], meta[j])], 1u);
         }
 #pragma unroll
         for (int j = 0; j < kScatterVec; ++j) {
-            if (tile[j] == ~0u) continue;
+            if (tile[j] == kFlaggedSample) continue;
+            const bool ok = tile[j] != kUngriddedSample && finite_f(w[j]) && w[j] > 0.0f;
+            if (!ok) ++n_skip;
+            if (tile[j] == kUngriddedSample) continue;
             const int64_t i = (int64_t)c * a.R + base + lane + 32 * j;
-            float vr = 0.0f, vi = 0.0f;
-            if (finite_f(vv[j].x) && finite_f(vv[j].y)) {
-                vr = __fmul_rn(vv[j].x, w[j]);
-                vi = __fmul_rn(vv[j].y, w[j]);
+            float vr = 0.0f, vi = 0.0f, wr = 0.0f;
+            uint32_t sample = kNullSample;
+            if (ok) {
+                if (finite_f(vv[j].x) && finite_f(vv[j].y)) {
+                    vr = __fmul_rn(vv[j].x, w[j]);
+                    vi = __fmul_rn(vv[j].y, w[j]);
+                }
+                wr = w[j];
+                sample = (uint32_t)i;
+                ++n_ok;
+                sw += (double)wr;
             }
-            a.rec[pos[j]] = make_uint4(meta[j], (uint32_t)i, __float_as_uint(vr),
+            a.rec[pos[j]] = make_uint4(meta[j], sample, __float_as_uint(vr),
                                        __float_as_uint(vi));
-            a.rec_w[pos[j]] = w[j];
+            a.rec_w[pos[j]] = wr;
         }
+    }
+    sw = warp_sum(sw);
+    n_ok = warp_sum(n_ok);
+    n_skip = warp_sum(n_skip);
+    const int warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_sum[warp] = sw;
+        s_ok[warp] = n_ok;
+        s_skip[warp] = n_skip;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        unsigned long long o = 0, k = 0;
+        for (int q = 0; q < kCubeThreads / 32; ++q) {
+            t += s_sum[q];
+            o += s_ok[q];
+            k += s_skip[q];
+        }
+        if (t != 0.0) atomicAdd(&a.sumwt[c], t);
+        if (o) atomicAdd(&a.counts[2 * c], o);
+        if (k) atomicAdd(&a.counts[2 * c + 1], k);
     }
 }
 
@@ -1036,7 +1079,7 @@ __global__ void __launch_bounds__(kCubeThreads) cube_degrid_kernel(
                 if (RESIDUAL) {
                     a.res[k] = make_float2(__fsub_rn(__uint_as_float(q.z), __fmul_rn(w, re)),
                                            __fsub_rn(__uint_as_float(q.w), __fmul_rn(w, im)));
-                } else {
+                } else if (sample != kNullSample) {
                     a.pred[sample] = make_float2(re, im);
                 }
             }
@@ -1191,14 +1234,17 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
     a.uvdf = uvdf;
     a.ev_tile = (uint32_t*)workspace(ctx, "cube_ev_tile", ns * 4);
     a.ev_meta = (uint32_t*)workspace(ctx, "cube_ev_meta", ns * 4);
-    a.ev_w = (float*)workspace(ctx, "cube_ev_w", ns * 4);
+    if (mode == CR_WEIGHT_NATURAL && in.R > 0) {
+        cube_density_kernel<false><<<grid, kCubeThreads, 0, ctx->stream>>>(a);
+        note_launch(ctx, "cube_plan_kernel");
+    }
     if (mode != CR_WEIGHT_NATURAL) {
         const int64_t cells = (int64_t)g->geom.nx * g->geom.ny;
         a.density = (float*)workspace(ctx, "cube_density", (size_t)(in.C * cells) * 4);
         a.dcell = (uint32_t*)workspace(ctx, "cube_dcell", ns * 4);
         CR_CUDA_CHECK(cudaMemsetAsync(a.density, 0, (size_t)(in.C * cells) * 4, ctx->stream));
         if (in.R > 0) {
-            cube_density_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
+            cube_density_kernel<true><<<grid, kCubeThreads, 0, ctx->stream>>>(a);
             note_launch(ctx, "cube_density_kernel");
         }
         float* f2 = (float*)workspace(ctx, "cube_f2", (size_t)in.C * 4);
@@ -1220,10 +1266,6 @@ CubeRecords cube_plan(cr_ctx* ctx, cr_gridder* g, const CubeInput& in, int32_t m
             note_launch(ctx, "cube_taps_kernel");
         }
         return cr;
-    }
-    if (in.R > 0) {
-        cube_hist_kernel<<<grid, kCubeThreads, 0, ctx->stream>>>(a);
-        note_launch(ctx, "cube_hist_kernel");
     }
     // in place: hist becomes each cell bin's first slot, the scatter's cursor
     exclusive_scan_u32(ctx, hist, hist, ncells, nullptr);

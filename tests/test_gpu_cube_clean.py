@@ -244,6 +244,7 @@ def test_cube_clean_nsigma_matches_oracle(ctx, cube):
     ref_planes = _oracle_planes(obs, flags, vis)
     for p in ref_planes:
         p["sidelobe"] = 0.2
+    dirty_peak = [float(np.max(np.abs(p["residual"]))) for p in ref_planes]
     kw = dict(gain=0.1, threshold=0.0, minor_cycle_length=40, nsigma=10.0)
     ref = O.cube_clean(ref_planes, 1000, **kw)
     assert ref["plane_stops"].count("NsigmaThresholdReached") >= 4
@@ -256,7 +257,12 @@ def test_cube_clean_nsigma_matches_oracle(ctx, cube):
     for c in range(obs.channels):
         assert [tuple(p) for p, _ in out.components[c]] == \
             [tuple(p) for p, _ in ref["components"][c]]
-        assert peak_norm_err(out.residuals[c].cpu().numpy(), ref["residuals"][c]) <= 1e-5
+        # residual errors scale with the plane's image before cleaning (float32
+        # sums of full-amplitude visibilities, in a run-dependent order), not
+        # with the small residual left at the 10-sigma stop
+        err = float(np.max(np.abs(out.residuals[c].cpu().numpy() - ref["residuals"][c])))
+        assert err <= 1e-5 * dirty_peak[c]
+        assert err <= 1e-4 * float(np.max(np.abs(ref["residuals"][c])))
 
 
 def test_hogbom_planes_per_plane_nsigma(ctx, cube):
