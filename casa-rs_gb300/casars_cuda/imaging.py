@@ -171,6 +171,13 @@ class Context:
         if self._lib.cr_ctx_set_image_fft_engine(self._h, code) != 0:
             raise ValueError(f"unsupported FFT engine {engine!r}")
 
+    def set_alloc_limit(self, nbytes: int = 0):
+        """Test hook: a budget for the context's device workspaces (0 lifts
+        it); a call that would grow them past it fails as a device
+        allocation failure does (CasarsCudaError kind "Cuda")."""
+        if self._lib.cr_ctx_set_alloc_limit(self._h, int(nbytes)) != 0:
+            raise ValueError("allocation limit must be >= 0")
+
     @property
     def image_fft_precision(self) -> str:
         return "f32" if getattr(self, "_image_fft_bits", 64) == 32 else "f64"

@@ -1328,6 +1328,12 @@ int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits) {
     return CR_OK;
 }
 
+int cr_ctx_set_alloc_limit(cr_ctx* ctx, int64_t bytes) {
+    if (!ctx || bytes < 0) return CR_INVALID;
+    ctx->alloc_limit = bytes;
+    return CR_OK;
+}
+
 int cr_ctx_set_image_fft_engine(cr_ctx* ctx, int32_t engine) {
     if (!ctx || (engine != 0 && engine != 1)) return CR_INVALID;
     ctx->image_fft_engine = engine;

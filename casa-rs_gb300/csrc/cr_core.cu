@@ -27,6 +27,13 @@ void* pool_alloc(cr_ctx* ctx, Pool& pool, const std::string& name, size_t bytes)
     DevBuf& b = pool[name];
     if (b.bytes >= bytes) return b.ptr;
     if (ctx->capturing) fail(CR_CUDA, "workspace '" + name + "' grew during graph capture");
+    if (ctx->alloc_limit > 0 && &pool == &ctx->ws) {
+        size_t held = 0;
+        for (const auto& kv : pool) held += kv.second.bytes;
+        if (held - b.bytes + bytes > (size_t)ctx->alloc_limit)
+            fail(CR_CUDA, "workspace '" + name + "' of " + std::to_string(bytes) +
+                              " bytes exceeds the context's allocation limit (out of memory)");
+    }
     ctx->ws_epoch++;
     if (b.ptr) CR_CUDA_CHECK(cudaFreeAsync(b.ptr, ctx->stream));
     size_t want = bytes + bytes / 8;

@@ -130,6 +130,9 @@ struct cr_ctx {
     // bounds of the first wait of a grid barrier (Hogbom) and of a
     // bulk-copy mbarrier (cube kernels); the drain waits after a timeout
     // keep the defaults
+    // test hook: a budget (bytes) for the context's workspaces, 0 = none; a
+    // call that would grow them past it fails as an allocation failure would
+    int64_t alloc_limit = 0;
     long long barrier_polls = cr::kBarrierPollsDefault;
     long long mbar_polls = cr::kMbarPollsDefault;
 };

@@ -199,6 +199,13 @@ int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits);
  * New; no counterpart in the reference (whose host FFT has no such
  * choice).  Returns CR_INVALID for other values. */
 int cr_ctx_set_image_fft_engine(cr_ctx* ctx, int32_t engine);
+/* For tests of the failure paths: a budget in bytes for the context's
+ * workspaces (0, the default, lifts it).  A call that would grow them past
+ * the budget fails with CR_CUDA, as a failed device allocation does, before
+ * any work; the context stays usable.  New; no counterpart in the reference
+ * (its allocation failures come from the host allocator).  CR_INVALID for a
+ * negative budget. */
+int cr_ctx_set_alloc_limit(cr_ctx* ctx, int64_t bytes);
 const char* cr_version(void);
 
 /* ---- gridders ------------------------------------------------------------
