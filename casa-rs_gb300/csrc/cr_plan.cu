@@ -13,6 +13,7 @@
 // record sums are accumulated in FP64.
 #include <cmath>
 
+#include "cr_fixed.cuh"
 #include "cr_internal.cuh"
 
 namespace cr {
@@ -38,6 +39,7 @@ struct WpPlanArgs {
     const float* norm;
     int64_t nty;
     int plane_bits, off_bits;
+    DfScale kx, ky;            // 1 / du, 1 / dv as float32 pairs
     uint64_t* keys;
     uint32_t* vals;
     double* sums;
@@ -95,8 +97,54 @@ __device__ void block_accumulate(double s0, double s1, unsigned long long c0,
 
 __device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
 
+// The anchor loc = round(x) and offset round((loc - x) s) of the grid
+// coordinate x = u / du + G/2 in float32 pairs (x - G/2 = p + e from one
+// pair product with 1/du): the decisions of cr_fixed.cuh's fast path, taken
+// only more than kDfMargin from their rounding boundaries, where they equal
+// the reference's FP64 ones.  False when undecided.
+__device__ __forceinline__ bool df_wp_axis(float p, float e, int64_t size, int32_t s,
+                                           int64_t* loc, int64_t* off) {
+    float a, dh;
+    if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return false;
+    const float sf = (float)s;
+    const float v = -__fmaf_rn(dh, sf, __fmul_rn(e, sf));
+    const float o = rintf(v);
+    if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return false;
+    *loc = (size >> 1) + (int64_t)a;
+    *off = (int64_t)o;
+    return true;
+}
+
+// The plane round(sqrt(q)) (half away from zero) of q = RN(w_scale |w|)
+// without the FP64 square root: the candidate from a float32 root, moved to
+// the k with (k - 1/2)^2 <= q < (k + 1/2)^2 by exact FP64 products, and
+// undecided (false) when q lies within 2^-40 relative of either bound,
+// where the reference's rounded root could land on the half-integer.
+// Planes at or above `planes` - 1 need no decision (they clamp).
+__device__ __forceinline__ bool wp_plane_of(double q, int32_t planes, int32_t* plane) {
+    const double top = ((double)planes - 0.5) * ((double)planes - 0.5);
+    if (q >= top) {
+        *plane = planes - 1;
+        return true;
+    }
+    int k = (int)rintf(sqrtf(__double2float_rn(q)));
+    auto lo = [](int j) {
+        const double t = (double)j - 0.5;
+        return __dmul_rn(t, t);
+    };
+    if (k > 0 && q < lo(k)) --k;
+    else if (q >= lo(k + 1)) ++k;
+    const double bl = lo(k), bh = lo(k + 1);
+    if ((k > 0 && __dsub_rn(q, bl) < bl * 0x1p-40) || __dsub_rn(bh, q) < bh * 0x1p-40)
+        return false;
+    *plane = min(k, planes - 1);
+    return true;
+}
+
 // WProjector::plan_sample (gridder.rs:3588-3624) + raw_w_project_sample_is_valid
 // (lib.rs:73666-73676) + w_project_accumulation_for_sample (lib.rs:71463-71470).
+// The anchors, offsets and plane come from the float32-pair path above when
+// it decides them, else from the reference's FP64 operations.
 __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
     double s_norm = 0.0, s_rep = 0.0;
     unsigned long long c_ok = 0, c_skip = 0;
@@ -112,20 +160,39 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
                   f > 0.0f && finite_f(vis.x) && finite_f(vis.y) && isfinite(u) &&
                   isfinite(v) && isfinite(w);
         if (ok) {
-            double px = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
-            double py = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
-            ok = isfinite(px) && isfinite(py) && fabs(px) < 1.0e15 && fabs(py) < 1.0e15;
-            if (ok) {
-                int64_t lx = (int64_t)round(px), ly = (int64_t)round(py);
-                int64_t ox = (int64_t)round(__dmul_rn(__dsub_rn((double)lx, px), (double)a.sampling));
-                int64_t oy = (int64_t)round(__dmul_rn(__dsub_rn((double)ly, py), (double)a.sampling));
-                int32_t plane = 0;
-                if (a.planes > 1) {
-                    double c = sqrt(fmax(__dmul_rn(a.w_scale, fabs(w)), 0.0));
-                    double r = round(c);
-                    r = fmin(fmax(r, 0.0), (double)(a.planes - 1));
-                    plane = (int32_t)r;
+            int64_t lx = 0, ly = 0, ox = 0, oy = 0;
+            int32_t plane = 0;
+            // float32 pairs first: u = uh + ul, x - G/2 = u (1/du), y - G/2 = -v (1/dv)
+            const float uh = __double2float_rn(u), vh = __double2float_rn(v);
+            const float ul = __double2float_rn(__dsub_rn(u, (double)uh));
+            const float vl = __double2float_rn(__dsub_rn(v, (double)vh));
+            float px32, ex, py32, ey;
+            df_product(uh, ul, a.kx, &px32, &ex);
+            df_product(-vh, -vl, a.ky, &py32, &ey);
+            bool fast = df_wp_axis(px32, ex, a.gnx, a.sampling, &lx, &ox) &&
+                        df_wp_axis(py32, ey, a.gny, a.sampling, &ly, &oy);
+            if (fast && a.planes > 1) fast = wp_plane_of(__dmul_rn(a.w_scale, fabs(w)), a.planes,
+                                                         &plane);
+            if (!fast) {
+                // the reference's FP64 operations
+                double px = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+                double py = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+                ok = isfinite(px) && isfinite(py) && fabs(px) < 1.0e15 && fabs(py) < 1.0e15;
+                if (ok) {
+                    lx = (int64_t)round(px);
+                    ly = (int64_t)round(py);
+                    ox = (int64_t)round(__dmul_rn(__dsub_rn((double)lx, px), (double)a.sampling));
+                    oy = (int64_t)round(__dmul_rn(__dsub_rn((double)ly, py), (double)a.sampling));
+                    plane = 0;
+                    if (a.planes > 1) {
+                        double c = sqrt(fmax(__dmul_rn(a.w_scale, fabs(w)), 0.0));
+                        double r = round(c);
+                        r = fmin(fmax(r, 0.0), (double)(a.planes - 1));
+                        plane = (int32_t)r;
+                    }
                 }
+            }
+            if (ok) {
                 int64_t s = a.support[plane];
                 ok = s > 0 && lx - s >= 0 && ly - s >= 0 && lx + s < a.gnx && ly + s < a.gny &&
                      ox >= -a.radius && ox <= a.radius && oy >= -a.radius && oy <= a.radius;
@@ -436,8 +503,9 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) 
         WpPlanArgs a{b.n, b.u, b.v, b.w, b.weight, b.sumwt_factor, b.gridable, b.vis,
                      gi.grid_nx, gi.grid_ny, gi.du, gi.dv, wp->info.w_scale,
                      wp->info.sampling, wp->info.planes, wp->radius, wp->axis,
-                     wp->support_d, wp->norm_d, nty, plane_bits, off_bits, r.keys, r.order,
-                     r.sums, r.counts};
+                     wp->support_d, wp->norm_d, nty, plane_bits, off_bits,
+                     df_scale_of(1.0, gi.du, false), df_scale_of(1.0, gi.dv, false), r.keys,
+                     r.order, r.sums, r.counts};
         wp_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
         note_launch(ctx, "wp_plan_kernel");
     }

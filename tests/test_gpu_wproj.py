@@ -82,6 +82,60 @@ def test_grid_and_degrid_match_oracle(ctx, case):
     assert peak_norm_err(pred_g, pred_o) <= TOL
 
 
+def _around(x):
+    """x and the doubles one and two ulps either side of it."""
+    lo1 = np.nextafter(x, -np.inf)
+    hi1 = np.nextafter(x, np.inf)
+    return [np.nextafter(lo1, -np.inf), lo1, x, hi1, np.nextafter(hi1, np.inf)]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_plan_decisions_at_rounding_boundaries(ctx, case):
+    """The plan's anchor, oversampling offset and plane decisions for samples
+    on and a few ulps either side of each kind of rounding boundary equal
+    the oracle's FP64 ones: the degridded value of every sample (which
+    selects its kernel by exactly those decisions) matches, and the same
+    samples are accepted."""
+    nx, cell_as, planes, sampling, law, wmax = case
+    og, ow, gg, gw = build(ctx, nx, cell_as, planes, sampling, law, wmax)
+    s = ow.sampling
+    G = og.gnx
+    rng = np.random.default_rng(77)
+    us, vs, ws = [], [], []
+    base_w = rng.uniform(-0.5 * wmax, 0.5 * wmax)
+    for k in rng.integers(G // 4, 3 * G // 4, 6):
+        # anchor boundaries x = k + 1/2 and offset boundaries x = k + (j + 1/2)/s
+        for frac in [0.5] + [(j + 0.5) / s for j in range(-s // 2, s // 2)]:
+            for du in _around((k + frac - G / 2) * og.du):
+                us.append(du)
+                vs.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                ws.append(base_w)
+                us.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                vs.append(-du)
+                ws.append(-base_w)
+    # plane boundaries |w| w_scale = (k + 1/2)^2
+    for k in range(planes):
+        for wv in _around((k + 0.5) ** 2 / ow.w_scale):
+            for sign in (1.0, -1.0):
+                us.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                vs.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                ws.append(sign * wv)
+    u, v, w = np.array(us), np.array(vs), np.array(ws)
+    n = len(u)
+    wt = np.ones(n, np.float32)
+    vis = np.ones(n, np.complex64)
+    b = cc.VisibilityBatch(u, v, vis, wt, w)
+    _, _, acc = ow.grid_dirty(u, v, w, wt, vis)
+    _, _, sums = cc.grid_dirty(gg, b, gw)
+    assert sums.gridded_samples == acc.gridded and sums.skipped_samples == acc.skipped
+    grid = (rng.normal(size=(og.gnx, og.gny)) + 1j * rng.normal(size=(og.gnx, og.gny))) \
+        .astype(np.complex64)
+    pred_o = ow.degrid(grid, u, v, w)
+    pred_g = cc.degrid(gg, b, grid, gw)
+    scale = np.maximum(np.abs(pred_o), 1e-3 * np.max(np.abs(pred_o)))
+    assert np.max(np.abs(pred_g - pred_o) / scale) <= 1e-3
+
+
 def test_plane_choice_and_conjugation(ctx):
     og, ow, gg, gw = build(ctx, *CASES[0][:5], CASES[0][5])
     # a single sample with w > 0 uses the conjugated kernel (lib.rs:95167);
