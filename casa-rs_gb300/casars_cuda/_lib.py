@@ -112,6 +112,7 @@ SIGNATURES = {
     "cr_ctx_set_image_fft_precision": (C.c_int, [_p, _i32]),
     "cr_ctx_set_image_fft_engine": (C.c_int, [_p, _i32]),
     "cr_ctx_set_alloc_limit": (C.c_int, [_p, _i64]),
+    "cr_ctx_set_timings": (C.c_int, [_p, _i32]),
     "cr_accumulator_create": (C.c_int, [_p, _p, C.POINTER(_p), _err]),
     "cr_accumulator_destroy": (None, [_p]),
     "cr_accumulator_add": (C.c_int, [_p, _p, C.POINTER(VisBatch), C.POINTER(Sums), _err]),

@@ -171,6 +171,12 @@ class Context:
         if self._lib.cr_ctx_set_image_fft_engine(self._h, code) != 0:
             raise ValueError(f"unsupported FFT engine {engine!r}")
 
+    def set_timings(self, enable: bool = True):
+        """Per-call stage and kernel timings (last_timings) on or off; off,
+        calls with device-resident outputs return without waiting."""
+        if self._lib.cr_ctx_set_timings(self._h, 1 if enable else 0) != 0:
+            raise ValueError("null context")
+
     def set_alloc_limit(self, nbytes: int = 0):
         """Test hook: a budget for the context's device workspaces (0 lifts
         it); a call that would grow them past it fails as a device

@@ -52,12 +52,15 @@ struct AuxFork {
     }
 };
 
+// Stage times of a call from events on its stream.  With the context's
+// timings off nothing is recorded and nothing waits for the events.
 struct StageTimer {
     cr_ctx* ctx;
     int n = 0;
     explicit StageTimer(cr_ctx* c) : ctx(c) { ctx->kev_used = 0; }
     void mark() {
-        if (n < 8) CR_CUDA_CHECK(cudaEventRecord(ctx->ev[n++], ctx->stream));
+        if (ctx->timings_enabled && n < 8)
+            CR_CUDA_CHECK(cudaEventRecord(ctx->ev[n++], ctx->stream));
     }
     float between(int a, int b) {
         if (b >= n || a >= n) return 0.0f;
@@ -70,6 +73,11 @@ struct StageTimer {
 
 // Stage times of a call plus the bracketed kernel times recorded during it.
 void set_timings(cr_ctx* ctx, cr_timings t) {
+    if (!ctx->timings_enabled) {
+        ctx->kev_used = 0;
+        ctx->timings = cr_timings{};
+        return;
+    }
     for (int k = 0; k < 2; ++k) {
         if (!(ctx->kev_used & (1 << k))) continue;
         float ms = 0.0f;
@@ -849,8 +857,8 @@ int cr_plan_create(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
 void cr_plan_destroy(cr_plan* p) {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
+    // the frees are ordered on the context's stream after the plan's work
     pool_free(p->ctx, p->pool);
-    cudaStreamSynchronize(p->ctx->stream);
     delete p;
 }
 
@@ -1325,6 +1333,12 @@ int cr_ctx_set_cube_graphs(cr_ctx* ctx, int32_t enable) {
 int cr_ctx_set_image_fft_precision(cr_ctx* ctx, int32_t bits) {
     if (!ctx || (bits != 0 && bits != 32 && bits != 64)) return CR_INVALID;
     ctx->image_fft_bits = bits == 32 ? 32 : 64;
+    return CR_OK;
+}
+
+int cr_ctx_set_timings(cr_ctx* ctx, int32_t enable) {
+    if (!ctx) return CR_INVALID;
+    ctx->timings_enabled = enable != 0;
     return CR_OK;
 }
 

@@ -69,7 +69,8 @@ void check_device_status(cr_ctx* ctx) {
 }
 
 void kernel_mark(cr_ctx* ctx, int which, bool end) {
-    if (ctx->capturing) return;   // a captured graph is timed as a whole
+    // a captured graph is timed as a whole; with timings off nothing is recorded
+    if (ctx->capturing || !ctx->timings_enabled) return;
     CR_CUDA_CHECK(cudaEventRecord(ctx->kev[which * 2 + (end ? 1 : 0)], ctx->stream));
     if (end) ctx->kev_used |= 1 << which;
 }

@@ -133,6 +133,9 @@ struct cr_ctx {
     // test hook: a budget (bytes) for the context's workspaces, 0 = none; a
     // call that would grow them past it fails as an allocation failure would
     int64_t alloc_limit = 0;
+    // per-call stage and kernel timings (cr_ctx_last_timings); off, calls
+    // record no events and do not wait for them
+    bool timings_enabled = true;
     long long barrier_polls = cr::kBarrierPollsDefault;
     long long mbar_polls = cr::kMbarPollsDefault;
 };

@@ -241,6 +241,7 @@ extern "C" {
     pub fn cr_ctx_set_image_fft_precision(ctx: *mut cr_ctx, bits: i32) -> c_int;
     pub fn cr_ctx_set_image_fft_engine(ctx: *mut cr_ctx, engine: i32) -> c_int;
     pub fn cr_ctx_set_alloc_limit(ctx: *mut cr_ctx, bytes: i64) -> c_int;
+    pub fn cr_ctx_set_timings(ctx: *mut cr_ctx, enable: i32) -> c_int;
     pub fn cr_version() -> *const c_char;
     pub fn cr_gridder_create(ctx: *mut cr_ctx, geom: *const cr_geometry, padding: f64, oversampling: i32, out: *mut *mut cr_gridder, info: *mut cr_grid_info, err: *mut *mut c_char) -> c_int;
     pub fn cr_gridder_destroy(g: *mut cr_gridder);

@@ -206,6 +206,14 @@ int cr_ctx_set_image_fft_engine(cr_ctx* ctx, int32_t engine);
  * (its allocation failures come from the host allocator).  CR_INVALID for a
  * negative budget. */
 int cr_ctx_set_alloc_limit(cr_ctx* ctx, int64_t bytes);
+/* Per-call stage and kernel timings (cr_ctx_last_timings) on (nonzero, the
+ * default) or off.  Collecting them makes every call wait for its events;
+ * with them off, cr_ctx_last_timings reports zeros and a call whose outputs
+ * all stay in device memory returns once its work is queued on the
+ * context's stream (calls that return host values still wait for them).
+ * New; no counterpart in the reference (ImagingStageTimings is always
+ * filled there). */
+int cr_ctx_set_timings(cr_ctx* ctx, int32_t enable);
 const char* cr_version(void);
 
 /* ---- gridders ------------------------------------------------------------
