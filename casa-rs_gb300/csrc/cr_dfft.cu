@@ -18,11 +18,12 @@
 // composite padding of gridder.rs:4152-4173) over an input loaded in
 // digit-reversed order, twiddles from a per-length table of
 // exp(2 pi i k / N) split into float pairs on the host.
-//   grid -> image: columns first (every grid column, only the image's rows
-//     kept), then the image's rows, whose output goes straight through the
-//     crop and correction of crop_correct_body;
-//   image -> grid: the image's rows first (the apodised image is zero
-//     outside them), then every grid column, written as the float32 grid.
+//   grid -> image: columns first (half of the grid's columns, only the
+//     image's rows kept), then the image's rows, two to a line, whose output
+//     goes straight through the crop and correction of crop_correct_body;
+//   image -> grid: the image's rows first, two to a line (the apodised
+//     image is zero outside them), then half of the grid's columns, written
+//     with their mirror images as the float32 grid.
 // The centring is the checkerboard modulation of cr_fft.cu.
 #include <cmath>
 #include <memory>
@@ -228,55 +229,90 @@ __device__ void line_transform(float4* sm, const DfStages& s, const float4* tw,
     }
 }
 
-// grid -> image, pass 1: column y of the modulated grid transformed along x;
-// the image's rows [bx0, bx0 + nx) kept in t[(x - bx0) gny + y].
+// Only real images leave and enter these transforms, so each works on half
+// of the spectrum.  With gnx and gny even, negating both indices keeps the
+// checkerboard's sign, and with g' the modulated grid:
+//   grid -> image: the real part of the inverse transform of g' is the
+//     inverse transform of its Hermitian part h(x, y) = (g'(x, y) +
+//     conj(g'(-x, -y))) / 2.  After the pass along x, column -y of h is the
+//     conjugate of column y, so only columns 0..gny/2 are transformed, and
+//     each image row is the real transform of a Hermitian line: two image
+//     rows r1, r2 go through one complex line as r1 + i r2.
+//   image -> grid: two real image rows go through one complex line as
+//     m1 + i m2 and are separated by the same symmetry (columns 0..gny/2
+//     kept); then columns 0..gny/2 are transformed along x and column -y
+//     written as the conjugate of column y.
+// The halves h, (Z + conj(Z')) / 2 are float-pair operations; h itself is
+// exact (a two-sum halved).
+
+// grid -> image, pass 1: column y (0 <= y <= gny/2) of h transformed along
+// x; the image's rows [bx0, bx0 + nx) kept in t[(x - bx0) gnyh + y].
 __global__ void __launch_bounds__(kDfThreads, 2) dfft_inv_cols(
-    const float2* grid, const float* real_grid, int64_t gny, int64_t bx0, int32_t nx,
-    const int32_t* src, const float4* tw, DfStages s, DfConsts c, float4* t) {
+    const float2* grid, const float* real_grid, int64_t gnx, int64_t gny, int64_t gnyh,
+    int64_t bx0, int32_t nx, const int32_t* src, const float4* tw, DfStages s, DfConsts c,
+    float4* t) {
     extern __shared__ float4 sm[];
-    const int64_t y = blockIdx.x;
+    const int64_t y = blockIdx.x, ym = y ? gny - y : 0;
     for (int i = threadIdx.x; i < s.n; i += blockDim.x) {
-        const int64_t x = src[i];
-        float re, im = 0.0f;
+        const int64_t x = src[i], xm = x ? gnx - x : 0;
+        float ar, ai = 0.0f, br, bi = 0.0f;
         if (real_grid) {
-            re = real_grid[x * gny + y];
+            ar = real_grid[x * gny + y];
+            br = real_grid[xm * gny + ym];
         } else {
-            const float2 v = grid[x * gny + y];
-            re = v.x;
-            im = v.y;
+            const float2 a = grid[x * gny + y], b = grid[xm * gny + ym];
+            ar = a.x;
+            ai = a.y;
+            br = b.x;
+            bi = b.y;
         }
-        if ((x + y) & 1) {
-            re = -re;
-            im = -im;
-        }
-        sm[i] = make_float4(re, 0.0f, im, 0.0f);
+        const dd re = two_sum(ar, br), im = two_sum(ai, -bi);
+        const float h = ((x + y) & 1) ? -0.5f : 0.5f;
+        sm[i] = make_float4(h * re.h, h * re.l, h * im.h, h * im.l);
     }
     __syncthreads();
     line_transform<true>(sm, s, tw, c);
-    for (int xr = threadIdx.x; xr < nx; xr += blockDim.x) t[xr * gny + y] = sm[bx0 + xr];
+    for (int xr = threadIdx.x; xr < nx; xr += blockDim.x) t[xr * gnyh + y] = sm[bx0 + xr];
 }
 
-// grid -> image, pass 2: image row xr transformed along y, then the crop and
-// correction of crop_correct_body (the same operations on the FP64 value).
+// grid -> image, pass 2: image rows 2b and 2b + 1 as one Hermitian-extended
+// line r1 + i r2 transformed along y (the real part is row 2b, the imaginary
+// part row 2b + 1), then the crop and correction of crop_correct_body (the
+// same operations on the FP64 value).
 __global__ void __launch_bounds__(kDfThreads, 2) dfft_inv_rows(
-    const float4* t, int64_t gny, int32_t ny, int64_t bx0, int64_t by0, int parity,
-    double scale, const float* corr_x, const float* corr_y, const float* sx, const float* sy,
-    int sinc_mode, const int32_t* src, const float4* tw, DfStages s, DfConsts c,
-    float* image) {
+    const float4* t, int64_t gny, int64_t gnyh, int32_t nx, int32_t ny, int64_t bx0,
+    int64_t by0, int parity, double scale, const float* corr_x, const float* corr_y,
+    const float* sx, const float* sy, int sinc_mode, const int32_t* src, const float4* tw,
+    DfStages s, DfConsts c, float* image) {
     extern __shared__ float4 sm[];
-    const int64_t xr = blockIdx.x, gx = bx0 + xr;
-    const float4* row = t + xr * gny;
-    for (int i = threadIdx.x; i < s.n; i += blockDim.x) sm[i] = row[src[i]];
+    const int64_t xr0 = 2 * (int64_t)blockIdx.x;
+    const bool two = xr0 + 1 < nx;
+    const float4* row1 = t + xr0 * gnyh;
+    const float4* row2 = row1 + gnyh;
+    for (int i = threadIdx.x; i < s.n; i += blockDim.x) {
+        const int64_t y = src[i];
+        const bool lower = y < gnyh;
+        const int64_t yy = lower ? y : gny - y;
+        const float4 a = row1[yy];
+        const float4 b = two ? row2[yy] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        // r1 + i r2 with r(-y) = conj(r(y)) for the upper half
+        const dd ar{a.x, a.y}, ai{a.z, a.w}, br{b.x, b.y}, bi{b.z, b.w};
+        const dd zr = lower ? dsub(ar, bi) : dadd(ar, bi);
+        const dd zi = lower ? dadd(ai, br) : dsub(br, ai);
+        sm[i] = make_float4(zr.h, zr.l, zi.h, zi.l);
+    }
     __syncthreads();
     line_transform<true>(sm, s, tw, c);
     // the scale as a float pair: the product's high part is the float32
     // value (float)(r * scale) of the FP64 path, but for ties at half an ulp
     const float sh = (float)scale;
     const dd sc{sh, (float)(scale - (double)sh)};
-    for (int yr = threadIdx.x; yr < ny; yr += blockDim.x) {
-        const int64_t gy = by0 + yr;
+    for (int k = threadIdx.x; k < (two ? 2 * ny : ny); k += blockDim.x) {
+        const int q = k >= ny;
+        const int64_t yr = k - q * ny, gy = by0 + yr, xr = xr0 + q, gx = bx0 + xr;
         const float4 w = sm[gy];
-        const dd r = ((gx + gy + parity) & 1) ? dd{-w.x, -w.y} : dd{w.x, w.y};
+        dd r = q ? dd{w.z, w.w} : dd{w.x, w.y};
+        if ((gx + gy + parity) & 1) r = dneg(r);
         float v = dmul(r, sc).h;
         const float factor = __fmul_rn(corr_x[gx], corr_y[gy]);
         if (sinc_mode == 1) {
@@ -291,46 +327,64 @@ __global__ void __launch_bounds__(kDfThreads, 2) dfft_inv_rows(
     }
 }
 
-// image -> grid, pass 1: row xr of the apodised, modulated model (zero
-// outside the image's columns) transformed along y into t[xr gny + y].
+// image -> grid, pass 1: rows 2b and 2b + 1 of the apodised, modulated model
+// (zero outside the image's columns) as one line m1 + i m2 transformed along
+// y, separated into each row's half spectrum t[xr gnyh + y], y <= gny/2.
 __global__ void __launch_bounds__(kDfThreads, 2) dfft_fwd_rows(
-    const float* model, int32_t ny, int64_t gny, int64_t bx0, int64_t by0, const float* corr_x,
-    const float* corr_y, const float* sinc_x, const float* sinc_y, const int32_t* src,
-    const float4* tw, DfStages s, DfConsts c, float4* t) {
+    const float* model, int32_t nx, int32_t ny, int64_t gny, int64_t gnyh, int64_t bx0,
+    int64_t by0, const float* corr_x, const float* corr_y, const float* sinc_x,
+    const float* sinc_y, const int32_t* src, const float4* tw, DfStages s, DfConsts c,
+    float4* t) {
     extern __shared__ float4 sm[];
-    const int64_t xr = blockIdx.x, gx = bx0 + xr;
+    const int64_t xr0 = 2 * (int64_t)blockIdx.x, gx0 = bx0 + xr0;
+    const bool two = xr0 + 1 < nx;
     for (int i = threadIdx.x; i < s.n; i += blockDim.x) {
         const int64_t gy = src[i];
-        float v = 0.0f;
+        float v[2] = {0.0f, 0.0f};
         if (gy >= by0 && gy < by0 + ny) {
-            // apodize_body's operations
-            float f = __fmul_rn(corr_x[gx], corr_y[gy]);
-            if (sinc_x) f = __fmul_rn(__fmul_rn(f, sinc_x[gx]), sinc_y[gy]);
-            v = model[xr * ny + (gy - by0)] * f;
-            if ((gx + gy) & 1) v = -v;
+            for (int q = 0; q < (two ? 2 : 1); ++q) {
+                const int64_t gx = gx0 + q;
+                // apodize_body's operations
+                float f = __fmul_rn(corr_x[gx], corr_y[gy]);
+                if (sinc_x) f = __fmul_rn(__fmul_rn(f, sinc_x[gx]), sinc_y[gy]);
+                float u = model[(xr0 + q) * ny + (gy - by0)] * f;
+                if ((gx + gy) & 1) u = -u;
+                v[q] = u;
+            }
         }
-        sm[i] = make_float4(v, 0.0f, 0.0f, 0.0f);
+        sm[i] = make_float4(v[0], 0.0f, v[1], 0.0f);
     }
     __syncthreads();
     line_transform<false>(sm, s, tw, c);
-    float4* row = t + xr * gny;
-    for (int y = threadIdx.x; y < s.n; y += blockDim.x) row[y] = sm[y];
+    float4* row1 = t + xr0 * gnyh;
+    for (int k = threadIdx.x; k < (two ? 2 * gnyh : gnyh); k += blockDim.x) {
+        const int q = k >= gnyh;
+        const int64_t y = k - q * gnyh;
+        const float4 a = sm[y], b = sm[y ? gny - y : 0];
+        const dd ar{a.x, a.y}, ai{a.z, a.w}, br{b.x, b.y}, bi{b.z, b.w};
+        // row 1: (Z(y) + conj(Z(-y))) / 2; row 2: (Z(y) - conj(Z(-y))) / 2i
+        const dd re = q ? dadd(ai, bi) : dadd(ar, br);
+        const dd im = q ? dsub(br, ar) : dsub(ai, bi);
+        row1[q * gnyh + y] = make_float4(0.5f * re.h, 0.5f * re.l, 0.5f * im.h, 0.5f * im.l);
+    }
 }
 
-// image -> grid, pass 2: column y transformed along x (rows outside
-// [bx0, bx0 + nx) are zero), the output checkerboard, float32 grid.
+// image -> grid, pass 2: column y (0 <= y <= gny/2) transformed along x
+// (rows outside [bx0, bx0 + nx) are zero), the output checkerboard, float32
+// grid; column -y written as the conjugate of column y at -x.
 __global__ void __launch_bounds__(kDfThreads, 2) dfft_fwd_cols(
-    const float4* t, int64_t gny, int32_t nx, int64_t bx0, int parity, const int32_t* src,
-    const float4* tw, DfStages s, DfConsts c, float2* grid) {
+    const float4* t, int64_t gny, int64_t gnyh, int32_t nx, int64_t bx0, int parity,
+    const int32_t* src, const float4* tw, DfStages s, DfConsts c, float2* grid) {
     extern __shared__ float4 sm[];
     const int64_t y = blockIdx.x;
     for (int i = threadIdx.x; i < s.n; i += blockDim.x) {
         const int64_t x = src[i];
-        sm[i] = (x >= bx0 && x < bx0 + nx) ? t[(x - bx0) * gny + y]
+        sm[i] = (x >= bx0 && x < bx0 + nx) ? t[(x - bx0) * gnyh + y]
                                            : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     __syncthreads();
     line_transform<false>(sm, s, tw, c);
+    const bool mirror = y != 0 && y != gnyh - 1;
     for (int x = threadIdx.x; x < s.n; x += blockDim.x) {
         const float4 w = sm[x];
         // the pairs are normalised: the high part is the float32 value
@@ -340,6 +394,7 @@ __global__ void __launch_bounds__(kDfThreads, 2) dfft_fwd_cols(
             im = -im;
         }
         grid[(int64_t)x * gny + y] = make_float2(re, im);
+        if (mirror) grid[(int64_t)(x ? s.n - x : 0) * gny + (gny - y)] = make_float2(re, -im);
     }
 }
 
@@ -438,43 +493,43 @@ bool dfft_supported(int64_t gnx, int64_t gny) {
 void dfft_grid_to_image(cr_ctx* ctx, cr_gridder* g, const float2* grid, const float* real_grid,
                         double scale, const float* sx, const float* sy, int sinc_mode,
                         float* image) {
-    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny, gnyh = gny / 2 + 1;
     const int32_t nx = g->geom.nx, ny = g->geom.ny;
     const DfPlan& px = plan_for(ctx, gnx);
     const DfPlan& py = plan_for(ctx, gny);
     const DfConsts c = consts();
-    float4* t = (float4*)workspace(ctx, "dfft_t", (size_t)nx * gny * 16);
+    float4* t = (float4*)workspace(ctx, "dfft_t", (size_t)nx * gnyh * 16);
     const size_t smx = (size_t)gnx * 16, smy = (size_t)gny * 16;
     allow_smem(dfft_inv_cols, smx);
     allow_smem(dfft_inv_rows, smy);
-    dfft_inv_cols<<<(unsigned)gny, kDfThreads, smx, ctx->stream>>>(
-        grid, real_grid, gny, g->info.blc_x, nx, px.src, px.tw, stages(px), c, t);
+    dfft_inv_cols<<<(unsigned)gnyh, kDfThreads, smx, ctx->stream>>>(
+        grid, real_grid, gnx, gny, gnyh, g->info.blc_x, nx, px.src, px.tw, stages(px), c, t);
     note_launch(ctx, "dfft_inv_cols");
     const int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
-    dfft_inv_rows<<<(unsigned)nx, kDfThreads, smy, ctx->stream>>>(
-        t, gny, ny, g->info.blc_x, g->info.blc_y, parity, scale, g->corr_x_d, g->corr_y_d, sx,
-        sy, sinc_mode, py.src, py.tw, stages(py), c, image);
+    dfft_inv_rows<<<(unsigned)((nx + 1) / 2), kDfThreads, smy, ctx->stream>>>(
+        t, gny, gnyh, nx, ny, g->info.blc_x, g->info.blc_y, parity, scale, g->corr_x_d,
+        g->corr_y_d, sx, sy, sinc_mode, py.src, py.tw, stages(py), c, image);
     note_launch(ctx, "dfft_inv_rows");
 }
 
 void dfft_image_to_grid(cr_ctx* ctx, cr_gridder* g, const float* model, const float* sinc_x,
                         const float* sinc_y, float2* grid) {
-    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny;
+    const int64_t gnx = g->info.grid_nx, gny = g->info.grid_ny, gnyh = gny / 2 + 1;
     const int32_t nx = g->geom.nx, ny = g->geom.ny;
     const DfPlan& px = plan_for(ctx, gnx);
     const DfPlan& py = plan_for(ctx, gny);
     const DfConsts c = consts();
-    float4* t = (float4*)workspace(ctx, "dfft_t", (size_t)nx * gny * 16);
+    float4* t = (float4*)workspace(ctx, "dfft_t", (size_t)nx * gnyh * 16);
     const size_t smx = (size_t)gnx * 16, smy = (size_t)gny * 16;
     allow_smem(dfft_fwd_rows, smy);
     allow_smem(dfft_fwd_cols, smx);
-    dfft_fwd_rows<<<(unsigned)nx, kDfThreads, smy, ctx->stream>>>(
-        model, ny, gny, g->info.blc_x, g->info.blc_y, g->corr_x_d, g->corr_y_d, sinc_x, sinc_y,
-        py.src, py.tw, stages(py), c, t);
+    dfft_fwd_rows<<<(unsigned)((nx + 1) / 2), kDfThreads, smy, ctx->stream>>>(
+        model, nx, ny, gny, gnyh, g->info.blc_x, g->info.blc_y, g->corr_x_d, g->corr_y_d,
+        sinc_x, sinc_y, py.src, py.tw, stages(py), c, t);
     note_launch(ctx, "dfft_fwd_rows");
     const int parity = (int)(((gnx / 2) + (gny / 2)) & 1);
-    dfft_fwd_cols<<<(unsigned)gny, kDfThreads, smx, ctx->stream>>>(
-        t, gny, nx, g->info.blc_x, parity, px.src, px.tw, stages(px), c, grid);
+    dfft_fwd_cols<<<(unsigned)gnyh, kDfThreads, smx, ctx->stream>>>(
+        t, gny, gnyh, nx, g->info.blc_x, parity, px.src, px.tw, stages(px), c, grid);
     note_launch(ctx, "dfft_fwd_cols");
 }
 

@@ -7,7 +7,8 @@ model grids they return may differ only where the last rounding to float32
 falls on the other side: within four float32 ulps of each value (plus 1e-10
 of the peak for values near zero).  Checked for standard and W-projection
 geometries (sinc division and the adjoint's sinc product), the PSF's
-real-grid input, and the headline 4096^2 image on its 5000^2 grid.  The
+real-grid input, odd image sizes (the transforms take image rows two at a
+time), and the headline 4096^2 image on its 5000^2 grid.  The
 oracle-parity tests of the other files run on the float-pair default.
 """
 import numpy as np
@@ -54,7 +55,7 @@ def _random_grid(rng, shape):
     return (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64)
 
 
-@pytest.mark.parametrize("nx", [64, 96, 250, 512])
+@pytest.mark.parametrize("nx", [64, 75, 96, 101, 250, 512])   # odd nx: a last row unpaired
 def test_grid_to_image_and_back(ctx, nx):
     rng = np.random.default_rng(nx)
     cell = 2e-5
