@@ -99,6 +99,10 @@ def _device_of(*arrays):
 # ----------------------------------------------------------------------------
 # context and data types
 # ----------------------------------------------------------------------------
+# cudaStreamLegacy: the handle of CUDA's legacy default stream
+CUDA_STREAM_LEGACY = 1
+
+
 class Context:
     """One CUDA device and stream (the library's cr_ctx)."""
 
@@ -126,8 +130,14 @@ class Context:
             pass
 
     def use_torch_stream(self):
+        """Run the following calls on torch's current stream, so that they are
+        ordered with the torch work that makes their inputs and reads their
+        outputs.  Torch's default stream is CUDA's legacy default stream
+        (handle 0), which the library takes as cudaStreamLegacy (1): a null
+        handle would select the context's own stream instead."""
         if torch is not None and torch.cuda.is_available():
-            call("cr_ctx_set_stream", self._h, C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+            handle = torch.cuda.current_stream(self.device).cuda_stream
+            call("cr_ctx_set_stream", self._h, C.c_void_p(handle if handle else CUDA_STREAM_LEGACY))
 
     def use_own_stream(self):
         call("cr_ctx_set_stream", self._h, None)

@@ -361,6 +361,8 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err) {
         CR_CUDA_CHECK(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
         CR_CUDA_CHECK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
         CR_CUDA_CHECK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
+        for (auto& e : c->stage_ev)
+            CR_CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         for (auto& e : c->ev) CR_CUDA_CHECK(cudaEventCreate(&e));
         for (auto& e : c->kev) CR_CUDA_CHECK(cudaEventCreate(&e));
         CR_CUDA_CHECK(cudaMallocHost(&c->pinned, 4096));
@@ -396,6 +398,8 @@ void cr_ctx_destroy(cr_ctx* ctx) {
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+    for (auto& e : ctx->stage_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -570,7 +574,7 @@ int cr_grid_dirty(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* 
         bind(ctx);
         StageTimer tm(ctx);
         tm.mark();
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         float2* psf = out_ptr<float2>(ctx, psf_grid, out_location, gb, "psf_grid");
         float2* dirty = out_ptr<float2>(ctx, dirty_grid, out_location, gb, "dirty_grid");
@@ -600,7 +604,7 @@ int cr_degrid(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* batc
         bind(ctx);
         StageTimer tm(ctx);
         tm.mark();
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         const float2* grid = (const float2*)device_input(ctx, model_grid, grid_bytes(g),
                                                          grid_location, "model_grid");
         Records r = plan(ctx, g, wp, b);
@@ -622,7 +626,7 @@ int cr_grid_residual(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batc
         need(ctx != nullptr, "context is null");
         check_wp(g, wp);
         bind(ctx);
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         Records r = plan(ctx, g, wp, b);
         if (model_grid) {
@@ -699,21 +703,27 @@ static void dirty_products(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, float2* psf
     unsigned int* peak_d = (unsigned int*)workspace(ctx, "di_peak", 4);
     grid_to_image(ctx, g, wp, psf, k / sumwt_f, psf_img, image_single(ctx));
     abs_peak(ctx, psf_img, (int64_t)np, peak_d);
-    unsigned int peak_bits = 0;
-    CR_CUDA_CHECK(cudaMemcpyAsync(&peak_bits, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
-    float peak;
-    std::memcpy(&peak, &peak_bits, 4);
-    if (!(std::isfinite(peak) && peak > 0.0f))
-        fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
+    // the scaling reads the peak on the device; the host checks it once both
+    // images are done, so nothing waits in between
+    unsigned int* peak_h = (unsigned int*)((char*)ctx->pinned + 256);
+    CR_CUDA_CHECK(cudaMemcpyAsync(peak_h, peak_d, 4, cudaMemcpyDeviceToHost, ctx->stream));
     scale_image(ctx, psf_img, (int64_t)np, 1.0f, peak_d);
+    AuxFork fork(ctx);
+    if (out_location == CR_HOST) {
+        // the PSF image goes back while the residual is transformed
+        fork.to_aux();
+        copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
+        fork.to_main();
+    }
     grid_to_image(ctx, g, wp, dirty, k / sumwt_f, res_img, image_single(ctx));
     scale_image(ctx, res_img, (int64_t)np, 1.0f, peak_d);
-    if (out_location == CR_HOST) {
-        copy_out(ctx, psf_out, psf_img, np * 4, CR_HOST);
-        copy_out(ctx, residual_out, res_img, np * 4, CR_HOST);
-    }
+    if (out_location == CR_HOST) copy_out(ctx, residual_out, res_img, np * 4, CR_HOST);
+    fork.join();
     CR_CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+    float peak;
+    std::memcpy(&peak, peak_h, 4);
+    if (!(std::isfinite(peak) && peak > 0.0f))
+        fail(CR_NORMALIZATION, "PSF peak is non-finite or zero");
     if (state) *state = cr_psf_state{peak, sumwt_f, (float)s.reported_sumwt};
 }
 
@@ -726,7 +736,7 @@ int cr_dirty_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
         bind(ctx);
         StageTimer tm(ctx);
         tm.mark();
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         float2* psf = (float2*)workspace(ctx, "di_psf", gb);
         float2* dirty = (float2*)workspace(ctx, "di_dirty", gb);
@@ -753,7 +763,7 @@ int cr_residual_image(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_bat
         need(state->normalization_sumwt > 0.0f && state->psf_peak > 0.0f, "invalid PSF state");
         check_wp(g, wp);
         bind(ctx);
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         const size_t np = image_pixels(g);
         const float* m = (const float*)device_input(ctx, model, np * 4, model_location, "model");
@@ -782,7 +792,7 @@ int cr_predict(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         need(ctx != nullptr && model != nullptr, "null argument");
         check_wp(g, wp);
         bind(ctx);
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         // the model's upload and transform run beside the plan
         AuxFork fork(ctx);
@@ -808,7 +818,7 @@ int cr_adjoint(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch* bat
         need(ctx != nullptr, "context is null");
         check_wp(g, wp);
         bind(ctx);
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         size_t gb = grid_bytes(g);
         Records r = plan(ctx, g, wp, b);
         CR_CUDA_CHECK(cudaMemsetAsync(r.rec_pred, 0, (size_t)(b.n > 0 ? b.n : 1) * 8, ctx->stream));
@@ -835,7 +845,7 @@ int cr_plan_create(cr_ctx* ctx, cr_gridder* g, cr_wproj* wp, const cr_vis_batch*
         bind(ctx);
         StageTimer tm(ctx);
         tm.mark();
-        DeviceBatch b = device_batch(ctx, batch, wp != nullptr);
+        StagedBatch b(ctx, batch, wp != nullptr);
         cr_plan* p = new cr_plan();
         p->ctx = ctx;
         p->g = g;
@@ -1720,7 +1730,7 @@ int cr_accumulator_add(cr_ctx* ctx, cr_accumulator* a, const cr_vis_batch* batch
         bind(ctx);
         StageTimer tm(ctx);
         tm.mark();
-        DeviceBatch b = device_batch(ctx, batch, false);
+        StagedBatch b(ctx, batch, false);
         Records r = plan(ctx, a->g, nullptr, b);
         tm.mark();
         grid_records(ctx, a->g, nullptr, r, a->psf, a->dirty, 0);

@@ -465,6 +465,74 @@ DeviceBatch device_batch(cr_ctx* ctx, const cr_vis_batch* b, bool need_w) {
     return d;
 }
 
+// Host batches below this many samples are uploaded in one go.
+constexpr int64_t kStageMinSamples = (int64_t)1 << 20;
+
+StagedBatch::StagedBatch(cr_ctx* c, const cr_vis_batch* b, bool need_w) : ctx(c) {
+    if (!b || b->location != CR_HOST || b->n < kStageMinSamples) {
+        static_cast<DeviceBatch&>(*this) = device_batch(c, b, need_w);
+        return;
+    }
+    // device_batch's checks
+    if (b->n >= (int64_t)1 << 31) fail(CR_INVALID, "batch larger than 2^31 samples");
+    if (!b->u || !b->v || !b->weight || !b->vis) fail(CR_INVALID, "batch lacks u, v, weight or vis");
+    if (need_w && !b->w) fail(CR_INVALID, "W-projection needs w coordinates");
+    const size_t n_s = (size_t)b->n;
+    struct Col {
+        const void* host;
+        size_t elem;
+        const char* name;
+        void* dev;
+    } cols[7] = {{b->u, 8, "u", nullptr},
+                 {b->v, 8, "v", nullptr},
+                 {need_w ? b->w : nullptr, 8, "w", nullptr},
+                 {b->weight, 4, "weight", nullptr},
+                 {b->sumwt_factor, 4, "sumwt", nullptr},
+                 {b->gridable, 1, "gridable", nullptr},
+                 {b->vis, 8, "vis", nullptr}};
+    // the same workspaces as device_input's, allocated on the main stream
+    // before the auxiliary stream is forked from it
+    for (Col& col : cols)
+        if (col.host) col.dev = workspace(c, std::string("in_") + col.name, n_s * col.elem);
+    n = b->n;
+    u = (const double*)cols[0].dev;
+    v = (const double*)cols[1].dev;
+    w = (const double*)cols[2].dev;
+    weight = (const float*)cols[3].dev;
+    sumwt_factor = (const float*)cols[4].dev;
+    gridable = (const uint8_t*)cols[5].dev;
+    vis = (const float2*)cols[6].dev;
+    CR_CUDA_CHECK(cudaEventRecord(c->fork_ev, c->stream));
+    CR_CUDA_CHECK(cudaStreamWaitEvent(c->aux_stream, c->fork_ev, 0));
+    // from here on the destructor joins whatever was queued
+    nchunks = kStageChunks;
+    stage_ev = c->stage_ev;
+    int64_t lo = 0;
+    try {
+        for (int k = 0; k < kStageChunks; ++k) {
+            const int64_t hi = b->n * (k + 1) / kStageChunks;
+            chunk_end[k] = hi;
+            for (const Col& col : cols)
+                if (col.host)
+                    CR_CUDA_CHECK(cudaMemcpyAsync((char*)col.dev + lo * col.elem,
+                                                  (const char*)col.host + lo * col.elem,
+                                                  (size_t)(hi - lo) * col.elem,
+                                                  cudaMemcpyHostToDevice, c->aux_stream));
+            CR_CUDA_CHECK(cudaEventRecord(c->stage_ev[k], c->aux_stream));
+            lo = hi;
+        }
+    } catch (...) {
+        // no destructor runs for a half-built batch: join the copies here
+        cudaEventRecord(c->join_ev, c->aux_stream);
+        cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+        throw;
+    }
+}
+
+StagedBatch::~StagedBatch() {
+    if (nchunks > 0) cudaStreamWaitEvent(ctx->stream, ctx->stage_ev[nchunks - 1], 0);
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against the driver library).
 bool encode_tensor_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1,

@@ -77,6 +77,8 @@ struct DfPlan;      // a float-pair transform plan for one line length (cr_dfft.
 // polls: milliseconds).  cr_ctx_set_wait_limits lowers them for tests.
 constexpr long long kBarrierPollsDefault = 1ll << 24;
 constexpr long long kMbarPollsDefault = 1ll << 22;
+// pieces of a staged host batch upload (StagedBatch)
+constexpr int kStageChunks = 4;
 
 }  // namespace cr
 
@@ -91,6 +93,8 @@ struct cr_ctx {
     // call, forked from and joined back to `stream` by these events
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    // one per chunk of a host batch uploaded on aux_stream (StagedBatch)
+    cudaEvent_t stage_ev[cr::kStageChunks] = {};
     cr::Pool ws;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans;
     std::map<std::pair<int64_t, int64_t>, cufftHandle> fft_plans_c2c;
@@ -227,8 +231,28 @@ struct DeviceBatch {
     const float* sumwt_factor = nullptr;
     const uint8_t* gridable = nullptr;
     const float2* vis = nullptr;
+    // staged uploads (StagedBatch): piece k, samples [chunk_end[k - 1],
+    // chunk_end[k]), is on the device once stage_ev[k] has completed
+    int nchunks = 0;
+    int64_t chunk_end[kStageChunks] = {};
+    const cudaEvent_t* stage_ev = nullptr;
 };
 DeviceBatch device_batch(cr_ctx* ctx, const cr_vis_batch* b, bool need_w);
+
+// A batch for the calls that plan it straight away.  A large host batch is
+// uploaded in kStageChunks pieces on the auxiliary stream, each followed by
+// one of ctx->stage_ev, so that the plan kernel starts on the first piece
+// while the others are still copying (plan_wproj / plan_standard wait for
+// each piece before planning it).  Otherwise it is device_batch's.  When the
+// batch goes out of scope the main stream waits for the last piece, so no
+// copy outlives the call whatever path it takes.
+struct StagedBatch : DeviceBatch {
+    cr_ctx* ctx = nullptr;
+    StagedBatch(cr_ctx* c, const cr_vis_batch* b, bool need_w);
+    StagedBatch(const StagedBatch&) = delete;
+    StagedBatch& operator=(const StagedBatch&) = delete;
+    ~StagedBatch();
+};
 
 // Host or device source -> device pointer (copies host data into a named
 // workspace).

@@ -27,7 +27,7 @@ __host__ __device__ inline int bits_for(uint64_t max_value) {
 }
 
 struct WpPlanArgs {
-    int64_t n;
+    int64_t first, n;   // samples [first, n)
     const double *u, *v, *w;
     const float *weight, *sumwt;
     const uint8_t* gridable;
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
     double s_norm = 0.0, s_rep = 0.0;
     unsigned long long c_ok = 0, c_skip = 0;
     const uint64_t invalid = ~0ull;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+    for (int64_t i = a.first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t key = invalid;
         float wt = a.weight[i];
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
 }
 
 struct StdPlanArgs {
-    int64_t n;
+    int64_t first, n;   // samples [first, n)
     const double *u, *v;
     const float *weight, *sumwt;
     const uint8_t* gridable;
@@ -256,7 +256,7 @@ __device__ __forceinline__ bool tap_span(double coord, int64_t size, int32_t os,
 __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
     double s_norm = 0.0;
     unsigned long long c_ok = 0, c_skip = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+    for (int64_t i = a.first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t key = ~0ull;
         float wt = a.weight[i];
@@ -426,6 +426,23 @@ __global__ void tile_starts(const uint32_t* tile_of, const unsigned long long* c
     }
 }
 
+// fn(lo, hi) over the batch's samples: once over all of them, or piece by
+// piece for a staged upload, each after the main stream has waited for its
+// copies (the last wait also orders every later use of the batch)
+template <typename F>
+void for_each_piece(cr_ctx* ctx, const DeviceBatch& b, F fn) {
+    if (b.nchunks == 0) {
+        fn(0, b.n);
+        return;
+    }
+    int64_t lo = 0;
+    for (int k = 0; k < b.nchunks; ++k) {
+        CR_CUDA_CHECK(cudaStreamWaitEvent(ctx->stream, b.stage_ev[k], 0));
+        if (b.chunk_end[k] > lo) fn(lo, b.chunk_end[k]);
+        lo = b.chunk_end[k];
+    }
+}
+
 Records allocate_records(cr_ctx* ctx, int64_t n, int64_t ntx, int64_t nty, Pool* pool) {
     Records r;
     size_t nn = (size_t)(n > 0 ? n : 1);
@@ -500,14 +517,18 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) 
     int key_bits = tile_bits + plane_bits + 1 + off_bits + 10;
     if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");
     if (b.n > 0) {
-        WpPlanArgs a{b.n, b.u, b.v, b.w, b.weight, b.sumwt_factor, b.gridable, b.vis,
+        WpPlanArgs a{0, b.n, b.u, b.v, b.w, b.weight, b.sumwt_factor, b.gridable, b.vis,
                      gi.grid_nx, gi.grid_ny, gi.du, gi.dv, wp->info.w_scale,
                      wp->info.sampling, wp->info.planes, wp->radius, wp->axis,
                      wp->support_d, wp->norm_d, nty, plane_bits, off_bits,
                      df_scale_of(1.0, gi.du, false), df_scale_of(1.0, gi.dv, false), r.keys,
                      r.order, r.sums, r.counts};
-        wp_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
-        note_launch(ctx, "wp_plan_kernel");
+        for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
+            a.first = lo;
+            a.n = hi;
+            wp_plan_kernel<<<grid_blocks(hi - lo, 256), 256, 0, ctx->stream>>>(a);
+            note_launch(ctx, "wp_plan_kernel");
+        });
     }
     finish_records(ctx, r, 0, key_bits, plane_bits, off_bits, b, wp->support_d);
     return r;
@@ -521,11 +542,15 @@ Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* po
     int key_bits = tile_bits + 16 + 10;
     if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");
     if (b.n > 0) {
-        StdPlanArgs a{b.n, b.u, b.v, b.weight, b.sumwt_factor, b.gridable, gi.grid_nx,
+        StdPlanArgs a{0, b.n, b.u, b.v, b.weight, b.sumwt_factor, b.gridable, gi.grid_nx,
                       gi.grid_ny, gi.du, gi.dv, gi.oversampling, g->tap_rows, nty, r.keys,
                       r.order, r.sums, r.counts};
-        std_plan_kernel<<<grid_blocks(b.n, 256), 256, 0, ctx->stream>>>(a);
-        note_launch(ctx, "std_plan_kernel");
+        for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
+            a.first = lo;
+            a.n = hi;
+            std_plan_kernel<<<grid_blocks(hi - lo, 256), 256, 0, ctx->stream>>>(a);
+            note_launch(ctx, "std_plan_kernel");
+        });
     }
     finish_records(ctx, r, 1, key_bits, 0, 0, b, nullptr);
     return r;

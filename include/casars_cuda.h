@@ -165,7 +165,9 @@ int cr_ctx_create(int32_t device, cr_ctx** out, char** err);
 void cr_ctx_destroy(cr_ctx* ctx);
 void cr_free_error(char* err);
 /* Use an external cudaStream_t (e.g. torch's current stream); NULL restores
- * the context's own stream. */
+ * the context's own stream (non-blocking: not ordered with the legacy
+ * default stream).  To run on the legacy default stream (torch's default
+ * stream, whose handle is 0) pass cudaStreamLegacy ((void*)1). */
 int cr_ctx_set_stream(cr_ctx* ctx, void* stream, char** err);
 void* cr_ctx_stream(cr_ctx* ctx);
 int cr_ctx_synchronize(cr_ctx* ctx, char** err);
