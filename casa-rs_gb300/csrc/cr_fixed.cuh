@@ -113,8 +113,8 @@ __device__ __forceinline__ int fix_tap_span(long long X, int64_t size, int32_t o
 
 // ---- float32-pair fast path ---------------------------------------------------
 // Before the integer path, the same decisions are tried in float32 pairs:
-// a = ah + al (ah = RN32(a), al = RN32(a - ah)) and K = kh + kl, both to
-// about 2^-48 relative; the product a K is then p + e with p = RN(ah kh),
+// a = ah + al (ah = RN32(a), al = RN32(a - ah), or df_split's truncated ah)
+// and K = kh + kl, both to about 2^-47 relative; the product a K is then p + e with p = RN(ah kh),
 // e = fma(ah, kh, -p) + ah kl + al kh (three FMAs), about 2^-44 |a K| from
 // the exact value.  A decision is taken only when the exact value lies more
 // than kDfMargin (in the decision's own units: cells for the anchor,
@@ -148,6 +148,29 @@ __device__ __forceinline__ void df_product(float ah, float al, DfScale k, float*
     er = __fmaf_rn(al, k.hi, er);
     *p = ph;
     *e = er;
+}
+
+// The float32 pair of a double from its bits, without FP64 instructions
+// (GB300 issues FP64 at a small fraction of its float32 rate): hi = x with
+// its significand truncated to 24 bits, lo = RN32(x - hi) (x - hi is the
+// low 29 significand bits, converted as an integer and scaled by an exact
+// power of two), so |x - (hi + lo)| <= 2^-47 |x|.  False for non-finite x
+// and for 0 < |x| < 2^-70 or |x| >= 2^100; zero splits into (+-0, 0).
+__device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    if ((b << 1) == 0ull) {
+        *hi = __uint_as_float(sign);
+        *lo = 0.0f;
+        return true;
+    }
+    const int e = (int)((b >> 52) & 0x7ffull) - 1023;
+    if (e < -70 || e >= 100) return false;
+    *hi = __uint_as_float(sign | (unsigned)(e + 127) << 23 | (unsigned)((b >> 29) & 0x7fffffull));
+    const float r = __int2float_rn((int)(b & 0x1fffffffull)) *
+                    __uint_as_float((unsigned)(e - 52 + 127) << 23);
+    *lo = sign ? -r : r;
+    return true;
 }
 
 // The integer a nearest to x = p + e + h (h = 0 or 1/2) and dh = RN(p + h) - a

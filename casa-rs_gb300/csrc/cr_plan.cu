@@ -3,14 +3,19 @@
 //
 // The plan restates WProjector::plan_sample (gridder.rs:3588-3624) and
 // StandardGridder::plan_positive_taps / sample_tap_span (gridder.rs:540-566,
-// 1877-1886, 1958-1995) in FP64 with the reference's rounding (round half
-// away from zero), so the chosen cell, oversampling offset and w-plane are
-// bit-identical to the reference's.  Each valid sample gets a 64-bit key
+// 1877-1886, 1958-1995) with the reference's FP64 rounding (round half away
+// from zero), so the chosen cell, oversampling offset and w-plane are
+// bit-identical to the reference's.  The decisions are taken on float32
+// pairs where they lie clear of a rounding boundary (cr_fixed.cuh) and by
+// the reference's FP64 operations otherwise: GB300 issues FP64 at a small
+// fraction of its float32 rate, and planning was FP64-bound.  Each valid
+// sample gets a 64-bit key
 //   home tile | (plane | conj | offset)  or  (x tap row | y tap row) | cell
 // and the keys are radix-sorted.  Samples with equal keys have identical taps;
 // their weighted visibilities and weights are summed into one record, so
-// every distinct tap footprint is convolved once.  The sort is stable and the
-// record sums are accumulated in FP64.
+// every distinct tap footprint is convolved once.  The sort is stable; the
+// sums of weights and the record sums are compensated float32-pair sums of
+// exact products, carried in FP64 across warps.
 #include <cmath>
 
 #include "cr_fixed.cuh"
@@ -40,6 +45,7 @@ struct WpPlanArgs {
     int64_t nty;
     int plane_bits, off_bits;
     DfScale kx, ky;            // 1 / du, 1 / dv as float32 pairs
+    DfScale kw;                // w_scale as a float32 pair
     uint64_t* keys;
     uint32_t* vals;
     double* sums;
@@ -58,16 +64,12 @@ __device__ __forceinline__ unsigned long long warp_sum_u(unsigned long long x) {
     return x;
 }
 
-// Block-wide accumulation of the two FP64 sums and two counters.
-__device__ void block_accumulate(double s0, double s1, unsigned long long c0,
-                                 unsigned long long c1, double* sums,
-                                 unsigned long long* counts) {
+// Block-wide accumulation of two FP64 sums and two counters, from values
+// already summed over each warp (held by lane 0).
+__device__ void block_finish(double s0, double s1, unsigned long long c0, unsigned long long c1,
+                             double* sums, unsigned long long* counts) {
     __shared__ double sh_s[2][32];
     __shared__ unsigned long long sh_c[2][32];
-    s0 = warp_sum_d(s0);
-    s1 = warp_sum_d(s1);
-    c0 = warp_sum_u(c0);
-    c1 = warp_sum_u(c1);
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (lane == 0) {
         sh_s[0][warp] = s0;
@@ -95,7 +97,62 @@ __device__ void block_accumulate(double s0, double s1, unsigned long long c0,
     __syncthreads();
 }
 
+// A sum held as an unevaluated float32 pair h + l (Knuth's two-sum; about
+// 2^-47 relative per addition): the planning sums without FP64
+// instructions, which GB300 issues at a small fraction of its float32 rate.
+struct PairSum {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add(float ph, float pl) {
+        const float s = __fadd_rn(h, ph);
+        const float bb = __fsub_rn(s, h);
+        const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+        const float t = __fadd_rn(err, __fadd_rn(l, pl));
+        h = __fadd_rn(s, t);
+        l = __fsub_rn(t, __fsub_rn(h, s));
+    }
+    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
+// m a b (m a power of two) into s exactly, as the pair (p, fma(a, b, -p));
+// a product outside the range where that pair is exact goes to the FP64
+// sum fb instead.
+__device__ __forceinline__ void add_product(PairSum& s, double& fb, float a, float b, float m) {
+    const float p = __fmul_rn(a, b);
+    const float ap = fabsf(p);
+    if (ap < 0x1p100f && ap > 0x1p-90f)
+        s.add(__fmul_rn(p, m), __fmul_rn(__fmaf_rn(a, b, -p), m));
+    else if (a != 0.0f && b != 0.0f)
+        fb += (double)m * ((double)a * (double)b);
+}
+
+__device__ __forceinline__ PairSum warp_sum_pair(PairSum s) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        s.add(__shfl_xor_sync(0xffffffffu, s.h, o), __shfl_xor_sync(0xffffffffu, s.l, o));
+    return s;
+}
+
+// Block accumulation of two pair sums (plus their rare FP64 parts) and two
+// counters.
+__device__ void block_accumulate(PairSum s0, PairSum s1, double f0, double f1,
+                                 unsigned long long c0, unsigned long long c1, double* sums,
+                                 unsigned long long* counts) {
+    s0 = warp_sum_pair(s0);
+    s1 = warp_sum_pair(s1);
+    if (__any_sync(0xffffffffu, f0 != 0.0 || f1 != 0.0)) {
+        f0 = warp_sum_d(f0);
+        f1 = warp_sum_d(f1);
+    }
+    c0 = warp_sum_u(c0);
+    c1 = warp_sum_u(c1);
+    block_finish(s0.value() + f0, s1.value() + f1, c0, c1, sums, counts);
+}
+
 __device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
+// finiteness of a double from its exponent bits (no FP64 instruction)
+__device__ __forceinline__ bool finite_d(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
 
 // The anchor loc = round(x) and offset round((loc - x) s) of the grid
 // coordinate x = u / du + G/2 in float32 pairs (x - G/2 = p + e from one
@@ -141,12 +198,43 @@ __device__ __forceinline__ bool wp_plane_of(double q, int32_t planes, int32_t* p
     return true;
 }
 
+// wp_plane_of on float32 pairs: q = w_scale |w| from |w| and w_scale as
+// pairs (about 2^-44 relative), the candidate from a float32 root moved to
+// the k with (k - 1/2)^2 <= q < (k + 1/2)^2 (bounds exact in float32 for
+// k <= 2000), and decided only when q lies more than 2^-36 of a bound from
+// both, where RN64(q) and the reference's rounded root give the same k.
+// False when undecided (then wp_plane_of decides on exact FP64 products).
+__device__ __forceinline__ bool df_plane_of(float wh, float wl, DfScale ws, int32_t planes,
+                                            int32_t* plane) {
+    float qh, ql;
+    df_product(fabsf(wh), fabsf(wl), ws, &qh, &ql);
+    if (!(qh < 4.0e6f)) return false;
+    int k = (int)rintf(sqrtf(qh));
+    // q - (j - 1/2)^2 as a float: qh - b is exact when b/2 <= qh <= 2b, and
+    // its sign is plain otherwise
+    auto diff = [&](int j) {
+        const float t = (float)j - 0.5f;
+        return __fadd_rn(__fsub_rn(qh, __fmul_rn(t, t)), ql);
+    };
+    if (k > 0 && diff(k) < 0.0f)
+        --k;
+    else if (diff(k + 1) >= 0.0f)
+        ++k;
+    const float tl = (float)k - 0.5f, th = (float)k + 0.5f;
+    if ((k > 0 && !(diff(k) > __fmul_rn(tl, tl) * 0x1p-36f)) ||
+        !(-diff(k + 1) > __fmul_rn(th, th) * 0x1p-36f))
+        return false;
+    *plane = min(k, planes - 1);
+    return true;
+}
+
 // WProjector::plan_sample (gridder.rs:3588-3624) + raw_w_project_sample_is_valid
 // (lib.rs:73666-73676) + w_project_accumulation_for_sample (lib.rs:71463-71470).
 // The anchors, offsets and plane come from the float32-pair path above when
 // it decides them, else from the reference's FP64 operations.
 __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
-    double s_norm = 0.0, s_rep = 0.0;
+    PairSum s_norm, s_rep;
+    double f_norm = 0.0, f_rep = 0.0;
     unsigned long long c_ok = 0, c_skip = 0;
     const uint64_t invalid = ~0ull;
     for (int64_t i = a.first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
@@ -157,22 +245,26 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
         float2 vis = a.vis[i];
         double u = a.u[i], v = a.v[i], w = a.w[i];
         bool ok = (!a.gridable || a.gridable[i]) && finite_f(wt) && wt > 0.0f && finite_f(f) &&
-                  f > 0.0f && finite_f(vis.x) && finite_f(vis.y) && isfinite(u) &&
-                  isfinite(v) && isfinite(w);
+                  f > 0.0f && finite_f(vis.x) && finite_f(vis.y) && finite_d(u) &&
+                  finite_d(v) && finite_d(w);
         if (ok) {
             int64_t lx = 0, ly = 0, ox = 0, oy = 0;
             int32_t plane = 0;
             // float32 pairs first: u = uh + ul, x - G/2 = u (1/du), y - G/2 = -v (1/dv)
-            const float uh = __double2float_rn(u), vh = __double2float_rn(v);
-            const float ul = __double2float_rn(__dsub_rn(u, (double)uh));
-            const float vl = __double2float_rn(__dsub_rn(v, (double)vh));
-            float px32, ex, py32, ey;
-            df_product(uh, ul, a.kx, &px32, &ex);
-            df_product(-vh, -vl, a.ky, &py32, &ey);
-            bool fast = df_wp_axis(px32, ex, a.gnx, a.sampling, &lx, &ox) &&
-                        df_wp_axis(py32, ey, a.gny, a.sampling, &ly, &oy);
-            if (fast && a.planes > 1) fast = wp_plane_of(__dmul_rn(a.w_scale, fabs(w)), a.planes,
-                                                         &plane);
+            float uh, ul, vh, vl;
+            bool fast = df_split(u, &uh, &ul) && df_split(v, &vh, &vl);
+            if (fast) {
+                float px32, ex, py32, ey;
+                df_product(uh, ul, a.kx, &px32, &ex);
+                df_product(-vh, -vl, a.ky, &py32, &ey);
+                fast = df_wp_axis(px32, ex, a.gnx, a.sampling, &lx, &ox) &&
+                       df_wp_axis(py32, ey, a.gny, a.sampling, &ly, &oy);
+            }
+            if (fast && a.planes > 1) {
+                float wh, wl;
+                fast = (df_split(w, &wh, &wl) && df_plane_of(wh, wl, a.kw, a.planes, &plane)) ||
+                       wp_plane_of(__dmul_rn(a.w_scale, fabs(w)), a.planes, &plane);
+            }
             if (!fast) {
                 // the reference's FP64 operations
                 double px = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
@@ -199,13 +291,17 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
                 if (ok) {
                     int offidx = (int)(ox + a.radius) * a.axis + (int)(oy + a.radius);
                     float nrm = a.norm[((int64_t)plane * a.axis) * a.axis + offidx];
-                    s_norm += 2.0 * (double)wt * (double)nrm;
-                    s_rep += (double)wt * (double)f;
+                    // 2 w nrm and w f, exact products of floats, summed in pairs
+                    add_product(s_norm, f_norm, wt, nrm, 2.0f);
+                    add_product(s_rep, f_rep, wt, f, 1.0f);
+                    // w > 0 from the bits (w is finite here)
+                    const long long wb = __double_as_longlong(w);
+                    const uint64_t wpos = (wb > 0) ? 1u : 0u;
                     uint64_t tile = (uint64_t)(lx >> 5) * (uint64_t)a.nty + (uint64_t)(ly >> 5);
                     uint64_t cell = (uint64_t)(((lx & 31) << 5) | (ly & 31));
                     key = tile;
                     key = (key << a.plane_bits) | (uint64_t)plane;
-                    key = (key << 1) | (uint64_t)(w > 0.0 ? 1 : 0);
+                    key = (key << 1) | wpos;
                     key = (key << a.off_bits) | (uint64_t)offidx;
                     key = (key << 10) | cell;
                 }
@@ -218,7 +314,7 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
         a.keys[i] = key;
         a.vals[i] = (uint32_t)i;
     }
-    block_accumulate(s_norm, s_rep, c_ok, c_skip, a.sums, a.counts);
+    block_accumulate(s_norm, s_rep, f_norm, f_rep, c_ok, c_skip, a.sums, a.counts);
 }
 
 struct StdPlanArgs {
@@ -230,6 +326,7 @@ struct StdPlanArgs {
     double du, dv;
     int32_t os, tap_rows;
     int64_t nty;
+    DfScale kx, ky;            // 1 / du, 1 / dv as float32 pairs
     uint64_t* keys;
     uint32_t* vals;
     double* sums;
@@ -254,7 +351,8 @@ __device__ __forceinline__ bool tap_span(double coord, int64_t size, int32_t os,
 // accumulate_dirty_psf_and_residual_standard_streaming_grid_serial
 // (lib.rs:68433-68500): validity, taps, sum of weights grid_weight = w*f.
 __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
-    double s_norm = 0.0;
+    PairSum s_norm;
+    double f_norm = 0.0;
     unsigned long long c_ok = 0, c_skip = 0;
     for (int64_t i = a.first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -264,14 +362,31 @@ __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
         bool ok = (!a.gridable || a.gridable[i]) && finite_f(wt) && wt > 0.0f && finite_f(f) &&
                   f > 0.0f;
         if (ok) {
-            double x = __dadd_rn(__ddiv_rn(a.u[i], a.du), (double)a.gnx / 2.0);
-            double y = __dadd_rn(__ddiv_rn(-a.v[i], a.dv), (double)a.gny / 2.0);
             int64_t x0 = 0, y0 = 0;
             int32_t rx = 0, ry = 0;
-            ok = tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) &&
-                 tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry);
+            // float32 pairs first (cr_fixed.cuh's decisions, 1 / 0 / -1 =
+            // accepted / rejected / undecided), the FP64 operations otherwise
+            const double u = a.u[i], v = a.v[i];
+            int dx = -1, dy = -1;
+            float uh, ul, vh, vl;
+            if (df_split(u, &uh, &ul) && df_split(v, &vh, &vl)) {
+                float px, ex, py, ey;
+                df_product(uh, ul, a.kx, &px, &ex);
+                df_product(-vh, -vl, a.ky, &py, &ey);
+                dx = df_tap_span(px, ex, a.gnx, a.os, a.tap_rows, &x0, &rx);
+                if (dx == 1) dy = df_tap_span(py, ey, a.gny, a.os, a.tap_rows, &y0, &ry);
+            }
+            if (dx == 0 || dy == 0) {
+                ok = false;
+            } else if (dx != 1 || dy != 1) {
+                double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
+                double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
+                ok = tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) &&
+                     tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry);
+            }
             if (ok) {
-                s_norm += (double)(wt * f);
+                // the float32 product w f, as the reference sums it
+                s_norm.add(__fmul_rn(wt, f), 0.0f);
                 uint64_t tile = (uint64_t)(x0 >> 5) * (uint64_t)a.nty + (uint64_t)(y0 >> 5);
                 uint64_t cell = (uint64_t)(((x0 & 31) << 5) | (y0 & 31));
                 key = (((tile << 8 | (uint64_t)rx) << 8 | (uint64_t)ry) << 10) | cell;
@@ -284,7 +399,7 @@ __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
         a.keys[i] = key;
         a.vals[i] = (uint32_t)i;
     }
-    block_accumulate(s_norm, s_norm, c_ok, c_skip, a.sums, a.counts);
+    block_accumulate(s_norm, s_norm, f_norm, f_norm, c_ok, c_skip, a.sums, a.counts);
 }
 
 __global__ void head_flags(const uint64_t* keys, const unsigned long long* counts, int64_t n,
@@ -359,7 +474,7 @@ __global__ void records_init(RecArgs a) {
 }
 
 // Sums of weight * vis per record: a warp-level segmented reduction over the
-// sorted run, then one FP64 atomic per segment piece.
+// sorted run in float32 pairs, then one FP64 atomic per segment piece.
 __global__ void records_accumulate(RecArgs a) {
     int64_t nv = (int64_t)a.counts[0];
     const int lane = threadIdx.x & 31;
@@ -369,7 +484,9 @@ __global__ void records_accumulate(RecArgs a) {
     for (int64_t i = start; i < limit; i += stride) {
         bool valid = i < nv;
         int32_t r = -1;
-        double vr = 0.0, vi = 0.0, ww = 0.0;
+        // w vis and w as float32 pairs: the products of two floats exact,
+        // the segment sums compensated (FP64 only for the per-segment atomics)
+        PairSum vr, vi, ww;
         if (valid) {
             r = (int32_t)(a.flags[i] ? a.excl[i] : a.excl[i] - 1);
             uint32_t s = a.vals[i];
@@ -378,31 +495,36 @@ __global__ void records_accumulate(RecArgs a) {
             float f = a.sumwt ? a.sumwt[s] : 1.0f;
             float gw = a.mode == 0 ? wt : wt * f;
             float2 v = a.vis[s];
-            ww = (double)gw;
+            ww.h = gw;
             if (isfinite(v.x) && isfinite(v.y)) {
-                vr = (double)v.x * ww;
-                vi = (double)v.y * ww;
+                vr.h = __fmul_rn(v.x, gw);
+                vr.l = __fmaf_rn(v.x, gw, -vr.h);
+                vi.h = __fmul_rn(v.y, gw);
+                vi.l = __fmaf_rn(v.y, gw, -vi.h);
             }
         }
         // segmented inclusive scan by record id
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            double tr = __shfl_up_sync(0xffffffffu, vr, o);
-            double ti = __shfl_up_sync(0xffffffffu, vi, o);
-            double tw = __shfl_up_sync(0xffffffffu, ww, o);
+            const float trh = __shfl_up_sync(0xffffffffu, vr.h, o);
+            const float trl = __shfl_up_sync(0xffffffffu, vr.l, o);
+            const float tih = __shfl_up_sync(0xffffffffu, vi.h, o);
+            const float til = __shfl_up_sync(0xffffffffu, vi.l, o);
+            const float twh = __shfl_up_sync(0xffffffffu, ww.h, o);
+            const float twl = __shfl_up_sync(0xffffffffu, ww.l, o);
             int32_t rr = __shfl_up_sync(0xffffffffu, r, o);
             if (lane >= o && rr == r) {
-                vr += tr;
-                vi += ti;
-                ww += tw;
+                vr.add(trh, trl);
+                vi.add(tih, til);
+                ww.add(twh, twl);
             }
         }
         int32_t next = __shfl_down_sync(0xffffffffu, r, 1);
         bool last = (lane == 31) || (next != r);
         if (valid && last) {
-            atomicAdd(&a.vsum[r].x, vr);
-            atomicAdd(&a.vsum[r].y, vi);
-            atomicAdd(&a.wsum[r], ww);
+            atomicAdd(&a.vsum[r].x, vr.value());
+            atomicAdd(&a.vsum[r].y, vi.value());
+            atomicAdd(&a.wsum[r], ww.value());
         }
     }
 }
@@ -521,7 +643,8 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) 
                      gi.grid_nx, gi.grid_ny, gi.du, gi.dv, wp->info.w_scale,
                      wp->info.sampling, wp->info.planes, wp->radius, wp->axis,
                      wp->support_d, wp->norm_d, nty, plane_bits, off_bits,
-                     df_scale_of(1.0, gi.du, false), df_scale_of(1.0, gi.dv, false), r.keys,
+                     df_scale_of(1.0, gi.du, false), df_scale_of(1.0, gi.dv, false),
+                     df_scale_of(wp->info.w_scale, 1.0, true), r.keys,
                      r.order, r.sums, r.counts};
         for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
             a.first = lo;
@@ -543,7 +666,8 @@ Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* po
     if (key_bits > 64) fail(CR_INVALID, "grid too large for the 64-bit sample key");
     if (b.n > 0) {
         StdPlanArgs a{0, b.n, b.u, b.v, b.weight, b.sumwt_factor, b.gridable, gi.grid_nx,
-                      gi.grid_ny, gi.du, gi.dv, gi.oversampling, g->tap_rows, nty, r.keys,
+                      gi.grid_ny, gi.du, gi.dv, gi.oversampling, g->tap_rows, nty,
+                      df_scale_of(1.0, gi.du, false), df_scale_of(1.0, gi.dv, false), r.keys,
                       r.order, r.sums, r.counts};
         for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
             a.first = lo;
