@@ -150,6 +150,24 @@ __device__ __forceinline__ void df_product(float ah, float al, DfScale k, float*
     *e = er;
 }
 
+// Float <-> integer without conversion instructions, which GB300 issues on
+// its narrow FP64 pipe: adding 1.5 * 2^23 puts an integer of magnitude below
+// 2^22 in the low significand bits of a float of the binade [2^23, 2^24),
+// where consecutive integers are consecutive bit patterns.
+constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23, bits 0x4B400000
+// rintf(x) (round to nearest, ties to even) for |x| < 2^22
+__device__ __forceinline__ float round_f(float x) {
+    return __fsub_rn(__fadd_rn(x, kMagic), kMagic);
+}
+// the nearest integer to x (ties to even) for |x| < 2^22
+__device__ __forceinline__ int int_of(float x) {
+    return __float_as_int(__fadd_rn(x, kMagic)) - 0x4B400000;
+}
+// (float)n for |n| < 2^22
+__device__ __forceinline__ float float_of(int n) {
+    return __fsub_rn(__int_as_float(0x4B400000 + n), kMagic);
+}
+
 // The float32 pair of a double from its bits, without FP64 instructions
 // (GB300 issues FP64 at a small fraction of its float32 rate): hi = x with
 // its significand truncated to 24 bits, lo = RN32(x - hi) (x - hi is the
@@ -157,18 +175,26 @@ __device__ __forceinline__ void df_product(float ah, float al, DfScale k, float*
 // power of two), so |x - (hi + lo)| <= 2^-47 |x|.  False for non-finite x
 // and for 0 < |x| < 2^-70 or |x| >= 2^100; zero splits into (+-0, 0).
 __device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    if ((b << 1) == 0ull) {
+    // on the 32-bit halves of the double: 64-bit shifts also run on the
+    // FP64 pipe
+    const unsigned bh = (unsigned)__double2hiint(x), bl = (unsigned)__double2loint(x);
+    const unsigned sign = bh & 0x80000000u;
+    if (((bh & 0x7fffffffu) | bl) == 0u) {
         *hi = __uint_as_float(sign);
         *lo = 0.0f;
         return true;
     }
-    const int e = (int)((b >> 52) & 0x7ffull) - 1023;
+    const int e = (int)((bh >> 20) & 0x7ffu) - 1023;
     if (e < -70 || e >= 100) return false;
-    *hi = __uint_as_float(sign | (unsigned)(e + 127) << 23 | (unsigned)((b >> 29) & 0x7fffffull));
-    const float r = __int2float_rn((int)(b & 0x1fffffffull)) *
-                    __uint_as_float((unsigned)(e - 52 + 127) << 23);
+    *hi = __uint_as_float(sign | (unsigned)(e + 127) << 23 | (bh & 0xfffffu) << 3 | bl >> 29);
+    // RN32 of the low 29 significand bits as an integer: its top 6 bits
+    // times 2^23 plus its low 23 bits, both exact floats, in one rounded
+    // addition; then scaled by an exact power of two
+    const unsigned low = bl & 0x1fffffffu;
+    const float top = __fmul_rn(__fsub_rn(__uint_as_float(0x4B000000u | (low >> 23)), 8388608.0f),
+                                8388608.0f);
+    const float bot = __fsub_rn(__uint_as_float(0x4B000000u | (low & 0x7fffffu)), 8388608.0f);
+    const float r = __fmul_rn(__fadd_rn(top, bot), __uint_as_float((unsigned)(e - 52 + 127) << 23));
     *lo = sign ? -r : r;
     return true;
 }
@@ -179,7 +205,7 @@ __device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
 __device__ __forceinline__ bool df_nearest(float p, float e, float h, float* a, float* dh) {
     if (!(fabsf(p) < kDfLimit)) return false;
     const float q = __fadd_rn(p, h);
-    const float r = rintf(q);
+    const float r = round_f(q);
     const float d = __fadd_rn(__fsub_rn(q, r), e);
     if (!(fabsf(fabsf(d) - 0.5f) > kDfMargin)) return false;
     float n = r;
@@ -196,14 +222,15 @@ __device__ __forceinline__ int df_tap_span(float p, float e, int64_t size, int32
                                            int32_t rows, int64_t* start, int32_t* row) {
     float a, dh;
     if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return -1;
-    const int64_t anchor = (size >> 1) + (int64_t)a;
+    // |a| < 2^20
+    const int64_t anchor = (size >> 1) + int_of(a);
     if (anchor - 3 < 0 || anchor + 3 >= size) return 0;
     // offset round((anchor - x) os) = round(-(dh + e) os)
-    const float osf = (float)os;
+    const float osf = float_of(os);
     const float v = -__fmaf_rn(dh, osf, __fmul_rn(e, osf));
-    const float o = rintf(v);
+    const float o = round_f(v);
     if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return -1;
-    const int64_t idx = (int64_t)o + os / 2;
+    const int64_t idx = int_of(o) + os / 2;
     if (idx < 0 || idx >= rows) return 0;
     *start = anchor - 3;
     *row = (int32_t)idx;

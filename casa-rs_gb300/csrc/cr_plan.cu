@@ -110,19 +110,48 @@ struct PairSum {
         h = __fadd_rn(s, t);
         l = __fsub_rn(t, __fsub_rn(h, s));
     }
-    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
 };
+
+// The FP64 operations kept out of line, so that the compiler branches around
+// them instead of predicating them on the common path.
+__device__ __noinline__ double fp64_product(float a, float b, float m) {
+    return (double)m * ((double)a * (double)b);
+}
+__device__ __noinline__ double fp64_of(float f) { return (double)f; }
 
 // m a b (m a power of two) into s exactly, as the pair (p, fma(a, b, -p));
 // a product outside the range where that pair is exact goes to the FP64
-// sum fb instead.
-__device__ __forceinline__ void add_product(PairSum& s, double& fb, float a, float b, float m) {
+// sum fb instead (and sets used).
+__device__ __forceinline__ void add_product(PairSum& s, double& fb, bool& used, float a, float b,
+                                            float m) {
     const float p = __fmul_rn(a, b);
     const float ap = fabsf(p);
-    if (ap < 0x1p100f && ap > 0x1p-90f)
+    if (ap < 0x1p100f && ap > 0x1p-90f) {
         s.add(__fmul_rn(p, m), __fmul_rn(__fmaf_rn(a, b, -p), m));
-    else if (a != 0.0f && b != 0.0f)
-        fb += (double)m * ((double)a * (double)b);
+    } else if (a != 0.0f && b != 0.0f) {
+        fb += fp64_product(a, b, m);
+        used = true;
+    }
+}
+
+// float -> double from the bits (exact, no FP64 instruction); zeros keep
+// their sign, subnormal, infinite and NaN values take the conversion.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    if (e == 0u || e == 0xffu) {
+        if ((u << 1) == 0u) return __longlong_as_double((long long)sign);
+        return fp64_of(f);
+    }
+    return __longlong_as_double((long long)(sign | (unsigned long long)(e + 896u) << 52 |
+                                            (unsigned long long)(u & 0x7fffffu) << 29));
+}
+
+// *p += h + l, one FP64 atomic per nonzero part
+__device__ __forceinline__ void atomic_add_pair(double* p, float h, float l) {
+    if (h != 0.0f) atomicAdd(p, f2d(h));
+    if (l != 0.0f) atomicAdd(p, f2d(l));
 }
 
 __device__ __forceinline__ PairSum warp_sum_pair(PairSum s) {
@@ -133,25 +162,59 @@ __device__ __forceinline__ PairSum warp_sum_pair(PairSum s) {
 }
 
 // Block accumulation of two pair sums (plus their rare FP64 parts) and two
-// counters.
-__device__ void block_accumulate(PairSum s0, PairSum s1, double f0, double f1,
+// counters: pairs summed over the warps, then over the block's warps, and
+// added to the FP64 totals by their parts.
+__device__ void block_accumulate(PairSum s0, PairSum s1, double f0, double f1, bool fb_used,
                                  unsigned long long c0, unsigned long long c1, double* sums,
                                  unsigned long long* counts) {
-    s0 = warp_sum_pair(s0);
-    s1 = warp_sum_pair(s1);
-    if (__any_sync(0xffffffffu, f0 != 0.0 || f1 != 0.0)) {
+    __shared__ float4 sh_s[32];
+    __shared__ unsigned long long sh_c[2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (__any_sync(0xffffffffu, fb_used)) {
         f0 = warp_sum_d(f0);
         f1 = warp_sum_d(f1);
+        if (lane == 0) {
+            if (f0 != 0.0) atomicAdd(&sums[0], f0);
+            if (f1 != 0.0) atomicAdd(&sums[1], f1);
+        }
     }
+    s0 = warp_sum_pair(s0);
+    s1 = warp_sum_pair(s1);
     c0 = warp_sum_u(c0);
     c1 = warp_sum_u(c1);
-    block_finish(s0.value() + f0, s1.value() + f1, c0, c1, sums, counts);
+    if (lane == 0) {
+        sh_s[warp] = make_float4(s0.h, s0.l, s1.h, s1.l);
+        sh_c[0][warp] = c0;
+        sh_c[1][warp] = c1;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const float4 v = lane < nw ? sh_s[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s0.h = v.x;
+        s0.l = v.y;
+        s1.h = v.z;
+        s1.l = v.w;
+        c0 = lane < nw ? sh_c[0][lane] : 0ull;
+        c1 = lane < nw ? sh_c[1][lane] : 0ull;
+        s0 = warp_sum_pair(s0);
+        s1 = warp_sum_pair(s1);
+        c0 = warp_sum_u(c0);
+        c1 = warp_sum_u(c1);
+        if (lane == 0) {
+            atomic_add_pair(&sums[0], s0.h, s0.l);
+            atomic_add_pair(&sums[1], s1.h, s1.l);
+            if (c0) atomicAdd(&counts[0], c0);
+            if (c1) atomicAdd(&counts[1], c1);
+        }
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ bool finite_f(float x) { return isfinite(x); }
-// finiteness of a double from its exponent bits (no FP64 instruction)
+// finiteness of a double from the exponent bits of its high half (no FP64
+// instruction, no 64-bit shift)
 __device__ __forceinline__ bool finite_d(double x) {
-    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+    return (((unsigned)__double2hiint(x) >> 20) & 0x7ffu) != 0x7ffu;
 }
 
 // The anchor loc = round(x) and offset round((loc - x) s) of the grid
@@ -163,12 +226,13 @@ __device__ __forceinline__ bool df_wp_axis(float p, float e, int64_t size, int32
                                            int64_t* loc, int64_t* off) {
     float a, dh;
     if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return false;
-    const float sf = (float)s;
+    const float sf = float_of(s);
     const float v = -__fmaf_rn(dh, sf, __fmul_rn(e, sf));
-    const float o = rintf(v);
+    const float o = round_f(v);
     if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return false;
-    *loc = (size >> 1) + (int64_t)a;
-    *off = (int64_t)o;
+    // |a|, |o| < 2^20
+    *loc = (size >> 1) + int_of(a);
+    *off = int_of(o);
     return true;
 }
 
@@ -209,23 +273,59 @@ __device__ __forceinline__ bool df_plane_of(float wh, float wl, DfScale ws, int3
     float qh, ql;
     df_product(fabsf(wh), fabsf(wl), ws, &qh, &ql);
     if (!(qh < 4.0e6f)) return false;
-    int k = (int)rintf(sqrtf(qh));
+    int k = int_of(sqrtf(qh));
     // q - (j - 1/2)^2 as a float: qh - b is exact when b/2 <= qh <= 2b, and
     // its sign is plain otherwise
     auto diff = [&](int j) {
-        const float t = (float)j - 0.5f;
+        const float t = float_of(j) - 0.5f;
         return __fadd_rn(__fsub_rn(qh, __fmul_rn(t, t)), ql);
     };
     if (k > 0 && diff(k) < 0.0f)
         --k;
     else if (diff(k + 1) >= 0.0f)
         ++k;
-    const float tl = (float)k - 0.5f, th = (float)k + 0.5f;
+    const float tl = float_of(k) - 0.5f, th = float_of(k) + 0.5f;
     if ((k > 0 && !(diff(k) > __fmul_rn(tl, tl) * 0x1p-36f)) ||
         !(-diff(k + 1) > __fmul_rn(th, th) * 0x1p-36f))
         return false;
     *plane = min(k, planes - 1);
     return true;
+}
+
+// The FP64 decisions, out of line so that the common float32-pair path
+// branches around them instead of issuing them predicated.
+// wp_plane_of of RN64(w_scale |w|): the plane, or -1 when undecided.
+__device__ __noinline__ int wp_plane_fp64(double w_scale, double w, int32_t planes) {
+    int32_t plane = 0;
+    return wp_plane_of(__dmul_rn(w_scale, fabs(w)), planes, &plane) ? plane : -1;
+}
+
+struct WpDecision {
+    long long lx, ly, ox, oy;
+    int plane, ok;
+};
+
+// Anchors, offsets and plane in the reference's FP64 operations.
+__device__ __noinline__ WpDecision wp_decide_fp64(double u, double v, double w, double du,
+                                                  double dv, int64_t gnx, int64_t gny,
+                                                  int32_t sampling, int32_t planes,
+                                                  double w_scale) {
+    WpDecision d{0, 0, 0, 0, 0, 0};
+    const double px = __dadd_rn(__ddiv_rn(u, du), (double)gnx / 2.0);
+    const double py = __dadd_rn(__ddiv_rn(-v, dv), (double)gny / 2.0);
+    if (!(isfinite(px) && isfinite(py) && fabs(px) < 1.0e15 && fabs(py) < 1.0e15)) return d;
+    d.ok = 1;
+    d.lx = (long long)round(px);
+    d.ly = (long long)round(py);
+    d.ox = (long long)round(__dmul_rn(__dsub_rn((double)d.lx, px), (double)sampling));
+    d.oy = (long long)round(__dmul_rn(__dsub_rn((double)d.ly, py), (double)sampling));
+    if (planes > 1) {
+        const double c = sqrt(fmax(__dmul_rn(w_scale, fabs(w)), 0.0));
+        double r = round(c);
+        r = fmin(fmax(r, 0.0), (double)(planes - 1));
+        d.plane = (int)r;
+    }
+    return d;
 }
 
 // WProjector::plan_sample (gridder.rs:3588-3624) + raw_w_project_sample_is_valid
@@ -235,6 +335,7 @@ __device__ __forceinline__ bool df_plane_of(float wh, float wl, DfScale ws, int3
 __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
     PairSum s_norm, s_rep;
     double f_norm = 0.0, f_rep = 0.0;
+    bool fb_used = false;
     unsigned long long c_ok = 0, c_skip = 0;
     const uint64_t invalid = ~0ull;
     for (int64_t i = a.first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
@@ -262,27 +363,20 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
             }
             if (fast && a.planes > 1) {
                 float wh, wl;
-                fast = (df_split(w, &wh, &wl) && df_plane_of(wh, wl, a.kw, a.planes, &plane)) ||
-                       wp_plane_of(__dmul_rn(a.w_scale, fabs(w)), a.planes, &plane);
+                if (!(df_split(w, &wh, &wl) && df_plane_of(wh, wl, a.kw, a.planes, &plane))) {
+                    plane = wp_plane_fp64(a.w_scale, w, a.planes);
+                    fast = plane >= 0;
+                }
             }
             if (!fast) {
-                // the reference's FP64 operations
-                double px = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
-                double py = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
-                ok = isfinite(px) && isfinite(py) && fabs(px) < 1.0e15 && fabs(py) < 1.0e15;
-                if (ok) {
-                    lx = (int64_t)round(px);
-                    ly = (int64_t)round(py);
-                    ox = (int64_t)round(__dmul_rn(__dsub_rn((double)lx, px), (double)a.sampling));
-                    oy = (int64_t)round(__dmul_rn(__dsub_rn((double)ly, py), (double)a.sampling));
-                    plane = 0;
-                    if (a.planes > 1) {
-                        double c = sqrt(fmax(__dmul_rn(a.w_scale, fabs(w)), 0.0));
-                        double r = round(c);
-                        r = fmin(fmax(r, 0.0), (double)(a.planes - 1));
-                        plane = (int32_t)r;
-                    }
-                }
+                const WpDecision d = wp_decide_fp64(u, v, w, a.du, a.dv, a.gnx, a.gny,
+                                                    a.sampling, a.planes, a.w_scale);
+                ok = d.ok;
+                lx = d.lx;
+                ly = d.ly;
+                ox = d.ox;
+                oy = d.oy;
+                plane = d.plane;
             }
             if (ok) {
                 int64_t s = a.support[plane];
@@ -292,11 +386,11 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
                     int offidx = (int)(ox + a.radius) * a.axis + (int)(oy + a.radius);
                     float nrm = a.norm[((int64_t)plane * a.axis) * a.axis + offidx];
                     // 2 w nrm and w f, exact products of floats, summed in pairs
-                    add_product(s_norm, f_norm, wt, nrm, 2.0f);
-                    add_product(s_rep, f_rep, wt, f, 1.0f);
+                    add_product(s_norm, f_norm, fb_used, wt, nrm, 2.0f);
+                    add_product(s_rep, f_rep, fb_used, wt, f, 1.0f);
                     // w > 0 from the bits (w is finite here)
-                    const long long wb = __double_as_longlong(w);
-                    const uint64_t wpos = (wb > 0) ? 1u : 0u;
+                    const int wh32 = __double2hiint(w);
+                    const uint64_t wpos = (wh32 > 0 || (wh32 == 0 && __double2loint(w) != 0)) ? 1u : 0u;
                     uint64_t tile = (uint64_t)(lx >> 5) * (uint64_t)a.nty + (uint64_t)(ly >> 5);
                     uint64_t cell = (uint64_t)(((lx & 31) << 5) | (ly & 31));
                     key = tile;
@@ -314,7 +408,7 @@ __global__ void __launch_bounds__(256) wp_plan_kernel(WpPlanArgs a) {
         a.keys[i] = key;
         a.vals[i] = (uint32_t)i;
     }
-    block_accumulate(s_norm, s_rep, f_norm, f_rep, c_ok, c_skip, a.sums, a.counts);
+    block_accumulate(s_norm, s_rep, f_norm, f_rep, fb_used, c_ok, c_skip, a.sums, a.counts);
 }
 
 struct StdPlanArgs {
@@ -348,6 +442,29 @@ __device__ __forceinline__ bool tap_span(double coord, int64_t size, int32_t os,
     return true;
 }
 
+struct StdSpans {
+    long long x0, y0;
+    int rx, ry, ok;
+};
+
+// Both axes' tap spans in the reference's FP64 operations, out of line (the
+// common path takes them on float32 pairs).
+__device__ __noinline__ StdSpans std_spans_fp64(double u, double v, double du, double dv,
+                                                int64_t gnx, int64_t gny, int32_t os,
+                                                int32_t rows) {
+    StdSpans d{0, 0, 0, 0, 0};
+    int64_t x0 = 0, y0 = 0;
+    int32_t rx = 0, ry = 0;
+    const double x = __dadd_rn(__ddiv_rn(u, du), (double)gnx / 2.0);
+    const double y = __dadd_rn(__ddiv_rn(-v, dv), (double)gny / 2.0);
+    d.ok = tap_span(x, gnx, os, rows, &x0, &rx) && tap_span(y, gny, os, rows, &y0, &ry);
+    d.x0 = x0;
+    d.y0 = y0;
+    d.rx = rx;
+    d.ry = ry;
+    return d;
+}
+
 // accumulate_dirty_psf_and_residual_standard_streaming_grid_serial
 // (lib.rs:68433-68500): validity, taps, sum of weights grid_weight = w*f.
 __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
@@ -379,10 +496,13 @@ __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
             if (dx == 0 || dy == 0) {
                 ok = false;
             } else if (dx != 1 || dy != 1) {
-                double x = __dadd_rn(__ddiv_rn(u, a.du), (double)a.gnx / 2.0);
-                double y = __dadd_rn(__ddiv_rn(-v, a.dv), (double)a.gny / 2.0);
-                ok = tap_span(x, a.gnx, a.os, a.tap_rows, &x0, &rx) &&
-                     tap_span(y, a.gny, a.os, a.tap_rows, &y0, &ry);
+                const StdSpans d = std_spans_fp64(u, v, a.du, a.dv, a.gnx, a.gny, a.os,
+                                                  a.tap_rows);
+                ok = d.ok;
+                x0 = d.x0;
+                y0 = d.y0;
+                rx = d.rx;
+                ry = d.ry;
             }
             if (ok) {
                 // the float32 product w f, as the reference sums it
@@ -399,7 +519,7 @@ __global__ void __launch_bounds__(256) std_plan_kernel(StdPlanArgs a) {
         a.keys[i] = key;
         a.vals[i] = (uint32_t)i;
     }
-    block_accumulate(s_norm, s_norm, f_norm, f_norm, c_ok, c_skip, a.sums, a.counts);
+    block_accumulate(s_norm, s_norm, f_norm, f_norm, false, c_ok, c_skip, a.sums, a.counts);
 }
 
 __global__ void head_flags(const uint64_t* keys, const unsigned long long* counts, int64_t n,
@@ -522,9 +642,9 @@ __global__ void records_accumulate(RecArgs a) {
         int32_t next = __shfl_down_sync(0xffffffffu, r, 1);
         bool last = (lane == 31) || (next != r);
         if (valid && last) {
-            atomicAdd(&a.vsum[r].x, vr.value());
-            atomicAdd(&a.vsum[r].y, vi.value());
-            atomicAdd(&a.wsum[r], ww.value());
+            atomic_add_pair(&a.vsum[r].x, vr.h, vr.l);
+            atomic_add_pair(&a.vsum[r].y, vi.h, vi.l);
+            atomic_add_pair(&a.wsum[r], ww.h, ww.l);
         }
     }
 }
@@ -547,6 +667,11 @@ __global__ void tile_starts(const uint32_t* tile_of, const unsigned long long* c
         for (int64_t t = prev + 1; t <= cur; ++t) start[t] = (uint32_t)r;
     }
 }
+
+// The plan kernels' grids: one resident wave (4 blocks of 256 per SM), each
+// thread striding over many samples, so that the block reduction of the
+// sums is paid once per thread rather than once per sample.
+inline int64_t plan_wave(cr_ctx* ctx) { return (int64_t)ctx->sms * 4; }
 
 // fn(lo, hi) over the batch's samples: once over all of them, or piece by
 // piece for a staged upload, each after the main stream has waited for its
@@ -649,7 +774,7 @@ Records plan_wproj(cr_ctx* ctx, cr_wproj* wp, const DeviceBatch& b, Pool* pool) 
         for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
             a.first = lo;
             a.n = hi;
-            wp_plan_kernel<<<grid_blocks(hi - lo, 256), 256, 0, ctx->stream>>>(a);
+            wp_plan_kernel<<<grid_blocks(hi - lo, 256, plan_wave(ctx)), 256, 0, ctx->stream>>>(a);
             note_launch(ctx, "wp_plan_kernel");
         });
     }
@@ -672,7 +797,7 @@ Records plan_standard(cr_ctx* ctx, cr_gridder* g, const DeviceBatch& b, Pool* po
         for_each_piece(ctx, b, [&](int64_t lo, int64_t hi) {
             a.first = lo;
             a.n = hi;
-            std_plan_kernel<<<grid_blocks(hi - lo, 256), 256, 0, ctx->stream>>>(a);
+            std_plan_kernel<<<grid_blocks(hi - lo, 256, plan_wave(ctx)), 256, 0, ctx->stream>>>(a);
             note_launch(ctx, "std_plan_kernel");
         });
     }
