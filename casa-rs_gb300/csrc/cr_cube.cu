@@ -484,7 +484,9 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
     const float f2 = a.mode == CR_WEIGHT_BRIGGS ? a.f2[c] : 0.0f;
     const float* dens = a.mode != CR_WEIGHT_NATURAL ? a.density + (int64_t)c * a.nx * a.ny
                                                     : nullptr;
-    double sw = 0.0;
+    // the channel's sum of weights as a float pair (no FP64 instruction per
+    // sample), in FP64 from the warp sums on
+    PairSum swp;
     unsigned long long n_ok = 0, n_skip = 0;
     for (int64_t base = r0 + wp * 32 * kScatterVec; base < r1;
          base += kCubeThreads * kScatterVec) {
@@ -545,13 +547,14 @@ __global__ void __launch_bounds__(kCubeThreads, 4) cube_scatter_kernel(CubeArgs 
                 wr = w[j];
                 sample = (uint32_t)i;
                 ++n_ok;
-                sw += (double)wr;
+                swp.add(wr, 0.0f);
             }
             a.rec[pos[j]] = make_uint4(meta[j], sample, __float_as_uint(vr),
                                        __float_as_uint(vi));
             a.rec_w[pos[j]] = wr;
         }
     }
+    double sw = (double)swp.h + (double)swp.l;
     sw = warp_sum(sw);
     n_ok = warp_sum(n_ok);
     n_skip = warp_sum(n_skip);

@@ -150,24 +150,6 @@ __device__ __forceinline__ void df_product(float ah, float al, DfScale k, float*
     *e = er;
 }
 
-// Float <-> integer without conversion instructions, which GB300 issues on
-// its narrow FP64 pipe: adding 1.5 * 2^23 puts an integer of magnitude below
-// 2^22 in the low significand bits of a float of the binade [2^23, 2^24),
-// where consecutive integers are consecutive bit patterns.
-constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23, bits 0x4B400000
-// rintf(x) (round to nearest, ties to even) for |x| < 2^22
-__device__ __forceinline__ float round_f(float x) {
-    return __fsub_rn(__fadd_rn(x, kMagic), kMagic);
-}
-// the nearest integer to x (ties to even) for |x| < 2^22
-__device__ __forceinline__ int int_of(float x) {
-    return __float_as_int(__fadd_rn(x, kMagic)) - 0x4B400000;
-}
-// (float)n for |n| < 2^22
-__device__ __forceinline__ float float_of(int n) {
-    return __fsub_rn(__int_as_float(0x4B400000 + n), kMagic);
-}
-
 // The float32 pair of a double from its bits, without FP64 instructions
 // (GB300 issues FP64 at a small fraction of its float32 rate): hi = x with
 // its significand truncated to 24 bits, lo = RN32(x - hi) (x - hi is the
@@ -175,8 +157,8 @@ __device__ __forceinline__ float float_of(int n) {
 // power of two), so |x - (hi + lo)| <= 2^-47 |x|.  False for non-finite x
 // and for 0 < |x| < 2^-70 or |x| >= 2^100; zero splits into (+-0, 0).
 __device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
-    // on the 32-bit halves of the double: 64-bit shifts also run on the
-    // FP64 pipe
+    // on the 32-bit halves of the double (with the 64-bit form, the FP64
+    // pipe was half busy in the plan kernel)
     const unsigned bh = (unsigned)__double2hiint(x), bl = (unsigned)__double2loint(x);
     const unsigned sign = bh & 0x80000000u;
     if (((bh & 0x7fffffffu) | bl) == 0u) {
@@ -187,17 +169,27 @@ __device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
     const int e = (int)((bh >> 20) & 0x7ffu) - 1023;
     if (e < -70 || e >= 100) return false;
     *hi = __uint_as_float(sign | (unsigned)(e + 127) << 23 | (bh & 0xfffffu) << 3 | bl >> 29);
-    // RN32 of the low 29 significand bits as an integer: its top 6 bits
-    // times 2^23 plus its low 23 bits, both exact floats, in one rounded
-    // addition; then scaled by an exact power of two
-    const unsigned low = bl & 0x1fffffffu;
-    const float top = __fmul_rn(__fsub_rn(__uint_as_float(0x4B000000u | (low >> 23)), 8388608.0f),
-                                8388608.0f);
-    const float bot = __fsub_rn(__uint_as_float(0x4B000000u | (low & 0x7fffffu)), 8388608.0f);
-    const float r = __fmul_rn(__fadd_rn(top, bot), __uint_as_float((unsigned)(e - 52 + 127) << 23));
+    // RN32 of the low 29 significand bits as an integer, scaled by an exact
+    // power of two
+    const float r = __fmul_rn(__int2float_rn((int)(bl & 0x1fffffffu)),
+                              __uint_as_float((unsigned)(e - 52 + 127) << 23));
     *lo = sign ? -r : r;
     return true;
 }
+
+// A sum held as an unevaluated float32 pair h + l (Knuth's two-sum; about
+// 2^-47 relative per addition): sums of weights without FP64 instructions.
+struct PairSum {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add(float ph, float pl) {
+        const float s = __fadd_rn(h, ph);
+        const float bb = __fsub_rn(s, h);
+        const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+        const float t = __fadd_rn(err, __fadd_rn(l, pl));
+        h = __fadd_rn(s, t);
+        l = __fsub_rn(t, __fsub_rn(h, s));
+    }
+};
 
 // The integer a nearest to x = p + e + h (h = 0 or 1/2) and dh = RN(p + h) - a
 // (exact), or false when x is within the margin of a half-integer, is
@@ -205,7 +197,7 @@ __device__ __forceinline__ bool df_split(double x, float* hi, float* lo) {
 __device__ __forceinline__ bool df_nearest(float p, float e, float h, float* a, float* dh) {
     if (!(fabsf(p) < kDfLimit)) return false;
     const float q = __fadd_rn(p, h);
-    const float r = round_f(q);
+    const float r = rintf(q);
     const float d = __fadd_rn(__fsub_rn(q, r), e);
     if (!(fabsf(fabsf(d) - 0.5f) > kDfMargin)) return false;
     float n = r;
@@ -223,14 +215,14 @@ __device__ __forceinline__ int df_tap_span(float p, float e, int64_t size, int32
     float a, dh;
     if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return -1;
     // |a| < 2^20
-    const int64_t anchor = (size >> 1) + int_of(a);
+    const int64_t anchor = (size >> 1) + (int)a;
     if (anchor - 3 < 0 || anchor + 3 >= size) return 0;
     // offset round((anchor - x) os) = round(-(dh + e) os)
-    const float osf = float_of(os);
+    const float osf = (float)os;
     const float v = -__fmaf_rn(dh, osf, __fmul_rn(e, osf));
-    const float o = round_f(v);
+    const float o = rintf(v);
     if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return -1;
-    const int64_t idx = int_of(o) + os / 2;
+    const int64_t idx = (int)o + os / 2;
     if (idx < 0 || idx >= rows) return 0;
     *start = anchor - 3;
     *row = (int32_t)idx;

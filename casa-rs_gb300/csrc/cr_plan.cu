@@ -97,21 +97,6 @@ __device__ void block_finish(double s0, double s1, unsigned long long c0, unsign
     __syncthreads();
 }
 
-// A sum held as an unevaluated float32 pair h + l (Knuth's two-sum; about
-// 2^-47 relative per addition): the planning sums without FP64
-// instructions, which GB300 issues at a small fraction of its float32 rate.
-struct PairSum {
-    float h = 0.0f, l = 0.0f;
-    __device__ __forceinline__ void add(float ph, float pl) {
-        const float s = __fadd_rn(h, ph);
-        const float bb = __fsub_rn(s, h);
-        const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
-        const float t = __fadd_rn(err, __fadd_rn(l, pl));
-        h = __fadd_rn(s, t);
-        l = __fsub_rn(t, __fsub_rn(h, s));
-    }
-};
-
 // The FP64 operations kept out of line, so that the compiler branches around
 // them instead of predicating them on the common path.
 __device__ __noinline__ double fp64_product(float a, float b, float m) {
@@ -226,13 +211,12 @@ __device__ __forceinline__ bool df_wp_axis(float p, float e, int64_t size, int32
                                            int64_t* loc, int64_t* off) {
     float a, dh;
     if (!df_nearest(p, e, (size & 1) ? 0.5f : 0.0f, &a, &dh)) return false;
-    const float sf = float_of(s);
+    const float sf = (float)s;
     const float v = -__fmaf_rn(dh, sf, __fmul_rn(e, sf));
-    const float o = round_f(v);
+    const float o = rintf(v);
     if (!(0.5f - fabsf(__fsub_rn(v, o)) > kDfMargin)) return false;
-    // |a|, |o| < 2^20
-    *loc = (size >> 1) + int_of(a);
-    *off = int_of(o);
+    *loc = (size >> 1) + (int)a;
+    *off = (int)o;
     return true;
 }
 
@@ -273,18 +257,18 @@ __device__ __forceinline__ bool df_plane_of(float wh, float wl, DfScale ws, int3
     float qh, ql;
     df_product(fabsf(wh), fabsf(wl), ws, &qh, &ql);
     if (!(qh < 4.0e6f)) return false;
-    int k = int_of(sqrtf(qh));
+    int k = (int)rintf(sqrtf(qh));
     // q - (j - 1/2)^2 as a float: qh - b is exact when b/2 <= qh <= 2b, and
     // its sign is plain otherwise
     auto diff = [&](int j) {
-        const float t = float_of(j) - 0.5f;
+        const float t = (float)j - 0.5f;
         return __fadd_rn(__fsub_rn(qh, __fmul_rn(t, t)), ql);
     };
     if (k > 0 && diff(k) < 0.0f)
         --k;
     else if (diff(k + 1) >= 0.0f)
         ++k;
-    const float tl = float_of(k) - 0.5f, th = float_of(k) + 0.5f;
+    const float tl = (float)k - 0.5f, th = (float)k + 0.5f;
     if ((k > 0 && !(diff(k) > __fmul_rn(tl, tl) * 0x1p-36f)) ||
         !(-diff(k + 1) > __fmul_rn(th, th) * 0x1p-36f))
         return false;

@@ -150,21 +150,3 @@ def test_pair_sums_of_exact_products():
     got = Fraction(float(h)) + Fraction(float(l))
     assert abs(got - exact) <= exact * Fraction(1, 2 ** 40)
 
-
-def test_magic_conversions():
-    """round_f / int_of / float_of (cr_fixed.cuh): exact for |x| < 2^22."""
-    magic = f32(12582912.0)
-
-    def bits(x):
-        return int(np.float32(x).view(np.int32))
-
-    rng = np.random.default_rng(19)
-    xs = np.concatenate([rng.uniform(-2.0 ** 22 + 1, 2.0 ** 22 - 1, 20000),
-                         np.arange(-40, 40) * 0.25, [0.5, 1.5, 2.5, -0.5, -1.5]]).astype(np.float32)
-    for x in xs:
-        s = f32(x + magic)
-        assert f32(s - magic) == np.rint(x)                       # round_f
-        assert bits(s) - 0x4B400000 == int(np.rint(x))            # int_of
-    for n in list(rng.integers(-(2 ** 22) + 1, 2 ** 22, 20000)) + [0, 1, -1]:
-        v = np.int32(0x4B400000 + int(n)).view(np.float32)
-        assert f32(v - magic) == f32(n)                           # float_of
