@@ -213,8 +213,10 @@ int cr_ctx_set_alloc_limit(cr_ctx* ctx, int64_t bytes);
  * with them off, cr_ctx_last_timings reports zeros and a call whose outputs
  * all stay in device memory returns once its work is queued on the
  * context's stream (calls that return host values still wait for them).
- * New; no counterpart in the reference (ImagingStageTimings is always
- * filled there). */
+ * Such a call may still be copying its host inputs when it returns: keep
+ * them unchanged until the stream has passed the call (cr_ctx_synchronize,
+ * or an event on the stream).  New; no counterpart in the reference
+ * (ImagingStageTimings is always filled there). */
 int cr_ctx_set_timings(cr_ctx* ctx, int32_t enable);
 const char* cr_version(void);
 
