@@ -189,18 +189,15 @@ __device__ __forceinline__ int cube_b(int t, int off, int q, const CubeGeom& c) 
 // ---- gridding ---------------------------------------------------------------------
 // One warp per work item (output tile, band of kBandRows rows, chunk of
 // candidate records); no block-level barriers.  Lane l owns column l of the
-// tile and keeps per band row four float accumulators,
-//   dirty re += kr vr + ki (-t vi),  dirty im += kr vi + ki (t vr),
-//   psf re += kr w,  psf im += ki (t w)
-// (k = (kr, ki) the kernel value, t = -1 for a conjugated record), six
-// scalar FMAs per tap.  (Paired FMAs on float2 accumulators issue half the
-// FMA instructions but hold 16 more registers: 80 registers and 3 blocks
-// per SM against 64 and 4, and the kernel waits on its kernel-value loads,
-// so the extra warps win: 6.53 -> 6.37 ms on the benchmark pass.)  The warp
-// examines its candidates 32 at a time, one per lane, from records packed
-// once per pass (16 bytes each, prefetched a batch ahead with cp.async), and
-// compacts those whose window reaches its band into warp-private shared
-// memory with their row addresses.
+// tile and keeps per band row three float2 accumulators,
+//   X = sum k (.) (vr, -t vi),  Y = sum k (.) (vi, t vr),  P = sum k (.) (w, t w)
+// (k = (kr, ki) the kernel value, t = -1 for a conjugated record, (.) the
+// element-wise product), one paired FMA each per tap; the flush forms
+// dirty = (X.x + X.y, Y.x + Y.y) and psf = P.  The warp examines its
+// candidates 32 at a time, one per lane, from records packed once per pass
+// (16 bytes each, prefetched a batch ahead with cp.async), and compacts those
+// whose window reaches its band into warp-private shared memory with their
+// row addresses.
 constexpr int kBandRows = 8;
 constexpr int kBands = kTile / kBandRows;   // 4 bands per tile
 constexpr int kBandWarps = 8;               // warps per block
@@ -298,7 +295,7 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 template <bool RESIDUAL>
-__global__ void __launch_bounds__(kBandWarps * 32, 4) wp_grid_kernel(BandArgs a) {
+__global__ void __launch_bounds__(kBandWarps * 32, 3) wp_grid_kernel(BandArgs a) {
     __shared__ BandEntry s_ent[kBandWarps][32];
     __shared__ __align__(16) int s_rows[kBandWarps][32][kBandRows];
     __shared__ uint32_t s_lo[kBandWarps][kNbr];
@@ -344,9 +341,9 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wp_grid_kernel(BandArgs a)
         fetch(cbeg + lane, 0);
         int buf = 0;
 
-        float Dr[kBandRows], Di[kBandRows], Pr[kBandRows], Pi[kBandRows];
+        float2 X[kBandRows], Y[kBandRows], P[kBandRows];
 #pragma unroll
-        for (int k = 0; k < kBandRows; ++k) Dr[k] = Di[k] = Pr[k] = Pi[k] = 0.0f;
+        for (int k = 0; k < kBandRows; ++k) X[k] = Y[k] = P[k] = make_float2(0.f, 0.f);
 
         for (uint32_t c0 = cbeg; c0 < cend; c0 += 32) {
             // 1. one candidate per lane: does its window reach the band?  The
@@ -411,19 +408,13 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wp_grid_kernel(BandArgs a)
                 for (int k = 0; k < kBandRows; ++k)
                     kv[k] = (colok && av[k] >= 0) ? __ldg(kp + av[k]) : make_float2(0.f, 0.f);
                 const float4 vx = E.vx;
+                const float2 v1 = make_float2(vx.x, vx.y), v2 = make_float2(vx.z, vx.w);
                 const float2 pw = E.pw;
 #pragma unroll
                 for (int k = 0; k < kBandRows; ++k) {
-                    // each part's two products in turn: kr vr then
-                    // ki (-t vi); kr vi then ki (t vr)
-                    Dr[k] = __fmaf_rn(kv[k].x, vx.x, Dr[k]);
-                    Di[k] = __fmaf_rn(kv[k].x, vx.z, Di[k]);
-                    Dr[k] = __fmaf_rn(kv[k].y, vx.y, Dr[k]);
-                    Di[k] = __fmaf_rn(kv[k].y, vx.w, Di[k]);
-                    if (!RESIDUAL) {
-                        Pr[k] = __fmaf_rn(kv[k].x, pw.x, Pr[k]);
-                        Pi[k] = __fmaf_rn(kv[k].y, pw.y, Pi[k]);
-                    }
+                    X[k] = __ffma2_rn(kv[k], v1, X[k]);
+                    Y[k] = __ffma2_rn(kv[k], v2, Y[k]);
+                    if (!RESIDUAL) P[k] = __ffma2_rn(kv[k], pw, P[k]);
                 }
             }
             __syncwarp();
@@ -434,9 +425,8 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wp_grid_kernel(BandArgs a)
             const int64_t x = x0 + k, y = y0 + lane;
             if (x < a.gnx && y < a.gny) {
                 const int64_t cell = x * a.gny + y;
-                const float2 d = make_float2(Dr[k], Di[k]);
-                const float2 pk = make_float2(Pr[k], Pi[k]);
-                if (!RESIDUAL && (pk.x != 0.0f || pk.y != 0.0f)) atomicAdd(&a.psf[cell], pk);
+                const float2 d = make_float2(X[k].x + X[k].y, Y[k].x + Y[k].y);
+                if (!RESIDUAL && (P[k].x != 0.0f || P[k].y != 0.0f)) atomicAdd(&a.psf[cell], P[k]);
                 if (d.x != 0.0f || d.y != 0.0f) atomicAdd(&a.dirty[cell], d);
             }
         }
