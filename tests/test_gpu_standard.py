@@ -198,3 +198,45 @@ def test_pinned_host_inputs_give_pinned_outputs(ctx):
     assert peak_norm_err(psf_p.numpy(), psf) <= TOL
     assert peak_norm_err(res_p.numpy(), res) <= TOL
     assert state_p.psf_peak == pytest.approx(state.psf_peak, rel=1e-6)
+
+
+def _around(x):
+    """x and the doubles one and two ulps either side of it."""
+    lo1 = np.nextafter(x, -np.inf)
+    hi1 = np.nextafter(x, np.inf)
+    return [np.nextafter(lo1, -np.inf), lo1, x, hi1, np.nextafter(hi1, np.inf)]
+
+
+@pytest.mark.parametrize("os_", [100, 128])
+def test_plan_decisions_at_rounding_boundaries(ctx, os_):
+    """The standard plan takes its anchor and tap-row decisions on float32
+    pairs and falls back to the reference's FP64 operations near a rounding
+    boundary.  Samples on and a few ulps either side of each anchor boundary
+    (x = k + 1/2) and tap-row boundary (x = k + (j + 1/2)/os) must get the
+    oracle's FP64 decisions: the same samples accepted, and degridded values
+    (which select the taps by exactly those decisions) that match; the grid
+    edges (anchors 3 cells from either end) too."""
+    geom, og, gg = make(ctx, 256, 2e-5, os_)
+    G = og.gnx
+    rng = np.random.default_rng(91 + os_)
+    us, vs = [], []
+    ks = list(rng.integers(G // 4, 3 * G // 4, 4)) + [3, G - 4]
+    for k in ks:
+        for frac in [0.5] + [(j + 0.5) / os_ for j in range(-os_ // 2, os_ // 2, 7)]:
+            for du in _around((k + frac - G / 2) * og.du):
+                us.append(du)
+                vs.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                us.append(rng.uniform(-0.2, 0.2) * G * og.du)
+                vs.append(-du)
+    u, v = np.array(us), np.array(vs)
+    n = len(u)
+    wt = np.ones(n, np.float32)
+    vis = np.ones(n, np.complex64)
+    _, _, acc = og.grid_dirty(u, v, wt, vis)
+    _, _, sums = cc.grid_dirty(gg, cc.VisibilityBatch(u, v, vis, wt))
+    assert sums.gridded_samples == acc.gridded and sums.skipped_samples == acc.skipped
+    grid = (rng.normal(size=(G, G)) + 1j * rng.normal(size=(G, G))).astype(np.complex64)
+    pred_o = og.degrid(grid, u, v)
+    pred_g = cc.degrid(gg, cc.VisibilityBatch(u, v, vis, wt), grid)
+    scale = np.maximum(np.abs(pred_o), 1e-3 * np.max(np.abs(pred_o)))
+    assert np.max(np.abs(pred_g - pred_o) / scale) <= 1e-3
