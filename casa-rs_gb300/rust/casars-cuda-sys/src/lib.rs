@@ -16,7 +16,7 @@ pub mod sys;
 use std::ffi::CStr;
 use std::fmt;
 use std::marker::PhantomData;
-use std::os::raw::c_char;
+use std::os::raw::{c_char, c_void};
 use std::ptr::{null, null_mut};
 
 pub use sys::{cr_beam, cr_grid_info, cr_psf_state, cr_sums, cr_timings, cr_wproj_info};
@@ -142,6 +142,58 @@ impl Context {
     /// kernels where the grid allows, 1 cuFFT FP64.
     pub fn set_image_fft_engine(&self, engine: i32) -> Result<()> {
         check(unsafe { sys::cr_ctx_set_image_fft_engine(self.raw, engine) }, null_mut())
+    }
+
+    /// Run the following calls on `stream` (a `cudaStream_t`); null returns
+    /// to the context's own non-blocking stream.  The legacy default stream
+    /// is passed as `cudaStreamLegacy` (`1 as *mut c_void`).
+    ///
+    /// # Safety
+    /// `stream` must stay a valid stream of this context's device while the
+    /// context uses it.
+    pub unsafe fn set_stream(&self, stream: *mut c_void) -> Result<()> {
+        call(|e| sys::cr_ctx_set_stream(self.raw, stream, e))
+    }
+
+    /// The stream the calls run on.
+    pub fn stream(&self) -> *mut c_void {
+        unsafe { sys::cr_ctx_stream(self.raw) }
+    }
+
+    /// Per-call stage timings on (the default) or off; with them off, calls
+    /// whose outputs stay on the device return once their work is queued.
+    pub fn set_timings(&self, enable: bool) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_timings(self.raw, enable as i32) }, null_mut())
+    }
+
+    /// A workspace budget in bytes (0: none), for tests of allocation failure.
+    pub fn set_alloc_limit(&self, bytes: i64) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_alloc_limit(self.raw, bytes) }, null_mut())
+    }
+
+    /// Poll limits of the bounded device waits, for tests of the timeout
+    /// path: 0 gives up at once (the call then fails with
+    /// `CudaError::Unsupported`, the `CR_TIMEOUT` mapping), a negative value
+    /// restores the default.
+    pub fn set_wait_limits(&self, barrier_polls: i64, mbar_polls: i64) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_wait_limits(self.raw, barrier_polls, mbar_polls) },
+              null_mut())
+    }
+
+    /// Repeated all-device cube calls captured into CUDA graphs (the
+    /// default) or run eagerly.
+    pub fn set_cube_graphs(&self, enable: bool) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_cube_graphs(self.raw, enable as i32) }, null_mut())
+    }
+
+    /// Records per cube gridding work item: 0 lets the tuner choose.
+    pub fn set_cube_grid_chunk(&self, chunk: i32) -> Result<()> {
+        check(unsafe { sys::cr_ctx_set_cube_grid_chunk(self.raw, chunk) }, null_mut())
+    }
+
+    /// Device scratch the context holds, in bytes.
+    pub fn workspace_bytes(&self) -> i64 {
+        unsafe { sys::cr_ctx_workspace_bytes(self.raw) }
     }
 
     pub fn synchronize(&self) -> Result<()> {
