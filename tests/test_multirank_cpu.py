@@ -2,6 +2,7 @@
 rank's time wins, the whole-job rate counts every replica, ranks read their
 identity from the launcher's environment, and only rank 0 runs the
 reference arm."""
+import json
 import os
 import socket
 import sys
@@ -66,3 +67,24 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1"])
     bench.run_reference(bench.parse())
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """The reference arm on rank 0: one JSON line with the contract's keys,
+    timed on the host (the oracle's Complex32 restatement of the path)."""
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1",
+                                      "--warmup", "0"])
+    bench.run_reference(bench.parse())
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "Mvis/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1
+    assert d["config"]["workload"]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
+    assert cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
